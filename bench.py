@@ -1,0 +1,332 @@
+"""Benchmark of the GB300 VBD step: vertex-solves/s and steps/s.
+
+Default workload (the headline configuration): the 100^3-vertex lattice cube
+twist test (1.0 M vertices, 4.85 M tets, both x faces Dirichlet, one rotating at
+2 rad/s), dt = 1/300 s, 50 VBD iterations per step, synthetic seeded inputs.
+
+One JSON line on rank 0 with:
+  value   = vertex-solves/s of the FP32-mixed engine, inputs resident in HBM,
+            device-timed with CUDA events on the library's stream;
+  e2e     = the same metric through the public C ABI with host buffers
+            (per step: H2D of positions+velocities, the step, D2H of both);
+  fp64    = the plain FP64 engine on the same workload (same kernels in FP64);
+  error   = relative position error of the mixed engine vs the FP64 engine
+            after --error-steps steps from the same initial state;
+  roofline, cpu_baseline, clocks, gpu_launches.
+
+``--impl reference`` times the CPU restatement of the reference's VBD path (the
+oracle, all host threads) on bounded samples of the same workload.
+Multi-GPU (torchrun): one independent replica per rank (weak scaling, no
+collective on the data path); rank 0 reports the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "VBD vertex-solves/s & steps/s, FP32-mixed vs plain FP64 at <=1e-5 rel pos err"
+
+
+def load_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allmax(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_scene(workload: str, d: str, precision: str, size: int, iterations: int):
+    from gaia_gb300 import scenes
+
+    if workload == "twist":
+        return scenes.twist_cube(d, n=size, iterations=iterations, precision=precision)
+    if workload == "drop":
+        return scenes.drop_cube(d, n=size, iterations=iterations, precision=precision)
+    if workload == "batch":
+        return scenes.batch_cubes(d, n_scenes=512, iterations=iterations, precision=precision)
+    raise ValueError(workload)
+
+
+def cpu_sample(mp: str, pp: str, iters: int, reps: int, nthreads: int = 0) -> dict:
+    """Oracle (CPU restatement of the reference VBD step, FP64, all host threads):
+    `reps` samples of one substep with `iters` iterations each."""
+    from oracle import oracle as orc
+    from oracle import scene_io
+
+    sc = scene_io.load_scene(mp, pp)
+    o = orc.OracleScene(sc, precision=64, nthreads=nthreads)
+    nact = sum(int(len(m["fixed"]) - m["fixed"].sum()) for m in sc["meshes"])
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        o.substep_sample(iters)
+    dt = time.perf_counter() - t0
+    cores = nthreads if nthreads > 0 else (os.cpu_count() or 1)
+    return {"vertex_solves_per_s": nact * iters * reps / dt, "seconds": dt, "cores": cores,
+            "active_vertices": nact, "iterations": iters, "reps": reps}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as d:
+        mp, pp = make_scene(args.workload, d, "fp64", args.size, args.iterations)
+        from oracle import oracle as orc
+        from oracle import scene_io
+
+        sc = scene_io.load_scene(mp, pp)
+        o = orc.OracleScene(sc, precision=64, nthreads=0)
+        nact = sum(int(len(m["fixed"]) - m["fixed"].sum()) for m in sc["meshes"])
+        for _ in range(args.warmup):
+            o.substep_sample(args.ref_iters)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            o.substep_sample(args.ref_iters)
+        dt = time.perf_counter() - t0
+    v = nact * args.ref_iters * args.steps / dt
+    cores = os.cpu_count() or 1
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "vertex-solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "steps_per_s_extrapolated": v / (nact * args.iterations),
+        "config": {"workload": f"{args.workload}_{args.size}", "iterations_per_step": args.iterations,
+                   "sample": f"each step = one substep with {args.ref_iters} iterations"},
+        "cpu_baseline": {"value": v, "unit": "vertex-solves/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} samples of one substep x {args.ref_iters} iterations, "
+                                   f"{nact} active vertices"},
+        "e2e": {"value": v, "unit": "vertex-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gaia", choices=["gaia", "reference"])
+    ap.add_argument("--workload", default="twist", choices=["twist", "drop", "batch"])
+    ap.add_argument("--size", type=int, default=100)
+    ap.add_argument("--iterations", type=int, default=50)
+    ap.add_argument("--error-steps", type=int, default=100)
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--ref-iters", type=int, default=2)
+    ap.add_argument("--cpu-reps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import numpy as np
+    import torch
+
+    from gaia_gb300 import VBDPhysics, scenes
+
+    peak, peak_kind = load_peaks()
+    tmp = tempfile.TemporaryDirectory()
+    d = tmp.name
+    mp, pp = make_scene(args.workload, d, args.precision, args.size, args.iterations)
+
+    # ---- FP32-mixed engine: device-resident timing ---------------------------------
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, pp)
+    phys.initialize()
+    st = phys.stats()
+    nact = st["num_active_vertices"]
+    ninc = st["num_incidences"]
+    for _ in range(args.warmup):
+        phys.runStep(1)
+    phys.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    barrier(world)
+    total_ms, sweep_ms = phys.run_steps_timed(args.steps)
+    clocks = clk.stop()
+    total_ms = allmax(world, total_ms)
+    solves = nact * args.iterations * args.steps
+    value = world * solves / (total_ms / 1e3)
+    steps_per_s = args.steps / (total_ms / 1e3)
+    st = phys.stats()
+
+    # roofline of the solve kernel: algorithmic bytes per iteration (64 B/vertex + 61 B/incidence)
+    launches_solve = st["num_groups"] * args.iterations * args.steps
+    alg_bytes_iter = 64.0 * nact + 61.0 * ninc
+    achieved = alg_bytes_iter * args.iterations * args.steps / (sweep_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": alg_bytes_iter / st["num_groups"],
+                "avg_launch_us": 1e3 * sweep_ms / launches_solve}
+
+    # ---- e2e through the C ABI with host buffers ----------------------------------------
+    n = st["num_vertices"]
+    xh = torch.empty(3 * n, dtype=torch.float32, pin_memory=True)
+    vh = torch.empty(3 * n, dtype=torch.float32, pin_memory=True)
+    phys.get_positions_f32(xh.data_ptr())
+    phys.get_velocities_f32(vh.data_ptr())
+    e2e_steps = max(3, args.steps // 2)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        phys.set_state_f32(xh.data_ptr(), vh.data_ptr())
+        phys.runStep(1)
+        phys.get_positions_f32(xh.data_ptr())
+        phys.get_velocities_f32(vh.data_ptr())
+    e2e_s = allmax(world, time.perf_counter() - t0)
+    e2e_value = world * nact * args.iterations * e2e_steps / e2e_s
+
+    # ---- plain FP64 engine + error vs FP64 after --error-steps steps ------------------------
+    fp64 = None
+    err = None
+    if not args.no_fp64:
+        pp64 = scenes.set_precision(pp, "fp64")
+        p64 = VBDPhysics()
+        p64.loadRunningparameters(mp, pp64)
+        p64.initialize()
+        p64.runStep(2)
+        p64.synchronize()
+        t64, s64 = p64.run_steps_timed(args.fp64_steps)
+        v64 = nact * args.iterations * args.fp64_steps / (t64 / 1e3)
+        fp64 = {"value": v64, "unit": "vertex-solves/s", "ms_per_step": t64 / args.fp64_steps,
+                "speedup_mixed_over_fp64": value / world / v64}
+        if args.error_steps > 0:
+            p64.reset()
+            phys.reset()
+            x0 = phys.positions(0)
+            p64.runStep(args.error_steps)
+            phys.runStep(args.error_steps)
+            xr, xm = p64.positions(0), phys.positions(0)
+            err = {"steps": args.error_steps, "rel": float(np.linalg.norm(xm - xr) / np.linalg.norm(xr - x0)),
+                   "max_abs_m": float(np.abs(xm - xr).max()), "reference": "fp64 engine, same kernels"}
+        p64.close()
+    phys.close()
+
+    # ---- CPU baseline: the oracle on a bounded sample of the same workload ------------------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        s = cpu_sample(mp, pp, iters=args.ref_iters, reps=args.cpu_reps)
+        cpu = {"value": s["vertex_solves_per_s"], "unit": "vertex-solves/s", "cores": s["cores"], "kind": "port",
+               "sample": f"{s['reps']} x one substep with {s['iterations']} iterations over {s['active_vertices']} "
+                         f"active vertices ({s['seconds']:.1f} s), FP64 CPU restatement of the reference step"}
+    tmp.cleanup()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "vertex-solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "steps_per_s": steps_per_s * 1.0,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 state)",
+            "data": "synthetic (seeded PCG64 lattice)",
+            "config": {"workload": f"{args.workload}_cube_{args.size}^3 ({st['num_vertices']} vertices, "
+                                   f"{ninc} solved incidences), {args.iterations} iterations/step, dt=1/300",
+                       "precision": args.precision, "colors": st["num_groups"], "lanes_per_vertex": st["lanes_per_vertex"],
+                       "block": st["block_size"], "l2": "inputs larger than L2 (incidence records "
+                                                         f"{48 * ninc / 1e9:.2f} GB per iteration)"},
+            "e2e": {"value": e2e_value, "unit": "vertex-solves/s", "h2d_bytes_per_step": 24 * n,
+                    "d2h_bytes_per_step": 24 * n, "steps": e2e_steps},
+            "fp64": fp64, "error_vs_fp64": err, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": st["kernel_launches_per_step"] * args.steps,
+            "fp64_fallback_solves": st["fp64_fallback_solves"], "failed_solves": st["failed_solves"],
+        }
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,108 @@
+"""ctypes binding of libgaia_vbd.so (the C ABI in include/gaia_vbd.h).
+
+The library is built in-tree by ``gaia_gb300.build.build()``. There is no CPU
+fallback: if the library is missing or cannot be loaded, ``lib()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgaia_vbd.so")
+
+# status codes (include/gaia_vbd.h)
+OK = 0
+E_INVALID_ARG = 1
+E_INPUT = 2
+E_COLORING = 3
+E_MESH = 4
+E_CUDA = 5
+E_NONFINITE = 6
+E_NO_DEVICE = 7
+E_UNSUPPORTED = 8
+
+STATUS_NAMES = {
+    OK: "OK", E_INVALID_ARG: "INVALID_ARG", E_INPUT: "INPUT", E_COLORING: "COLORING", E_MESH: "MESH",
+    E_CUDA: "CUDA", E_NONFINITE: "NONFINITE", E_NO_DEVICE: "NO_DEVICE", E_UNSUPPORTED: "UNSUPPORTED",
+}
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int32), ("lanes_per_vertex", C.c_int32), ("block_size", C.c_int32),
+        ("num_groups", C.c_int32), ("num_vertices", C.c_int64), ("num_active_vertices", C.c_int64),
+        ("num_incidences", C.c_int64), ("kernel_launches_per_step", C.c_int64),
+        ("fp64_fallback_solves", C.c_int64), ("failed_solves", C.c_int64), ("device_bytes", C.c_int64),
+        ("autotune_ms_per_iteration", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# Every symbol the header declares, with its ctypes signature.
+_SIGNATURES = {
+    "gaia_vbd_create": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    "gaia_vbd_load": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    "gaia_vbd_initialize": (C.c_int, [C.c_void_p]),
+    "gaia_vbd_destroy": (None, [C.c_void_p]),
+    "gaia_vbd_last_error": (C.c_char_p, [C.c_void_p]),
+    "gaia_vbd_last_global_error": (C.c_char_p, []),
+    "gaia_vbd_run_step": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gaia_vbd_synchronize": (C.c_int, [C.c_void_p]),
+    "gaia_vbd_run_step_timed": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "gaia_vbd_autotune": (C.c_int, [C.c_void_p]),
+    "gaia_vbd_reset": (C.c_int, [C.c_void_p]),
+    "gaia_vbd_num_meshes": (C.c_int, [C.c_void_p]),
+    "gaia_vbd_num_vertices": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "gaia_vbd_num_tets": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "gaia_vbd_get_positions": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_vbd_set_positions": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_vbd_get_velocities": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_vbd_set_velocities": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_vbd_set_state_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gaia_vbd_get_positions_f32": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gaia_vbd_get_velocities_f32": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gaia_vbd_num_groups": (C.c_int, [C.c_void_p]),
+    "gaia_vbd_group_size": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "gaia_vbd_get_group": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_vbd_get_coloring": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_vbd_get_rest_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gaia_vbd_energy": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "gaia_vbd_vertex_force_hessian": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "gaia_vbd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "gaia_vbd_color_mcs": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "gaia_vbd_color_greedy": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "gaia_vbd_write_coloring": (C.c_int, [C.c_char_p, C.c_int32, C.c_void_p]),
+    "gaia_vbd_write_t": (C.c_int, [C.c_char_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libgaia_vbd.so. Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import gaia_gb300.build as b; b.build()'` "
+                "(there is no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGNATURES)
+
+
+class GaiaError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"gaia_vbd error {STATUS_NAMES.get(code, code)}: {message}")
+        self.code = code

@@ -1,0 +1,124 @@
+// Host-side scene model for the VBD step: the inputs Gaia's VBDPhysics reads
+// (Models.json / Parameters.json), the tet meshes, colorings and the merged
+// per-color "parallel groups". Everything here runs once at set-up on the
+// host; the per-step work lives in the CUDA engine.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace gaia {
+
+// Hot-path keys of BasePhysicsParams (Parameters/PhysicsParameters.h:9-178) and
+// VBDPhysicsParameters (VBD/VBDPhysicsParameters.h:5-147), with the same
+// defaults. Keys the VBD step does not read are ignored.
+struct PhysicsParams {
+    double gravity[3] = {0.0, -10.0, 0.0};
+    double timeStep = 0.01666666666666666666;
+    int numSubsteps = 20;
+    int iterations = 1;
+    bool usePlaneGround = true;
+    double worldLo[3] = {-1e7, -1e7, -1e7};
+    double worldHi[3] = {1e7, 1e7, 1e7};
+    double boundaryFrictionDynamic = 0.1;
+    double boundaryFrictionEpsV = 1.0;
+    double boundaryCollisionStiffness = 1e5;
+    double stepSize = 1.0;
+    double stepSizeGD = 1e-3;
+    int frictionStartIter = 0;
+    bool associateGravityWithInertia = true;
+    bool useAccelerator = false;
+    double acceleratorRho = 0.93;
+    bool useGPU = true;
+    bool handleCollision = false;
+    double collisionStiffness = 1e5;
+    int numThreadsVBDSolve = 16;
+    bool useDouble3x3 = false;
+    bool evaluateConvergence = false;
+    // derived (BasePhysicsFramework.cpp:245-249)
+    double dt = -1.0, dtSqrReciprocal = -1.0;
+    // GB300 engine keys (extensions; absent in reference files -> defaults)
+    std::string gpuPrecision = "mixed";  // "mixed" (FP64 state, FP32 element math), "fp32" or "fp64"
+    int lanesPerVertex = 0;              // 0 = autotune
+    int blockSize = 0;                   // 0 = autotune
+    bool autotune = true;
+};
+
+// ObjectParams (Materials/Materials.h:12-75) + ObjectParamsVBD
+// (VBD/VBD_BaseMaterial.h:21-49) + ObjectParametersVBDNeoHookean
+// (VBD/VBD_NeoHookean.h:16-33), same defaults.
+struct ObjectParams {
+    std::string path;
+    std::string materialName = "NeoHookean";
+    std::string verticesColoringCategoriesPath;
+    double translationBeforeScaling[3] = {0, 0, 0};
+    double scale[3] = {1, 1, 1};
+    double translation[3] = {0, 0, 0};
+    double rotation[3] = {0, 0, 0};
+    double initialVelocity[3] = {0, 0, 0};
+    double density = 1.0;
+    double maxVelocityMagnitude = -1.0;
+    int frameToAppear = -1;
+    std::vector<int32_t> fixedPoints;
+    double frictionDynamic = 0.1;
+    double frictionEpsV = 0.01;
+    double exponentialVelDamping = 1.0;
+    double constantVelDamping = 0.0;
+    int initializationType = 0;
+    double miu = 1e4;
+    double lmbd = 1e4;
+    double dampingDeviatoric = 0.0;
+    double dampingHydrostatic = 0.0;
+};
+
+// Deformers[] entries of Parameters.json (VBD/VBDDeformer.h:175-221).
+struct DeformerParams {
+    int type = 0;  // 0 = Rotator, 1 = Translator
+    double center[3] = {0, 0, 0};
+    double axis[3] = {1, 0, 0};
+    double angularVelocity = 0.0;
+    double endTime = -1.0;
+    double speed[3] = {0, 0, 0};
+    std::vector<int32_t> selectedMeshes;
+    std::vector<std::vector<int32_t>> selectedVertices;
+};
+
+struct TetMesh {
+    int32_t nv = 0, ntet = 0;
+    std::vector<float> X;          // 3*nv positions after rotation/scale/translation (FP32, as mVertPos)
+    std::vector<float> V;          // 3*nv initial velocities
+    std::vector<int32_t> tets;     // 4*ntet
+    std::vector<double> dminv;     // 9*ntet column-major, FP64 precompute
+    std::vector<double> vol;       // ntet
+    std::vector<double> mass;      // nv
+    std::vector<uint8_t> fixed;    // nv
+    std::vector<std::vector<int32_t>> colors;  // sorted by size, large to small
+    std::vector<int32_t> nbr_ofs, nbr_tet, nbr_order;  // CSR vertex -> incident tets
+};
+
+struct Scene {
+    PhysicsParams p;
+    std::vector<ObjectParams> objs;
+    std::vector<TetMesh> meshes;
+    std::vector<DeformerParams> defs;
+    std::vector<std::vector<int32_t>> groups;  // merged colors: (mesh, vertex) pairs
+};
+
+// Loading (throws std::runtime_error with a message on any failure).
+void load_scene(const std::string& models_json, const std::string& params_json, const std::string& repo_root,
+                Scene& scene);
+void load_t(const std::string& path, std::vector<float>& X, std::vector<int32_t>& tets);
+std::vector<std::vector<int32_t>> load_coloring(const std::string& path);
+void prepare_mesh(const PhysicsParams& p, const ObjectParams& o, TetMesh& m);  // rest shape, CSR, fixed
+void build_parallel_groups(Scene& scene);
+void validate_coloring(const TetMesh& m);  // every vertex exactly once; no two tet-neighbours share a color
+
+// Colorings (bit-exact with GraphColoring/mcs.cpp and gready.cpp, in O(E log V)).
+int32_t color_mcs(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
+int32_t color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
+std::vector<std::vector<int32_t>> colors_to_categories(int32_t nv, const int32_t* colors);
+
+void write_t(const std::string& path, int32_t nv, const double* X, int32_t ntet, const int32_t* tets);
+void write_coloring(const std::string& path, const std::vector<std::vector<int32_t>>& cats);
+
+}  // namespace gaia

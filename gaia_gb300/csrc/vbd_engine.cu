@@ -1,0 +1,1023 @@
+// GB300 VBD engine and the C ABI of libgaia_vbd.so (declared in include/gaia_vbd.h).
+//
+// One handle = one scene on one GPU: device buffers in the slot layout
+// described in vbd_kernels.cuh, one CUDA stream, and three CUDA graphs per
+// substep (initial step + deformers | all color sweeps of all iterations |
+// velocity update). The graphs replace the reference's per-iteration graph
+// (VBDPhysics.cpp:1546-1570) and its host<->device syncs per substep.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gaia_vbd.h"
+#include "scene.hpp"
+#include "vbd_kernels.cuh"
+
+namespace gaia {
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+#define GAIA_CUDA(call)                                                                                  \
+    do {                                                                                                 \
+        cudaError_t e__ = (call);                                                                        \
+        if (e__ != cudaSuccess)                                                                          \
+            throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e__) + " (" + __FILE__ + ":" + \
+                            std::to_string(__LINE__) + ")");                                             \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    void alloc(size_t count, size_t* total) {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = count;
+        if (count) {
+            GAIA_CUDA(cudaMalloc(&p, count * sizeof(T)));
+            if (total) *total += count * sizeof(T);
+        }
+    }
+    void upload(const std::vector<T>& h, size_t* total, cudaStream_t st) {
+        alloc(h.size(), total);
+        if (!h.empty()) GAIA_CUDA(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    }
+};
+
+inline int div_up(int64_t a, int64_t b) { return int((a + b - 1) / b); }
+
+}  // namespace
+
+// One incidence record (layout in vbd_kernels.cuh).
+template <typename R>
+void make_record(int4& n, dev::R4<R>& a, dev::R4<R>& b, R* c, const int* nb, double mv[3][3]);
+
+class EngineBase {
+public:
+    virtual ~EngineBase() {}
+    virtual void run_steps(int n) = 0;
+    virtual void run_steps_timed(int n, float* total_ms, float* sweep_ms) = 0;
+    virtual void autotune() = 0;
+    virtual void reset() = 0;
+    virtual void get_positions(int mesh, double* out) = 0;
+    virtual void set_positions(int mesh, const double* in) = 0;
+    virtual void get_velocities(int mesh, double* out) = 0;
+    virtual void set_velocities(int mesh, const double* in) = 0;
+    virtual void set_state_f32(const float* x, const float* v) = 0;
+    virtual void get_positions_f32(float* x) = 0;
+    virtual void get_velocities_f32(float* v) = 0;
+    virtual double energy() = 0;
+    virtual void vertex_force_hessian(int mesh, int v, int friction, double* f3, double* h9) = 0;
+    virtual void stats(gaia_vbd_stats* s) = 0;
+    virtual void sync() = 0;
+};
+
+template <typename ST, typename R>
+class Engine : public EngineBase {
+    using S4 = typename ST::U;   // per-vertex displacement state
+    using V4 = typename ST::V;   // per-vertex velocity
+    using Sc = typename ST::Sc;
+    using R4 = dev::R4<R>;
+
+public:
+    explicit Engine(const Scene& s) : sc_(s) {
+        GAIA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+        GAIA_CUDA(cudaEventCreate(&ev_a_));
+        GAIA_CUDA(cudaEventCreate(&ev_b_));
+        GAIA_CUDA(cudaEventCreate(&ev_c_));
+        build_layout();
+        upload();
+        lanes_ = sc_.p.lanesPerVertex;
+        block_ = sc_.p.blockSize;
+        if (lanes_ != 0 && lanes_ != 2 && lanes_ != 4 && lanes_ != 8 && lanes_ != 16 && lanes_ != 32)
+            throw std::runtime_error("lanesPerVertex must be 2, 4, 8, 16 or 32");
+        if (block_ != 0 && (block_ < 64 || block_ > 512 || block_ % 32))
+            throw std::runtime_error("blockSize must be a multiple of 32 in [64, 512]");
+        if (lanes_ == 0 || block_ == 0) {
+            if (sc_.p.autotune) autotune_impl();
+            if (lanes_ == 0) lanes_ = 4;
+            if (block_ == 0) block_ = 256;
+        }
+        capture();
+    }
+
+    ~Engine() override {
+        destroy_graphs();
+        if (ev_a_) cudaEventDestroy(ev_a_);
+        if (ev_b_) cudaEventDestroy(ev_b_);
+        if (ev_c_) cudaEventDestroy(ev_c_);
+        if (st_) cudaStreamDestroy(st_);
+    }
+
+    // ---- layout ---------------------------------------------------------------
+    void build_layout() {
+        const auto& meshes = sc_.meshes;
+        nmesh_ = int(meshes.size());
+        mesh_off_.assign(nmesh_ + 1, 0);
+        for (int m = 0; m < nmesh_; ++m) mesh_off_[m + 1] = mesh_off_[m] + meshes[m].nv;
+        nslots_ = mesh_off_[nmesh_];
+        if (nslots_ > int64_t(INT32_MAX) / 2) throw std::runtime_error("scene too large for 32-bit vertex indices");
+        slot_of_.assign(nslots_, -1);
+        int32_t slot = 0;
+        group_beg_.clear();
+        group_end_.clear();
+        for (auto& g : sc_.groups) {
+            group_beg_.push_back(slot);
+            for (size_t i = 0; i + 1 < g.size(); i += 2) {
+                int m = g[i], v = g[i + 1];
+                if (!meshes[m].fixed[v]) slot_of_[mesh_off_[m] + v] = slot++;
+            }
+            group_end_.push_back(slot);
+        }
+        nactive_ = slot;
+        for (int64_t gi = 0; gi < nslots_; ++gi)
+            if (slot_of_[gi] < 0) slot_of_[gi] = slot++;
+        if (slot != nslots_) throw std::runtime_error("internal: slot assignment incomplete");
+        orig_of_.assign(nslots_, 0);
+        for (int64_t gi = 0; gi < nslots_; ++gi) orig_of_[slot_of_[gi]] = int32_t(gi);
+        slot_mesh_.assign(nslots_, 0);
+        for (int m = 0; m < nmesh_; ++m)
+            for (int v = 0; v < meshes[m].nv; ++v) slot_mesh_[slot_of_[mesh_off_[m] + v]] = m;
+
+        // incidence records in slot order
+        inc_ofs_.assign(size_t(nactive_) + 1, 0);
+        for (int32_t s = 0; s < nactive_; ++s) {
+            int32_t gi = orig_of_[s];
+            int m = slot_mesh_[s];
+            int v = gi - int32_t(mesh_off_[m]);
+            inc_ofs_[s + 1] = inc_ofs_[s] + (meshes[m].nbr_ofs[v + 1] - meshes[m].nbr_ofs[v]);
+        }
+        ninc_ = inc_ofs_[nactive_];
+        if (int64_t(ninc_) > int64_t(INT32_MAX)) throw std::runtime_error("too many incidences");
+        h_rec_n_.resize(ninc_);
+        h_rec_a_.resize(ninc_);
+        h_rec_b_.resize(ninc_);
+        if (sizeof(R) == 8) h_rec_c_.resize(ninc_);
+        for (int32_t s = 0; s < nactive_; ++s) {
+            int32_t gi = orig_of_[s];
+            int m = slot_mesh_[s];
+            const TetMesh& M = meshes[m];
+            int v = gi - int32_t(mesh_off_[m]);
+            int32_t r = inc_ofs_[s];
+            for (int k = M.nbr_ofs[v]; k < M.nbr_ofs[v + 1]; ++k, ++r) {
+                int t = M.nbr_tet[k], o = M.nbr_order[k];
+                const double* Di = &M.dminv[9 * size_t(t)];
+                int others[3], q = 0;
+                for (int j = 0; j < 4; ++j)
+                    if (j != o) others[q++] = j;
+                if (o & 1) std::swap(others[0], others[1]);  // keeps det[m0;m1;m2] = det(DmInv)
+                double mv[3][3];
+                int nb[3];
+                for (int i = 0; i < 3; ++i) {
+                    int j = others[i];
+                    for (int c = 0; c < 3; ++c)
+                        mv[i][c] = j == 0 ? -(Di[3 * c] + Di[3 * c + 1] + Di[3 * c + 2]) : Di[3 * c + (j - 1)];
+                    nb[i] = slot_of_[mesh_off_[m] + M.tets[4 * size_t(t) + j]];
+                }
+                set_record(r, nb, mv);
+            }
+        }
+        // per-slot state
+        h_pos_.resize(nslots_);
+        h_vel_.resize(nslots_);
+        h_rest_.resize(nslots_);
+        for (int m = 0; m < nmesh_; ++m) {
+            const TetMesh& M = meshes[m];
+            for (int v = 0; v < M.nv; ++v) {
+                int32_t s = slot_of_[mesh_off_[m] + v];
+                h_rest_[s] = make_float4(M.X[3 * size_t(v)], M.X[3 * size_t(v) + 1], M.X[3 * size_t(v) + 2], 0.f);
+                const double zero[3] = {0.0, 0.0, 0.0};
+                h_pos_[s] = ST::from_d(zero, M.mass[v]);  // displacement from rest, mass
+                h_vel_[s] = V4{Sc(M.V[3 * size_t(v)]), Sc(M.V[3 * size_t(v) + 1]), Sc(M.V[3 * size_t(v) + 2]), Sc(0)};
+            }
+        }
+        // materials
+        h_mats_.resize(nmesh_);
+        for (int m = 0; m < nmesh_; ++m) {
+            const ObjectParams& o = sc_.objs[m];
+            dev::MeshMat<R> mm{};
+            mm.mu = R(o.miu);
+            mm.lmbd = R(o.lmbd);
+            mm.a = R(1.0 + o.miu / o.lmbd);
+            mm.kh = R(o.dampingHydrostatic);
+            mm.kd = R(o.dampingDeviatoric);
+            mm.exp_damp = R(std::pow(o.exponentialVelDamping, sc_.p.dt));  // VBDPhysics.cpp:794-807
+            mm.const_damp = R(o.constantVelDamping * sc_.p.dt);
+            mm.init_type = o.initializationType;
+            h_mats_[m] = mm;
+        }
+        // deformers
+        for (size_t di = 0; di < sc_.defs.size(); ++di) {
+            const DeformerParams& d = sc_.defs[di];
+            dev::DeformerDev dd{};
+            dd.type = d.type;
+            for (int k = 0; k < 3; ++k) {
+                dd.axis[k] = d.axis[k];
+                dd.speed[k] = d.speed[k];
+            }
+            dd.omega = d.angularVelocity;
+            dd.end_time = d.endTime;
+            h_defs_.push_back(dd);
+            for (size_t k = 0; k < d.selectedMeshes.size(); ++k) {
+                int m = d.selectedMeshes[k];
+                for (int32_t v : d.selectedVertices[k]) {
+                    const float* X = &meshes[m].X[3 * size_t(v)];
+                    double P[3] = {X[0], X[1], X[2]};
+                    h_def_slot_.push_back(slot_of_[mesh_off_[m] + v]);
+                    h_def_idx_.push_back(int32_t(di));
+                    if (d.type == 0) {
+                        double OP[3] = {P[0] - d.center[0], P[1] - d.center[1], P[2] - d.center[2]};
+                        double dot = OP[0] * d.axis[0] + OP[1] * d.axis[1] + OP[2] * d.axis[2];
+                        for (int c = 0; c < 3; ++c) {
+                            double root = dot * d.axis[c];
+                            h_def_a_.push_back(root);
+                            h_def_b_.push_back(P[c] - root);
+                        }
+                    } else {
+                        for (int c = 0; c < 3; ++c) {
+                            h_def_a_.push_back(P[c]);
+                            h_def_b_.push_back(0.0);
+                        }
+                    }
+                }
+            }
+        }
+        // constants
+        const PhysicsParams& p = sc_.p;
+        c_.dt = R(p.dt);
+        c_.inv_dt = R(1.0 / p.dt);
+        c_.dt2inv = R(p.dtSqrReciprocal);
+        c_.dt_d = p.dt;
+        for (int k = 0; k < 3; ++k) {
+            c_.g[k] = p.gravity[k];
+            c_.lo[k] = p.worldLo[k];
+            c_.hi[k] = p.worldHi[k];
+        }
+        c_.kb = R(p.boundaryCollisionStiffness);
+        c_.fr_mu = R(p.boundaryFrictionDynamic);
+        c_.fr_epsU = R(p.boundaryFrictionEpsV * p.dt);
+        c_.step = R(p.stepSize);
+        c_.step_gd = R(p.stepSizeGD);
+        c_.plane = p.usePlaneGround ? 1 : 0;
+        c_.assoc_grav = p.associateGravityWithInertia ? 1 : 0;
+    }
+
+    void set_record(int32_t r, const int* nb, double mv[3][3]) {
+        make_record<R>(h_rec_n_[r], h_rec_a_[r], h_rec_b_[r], sizeof(R) == 8 ? &h_rec_c_[r] : nullptr, nb, mv);
+    }
+
+    void upload() {
+        bytes_ = 0;
+        d_pos_.upload(h_pos_, &bytes_, st_);
+        d_rest_.upload(h_rest_, &bytes_, st_);
+        d_vel_.upload(h_vel_, &bytes_, st_);
+        d_y_.upload(h_pos_, &bytes_, st_);
+        d_xprev_.upload(h_pos_, &bytes_, st_);
+        d_vprev_.upload(h_vel_, &bytes_, st_);
+        d_inc_ofs_.upload(inc_ofs_, &bytes_, st_);
+        d_rec_n_.upload(h_rec_n_, &bytes_, st_);
+        d_rec_a_.upload(h_rec_a_, &bytes_, st_);
+        d_rec_b_.upload(h_rec_b_, &bytes_, st_);
+        d_rec_c_.upload(h_rec_c_, &bytes_, st_);
+        d_slot_mesh_.upload(slot_mesh_, &bytes_, st_);
+        d_mats_.upload(h_mats_, &bytes_, st_);
+        d_slot_of_.upload(slot_of_, &bytes_, st_);
+        d_counters_.alloc(dev::CNT_N, &bytes_);
+        GAIA_CUDA(cudaMemsetAsync(d_counters_.p, 0, dev::CNT_N * sizeof(unsigned long long), st_));
+        d_time_.alloc(1, &bytes_);
+        GAIA_CUDA(cudaMemsetAsync(d_time_.p, 0, sizeof(double), st_));
+        d_def_slot_.upload(h_def_slot_, &bytes_, st_);
+        d_def_idx_.upload(h_def_idx_, &bytes_, st_);
+        d_def_a_.upload(h_def_a_, &bytes_, st_);
+        d_def_b_.upload(h_def_b_, &bytes_, st_);
+        d_defs_.upload(h_defs_, &bytes_, st_);
+        if (sc_.p.useAccelerator) {
+            d_acc_pp_.alloc(nslots_, &bytes_);
+            d_acc_prev_.alloc(nslots_, &bytes_);
+        }
+        d_stage_f32_.alloc(6 * size_t(nslots_), &bytes_);
+        d_stage_f64_.alloc(3 * size_t(nslots_), &bytes_);
+        d_probe_.alloc(12, &bytes_);
+        d_energy_.alloc(1, &bytes_);
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        // keep host copies small: records are device-only from here on
+        std::vector<int4>().swap(h_rec_n_);
+        std::vector<R4>().swap(h_rec_a_);
+        std::vector<R4>().swap(h_rec_b_);
+        std::vector<R>().swap(h_rec_c_);
+    }
+
+    dev::Ptrs<ST, R> ptrs() const {
+        dev::Ptrs<ST, R> P;
+        P.u = d_pos_.p;
+        P.rest = d_rest_.p;
+        P.y = d_y_.p;
+        P.xprev = d_xprev_.p;
+        P.vel = d_vel_.p;
+        P.vprev = d_vprev_.p;
+        P.inc_ofs = d_inc_ofs_.p;
+        P.rec_n = d_rec_n_.p;
+        P.rec_a = d_rec_a_.p;
+        P.rec_b = d_rec_b_.p;
+        P.rec_c = d_rec_c_.p;
+        P.slot_mesh = d_slot_mesh_.p;
+        P.mats = d_mats_.p;
+        P.counters = d_counters_.p;
+        P.nactive = nactive_;
+        P.nslots = int32_t(nslots_);
+        return P;
+    }
+
+    // ---- kernels ----------------------------------------------------------------
+    template <bool PROBE>
+    void launch_solve(int L, int B, int beg, int end, int friction, double* probe) {
+        if (end <= beg) return;
+        int grid = div_up(int64_t(end - beg) * L, B);
+        auto P = ptrs();
+        switch (L) {
+            case 2: dev::k_solve<2, ST, R, PROBE><<<grid, B, 0, st_>>>(P, c_, beg, end, friction, probe); break;
+            case 4: dev::k_solve<4, ST, R, PROBE><<<grid, B, 0, st_>>>(P, c_, beg, end, friction, probe); break;
+            case 8: dev::k_solve<8, ST, R, PROBE><<<grid, B, 0, st_>>>(P, c_, beg, end, friction, probe); break;
+            case 16: dev::k_solve<16, ST, R, PROBE><<<grid, B, 0, st_>>>(P, c_, beg, end, friction, probe); break;
+            default: dev::k_solve<32, ST, R, PROBE><<<grid, B, 0, st_>>>(P, c_, beg, end, friction, probe); break;
+        }
+        GAIA_CUDA(cudaGetLastError());
+    }
+
+    void enqueue_init() {
+        auto P = ptrs();
+        dev::k_initial_step<ST, R><<<div_up(nslots_, 256), 256, 0, st_>>>(P, c_);
+        GAIA_CUDA(cudaGetLastError());
+        if (!h_def_slot_.empty()) {
+            dev::DeformVerts D;
+            D.slot = d_def_slot_.p;
+            D.def = d_def_idx_.p;
+            D.a = d_def_a_.p;
+            D.b = d_def_b_.p;
+            D.defs = d_defs_.p;
+            D.n = int32_t(h_def_slot_.size());
+            dev::k_deformers<ST><<<div_up(D.n, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, D, d_time_.p, sc_.p.dt);
+            GAIA_CUDA(cudaGetLastError());
+        }
+        if (sc_.p.useAccelerator)
+            GAIA_CUDA(cudaMemcpyAsync(d_acc_pp_.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+    }
+
+    // One iteration's color sweep: VBDPhysics.cpp:879-953 (graph of per-color kernels).
+    void enqueue_iteration(int it, int L, int B, double* omega, bool accel) {
+        int friction = it >= sc_.p.frictionStartIter ? 1 : 0;
+        if (accel) {
+            // getAcceleratorOmega (VBDPhysics.cpp:3558-3574)
+            double rho = sc_.p.acceleratorRho;
+            int order = it + 1;
+            *omega = order == 1 ? 1.0 : (order == 2 ? 2.0 / (2.0 - rho * rho) : 4.0 / (4.0 - rho * rho * *omega));
+            GAIA_CUDA(cudaMemcpyAsync(d_acc_prev_.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+        }
+        for (size_t g = 0; g < group_beg_.size(); ++g)
+            launch_solve<false>(L, B, group_beg_[g], group_end_[g], friction, nullptr);
+        if (accel) {
+            dev::k_accel_apply<ST><<<div_up(nactive_, 256), 256, 0, st_>>>(d_pos_.p, d_acc_pp_.p, d_acc_prev_.p, nactive_, *omega);
+            GAIA_CUDA(cudaGetLastError());
+        }
+    }
+
+    void enqueue_velocity() {
+        dev::k_velocity<ST, R><<<div_up(nslots_, 256), 256, 0, st_>>>(ptrs(), c_, d_time_.p);
+        GAIA_CUDA(cudaGetLastError());
+    }
+
+    // ---- graphs -----------------------------------------------------------------
+    void destroy_graphs() {
+        for (auto* g : {&g_init_, &g_sweep_, &g_vel_})
+            if (*g) {
+                cudaGraphExecDestroy(*g);
+                *g = nullptr;
+            }
+    }
+
+    template <typename Fn>
+    cudaGraphExec_t capture_one(Fn&& fn) {
+        cudaGraph_t graph = nullptr;
+        GAIA_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+        try {
+            fn();
+        } catch (...) {
+            cudaStreamEndCapture(st_, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        GAIA_CUDA(cudaStreamEndCapture(st_, &graph));
+        cudaGraphExec_t exec = nullptr;
+        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        GAIA_CUDA(e);
+        return exec;
+    }
+
+    void capture() {
+        destroy_graphs();
+        g_init_ = capture_one([&] { enqueue_init(); });
+        g_sweep_ = capture_one([&] {
+            double omega = 1.0;
+            for (int it = 0; it < sc_.p.iterations; ++it) enqueue_iteration(it, lanes_, block_, &omega, sc_.p.useAccelerator);
+        });
+        g_vel_ = capture_one([&] { enqueue_velocity(); });
+        launches_per_substep_ = 1 + (h_def_slot_.empty() ? 0 : 1) + 1;
+        int64_t ng = 0;
+        for (size_t g = 0; g < group_beg_.size(); ++g) ng += group_end_[g] > group_beg_[g] ? 1 : 0;
+        launches_per_substep_ += int64_t(sc_.p.iterations) * (ng + (sc_.p.useAccelerator ? 1 : 0));
+    }
+
+    void run_steps(int n) override {
+        for (int k = 0; k < n; ++k)
+            for (int sub = 0; sub < sc_.p.numSubsteps; ++sub) {
+                GAIA_CUDA(cudaGraphLaunch(g_init_, st_));
+                GAIA_CUDA(cudaGraphLaunch(g_sweep_, st_));
+                GAIA_CUDA(cudaGraphLaunch(g_vel_, st_));
+            }
+    }
+
+    void run_steps_timed(int n, float* total_ms, float* sweep_ms) override {
+        // per-substep sweep events: [start, end] pairs recorded around the sweep graph
+        int nsub = n * sc_.p.numSubsteps;
+        std::vector<cudaEvent_t> ev(2 * size_t(nsub));
+        for (auto& e : ev) GAIA_CUDA(cudaEventCreate(&e));
+        GAIA_CUDA(cudaEventRecord(ev_a_, st_));
+        int q = 0;
+        for (int k = 0; k < n; ++k)
+            for (int sub = 0; sub < sc_.p.numSubsteps; ++sub, ++q) {
+                GAIA_CUDA(cudaGraphLaunch(g_init_, st_));
+                GAIA_CUDA(cudaEventRecord(ev[2 * q], st_));
+                GAIA_CUDA(cudaGraphLaunch(g_sweep_, st_));
+                GAIA_CUDA(cudaEventRecord(ev[2 * q + 1], st_));
+                GAIA_CUDA(cudaGraphLaunch(g_vel_, st_));
+            }
+        GAIA_CUDA(cudaEventRecord(ev_b_, st_));
+        GAIA_CUDA(cudaEventSynchronize(ev_b_));
+        float tot = 0.f, sw = 0.f;
+        GAIA_CUDA(cudaEventElapsedTime(&tot, ev_a_, ev_b_));
+        for (int i = 0; i < nsub; ++i) {
+            float t = 0.f;
+            GAIA_CUDA(cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]));
+            sw += t;
+        }
+        for (auto& e : ev) cudaEventDestroy(e);
+        if (total_ms) *total_ms = tot;
+        if (sweep_ms) *sweep_ms = sw;
+    }
+
+    // Autotuner: lanes per vertex x block size, timed over full color sweeps on
+    // the current state (positions restored afterwards).
+    void autotune_impl() {
+        if (nactive_ == 0) return;
+        DevBuf<S4> save;
+        save.alloc(nslots_, nullptr);
+        GAIA_CUDA(cudaMemcpyAsync(save.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+        const int Ls[] = {2, 4, 8, 16, 32};
+        const int Bs[] = {128, 256, 512};
+        float best = 1e30f;
+        int bestL = 4, bestB = 256;
+        double omega = 1.0;
+        for (int L : Ls) {
+            if (lanes_ && L != lanes_) continue;
+            for (int B : Bs) {
+                if (block_ && B != block_) continue;
+                for (size_t g = 0; g < group_beg_.size(); ++g)  // warm-up
+                    launch_solve<false>(L, B, group_beg_[g], group_end_[g], 1, nullptr);
+                GAIA_CUDA(cudaEventRecord(ev_a_, st_));
+                const int reps = 3;
+                for (int r = 0; r < reps; ++r) enqueue_iteration(1, L, B, &omega, false);
+                GAIA_CUDA(cudaEventRecord(ev_b_, st_));
+                GAIA_CUDA(cudaEventSynchronize(ev_b_));
+                float ms = 0.f;
+                GAIA_CUDA(cudaEventElapsedTime(&ms, ev_a_, ev_b_));
+                ms /= reps;
+                if (ms < best) {
+                    best = ms;
+                    bestL = L;
+                    bestB = B;
+                }
+                GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+            }
+        }
+        GAIA_CUDA(cudaMemsetAsync(d_counters_.p, 0, dev::CNT_N * sizeof(unsigned long long), st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        lanes_ = bestL;
+        block_ = bestB;
+        tuned_ms_ = best;
+    }
+
+    void reset() override {
+        GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, h_pos_.data(), nslots_ * sizeof(S4), cudaMemcpyHostToDevice, st_));
+        GAIA_CUDA(cudaMemcpyAsync(d_vel_.p, h_vel_.data(), nslots_ * sizeof(V4), cudaMemcpyHostToDevice, st_));
+        GAIA_CUDA(cudaMemcpyAsync(d_y_.p, h_pos_.data(), nslots_ * sizeof(S4), cudaMemcpyHostToDevice, st_));
+        GAIA_CUDA(cudaMemcpyAsync(d_xprev_.p, h_pos_.data(), nslots_ * sizeof(S4), cudaMemcpyHostToDevice, st_));
+        GAIA_CUDA(cudaMemsetAsync(d_time_.p, 0, sizeof(double), st_));
+        GAIA_CUDA(cudaMemsetAsync(d_counters_.p + dev::CNT_NONFINITE, 0, sizeof(unsigned long long), st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    void autotune() override {
+        int keepL = sc_.p.lanesPerVertex, keepB = sc_.p.blockSize;
+        lanes_ = keepL;
+        block_ = keepB;
+        autotune_impl();
+        if (lanes_ == 0) lanes_ = 4;
+        if (block_ == 0) block_ = 256;
+        capture();
+    }
+
+    // ---- state access -------------------------------------------------------------
+    void check_nonfinite() {
+        unsigned long long h[dev::CNT_N];
+        GAIA_CUDA(cudaMemcpyAsync(h, d_counters_.p, sizeof(h), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        if (h[dev::CNT_NONFINITE]) throw std::domain_error("a vertex solve produced a non-finite position");
+    }
+
+    void sync() override {
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        check_nonfinite();
+    }
+
+    void mesh_range(int mesh, int64_t& off, int64_t& n) {
+        if (mesh < 0 || mesh >= nmesh_) throw std::invalid_argument("mesh index out of range");
+        off = mesh_off_[mesh];
+        n = mesh_off_[mesh + 1] - off;
+    }
+
+    void get_positions(int mesh, double* out) override {
+        check_nonfinite();
+        int64_t off, n;
+        mesh_range(mesh, off, n);
+        if (n == 0) return;
+        dev::k_gather_positions<ST><<<div_up(n, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, nullptr, d_stage_f64_.p,
+                                                                     d_slot_of_.p + off, int32_t(n));
+        GAIA_CUDA(cudaGetLastError());
+        GAIA_CUDA(cudaMemcpyAsync(out, d_stage_f64_.p, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+    void get_velocities(int mesh, double* out) override {
+        int64_t off, n;
+        mesh_range(mesh, off, n);
+        if (n == 0) return;
+        dev::k_gather_velocities<V4><<<div_up(n, 256), 256, 0, st_>>>(d_vel_.p, nullptr, d_stage_f64_.p,
+                                                                      d_slot_of_.p + off, int32_t(n));
+        GAIA_CUDA(cudaGetLastError());
+        GAIA_CUDA(cudaMemcpyAsync(out, d_stage_f64_.p, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+    void set_positions(int mesh, const double* in) override {
+        int64_t off, n;
+        mesh_range(mesh, off, n);
+        if (n == 0) return;
+        GAIA_CUDA(cudaMemcpyAsync(d_stage_f64_.p, in, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st_));
+        dev::k_scatter_positions_f64<ST><<<div_up(n, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, d_stage_f64_.p,
+                                                                          d_slot_of_.p + off, int32_t(n));
+        GAIA_CUDA(cudaGetLastError());
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+    void set_velocities(int mesh, const double* in) override {
+        int64_t off, n;
+        mesh_range(mesh, off, n);
+        if (n == 0) return;
+        GAIA_CUDA(cudaMemcpyAsync(d_stage_f64_.p, in, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st_));
+        dev::k_scatter_velocities_f64<ST><<<div_up(n, 256), 256, 0, st_>>>(d_vel_.p, d_stage_f64_.p,
+                                                                           d_slot_of_.p + off, int32_t(n));
+        GAIA_CUDA(cudaGetLastError());
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    void set_state_f32(const float* x, const float* v) override {
+        float* dx = d_stage_f32_.p;
+        float* dv = d_stage_f32_.p + 3 * size_t(nslots_);
+        if (x) GAIA_CUDA(cudaMemcpyAsync(dx, x, 3 * nslots_ * sizeof(float), cudaMemcpyHostToDevice, st_));
+        if (v) GAIA_CUDA(cudaMemcpyAsync(dv, v, 3 * nslots_ * sizeof(float), cudaMemcpyHostToDevice, st_));
+        dev::k_scatter_state<ST><<<div_up(nslots_, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, d_vel_.p, x ? dx : nullptr,
+                                                                       v ? dv : nullptr, d_slot_of_.p,
+                                                                       int32_t(nslots_));
+        GAIA_CUDA(cudaGetLastError());
+    }
+
+    void get_positions_f32(float* x) override {
+        dev::k_gather_positions<ST><<<div_up(nslots_, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, d_stage_f32_.p,
+                                                                          nullptr, d_slot_of_.p, int32_t(nslots_));
+        GAIA_CUDA(cudaGetLastError());
+        GAIA_CUDA(cudaMemcpyAsync(x, d_stage_f32_.p, 3 * nslots_ * sizeof(float), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        check_nonfinite();
+    }
+    void get_velocities_f32(float* v) override {
+        dev::k_gather_velocities<V4><<<div_up(nslots_, 256), 256, 0, st_>>>(d_vel_.p, d_stage_f32_.p, nullptr,
+                                                                            d_slot_of_.p, int32_t(nslots_));
+        GAIA_CUDA(cudaGetLastError());
+        GAIA_CUDA(cudaMemcpyAsync(v, d_stage_f32_.p, 3 * nslots_ * sizeof(float), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    double energy() override {
+        if (!d_tet_slots_.p) {
+            // per-tet data for the energy reduction, built on first use
+            std::vector<int4> ts;
+            std::vector<double> dm, vol;
+            std::vector<int32_t> tm;
+            for (int m = 0; m < nmesh_; ++m) {
+                const TetMesh& M = sc_.meshes[m];
+                for (int t = 0; t < M.ntet; ++t) {
+                    const int32_t* tv = &M.tets[4 * size_t(t)];
+                    ts.push_back(make_int4(slot_of_[mesh_off_[m] + tv[0]], slot_of_[mesh_off_[m] + tv[1]],
+                                           slot_of_[mesh_off_[m] + tv[2]], slot_of_[mesh_off_[m] + tv[3]]));
+                    dm.insert(dm.end(), M.dminv.begin() + 9 * size_t(t), M.dminv.begin() + 9 * size_t(t) + 9);
+                    vol.push_back(M.vol[t]);
+                    tm.push_back(m);
+                }
+            }
+            d_tet_slots_.upload(ts, &bytes_, st_);
+            d_tet_dminv_.upload(dm, &bytes_, st_);
+            d_tet_vol_.upload(vol, &bytes_, st_);
+            d_tet_mesh_.upload(tm, &bytes_, st_);
+            std::vector<double2> ml;
+            for (int m = 0; m < nmesh_; ++m) ml.push_back(make_double2(sc_.objs[m].miu, sc_.objs[m].lmbd));
+            d_mu_lmbd_.upload(ml, &bytes_, st_);
+        }
+        GAIA_CUDA(cudaMemsetAsync(d_energy_.p, 0, sizeof(double), st_));
+        int32_t nt = int32_t(d_tet_slots_.n);
+        if (nt)
+            dev::k_energy_tets<ST><<<div_up(nt, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, d_tet_slots_.p,
+                                                                     d_tet_dminv_.p, d_tet_vol_.p, d_tet_mesh_.p,
+                                                                     d_mu_lmbd_.p, nt, d_energy_.p);
+        dev::k_energy_inertia<ST><<<div_up(nactive_, 256), 256, 0, st_>>>(d_pos_.p, d_y_.p, nactive_,
+                                                                         0.5 * sc_.p.dtSqrReciprocal, d_energy_.p);
+        GAIA_CUDA(cudaGetLastError());
+        double e = 0;
+        GAIA_CUDA(cudaMemcpyAsync(&e, d_energy_.p, sizeof(double), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        return e;
+    }
+
+    void vertex_force_hessian(int mesh, int v, int friction, double* f3, double* h9) override {
+        int64_t off, n;
+        mesh_range(mesh, off, n);
+        if (v < 0 || v >= n) throw std::invalid_argument("vertex index out of range");
+        int32_t s = slot_of_[off + v];
+        if (s >= nactive_) throw std::invalid_argument("vertex is fixed (not solved)");
+        launch_solve<true>(lanes_, block_, s, s + 1, friction, d_probe_.p);
+        double h[12];
+        GAIA_CUDA(cudaMemcpyAsync(h, d_probe_.p, sizeof(h), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        for (int i = 0; i < 3; ++i) f3[i] = h[i];
+        for (int i = 0; i < 9; ++i) h9[i] = h[3 + i];
+    }
+
+    void stats(gaia_vbd_stats* s) override {
+        unsigned long long h[dev::CNT_N];
+        GAIA_CUDA(cudaMemcpyAsync(h, d_counters_.p, sizeof(h), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        s->precision = sizeof(R) == 8 ? 64 : (sizeof(S4) == 32 ? 48 : 32);
+        s->lanes_per_vertex = lanes_;
+        s->block_size = block_;
+        s->num_groups = int32_t(group_beg_.size());
+        s->num_vertices = nslots_;
+        s->num_active_vertices = nactive_;
+        s->num_incidences = ninc_;
+        s->kernel_launches_per_step = launches_per_substep_ * sc_.p.numSubsteps;
+        s->fp64_fallback_solves = int64_t(h[dev::CNT_FP64_SOLVES]);
+        s->failed_solves = int64_t(h[dev::CNT_FAILED_SOLVES]);
+        s->device_bytes = int64_t(bytes_);
+        s->autotune_ms_per_iteration = tuned_ms_;
+    }
+
+private:
+    const Scene& sc_;
+    cudaStream_t st_ = nullptr;
+    cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr, ev_c_ = nullptr;
+    cudaGraphExec_t g_init_ = nullptr, g_sweep_ = nullptr, g_vel_ = nullptr;
+    int nmesh_ = 0;
+    int64_t nslots_ = 0;
+    int32_t nactive_ = 0, ninc_ = 0;
+    int lanes_ = 0, block_ = 0;
+    double tuned_ms_ = 0.0;
+    int64_t launches_per_substep_ = 0;
+    size_t bytes_ = 0;
+    dev::Consts<R> c_{};
+    std::vector<int64_t> mesh_off_;
+    std::vector<int32_t> slot_of_, orig_of_, slot_mesh_, inc_ofs_, group_beg_, group_end_;
+    std::vector<int4> h_rec_n_;
+    std::vector<R4> h_rec_a_, h_rec_b_;
+    std::vector<S4> h_pos_;
+    std::vector<V4> h_vel_;
+    std::vector<float4> h_rest_;
+    std::vector<R> h_rec_c_;
+    std::vector<dev::MeshMat<R>> h_mats_;
+    std::vector<dev::DeformerDev> h_defs_;
+    std::vector<int32_t> h_def_slot_, h_def_idx_;
+    std::vector<double> h_def_a_, h_def_b_;
+    DevBuf<S4> d_pos_, d_y_, d_xprev_, d_acc_pp_, d_acc_prev_;
+    DevBuf<V4> d_vel_, d_vprev_;
+    DevBuf<double2> d_mu_lmbd_;
+    DevBuf<int32_t> d_inc_ofs_, d_slot_mesh_, d_slot_of_, d_def_slot_, d_def_idx_, d_tet_mesh_;
+    DevBuf<int4> d_rec_n_, d_tet_slots_;
+    DevBuf<R4> d_rec_a_, d_rec_b_;
+    DevBuf<R> d_rec_c_;
+    DevBuf<dev::MeshMat<R>> d_mats_;
+    DevBuf<unsigned long long> d_counters_;
+    DevBuf<double> d_time_, d_def_a_, d_def_b_, d_stage_f64_, d_probe_, d_energy_, d_tet_dminv_, d_tet_vol_;
+    DevBuf<dev::DeformerDev> d_defs_;
+    DevBuf<float4> d_rest_;
+    DevBuf<float> d_stage_f32_;
+};
+
+template <>
+void make_record<float>(int4& n, dev::R4<float>& a, dev::R4<float>& b, float*, const int* nb, double mv[3][3]) {
+    float m2z = float(mv[2][2]);
+    int bits;
+    std::memcpy(&bits, &m2z, 4);
+    n = make_int4(nb[0], nb[1], nb[2], bits);
+    a = dev::R4<float>{float(mv[0][0]), float(mv[0][1]), float(mv[0][2]), float(mv[1][0])};
+    b = dev::R4<float>{float(mv[1][1]), float(mv[1][2]), float(mv[2][0]), float(mv[2][1])};
+}
+template <>
+void make_record<double>(int4& n, dev::R4<double>& a, dev::R4<double>& b, double* c, const int* nb, double mv[3][3]) {
+    n = make_int4(nb[0], nb[1], nb[2], 0);
+    a = dev::R4<double>{mv[0][0], mv[0][1], mv[0][2], mv[1][0]};
+    b = dev::R4<double>{mv[1][1], mv[1][2], mv[2][0], mv[2][1]};
+    *c = mv[2][2];
+}
+
+}  // namespace gaia
+
+// =============================================================================
+// C ABI
+// =============================================================================
+struct gaia_vbd {
+    gaia::Scene scene;
+    std::unique_ptr<gaia::EngineBase> eng;
+    std::string err;
+};
+
+namespace {
+
+template <typename Fn>
+int guarded(gaia_vbd* h, Fn&& fn) {
+    try {
+        fn();
+        if (h) h->err.clear();
+        return GAIA_VBD_OK;
+    } catch (const gaia::CudaError& e) {
+        (h ? h->err : gaia::g_last_error) = e.what();
+        return GAIA_VBD_E_CUDA;
+    } catch (const std::invalid_argument& e) {
+        (h ? h->err : gaia::g_last_error) = e.what();
+        return GAIA_VBD_E_INVALID_ARG;
+    } catch (const std::domain_error& e) {
+        (h ? h->err : gaia::g_last_error) = e.what();
+        return GAIA_VBD_E_NONFINITE;
+    } catch (const std::exception& e) {
+        (h ? h->err : gaia::g_last_error) = e.what();
+        std::string m = e.what();
+        if (m.find("coloring") != std::string::npos) return GAIA_VBD_E_COLORING;
+        if (m.find("degenerate") != std::string::npos || m.find("fixed point") != std::string::npos ||
+            m.find("out of range") != std::string::npos)
+            return GAIA_VBD_E_MESH;
+        if (m.find("not supported") != std::string::npos) return GAIA_VBD_E_UNSUPPORTED;
+        return GAIA_VBD_E_INPUT;
+    } catch (...) {
+        (h ? h->err : gaia::g_last_error) = "unknown error";
+        return GAIA_VBD_E_INPUT;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int gaia_vbd_load(const char* models_json, const char* params_json, const char* repo_root, gaia_vbd** out) {
+    if (!models_json || !params_json || !out) {
+        gaia::g_last_error = "null argument";
+        return GAIA_VBD_E_INVALID_ARG;
+    }
+    *out = nullptr;
+    std::unique_ptr<gaia_vbd> h(new gaia_vbd());
+    int rc = guarded(nullptr, [&] { gaia::load_scene(models_json, params_json, repo_root ? repo_root : "", h->scene); });
+    if (rc) return rc;
+    *out = h.release();
+    return GAIA_VBD_OK;
+}
+
+int gaia_vbd_initialize(gaia_vbd* h) {
+    if (!h) return GAIA_VBD_E_INVALID_ARG;
+    if (h->eng) return GAIA_VBD_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        h->err = gaia::g_last_error = "no CUDA device is visible";
+        return GAIA_VBD_E_NO_DEVICE;
+    }
+    return guarded(h, [&] {
+        const std::string& pr = h->scene.p.gpuPrecision;
+        if (pr == "fp64") h->eng.reset(new gaia::Engine<gaia::dev::StF64, double>(h->scene));
+        else if (pr == "fp32") h->eng.reset(new gaia::Engine<gaia::dev::StF32, float>(h->scene));
+        else h->eng.reset(new gaia::Engine<gaia::dev::StDF, float>(h->scene));
+    });
+}
+
+int gaia_vbd_create(const char* models_json, const char* params_json, const char* repo_root, gaia_vbd** out) {
+    gaia_vbd* h = nullptr;
+    int rc = gaia_vbd_load(models_json, params_json, repo_root, &h);
+    if (rc) return rc;
+    rc = gaia_vbd_initialize(h);
+    if (rc) {
+        gaia::g_last_error = h->err;
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GAIA_VBD_OK;
+}
+
+void gaia_vbd_destroy(gaia_vbd* h) { delete h; }
+
+const char* gaia_vbd_last_error(const gaia_vbd* h) { return h ? h->err.c_str() : gaia::g_last_error.c_str(); }
+const char* gaia_vbd_last_global_error(void) { return gaia::g_last_error.c_str(); }
+
+#define GAIA_NEED(h)                                                   \
+    do {                                                               \
+        if (!(h)) return GAIA_VBD_E_INVALID_ARG;                       \
+        if (!(h)->eng) {                                               \
+            (h)->err = "handle is not initialized (gaia_vbd_initialize)"; \
+            return GAIA_VBD_E_INVALID_ARG;                             \
+        }                                                              \
+    } while (0)
+
+int gaia_vbd_run_step(gaia_vbd* h, int32_t n_steps) {
+    GAIA_NEED(h);
+    if (n_steps < 0) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->run_steps(n_steps); });
+}
+
+int gaia_vbd_synchronize(gaia_vbd* h) {
+    GAIA_NEED(h);
+    return guarded(h, [&] { h->eng->sync(); });
+}
+
+int gaia_vbd_run_step_timed(gaia_vbd* h, int32_t n_steps, float* total_ms, float* sweep_ms) {
+    GAIA_NEED(h);
+    if (n_steps <= 0) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->run_steps_timed(n_steps, total_ms, sweep_ms); });
+}
+
+int gaia_vbd_reset(gaia_vbd* h) {
+    GAIA_NEED(h);
+    return guarded(h, [&] { h->eng->reset(); });
+}
+
+int gaia_vbd_autotune(gaia_vbd* h) {
+    GAIA_NEED(h);
+    return guarded(h, [&] { h->eng->autotune(); });
+}
+
+int gaia_vbd_num_meshes(const gaia_vbd* h) { return h ? int(h->scene.meshes.size()) : -1; }
+
+int64_t gaia_vbd_num_vertices(const gaia_vbd* h, int32_t mesh) {
+    if (!h || mesh < 0 || size_t(mesh) >= h->scene.meshes.size()) return -1;
+    return h->scene.meshes[mesh].nv;
+}
+
+int64_t gaia_vbd_num_tets(const gaia_vbd* h, int32_t mesh) {
+    if (!h || mesh < 0 || size_t(mesh) >= h->scene.meshes.size()) return -1;
+    return h->scene.meshes[mesh].ntet;
+}
+
+int gaia_vbd_get_positions(gaia_vbd* h, int32_t mesh, double* out) {
+    GAIA_NEED(h);
+    if (!out) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->get_positions(mesh, out); });
+}
+int gaia_vbd_set_positions(gaia_vbd* h, int32_t mesh, const double* in) {
+    GAIA_NEED(h);
+    if (!in) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->set_positions(mesh, in); });
+}
+int gaia_vbd_get_velocities(gaia_vbd* h, int32_t mesh, double* out) {
+    GAIA_NEED(h);
+    if (!out) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->get_velocities(mesh, out); });
+}
+int gaia_vbd_set_velocities(gaia_vbd* h, int32_t mesh, const double* in) {
+    GAIA_NEED(h);
+    if (!in) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->set_velocities(mesh, in); });
+}
+int gaia_vbd_set_state_f32(gaia_vbd* h, const float* x, const float* v) {
+    GAIA_NEED(h);
+    return guarded(h, [&] { h->eng->set_state_f32(x, v); });
+}
+int gaia_vbd_get_positions_f32(gaia_vbd* h, float* x) {
+    GAIA_NEED(h);
+    if (!x) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->get_positions_f32(x); });
+}
+int gaia_vbd_get_velocities_f32(gaia_vbd* h, float* v) {
+    GAIA_NEED(h);
+    if (!v) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->get_velocities_f32(v); });
+}
+
+int gaia_vbd_num_groups(const gaia_vbd* h) { return h ? int(h->scene.groups.size()) : -1; }
+
+int64_t gaia_vbd_group_size(const gaia_vbd* h, int32_t g) {
+    if (!h || g < 0 || size_t(g) >= h->scene.groups.size()) return -1;
+    return int64_t(h->scene.groups[g].size() / 2);
+}
+
+int gaia_vbd_get_group(const gaia_vbd* h, int32_t g, int32_t* out_pairs) {
+    if (!h || !out_pairs || g < 0 || size_t(g) >= h->scene.groups.size()) return GAIA_VBD_E_INVALID_ARG;
+    std::copy(h->scene.groups[g].begin(), h->scene.groups[g].end(), out_pairs);
+    return GAIA_VBD_OK;
+}
+
+int gaia_vbd_get_coloring(const gaia_vbd* h, int32_t mesh, int32_t* colors) {
+    if (!h || !colors || mesh < 0 || size_t(mesh) >= h->scene.meshes.size()) return GAIA_VBD_E_INVALID_ARG;
+    const auto& M = h->scene.meshes[mesh];
+    for (size_t c = 0; c < M.colors.size(); ++c)
+        for (int32_t v : M.colors[c]) colors[v] = int32_t(c);
+    return GAIA_VBD_OK;
+}
+
+int gaia_vbd_get_rest_shape(const gaia_vbd* h, int32_t mesh, double* dminv, double* vol, double* mass) {
+    if (!h || mesh < 0 || size_t(mesh) >= h->scene.meshes.size()) return GAIA_VBD_E_INVALID_ARG;
+    const auto& M = h->scene.meshes[mesh];
+    if (dminv) std::copy(M.dminv.begin(), M.dminv.end(), dminv);
+    if (vol) std::copy(M.vol.begin(), M.vol.end(), vol);
+    if (mass) std::copy(M.mass.begin(), M.mass.end(), mass);
+    return GAIA_VBD_OK;
+}
+
+int gaia_vbd_energy(gaia_vbd* h, double* out) {
+    GAIA_NEED(h);
+    if (!out) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { *out = h->eng->energy(); });
+}
+
+int gaia_vbd_vertex_force_hessian(gaia_vbd* h, int32_t mesh, int32_t vertex, int32_t apply_friction, double* f3,
+                                  double* h9) {
+    GAIA_NEED(h);
+    if (!f3 || !h9) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->vertex_force_hessian(mesh, vertex, apply_friction, f3, h9); });
+}
+
+int gaia_vbd_get_stats(gaia_vbd* h, gaia_vbd_stats* out) {
+    GAIA_NEED(h);
+    if (!out) return GAIA_VBD_E_INVALID_ARG;
+    std::memset(out, 0, sizeof(*out));
+    return guarded(h, [&] { h->eng->stats(out); });
+}
+
+int32_t gaia_vbd_color_mcs(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors) {
+    if (nv <= 0 || ntet < 0 || (!tets && ntet) || !colors) return -1;
+    int32_t n = -1;
+    if (guarded(nullptr, [&] { n = gaia::color_mcs(nv, ntet, tets, colors); })) return -1;
+    return n;
+}
+
+int32_t gaia_vbd_color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors) {
+    if (nv <= 0 || ntet < 0 || (!tets && ntet) || !colors) return -1;
+    int32_t n = -1;
+    if (guarded(nullptr, [&] { n = gaia::color_greedy(nv, ntet, tets, colors); })) return -1;
+    return n;
+}
+
+int gaia_vbd_write_coloring(const char* path, int32_t nv, const int32_t* colors) {
+    if (!path || nv <= 0 || !colors) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(nullptr, [&] {
+        for (int32_t i = 0; i < nv; ++i)
+            if (colors[i] < 0) throw std::invalid_argument("negative color");
+        gaia::write_coloring(path, gaia::colors_to_categories(nv, colors));
+    });
+}
+
+int gaia_vbd_write_t(const char* path, int32_t nv, const double* X, int32_t ntet, const int32_t* tets) {
+    if (!path || nv <= 0 || !X || ntet < 0 || (!tets && ntet)) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(nullptr, [&] { gaia::write_t(path, nv, X, ntet, tets); });
+}
+
+}  // extern "C"

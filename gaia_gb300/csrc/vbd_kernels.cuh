@@ -1,0 +1,674 @@
+// Device code of the GB300 VBD step.
+//
+// Precision modes (template parameters ST = state trait, R = compute type; see vbd_state.cuh):
+//   fp32  <StF32, float>  : everything FP32
+//   mixed <StDF,  float>  : displacements / inertia targets stored as double-float
+//                           pairs; every per-incidence force and Hessian term, their
+//                           accumulation and the 3x3 solve in FP32 (FP64 retry for
+//                           ill-conditioned blocks). No FP64 instruction runs per
+//                           incidence.
+//   fp64  <StF64, double> : everything FP64 (the plain FP64 baseline)
+//
+// The state is the displacement u = x - X from the FP32 rest positions X, and
+// the elastic terms are written in the displacement gradient G = F - I. Near
+// rest, the reference's P = mu F + lambda (J - a) cof F is a difference of
+// O(mu) terms (lambda (1 - a) = -mu), which costs FP32 three digits at strains
+// of 1e-3; in G the same stress is mu (G - Cg) + lambda dJ (I + Cg) with
+// Cg = cof(F) - I and dJ = det F - 1, built from small quantities only.
+//
+// Data layout in HBM (built once on the host, see vbd_engine.cu):
+//   * vertices are renumbered into "slots": the solvable vertices of merged
+//     color 0, then color 1, ..., then all fixed vertices. Per-slot arrays are
+//     therefore contiguous per color and every per-vertex access of a color
+//     sweep is coalesced.
+//   * u[s]     = displacement and mass (ST::U: 16 B FP32, 32 B double-float or FP64)
+//     rest[s]  = (X, Y, Z, unused)  float4, rest position
+//     y[s]     = inertia target, as a displacement (ST::U)
+//     xprev[s] = displacement at the start of the substep (ST::U)
+//     vel[s]   = velocity (ST::V: FP32, or FP64 in the fp64 mode)
+//   * incidence records, one per (solvable vertex, incident tet), stored in
+//     slot order (CSR offsets inc_ofs): the slots of the tet's three other
+//     vertices and their rows of dF/dx ("m vectors", from the FP64 DmInv):
+//       FP32: rec_n = int4{n0, n1, n2, bits(m2.z)}, rec_a = {m0.xyz, m1.x},
+//             rec_b = {m1.yz, m2.xy}                          -> 48 B
+//       FP64: rec_n = int4{n0, n1, n2, 0}, rec_a, rec_b (double4), rec_c = m2.z -> 88 B
+//     The own vertex's row is -(m0+m1+m2), and the rest volume is
+//     1 / (6 det[m0;m1;m2]) (the rows are stored in an order that makes the
+//     determinant equal det(DmInv)), so neither is stored.
+//
+// Per incidence the Neo-Hookean block is evaluated in closed form. With
+// G = sum_j (u_j - u_o) m_j^T (so F = I + G), J = det F, g = cof(F) m_o (= dJ/dx_o):
+//   force  -= A [ mu F m_o + lambda (J - a) g ]      (evaluated in G, see above)
+//   H      += A [ lambda g g^T ] + A mu |m_o|^2 I
+// which equals the reference's contraction of its 9x9 d2E/dF2 with the vertex
+// row of dF/dx (VBDPhysicsCompute.cu:2035-2232, VBD_NeoHookean.cpp:379-581):
+// det F is affine in x_o, so the (J - a) d2J/dF2 term contracts to zero.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vbd_state.cuh"
+
+namespace gaia {
+namespace dev {
+
+template <typename R>
+struct MeshMat {
+    R mu, lmbd, a, kh, kd, exp_damp, const_damp, pad;
+    int32_t init_type, pad2, pad3, pad4;
+};
+
+template <typename R>
+struct Consts {
+    R dt, inv_dt, dt2inv;
+    R kb, fr_mu, fr_epsU;
+    R step, step_gd;
+    double dt_d;
+    double g[3];
+    double lo[3], hi[3];
+    int32_t plane, assoc_grav;
+};
+
+// Counter slots in device memory.
+enum { CNT_FP64_SOLVES = 0, CNT_FAILED_SOLVES = 1, CNT_NONFINITE = 2, CNT_N = 4 };
+
+template <typename ST, typename R>
+struct Ptrs {
+    typename ST::U* u;
+    const float4* rest;
+    typename ST::U* y;
+    typename ST::U* xprev;
+    typename ST::V* vel;
+    typename ST::V* vprev;
+    const int32_t* inc_ofs;
+    const int4* rec_n;
+    const R4<R>* rec_a;
+    const R4<R>* rec_b;
+    const R* rec_c;            // FP64 only
+    const int32_t* slot_mesh;
+    const MeshMat<R>* mats;
+    unsigned long long* counters;
+    int32_t nactive, nslots;
+};
+
+struct DeformerDev {
+    int32_t type;              // 0 rotator, 1 translator
+    double axis[3], omega, end_time, speed[3];
+};
+
+struct DeformVerts {
+    const int32_t* slot;
+    const int32_t* def;        // deformer index
+    const double* a;           // root (rotator) or original position (translator), 3 per vertex
+    const double* b;           // root-relative point (rotator), 3 per vertex
+    const DeformerDev* defs;
+    int32_t n;
+};
+
+// ---------------------------------------------------------------------------
+// small math
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float f_bits(int v) { return __int_as_float(v); }
+
+// Symmetric 3x3 solve by LDL^T (the same algorithm as the oracle's
+// solve3x3_ldlt). H = {h00, h01, h02, h11, h12, h22}.
+template <typename R>
+__device__ __forceinline__ bool ldlt3(const R* H, const R* b, R* x, R rel_tol) {
+    R scale = fmax(fabs(H[0]), fmax(fabs(H[3]), fabs(H[5])));
+    if (!(scale > R(0))) return false;
+    R tol = rel_tol * scale;
+    R d0 = H[0];
+    if (!(d0 > tol)) return false;
+    R l10 = H[1] / d0, l20 = H[2] / d0;
+    R d1 = H[3] - l10 * H[1];
+    if (!(d1 > tol)) return false;
+    R l21 = (H[4] - l20 * H[1]) / d1;
+    R d2 = H[5] - l20 * H[2] - l21 * l21 * d1;
+    if (!(d2 > tol)) return false;
+    R z0 = b[0];
+    R z1 = b[1] - l10 * z0;
+    R z2 = b[2] - l20 * z0 - l21 * z1;
+    z0 /= d0;
+    z1 /= d1;
+    z2 /= d2;
+    x[2] = z2;
+    x[1] = z1 - l21 * x[2];
+    x[0] = z0 - l10 * x[1] - l20 * x[2];
+    return isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]);
+}
+
+// FP32 solve with FP64 retry for ill-conditioned blocks; FP64 solve directly.
+template <typename R>
+__device__ __forceinline__ bool solve3(const R* H, const R* b, R* x, unsigned long long* counters);
+template <>
+__device__ __forceinline__ bool solve3<float>(const float* H, const float* b, float* x, unsigned long long* counters) {
+    if (ldlt3<float>(H, b, x, 1e-5f)) return true;
+    double Hd[6], bd[3], xd[3];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) Hd[i] = H[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) bd[i] = b[i];
+    atomicAdd(&counters[CNT_FP64_SOLVES], 1ull);
+    if (!ldlt3<double>(Hd, bd, xd, 1e-12)) return false;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) x[i] = float(xd[i]);
+    return true;
+}
+template <>
+__device__ __forceinline__ bool solve3<double>(const double* H, const double* b, double* x, unsigned long long*) {
+    return ldlt3<double>(H, b, x, 1e-12);
+}
+
+template <typename R>
+__device__ __forceinline__ void load_record(const int4* rec_n, const R4<R>* rec_a, const R4<R>* rec_b, const R* rec_c,
+                                            int r, int& n0, int& n1, int& n2, R* m0, R* m1, R* m2);
+template <>
+__device__ __forceinline__ void load_record<float>(const int4* rec_n, const R4<float>* rec_a, const R4<float>* rec_b,
+                                                   const float*, int r, int& n0, int& n1, int& n2, float* m0,
+                                                   float* m1, float* m2) {
+    int4 n = __ldcs(rec_n + r);
+    float4 a = __ldcs(reinterpret_cast<const float4*>(rec_a) + r);
+    float4 b = __ldcs(reinterpret_cast<const float4*>(rec_b) + r);
+    n0 = n.x; n1 = n.y; n2 = n.z;
+    m0[0] = a.x; m0[1] = a.y; m0[2] = a.z;
+    m1[0] = a.w; m1[1] = b.x; m1[2] = b.y;
+    m2[0] = b.z; m2[1] = b.w; m2[2] = f_bits(n.w);
+}
+template <>
+__device__ __forceinline__ void load_record<double>(const int4* rec_n, const R4<double>* rec_a,
+                                                    const R4<double>* rec_b, const double* rec_c, int r, int& n0,
+                                                    int& n1, int& n2, double* m0, double* m1, double* m2) {
+    int4 n = __ldcs(rec_n + r);
+    const double2* pa = reinterpret_cast<const double2*>(rec_a + r);
+    const double2* pb = reinterpret_cast<const double2*>(rec_b + r);
+    double2 a0 = __ldcs(pa), a1 = __ldcs(pa + 1), b0 = __ldcs(pb), b1 = __ldcs(pb + 1);
+    n0 = n.x; n1 = n.y; n2 = n.z;
+    m0[0] = a0.x; m0[1] = a0.y; m0[2] = a1.x;
+    m1[0] = a1.y; m1[1] = b0.x; m1[2] = b0.y;
+    m2[0] = b1.x; m2[1] = b1.y; m2[2] = __ldcs(rec_c + r);
+}
+
+// Accumulator of one vertex: force (3), lambda-part of the Hessian (6, upper
+// triangle), and S = sum A mu |m_o|^2 (the isotropic part).
+template <typename R>
+struct Acc {
+    R f0, f1, f2, h00, h01, h02, h11, h12, h22, S;
+};
+
+// e0, e1, e2 = u_j - u_o (relative displacements) of the three other vertices.
+template <typename R>
+__device__ __forceinline__ void incidence(const R* e0, const R* e1, const R* e2, const R* m0, const R* m1,
+                                          const R* m2, R mu, R lmbd, Acc<R>& acc) {
+    R G[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) G[r][c] = e0[r] * m0[c] + e1[r] * m1[c] + e2[r] * m2[c];
+    // rest volume from the stored rows: A = 1 / (6 det[m0; m1; m2])
+    R detM = m0[0] * (m1[1] * m2[2] - m1[2] * m2[1]) - m0[1] * (m1[0] * m2[2] - m1[2] * m2[0]) +
+             m0[2] * (m1[0] * m2[1] - m1[1] * m2[0]);
+    R A = R(1) / (R(6) * detM);
+    R mo[3] = {-(m0[0] + m1[0] + m2[0]), -(m0[1] + m1[1] + m2[1]), -(m0[2] + m1[2] + m2[2])};
+    // Cg = cof(I + G) - I, entrywise
+    R C00 = G[1][1] + G[2][2] + (G[1][1] * G[2][2] - G[1][2] * G[2][1]);
+    R C11 = G[0][0] + G[2][2] + (G[0][0] * G[2][2] - G[0][2] * G[2][0]);
+    R C22 = G[0][0] + G[1][1] + (G[0][0] * G[1][1] - G[0][1] * G[1][0]);
+    R C01 = G[1][2] * G[2][0] - G[1][0] * (R(1) + G[2][2]);
+    R C02 = G[1][0] * G[2][1] - (R(1) + G[1][1]) * G[2][0];
+    R C10 = G[0][2] * G[2][1] - G[0][1] * (R(1) + G[2][2]);
+    R C12 = G[0][1] * G[2][0] - (R(1) + G[0][0]) * G[2][1];
+    R C20 = G[0][1] * G[1][2] - G[0][2] * (R(1) + G[1][1]);
+    R C21 = G[0][2] * G[1][0] - (R(1) + G[0][0]) * G[1][2];
+    // dJ = det(I + G) - 1 = G00 (1 + Cg00) + G01 C01 + G02 C02 + Cg00
+    R dJ = G[0][0] * (R(1) + C00) + G[0][1] * C01 + G[0][2] * C02 + C00;
+    // g = cof(F) m_o = m_o + Cg m_o
+    R cm0 = C00 * mo[0] + C01 * mo[1] + C02 * mo[2];
+    R cm1 = C10 * mo[0] + C11 * mo[1] + C12 * mo[2];
+    R cm2 = C20 * mo[0] + C21 * mo[1] + C22 * mo[2];
+    R g0 = mo[0] + cm0, g1 = mo[1] + cm1, g2 = mo[2] + cm2;
+    R Gm0 = G[0][0] * mo[0] + G[0][1] * mo[1] + G[0][2] * mo[2];
+    R Gm1 = G[1][0] * mo[0] + G[1][1] * mo[1] + G[1][2] * mo[2];
+    R Gm2 = G[2][0] * mo[0] + G[2][1] * mo[1] + G[2][2] * mo[2];
+    // P m_o = mu (G - Cg) m_o + lambda dJ g
+    R Am = A * mu;
+    R Ald = A * lmbd * dJ;
+    acc.f0 -= Am * (Gm0 - cm0) + Ald * g0;
+    acc.f1 -= Am * (Gm1 - cm1) + Ald * g1;
+    acc.f2 -= Am * (Gm2 - cm2) + Ald * g2;
+    R Al = A * lmbd;
+    R lg0 = Al * g0, lg1 = Al * g1, lg2 = Al * g2;
+    acc.h00 += lg0 * g0;
+    acc.h01 += lg0 * g1;
+    acc.h02 += lg0 * g2;
+    acc.h11 += lg1 * g1;
+    acc.h12 += lg1 * g2;
+    acc.h22 += lg2 * g2;
+    acc.S += Am * (mo[0] * mo[0] + mo[1] * mo[1] + mo[2] * mo[2]);
+}
+
+template <int L, typename R>
+__device__ __forceinline__ void reduce_group(Acc<R>& a) {
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1) {
+        a.f0 += __shfl_xor_sync(0xffffffffu, a.f0, off);
+        a.f1 += __shfl_xor_sync(0xffffffffu, a.f1, off);
+        a.f2 += __shfl_xor_sync(0xffffffffu, a.f2, off);
+        a.h00 += __shfl_xor_sync(0xffffffffu, a.h00, off);
+        a.h01 += __shfl_xor_sync(0xffffffffu, a.h01, off);
+        a.h02 += __shfl_xor_sync(0xffffffffu, a.h02, off);
+        a.h11 += __shfl_xor_sync(0xffffffffu, a.h11, off);
+        a.h12 += __shfl_xor_sync(0xffffffffu, a.h12, off);
+        a.h22 += __shfl_xor_sync(0xffffffffu, a.h22, off);
+        a.S += __shfl_xor_sync(0xffffffffu, a.S, off);
+    }
+}
+
+// IPC-style lagged friction (VBD_GeneralCompute.h:10-66; VBDPhysics.cpp:2563-2592)
+// for an axis-aligned contact normal along `d`: tangents e_{d+1}, e_{d+2}.
+template <typename R>
+__device__ __forceinline__ void axis_friction(int d, const R* dx, R mu, R lambda, R epsU, R* f, R* H) {
+    int t0 = (d + 1) % 3, t1 = (d + 2) % 3;
+    R u0 = dx[t0], u1 = dx[t1];
+    R un = sqrt(u0 * u0 + u1 * u1);
+    if (!(un > R(0))) return;
+    R f1 = un > epsU ? R(1) / un : (-un / epsU + R(2)) / epsU;
+    R s = mu * lambda * f1;
+    f[t0] -= s * u0;
+    f[t1] -= s * u1;
+    // H += s * (e_t0 e_t0^T + e_t1 e_t1^T): diagonal entries of the two tangents
+    H[t0 == 0 ? 0 : (t0 == 1 ? 3 : 5)] += s;
+    H[t1 == 0 ? 0 : (t1 == 1 ? 3 : 5)] += s;
+}
+
+// ---------------------------------------------------------------------------
+// Per-color block solve. One group of L lanes per vertex of the color range
+// [beg, end). PROBE = write force/Hessian of the single vertex `beg` to
+// probe_out instead of moving it.
+// ---------------------------------------------------------------------------
+template <int L, typename ST, typename R, bool PROBE>
+__global__ void __launch_bounds__(512) k_solve(Ptrs<ST, R> P, Consts<R> c, int beg, int end, int friction,
+                                               double* probe_out) {
+    using U = typename ST::U;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = tid & (L - 1);
+    const int v = beg + tid / L;
+    const bool valid = v < end;
+    Acc<R> acc = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    U uo{};
+    MeshMat<R> mat;
+    if (valid) {
+        uo = P.u[v];
+        mat = P.mats[P.slot_mesh[v]];
+        const int s = P.inc_ofs[v], e = P.inc_ofs[v + 1];
+        for (int r = s + lane; r < e; r += L) {
+            int n0, n1, n2;
+            R m0[3], m1[3], m2[3];
+            load_record<R>(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r, n0, n1, n2, m0, m1, m2);
+            const U q0 = ST::ldg(P.u, n0), q1 = ST::ldg(P.u, n1), q2 = ST::ldg(P.u, n2);
+            R e0[3], e1[3], e2[3];
+            ST::diff(q0, uo, e0);
+            ST::diff(q1, uo, e1);
+            ST::diff(q2, uo, e2);
+            incidence<R>(e0, e1, e2, m0, m1, m2, mat.mu, mat.lmbd, acc);
+        }
+    }
+    reduce_group<L, R>(acc);
+    if (!valid || lane != 0) return;
+
+    // ---- per-vertex tail (lane 0 of the group) --------------------------------
+    R f[3] = {acc.f0, acc.f1, acc.f2};
+    R H[6] = {acc.h00 + acc.S, acc.h01, acc.h02, acc.h11 + acc.S, acc.h12, acc.h22 + acc.S};
+    const U xp = P.xprev[v];
+    R dx[3];
+    ST::diff(uo, xp, dx);
+    if (mat.kh > R(0) || mat.kd > R(0)) {
+        // damping Hessian (k_h H_lambda + k_d S I) / dt (VBD_NeoHookean.cpp:562-574)
+        R D[6] = {mat.kh * acc.h00 + mat.kd * acc.S, mat.kh * acc.h01, mat.kh * acc.h02,
+                  mat.kh * acc.h11 + mat.kd * acc.S, mat.kh * acc.h12, mat.kh * acc.h22 + mat.kd * acc.S};
+#pragma unroll
+        for (int i = 0; i < 6; ++i) D[i] *= c.inv_dt;
+        f[0] -= D[0] * dx[0] + D[1] * dx[1] + D[2] * dx[2];
+        f[1] -= D[1] * dx[0] + D[3] * dx[1] + D[4] * dx[2];
+        f[2] -= D[2] * dx[0] + D[4] * dx[1] + D[5] * dx[2];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) H[i] += D[i];
+    }
+    // inertia (VBD_GeneralCompute.h:68-85)
+    {
+        const U yv = P.y[v];
+        R dy[3];
+        ST::diff(yv, uo, dy);
+        R w = R(ST::mass(uo)) * c.dt2inv;
+        f[0] += w * dy[0];
+        f[1] += w * dy[1];
+        f[2] += w * dy[2];
+        H[0] += w; H[3] += w; H[5] += w;
+    }
+    // plane ground / world box with friction on each violated axis (VBDPhysics.cpp:2858-2953)
+    if (c.plane) {
+        const float4 X = P.rest[v];
+        const float Xc[3] = {X.x, X.y, X.z};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            // below = lo - x, above = x - hi (x = X + u)
+            R below = ST::template sub_from<R>(c.lo[d], Xc[d], uo, d);
+            R depth;
+            if (below > R(0)) {
+                depth = below;
+                f[d] += depth * c.kb;
+            } else {
+                R above = -ST::template sub_from<R>(c.hi[d], Xc[d], uo, d);
+                if (!(above > R(0))) continue;
+                depth = above;
+                f[d] -= depth * c.kb;
+            }
+            H[d == 0 ? 0 : (d == 1 ? 3 : 5)] += c.kb;
+            if (friction) axis_friction<R>(d, dx, c.fr_mu, depth * c.kb, c.fr_epsU, f, H);
+        }
+    }
+    if (PROBE) {
+        probe_out[0] = f[0]; probe_out[1] = f[1]; probe_out[2] = f[2];
+        probe_out[3] = H[0]; probe_out[4] = H[1]; probe_out[5] = H[2];
+        probe_out[6] = H[1]; probe_out[7] = H[3]; probe_out[8] = H[4];
+        probe_out[9] = H[2]; probe_out[10] = H[4]; probe_out[11] = H[5];
+        return;
+    }
+    // CMP_EPSILON2 gate (Types/Types.h:20-21; VBDPhysics.cpp:2432)
+    if (!(f[0] * f[0] + f[1] * f[1] + f[2] * f[2] > R(1e-5f * 1e-5f))) return;
+    R d3[3];
+    R step = c.step;
+    if (!solve3<R>(H, f, d3, P.counters)) {
+        // VBDPhysics.cpp:2452-2458: gradient step along the force
+        atomicAdd(&P.counters[CNT_FAILED_SOLVES], 1ull);
+        step = c.step_gd;
+        d3[0] = f[0]; d3[1] = f[1]; d3[2] = f[2];
+    }
+    using Sc = typename ST::Sc;
+    const Sc s0 = Sc(step * d3[0]), s1 = Sc(step * d3[1]), s2 = Sc(step * d3[2]);
+    if (!(isfinite(s0) && isfinite(s1) && isfinite(s2))) {
+        atomicAdd(&P.counters[CNT_NONFINITE], 1ull);
+        return;
+    }
+    P.u[v] = ST::add(uo, s0, s1, s2);
+}
+
+// Initial step of a substep over all slots: VBD_BaseMaterial.h:201-259 and
+// VBD_BaseMaterial.cpp:7-31 (initialization types 0..4). Displacements: every
+// update is linear in x, so it reads as in positions.
+template <typename ST, typename R>
+__global__ void k_initial_step(Ptrs<ST, R> P, Consts<R> c) {
+    using U = typename ST::U;
+    using V = typename ST::V;
+    using Sc = typename ST::Sc;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.nslots) return;
+    const Sc dt = Sc(c.dt_d);
+    const U x = P.u[s];
+    V v = P.vel[s];
+    P.xprev[s] = x;
+    const bool fixed = s >= P.nactive;
+    const int init_type = P.mats[P.slot_mesh[s]].init_type;
+    if (init_type == 2 || init_type == 4) P.vprev[s] = v;
+    const V vp = v;
+    if (c.assoc_grav) {
+        v.x += dt * Sc(c.g[0]);
+        v.y += dt * Sc(c.g[1]);
+        v.z += dt * Sc(c.g[2]);
+    }
+    if (fixed) { v.x = 0; v.y = 0; v.z = 0; }
+    const U yv = ST::add(x, dt * v.x, dt * v.y, dt * v.z);
+    P.vel[s] = v;
+    P.y[s] = yv;
+    U xn;
+    switch (init_type) {
+        case 1: xn = x; break;
+        case 2: xn = ST::add(x, dt * vp.x, dt * vp.y, dt * vp.z); break;
+        case 3: xn = ST::add(x, Sc(0.5) * dt * v.x, Sc(0.5) * dt * v.y, Sc(0.5) * dt * v.z); break;
+        case 4: {
+            const Sc h = Sc(0.5) * dt * dt;
+            xn = ST::add(x, dt * vp.x + h * Sc(c.g[0]), dt * vp.y + h * Sc(c.g[1]), dt * vp.z + h * Sc(c.g[2]));
+            break;
+        }
+        default: xn = yv; break;
+    }
+    P.u[s] = xn;
+}
+
+// Deformers (VBD/VBDDeformer.h:45-172). Rotator: p = root + R(theta) rootP with
+// theta = omega * t; Translator: p = orig + speed * t. t = time after this substep's
+// advance, clamped to the end time. Per selected vertex, in FP64 (a few thousand
+// boundary vertices per substep).
+template <typename ST>
+__global__ void k_deformers(typename ST::U* u, const float4* rest, DeformVerts D, const double* time, double dt) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= D.n) return;
+    const DeformerDev d = D.defs[D.def[k]];
+    double t = time[0] + dt;
+    if (t >= d.end_time && d.end_time > 0) t = d.end_time;
+    int s = D.slot[k];
+    const float4 X = rest[s];
+    const double* a = D.a + 3 * size_t(k);
+    double p[3];
+    if (d.type == 0) {
+        const double* b = D.b + 3 * size_t(k);
+        double th = t * d.omega, co = cos(th), si = sin(th), C = 1 - co;
+        double ux = d.axis[0], uy = d.axis[1], uz = d.axis[2];
+        double Rm[9] = {co + ux * ux * C, ux * uy * C - uz * si, ux * uz * C + uy * si,
+                        uy * ux * C + uz * si, co + uy * uy * C, uy * uz * C - ux * si,
+                        uz * ux * C - uy * si, uz * uy * C + ux * si, co + uz * uz * C};
+        p[0] = a[0] + (Rm[0] * b[0] + Rm[1] * b[1] + Rm[2] * b[2]);
+        p[1] = a[1] + (Rm[3] * b[0] + Rm[4] * b[1] + Rm[5] * b[2]);
+        p[2] = a[2] + (Rm[6] * b[0] + Rm[7] * b[1] + Rm[8] * b[2]);
+    } else {
+        p[0] = d.speed[0] * t + a[0];
+        p[1] = d.speed[1] * t + a[1];
+        p[2] = d.speed[2] * t + a[2];
+    }
+    double du[3] = {p[0] - double(X.x), p[1] - double(X.y), p[2] - double(X.z)};
+    u[s] = ST::from_d(du, ST::mass(u[s]));
+}
+
+// Velocity update with the CPU path's damping (VBDPhysics.cpp:2486-2561);
+// fixed vertices get zero velocity. Thread 0 advances the substep clock.
+template <typename ST, typename R>
+__global__ void k_velocity(Ptrs<ST, R> P, Consts<R> c, double* time) {
+    using V = typename ST::V;
+    using Sc = typename ST::Sc;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) time[0] += c.dt_d;
+    if (s >= P.nslots) return;
+    V v{0, 0, 0, 0};
+    if (s < P.nactive) {
+        const Sc dt = Sc(c.dt_d);
+        Sc d[3];
+        ST::diff(P.u[s], P.xprev[s], d);
+        v.x = d[0] / dt;
+        v.y = d[1] / dt;
+        v.z = d[2] / dt;
+        const MeshMat<R> mat = P.mats[P.slot_mesh[s]];
+        Sc vm = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+        if (vm > Sc(1e-6f)) {
+            Sc vn = vm * Sc(mat.exp_damp) - Sc(mat.const_damp);
+            vn = vn > Sc(1e-6f) ? vn : Sc(0);
+            Sc sc = vn / vm;
+            v.x *= sc; v.y *= sc; v.z *= sc;
+        } else {
+            v.x *= Sc(0); v.y *= Sc(0); v.z *= Sc(0);
+        }
+    }
+    P.vel[s] = v;
+}
+
+// Chebyshev over-relaxation of the iterate (VBDPhysicsCompute.cu:910-944):
+// x = pp + omega (x - pp), then pp = the iterate before this iteration's sweep.
+template <typename ST>
+__global__ void k_accel_apply(typename ST::U* u, typename ST::U* prevprev, const typename ST::U* prev_iter,
+                              int32_t nactive, double omega) {
+    using Sc = typename ST::Sc;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nactive) return;
+    const typename ST::U x = u[s], pp = prevprev[s];
+    Sc d[3];
+    ST::diff(x, pp, d);
+    const Sc om = Sc(omega);
+    typename ST::U r = ST::add(pp, om * d[0], om * d[1], om * d[2]);
+    r.w = x.w;
+    u[s] = r;
+    prevprev[s] = prev_iter[s];
+}
+
+// ---------------------------------------------------------------------------
+// Host-order state <-> slots (positions = X + u).
+// ---------------------------------------------------------------------------
+template <typename ST>
+__global__ void k_scatter_state(typename ST::U* u, const float4* rest, typename ST::V* vel, const float* x,
+                                const float* v, const int32_t* slot_of, int32_t n) {
+    using Sc = typename ST::Sc;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int s = slot_of[i];
+    if (x) {
+        const float4 X = rest[s];
+        double du[3] = {double(x[3 * size_t(i)]) - double(X.x), double(x[3 * size_t(i) + 1]) - double(X.y),
+                        double(x[3 * size_t(i) + 2]) - double(X.z)};
+        u[s] = ST::from_d(du, ST::mass(u[s]));
+    }
+    if (v) {
+        typename ST::V w{Sc(v[3 * size_t(i)]), Sc(v[3 * size_t(i) + 1]), Sc(v[3 * size_t(i) + 2]), Sc(0)};
+        vel[s] = w;
+    }
+}
+
+template <typename ST>
+__global__ void k_gather_positions(const typename ST::U* u, const float4* rest, float* out32, double* out64,
+                                   const int32_t* slot_of, int32_t n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int s = slot_of[i];
+    double p[3];
+    ST::to_d(u[s], p);
+    const float4 X = rest[s];
+    p[0] += double(X.x);
+    p[1] += double(X.y);
+    p[2] += double(X.z);
+    if (out32) {
+        out32[3 * size_t(i)] = float(p[0]);
+        out32[3 * size_t(i) + 1] = float(p[1]);
+        out32[3 * size_t(i) + 2] = float(p[2]);
+    } else {
+        out64[3 * size_t(i)] = p[0];
+        out64[3 * size_t(i) + 1] = p[1];
+        out64[3 * size_t(i) + 2] = p[2];
+    }
+}
+
+template <typename V>
+__global__ void k_gather_velocities(const V* vel, float* out32, double* out64, const int32_t* slot_of, int32_t n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const V v = vel[slot_of[i]];
+    if (out32) {
+        out32[3 * size_t(i)] = float(v.x);
+        out32[3 * size_t(i) + 1] = float(v.y);
+        out32[3 * size_t(i) + 2] = float(v.z);
+    } else {
+        out64[3 * size_t(i)] = double(v.x);
+        out64[3 * size_t(i) + 1] = double(v.y);
+        out64[3 * size_t(i) + 2] = double(v.z);
+    }
+}
+
+template <typename ST>
+__global__ void k_scatter_positions_f64(typename ST::U* u, const float4* rest, const double* in,
+                                        const int32_t* slot_of, int32_t n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int s = slot_of[i];
+    const float4 X = rest[s];
+    double du[3] = {in[3 * size_t(i)] - double(X.x), in[3 * size_t(i) + 1] - double(X.y),
+                    in[3 * size_t(i) + 2] - double(X.z)};
+    u[s] = ST::from_d(du, ST::mass(u[s]));
+}
+
+template <typename ST>
+__global__ void k_scatter_velocities_f64(typename ST::V* vel, const double* in, const int32_t* slot_of, int32_t n) {
+    using Sc = typename ST::Sc;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    vel[slot_of[i]] = typename ST::V{Sc(in[3 * size_t(i)]), Sc(in[3 * size_t(i) + 1]), Sc(in[3 * size_t(i) + 2]), Sc(0)};
+}
+
+// ---------------------------------------------------------------------------
+// Energy: per-tet Neo-Hookean energy with the rest energy removed
+// (VBDPhysicsCompute.cu:1775-1810) and inertia energy 1/(2dt^2) m |x-y|^2
+// (VBD_BaseMaterial.h:223-241), evaluated and reduced in FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void block_add(double val, double* out) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) val += __shfl_xor_sync(0xffffffffu, val, off);
+    __shared__ double part[32];
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) part[w] = val;
+    __syncthreads();
+    if (w == 0) {
+        val = l < (blockDim.x >> 5) ? part[l] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) val += __shfl_xor_sync(0xffffffffu, val, off);
+        if (l == 0) atomicAdd(out, val);
+    }
+}
+
+// mu_lmbd: per mesh (mu, lambda) in FP64.
+template <typename ST>
+__global__ void k_energy_tets(const typename ST::U* u, const float4* rest, const int4* tet_slots,
+                              const double* tet_dminv, const double* tet_vol, const int32_t* tet_mesh,
+                              const double2* mu_lmbd, int32_t ntet, double* out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0;
+    if (t < ntet) {
+        int4 sv = tet_slots[t];
+        const int ids[4] = {sv.x, sv.y, sv.z, sv.w};
+        double p[4][3];
+        for (int k = 0; k < 4; ++k) {
+            ST::to_d(u[ids[k]], p[k]);
+            const float4 X = rest[ids[k]];
+            p[k][0] += double(X.x);
+            p[k][1] += double(X.y);
+            p[k][2] += double(X.z);
+        }
+        double Ds[9] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2],
+                        p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2],
+                        p[3][0] - p[0][0], p[3][1] - p[0][1], p[3][2] - p[0][2]};
+        const double* Di = tet_dminv + 9 * size_t(t);
+        double F[9];
+        for (int cc = 0; cc < 3; ++cc)
+            for (int r = 0; r < 3; ++r)
+                F[3 * cc + r] = Ds[r] * Di[3 * cc] + Ds[3 + r] * Di[3 * cc + 1] + Ds[6 + r] * Di[3 * cc + 2];
+        double det = F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
+                     F[6] * (F[1] * F[5] - F[4] * F[2]);
+        double n2 = 0;
+        for (int i = 0; i < 9; ++i) n2 += F[i] * F[i];
+        const double2 ml = mu_lmbd[tet_mesh[t]];
+        double mu = ml.x, lm = ml.y, a = 1.0 + mu / lm, A = tet_vol[t];
+        e = A * (mu * 0.5 * (n2 - 3.0) + lm * 0.5 * (det - a) * (det - a)) - 0.5 * A * lm * (1.0 - a) * (1.0 - a);
+    }
+    block_add(e, out);
+}
+
+template <typename ST>
+__global__ void k_energy_inertia(const typename ST::U* u, const typename ST::U* y, int32_t n, double half_dt2inv,
+                                 double* out) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0;
+    if (s < n) {
+        double p[3], q[3];
+        ST::to_d(u[s], p);
+        ST::to_d(y[s], q);
+        double dx = p[0] - q[0], dy = p[1] - q[1], dz = p[2] - q[2];
+        e = half_dt2inv * ST::mass(u[s]) * (dx * dx + dy * dy + dz * dz);
+    }
+    block_add(e, out);
+}
+
+}  // namespace dev
+}  // namespace gaia

@@ -1,0 +1,147 @@
+// Per-vertex state storage of the three precision modes.
+//
+//   StF32 : displacement as FP32                          (16 B per vertex, w = mass)
+//   StDF  : displacement as a double-float pair hi + lo,  (32 B per vertex, hi.w = mass)
+//           both FP32; |lo| <= ulp(hi) / 2. Differences and updates use FP32
+//           operations only (error-free two-sum), so the state carries ~48
+//           significant bits while no FP64 instruction runs per incidence:
+//           GB300 executes FP64 at a small fraction of its FP32 rate.
+//   StF64 : displacement as FP64                          (32 B per vertex, w = mass)
+//
+// Each trait provides load / read-only load / store, a - b rounded to the
+// compute type R, a + d for a delta d in the velocity type, conversions from
+// and to double, and (c - X - u) for the world-box tests.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gaia {
+namespace dev {
+
+template <typename R>
+struct alignas(4 * sizeof(R)) R4 {
+    R x, y, z, w;
+};
+
+struct alignas(32) DF4 {
+    float hx, hy, hz, w;   // high parts, mass
+    float lx, ly, lz, pad; // low parts
+};
+
+// error-free a + b = s + e (Knuth two-sum), in round-to-nearest FP32 without contraction
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (hi, lo) + d, renormalized
+__device__ __forceinline__ void df_add(float& hi, float& lo, float d) {
+    float s, e;
+    two_sum(hi, d, s, e);
+    e = __fadd_rn(e, lo);
+    two_sum(s, e, hi, lo);
+}
+
+struct StF32 {
+    using U = R4<float>;
+    using V = R4<float>;
+    using Sc = float;
+    __host__ __device__ static U from_d(const double* x, double w) {
+        return U{float(x[0]), float(x[1]), float(x[2]), float(w)};
+    }
+    __device__ static void to_d(const U& u, double* x) { x[0] = u.x; x[1] = u.y; x[2] = u.z; }
+    __device__ static double mass(const U& u) { return u.w; }
+    __device__ static U ldg(const U* p, int i) {
+        float4 v = __ldg(reinterpret_cast<const float4*>(p) + i);
+        return U{v.x, v.y, v.z, v.w};
+    }
+    template <typename R>
+    __device__ static void diff(const U& a, const U& b, R* o) {
+        o[0] = R(a.x - b.x); o[1] = R(a.y - b.y); o[2] = R(a.z - b.z);
+    }
+    __device__ static U add(U a, Sc d0, Sc d1, Sc d2) {
+        a.x += d0; a.y += d1; a.z += d2;
+        return a;
+    }
+    __device__ static float comp(const U& u, int d) { return d == 0 ? u.x : (d == 1 ? u.y : u.z); }
+    template <typename R>
+    __device__ static R sub_from(double c, float X, const U& u, int d) {
+        return R((float(c) - X) - comp(u, d));
+    }
+};
+
+struct StF64 {
+    using U = R4<double>;
+    using V = R4<double>;
+    using Sc = double;
+    __host__ __device__ static U from_d(const double* x, double w) { return U{x[0], x[1], x[2], w}; }
+    __device__ static void to_d(const U& u, double* x) { x[0] = u.x; x[1] = u.y; x[2] = u.z; }
+    __device__ static double mass(const U& u) { return u.w; }
+    __device__ static U ldg(const U* p, int i) {
+        const double2* q = reinterpret_cast<const double2*>(p + i);
+        double2 a = __ldg(q), b = __ldg(q + 1);
+        return U{a.x, a.y, b.x, b.y};
+    }
+    template <typename R>
+    __device__ static void diff(const U& a, const U& b, R* o) {
+        o[0] = R(a.x - b.x); o[1] = R(a.y - b.y); o[2] = R(a.z - b.z);
+    }
+    __device__ static U add(U a, Sc d0, Sc d1, Sc d2) {
+        a.x += d0; a.y += d1; a.z += d2;
+        return a;
+    }
+    __device__ static double comp(const U& u, int d) { return d == 0 ? u.x : (d == 1 ? u.y : u.z); }
+    template <typename R>
+    __device__ static R sub_from(double c, float X, const U& u, int d) {
+        return R((c - double(X)) - comp(u, d));
+    }
+};
+
+struct StDF {
+    using U = DF4;
+    using V = R4<float>;
+    using Sc = float;
+    __host__ __device__ static U from_d(const double* x, double w) {
+        U u;
+        u.hx = float(x[0]); u.lx = float(x[0] - double(u.hx));
+        u.hy = float(x[1]); u.ly = float(x[1] - double(u.hy));
+        u.hz = float(x[2]); u.lz = float(x[2] - double(u.hz));
+        u.w = float(w);
+        u.pad = 0.f;
+        return u;
+    }
+    __device__ static void to_d(const U& u, double* x) {
+        x[0] = double(u.hx) + double(u.lx);
+        x[1] = double(u.hy) + double(u.ly);
+        x[2] = double(u.hz) + double(u.lz);
+    }
+    __device__ static double mass(const U& u) { return u.w; }
+    __device__ static U ldg(const U* p, int i) {
+        const float4* q = reinterpret_cast<const float4*>(p + i);
+        float4 a = __ldg(q), b = __ldg(q + 1);
+        return U{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    }
+    // (a.hi - b.hi) + (a.lo - b.lo): relative error ~2^-23 of the result
+    template <typename R>
+    __device__ static void diff(const U& a, const U& b, R* o) {
+        o[0] = R(__fadd_rn(__fsub_rn(a.hx, b.hx), __fsub_rn(a.lx, b.lx)));
+        o[1] = R(__fadd_rn(__fsub_rn(a.hy, b.hy), __fsub_rn(a.ly, b.ly)));
+        o[2] = R(__fadd_rn(__fsub_rn(a.hz, b.hz), __fsub_rn(a.lz, b.lz)));
+    }
+    __device__ static U add(U a, Sc d0, Sc d1, Sc d2) {
+        df_add(a.hx, a.lx, d0);
+        df_add(a.hy, a.ly, d1);
+        df_add(a.hz, a.lz, d2);
+        return a;
+    }
+    template <typename R>
+    __device__ static R sub_from(double c, float X, const U& u, int d) {
+        float h = d == 0 ? u.hx : (d == 1 ? u.hy : u.hz);
+        float l = d == 0 ? u.lx : (d == 1 ? u.ly : u.lz);
+        return R(__fsub_rn(__fsub_rn(__fsub_rn(float(c), X), h), l));
+    }
+};
+
+}  // namespace dev
+}  // namespace gaia

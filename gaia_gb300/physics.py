@@ -1,0 +1,218 @@
+"""Python mirror of GAIA::VBDPhysics on the VBD-step path, over libgaia_vbd.so.
+
+Method names follow the reference (Simulator/Modules/VBD/VBDPhysics.h:36-254,
+Framework/BasePhysicsFramework.h:35-119): ``loadRunningparameters`` ->
+``initialize`` -> ``runStep`` / ``simulate``. All compute runs in the CUDA
+library; this class only marshals arguments and raises on error codes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from ._lib import GaiaError, Stats, lib
+
+
+def _check(rc: int, handle=None) -> None:
+    if rc != 0:
+        L = lib()
+        msg = (L.gaia_vbd_last_error(handle) if handle else L.gaia_vbd_last_global_error()) or b""
+        raise GaiaError(rc, msg.decode(errors="replace"))
+
+
+class VBDPhysics:
+    """One VBD scene on one GPU."""
+
+    def __init__(self):
+        self._h = None
+        self.models_json = None
+        self.params_json = None
+        self.out_folder = None
+        self.repo_root = None
+        self.frameId = 0
+
+    # -- VBDPhysics::loadRunningparameters (VBDPhysics.cpp:90-97): host only, no GPU needed
+    def loadRunningparameters(self, models_json: str, params_json: str, out_folder: str | None = None,
+                              repo_root: str | None = None) -> None:
+        self.close()
+        self.models_json = os.fspath(models_json)
+        self.params_json = os.fspath(params_json)
+        self.out_folder = out_folder
+        self.repo_root = repo_root
+        h = C.c_void_p()
+        rr = self.repo_root.encode() if self.repo_root else None
+        rc = lib().gaia_vbd_load(self.models_json.encode(), self.params_json.encode(), rr, C.byref(h))
+        _check(rc)
+        self._h = h
+
+    # -- VBDPhysics::initialize (VBDPhysics.cpp:208-454) + initializeGPU (:563-651)
+    def initialize(self) -> None:
+        if not self._h:
+            raise RuntimeError("call loadRunningparameters first")
+        _check(lib().gaia_vbd_initialize(self._h), self._h)
+
+    def close(self) -> None:
+        if self._h:
+            lib().gaia_vbd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        if not self._h:
+            raise RuntimeError("VBDPhysics is not initialized")
+        return self._h
+
+    # -- VBDPhysics::runStep (VBDPhysics.cpp:809-837)
+    def runStep(self, n: int = 1) -> None:
+        _check(lib().gaia_vbd_run_step(self.handle, n), self.handle)
+
+    # -- BasePhysicFramework::simulate (BasePhysicsFramework.cpp:284-393), without file output
+    def simulate(self, num_frames: int) -> None:
+        for _ in range(num_frames):
+            self.runStep(1)
+            self.frameId += 1
+        self.synchronize()
+
+    def synchronize(self) -> None:
+        _check(lib().gaia_vbd_synchronize(self.handle), self.handle)
+
+    def run_steps_timed(self, n: int) -> tuple[float, float]:
+        tot, sw = C.c_float(), C.c_float()
+        _check(lib().gaia_vbd_run_step_timed(self.handle, n, C.byref(tot), C.byref(sw)), self.handle)
+        return tot.value, sw.value
+
+    def reset(self) -> None:
+        """Back to the initial state (rest positions, initial velocities, t = 0)."""
+        _check(lib().gaia_vbd_reset(self.handle), self.handle)
+
+    def autotune(self) -> None:
+        _check(lib().gaia_vbd_autotune(self.handle), self.handle)
+
+    # -- state
+    def numMeshes(self) -> int:
+        return lib().gaia_vbd_num_meshes(self.handle)
+
+    def numVertices(self, mesh: int = 0) -> int:
+        return int(lib().gaia_vbd_num_vertices(self.handle, mesh))
+
+    def numTets(self, mesh: int = 0) -> int:
+        return int(lib().gaia_vbd_num_tets(self.handle, mesh))
+
+    def positions(self, mesh: int = 0) -> np.ndarray:
+        out = np.empty((self.numVertices(mesh), 3), np.float64)
+        _check(lib().gaia_vbd_get_positions(self.handle, mesh, out.ctypes.data), self.handle)
+        return out
+
+    def velocities(self, mesh: int = 0) -> np.ndarray:
+        out = np.empty((self.numVertices(mesh), 3), np.float64)
+        _check(lib().gaia_vbd_get_velocities(self.handle, mesh, out.ctypes.data), self.handle)
+        return out
+
+    def setPositions(self, mesh: int, x: np.ndarray) -> None:
+        x = np.ascontiguousarray(x, np.float64)
+        if x.size != 3 * self.numVertices(mesh):
+            raise ValueError("wrong size")
+        _check(lib().gaia_vbd_set_positions(self.handle, mesh, x.ctypes.data), self.handle)
+
+    def setVelocities(self, mesh: int, v: np.ndarray) -> None:
+        v = np.ascontiguousarray(v, np.float64)
+        if v.size != 3 * self.numVertices(mesh):
+            raise ValueError("wrong size")
+        _check(lib().gaia_vbd_set_velocities(self.handle, mesh, v.ctypes.data), self.handle)
+
+    def set_state_f32(self, x_ptr: int, v_ptr: int) -> None:
+        """Whole-scene FP32 state from host pointers (page-locked for full bandwidth)."""
+        _check(lib().gaia_vbd_set_state_f32(self.handle, x_ptr, v_ptr), self.handle)
+
+    def get_positions_f32(self, x_ptr: int) -> None:
+        _check(lib().gaia_vbd_get_positions_f32(self.handle, x_ptr), self.handle)
+
+    def get_velocities_f32(self, v_ptr: int) -> None:
+        _check(lib().gaia_vbd_get_velocities_f32(self.handle, v_ptr), self.handle)
+
+    # -- introspection
+    def parallelGroups(self) -> list[np.ndarray]:
+        L = lib()
+        out = []
+        for g in range(L.gaia_vbd_num_groups(self.handle)):
+            n = int(L.gaia_vbd_group_size(self.handle, g))
+            a = np.empty(2 * n, np.int32)
+            _check(L.gaia_vbd_get_group(self.handle, g, a.ctypes.data), self.handle)
+            out.append(a.reshape(-1, 2))
+        return out
+
+    def coloring(self, mesh: int = 0) -> np.ndarray:
+        out = np.empty(self.numVertices(mesh), np.int32)
+        _check(lib().gaia_vbd_get_coloring(self.handle, mesh, out.ctypes.data), self.handle)
+        return out
+
+    def restShape(self, mesh: int = 0):
+        nt, nv = self.numTets(mesh), self.numVertices(mesh)
+        dminv = np.empty((nt, 9), np.float64)
+        vol = np.empty(nt, np.float64)
+        mass = np.empty(nv, np.float64)
+        _check(lib().gaia_vbd_get_rest_shape(self.handle, mesh, dminv.ctypes.data, vol.ctypes.data,
+                                             mass.ctypes.data), self.handle)
+        return dminv, vol, mass
+
+    def energy(self) -> float:
+        e = C.c_double()
+        _check(lib().gaia_vbd_energy(self.handle, C.byref(e)), self.handle)
+        return e.value
+
+    def vertexForceHessian(self, mesh: int, v: int, apply_friction: bool = True):
+        f = np.empty(3, np.float64)
+        H = np.empty(9, np.float64)
+        _check(lib().gaia_vbd_vertex_force_hessian(self.handle, mesh, v, int(apply_friction), f.ctypes.data,
+                                                   H.ctypes.data), self.handle)
+        return f, H.reshape(3, 3)
+
+    def stats(self) -> dict:
+        s = Stats()
+        _check(lib().gaia_vbd_get_stats(self.handle, C.byref(s)), self.handle)
+        return s.as_dict()
+
+
+def color_greedy(nv: int, tets: np.ndarray) -> np.ndarray:
+    """GraphColoring tool, OrderedGreedy (gready.cpp:15-117), bit-exact."""
+    tets = np.ascontiguousarray(tets, np.int32)
+    out = np.empty(nv, np.int32)
+    n = lib().gaia_vbd_color_greedy(nv, len(tets), tets.ctypes.data, out.ctypes.data)
+    if n < 0:
+        raise GaiaError(2, (lib().gaia_vbd_last_global_error() or b"").decode())
+    return out
+
+
+def color_mcs(nv: int, tets: np.ndarray) -> np.ndarray:
+    """GraphColoring tool, MCS (mcs.cpp:14-168), bit-exact."""
+    tets = np.ascontiguousarray(tets, np.int32)
+    out = np.empty(nv, np.int32)
+    n = lib().gaia_vbd_color_mcs(nv, len(tets), tets.ctypes.data, out.ctypes.data)
+    if n < 0:
+        raise GaiaError(2, (lib().gaia_vbd_last_global_error() or b"").decode())
+    return out
+
+
+def write_coloring(path: str, colors: np.ndarray) -> None:
+    colors = np.ascontiguousarray(colors, np.int32)
+    _check(lib().gaia_vbd_write_coloring(os.fspath(path).encode(), len(colors), colors.ctypes.data))
+
+
+def write_t(path: str, X: np.ndarray, tets: np.ndarray) -> None:
+    X = np.ascontiguousarray(X, np.float64)
+    tets = np.ascontiguousarray(tets, np.int32)
+    _check(lib().gaia_vbd_write_t(os.fspath(path).encode(), len(X), X.ctypes.data, len(tets), tets.ctypes.data))

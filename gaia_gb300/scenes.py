@@ -1,0 +1,222 @@
+"""Synthetic scenes for the VBD step, written as the reference's inputs.
+
+Plays the role of the reference's ParameterGen scripts
+(Simulator/VBDDynamics/ParameterGen/M01_Parameters.py, S0*.py): builds tet
+meshes, colors them with the reference's OrderedGreedy algorithm (through the
+library's bit-exact implementation), and writes ``.t`` meshes, coloring JSON,
+``Models.json`` and ``Parameters.json`` that both this library and the
+reference's loader read. All randomness is seeded numpy PCG64; seeds are
+stored in the written JSON.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+
+
+def lame(E: float, nu: float) -> tuple[float, float]:
+    """Young's modulus / Poisson ratio -> (mu, lambda)."""
+    return E / (2.0 * (1.0 + nu)), E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+
+
+# Local corner (a, b, c) of a lattice cell -> index a + 2b + 4c.
+def _c(a, b, c):
+    return a + 2 * b + 4 * c
+
+
+# 5-tet split of a cube cell. Even cells use the central tet on corners
+# {100, 010, 001, 111}; odd cells are the mirror image in x, so that shared
+# faces use the same diagonal (a conforming mesh).
+_EVEN = [
+    (_c(1, 0, 0), _c(0, 1, 0), _c(0, 0, 1), _c(1, 1, 1)),
+    (_c(0, 0, 0), _c(1, 0, 0), _c(0, 1, 0), _c(0, 0, 1)),
+    (_c(1, 1, 0), _c(1, 0, 0), _c(0, 1, 0), _c(1, 1, 1)),
+    (_c(1, 0, 1), _c(1, 0, 0), _c(0, 0, 1), _c(1, 1, 1)),
+    (_c(0, 1, 1), _c(0, 1, 0), _c(0, 0, 1), _c(1, 1, 1)),
+]
+_ODD = [tuple(_c(1 - (k & 1), (k >> 1) & 1, (k >> 2) & 1) for k in t) for t in _EVEN]
+
+
+def lattice_cube(n: tuple[int, int, int], spacing: float = 0.01, origin=(0.0, 0.0, 0.0),
+                 jitter: float = 0.0, seed: int = 1) -> tuple[np.ndarray, np.ndarray]:
+    """A vertex lattice of n = (nx, ny, nz) vertices, each cell split into 5 tets.
+
+    Vertex (i, j, k) has index i + nx * (j + ny * k). Tets are positively
+    oriented (det(Dm) > 0). Positions are jittered by U(-jitter, +jitter) per
+    coordinate from numpy's PCG64 with `seed`.
+    """
+    nx, ny, nz = n
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    X = np.stack([i.transpose(2, 1, 0).ravel(), j.transpose(2, 1, 0).ravel(), k.transpose(2, 1, 0).ravel()], 1)
+    X = X.astype(np.float64) * spacing + np.asarray(origin, np.float64)
+    if jitter > 0:
+        rng = np.random.Generator(np.random.PCG64(seed))
+        X = X + rng.uniform(-jitter, jitter, size=X.shape)
+    ci, cj, ck = np.meshgrid(np.arange(nx - 1), np.arange(ny - 1), np.arange(nz - 1), indexing="ij")
+    ci, cj, ck = ci.transpose(2, 1, 0).ravel(), cj.transpose(2, 1, 0).ravel(), ck.transpose(2, 1, 0).ravel()
+    corner = np.stack([(ci + a) + nx * ((cj + b) + ny * (ck + c))
+                       for c in (0, 1) for b in (0, 1) for a in (0, 1)], 1)  # index a + 2b + 4c
+    parity = (ci + cj + ck) & 1
+    tets = np.empty((len(ci), 5, 4), np.int64)
+    for t in range(5):
+        even = corner[:, list(_EVEN[t])]
+        odd = corner[:, list(_ODD[t])]
+        tets[:, t, :] = np.where(parity[:, None] == 0, even, odd)
+    tets = tets.reshape(-1, 4)
+    # orient positively
+    d = X[tets[:, 1:]] - X[tets[:, :1]]
+    det = np.einsum("ij,ij->i", d[:, 0], np.cross(d[:, 1], d[:, 2]))
+    neg = det < 0
+    tets[neg, 2], tets[neg, 3] = tets[neg, 3].copy(), tets[neg, 2].copy()
+    return X, tets.astype(np.int32)
+
+
+def _write_mesh(dirname: str, name: str, X: np.ndarray, tets: np.ndarray, coloring: str = "greedy") -> tuple[str, str]:
+    from .physics import color_greedy, color_mcs, write_coloring, write_t
+    os.makedirs(dirname, exist_ok=True)
+    tpath = os.path.join(dirname, name + ".t")
+    cpath = tpath + ".vertexColoring.json"
+    write_t(tpath, X, tets)
+    colors = color_greedy(len(X), tets) if coloring == "greedy" else color_mcs(len(X), tets)
+    write_coloring(cpath, colors)
+    return tpath, cpath
+
+
+def model_entry(path: str, coloring_path: str, E: float = 1e6, nu: float = 0.4, density: float = 1000.0,
+                **extra) -> dict:
+    mu, lmbd = lame(E, nu)
+    m = {
+        "path": path,
+        "verticesColoringCategoriesPath": coloring_path,
+        "materialName": "NeoHookean",
+        "miu": mu,
+        "lmbd": lmbd,
+        "density": density,
+        "dampingHydrostatic": 0.0,
+        "dampingDeviatoric": 0.0,
+        "frictionDynamic": 0.1,
+        "frictionEpsV": 0.01,
+        "initializationType": 0,
+        "scale": [1.0, 1.0, 1.0],
+        "translation": [0.0, 0.0, 0.0],
+        "rotation": [0.0, 0.0, 0.0],
+        "initialVelocity": [0.0, 0.0, 0.0],
+        "fixedPoints": [],
+    }
+    m.update(extra)
+    return m
+
+
+def physics_params(timeStep: float, iterations: int, numSubsteps: int = 1, gravity=(0.0, -9.8, 0.0),
+                   ground_y: float | None = None, precision: str = "mixed", **extra) -> dict:
+    lo = [-1e7, -1e7, -1e7]
+    if ground_y is not None:
+        lo[1] = ground_y
+    p = {
+        "timeStep": timeStep,
+        "numSubsteps": numSubsteps,
+        "iterations": iterations,
+        "gravity": list(gravity),
+        "worldBounds": [lo, [1e7, 1e7, 1e7]],
+        "usePlaneGround": True,
+        "boundaryCollisionStiffness": 1e5,
+        "boundaryFrictionDynamic": 0.2,
+        "boundaryFrictionEpsV": 1.0,
+        "stepSize": 1.0,
+        "stepSizeGD": 1e-3,
+        "useGPU": True,
+        "handleCollision": False,
+        "gpuPrecision": precision,
+        "checkAndUpdateWorldBounds": False,
+        "saveOutputs": False,
+    }
+    p.update(extra)
+    return p
+
+
+def _write_json(dirname: str, models: list[dict], params: dict, deformers: list[dict] | None = None,
+                meta: dict | None = None) -> tuple[str, str]:
+    mp = os.path.join(dirname, "Models.json")
+    pp = os.path.join(dirname, "Parameters.json")
+    with open(mp, "w") as f:
+        json.dump({"Models": models}, f, indent=1)
+    P = {"PhysicsParams": params, "CollisionParams": {}, "ViewerParams": {"enableViewer": False}}
+    if deformers:
+        P["Deformers"] = deformers
+    if meta:
+        P["SceneInfo"] = meta
+    with open(pp, "w") as f:
+        json.dump(P, f, indent=1)
+    return mp, pp
+
+
+def drop_cube(dirname: str, n: int = 10, precision: str = "mixed", iterations: int = 20, seed: int = 1,
+              spacing: float = 0.01, height: float = 0.2) -> tuple[str, str]:
+    """Plain VBD drop: an n^3 vertex lattice cube (spacing 1 cm, jitter 1e-4, seed 1),
+    Neo-Hookean E=1e6, nu=0.4, rho=1000, bottom at `height` above a ground plane at
+    y=0 (stiffness 1e5, friction 0.2), dt=1/300, `iterations` per step."""
+    half = 0.5 * spacing * (n - 1)
+    X, T = lattice_cube((n, n, n), spacing, (-half, height, -half), jitter=1e-4, seed=seed)
+    tp, cp = _write_mesh(dirname, f"cube{n}", X, T)
+    models = [model_entry(tp, cp)]
+    params = physics_params(1.0 / 300.0, iterations, ground_y=0.0, precision=precision)
+    return _write_json(dirname, models, params, meta={"workload": f"drop_cube_{n}", "seed": seed})
+
+
+def twist_cube(dirname: str, n: int = 100, precision: str = "mixed", iterations: int = 50, seed: int = 1,
+               spacing: float = 0.01, omega: float = 2.0) -> tuple[str, str]:
+    """Twist test: an n^3 lattice cube with its long (x) axis on the world x axis;
+    both x-end faces are Dirichlet and the x-max face rotates at `omega` rad/s about
+    the x axis (Rotator deformer). Same material, dt=1/300, `iterations` per step."""
+    half = 0.5 * spacing * (n - 1)
+    X, T = lattice_cube((n, n, n), spacing, (0.0, -half, -half), jitter=1e-4, seed=seed)
+    tp, cp = _write_mesh(dirname, f"twist{n}", X, T)
+    idx = np.arange(n * n * n)
+    ii = idx % n
+    left = idx[ii == 0].tolist()
+    right = idx[ii == n - 1].tolist()
+    models = [model_entry(tp, cp, fixedPoints=left + right)]
+    params = physics_params(1.0 / 300.0, iterations, precision=precision)
+    deformers = [{"DeformerName": "Rotator", "center": [0.0, 0.0, 0.0], "axis": [1.0, 0.0, 0.0],
+                  "angularVelocity": omega, "selectedMeshes": [0], "selectedVertices": [right]}]
+    return _write_json(dirname, models, params, deformers, meta={"workload": f"twist_cube_{n}", "seed": seed})
+
+
+def batch_cubes(dirname: str, n_scenes: int = 512, side_range=(4, 24), precision: str = "mixed",
+                iterations: int = 20, seed: int = 7, spacing: float = 0.01) -> tuple[str, str]:
+    """Batching form: `n_scenes` independent lattice cubes, side drawn uniformly from
+    side_range (vertices per edge), E ~ U(1e5, 1e7), nu ~ U(0.3, 0.45), laid out on a
+    grid above one ground plane (no inter-object contact), dt=1/300."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sides = rng.integers(side_range[0], side_range[1] + 1, size=n_scenes)
+    Es = rng.uniform(1e5, 1e7, size=n_scenes)
+    nus = rng.uniform(0.3, 0.45, size=n_scenes)
+    files = {}
+    models = []
+    g = int(np.ceil(np.sqrt(n_scenes)))
+    pitch = spacing * side_range[1] + 0.1
+    for s in range(n_scenes):
+        n = int(sides[s])
+        if n not in files:
+            X, T = lattice_cube((n, n, n), spacing, (0.0, 0.0, 0.0), jitter=1e-4, seed=seed + n)
+            files[n] = _write_mesh(dirname, f"cube{n}", X, T)
+        tp, cp = files[n]
+        tx, tz = (s % g) * pitch, (s // g) * pitch
+        models.append(model_entry(tp, cp, E=float(Es[s]), nu=float(nus[s]), translation=[tx, 0.1, tz]))
+    params = physics_params(1.0 / 300.0, iterations, ground_y=0.0, precision=precision)
+    return _write_json(dirname, models, params,
+                       meta={"workload": f"batch_cubes_{n_scenes}", "seed": seed, "sides": sides.tolist()})
+
+
+def set_precision(params_json: str, precision: str, out_path: str | None = None, **overrides) -> str:
+    """Copy of a Parameters.json with gpuPrecision (and other PhysicsParams) replaced."""
+    with open(params_json) as f:
+        P = json.load(f)
+    P["PhysicsParams"]["gpuPrecision"] = precision
+    P["PhysicsParams"].update(overrides)
+    out = out_path or params_json.replace(".json", f".{precision}.json")
+    with open(out, "w") as f:
+        json.dump(P, f, indent=1)
+    return out

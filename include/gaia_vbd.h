@@ -1,0 +1,155 @@
+/*
+ * gaia_vbd.h — C ABI of the GB300-native VBD step (libgaia_vbd.so).
+ *
+ * This is the drop-in boundary for Gaia's Vertex Block Descent step. Each
+ * entry point names the reference interface it replaces (paths relative to the
+ * reference project's Simulator/ directory). The reference binds these
+ * through C++ class methods of GAIA::VBDPhysics; here they are plain C symbols
+ * with pointers and sizes, no exceptions cross the boundary, and every call
+ * returns a status code (GAIA_VBD_OK = 0).
+ *
+ * Threading: one handle owns one CUDA stream and all its device memory. Calls
+ * on one handle must not run concurrently; separate handles are independent.
+ * Memory: arrays are caller-owned host memory unless stated otherwise.
+ */
+#ifndef GAIA_VBD_H
+#define GAIA_VBD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GAIA_VBD_VERSION 1
+
+/* Status codes. */
+enum {
+    GAIA_VBD_OK = 0,
+    GAIA_VBD_E_INVALID_ARG = 1,  /* null pointer, index out of range, bad size */
+    GAIA_VBD_E_INPUT = 2,        /* unreadable or malformed JSON / mesh / coloring file */
+    GAIA_VBD_E_COLORING = 3,     /* coloring misses or repeats vertices, or is not an independent set */
+    GAIA_VBD_E_MESH = 4,         /* degenerate tet (zero rest volume), bad fixed point */
+    GAIA_VBD_E_CUDA = 5,         /* a CUDA runtime call failed (message in last_error) */
+    GAIA_VBD_E_NONFINITE = 6,    /* a solve produced NaN/Inf; positions are left as they were written */
+    GAIA_VBD_E_NO_DEVICE = 7,    /* no CUDA device is visible */
+    GAIA_VBD_E_UNSUPPORTED = 8   /* input asks for a feature outside the VBD tet step */
+};
+
+typedef struct gaia_vbd gaia_vbd;
+
+/* Run-time counters of one handle. */
+typedef struct {
+    int32_t precision;            /* 32 = FP32-mixed engine, 64 = plain FP64 engine */
+    int32_t lanes_per_vertex;     /* threads cooperating on one vertex solve */
+    int32_t block_size;           /* threads per block of the solve kernel */
+    int32_t num_groups;           /* merged colors ("parallel groups") */
+    int64_t num_vertices;         /* all meshes */
+    int64_t num_active_vertices;  /* vertices that are solved (not fixed) */
+    int64_t num_incidences;       /* (vertex, incident tet) pairs over active vertices */
+    int64_t kernel_launches_per_step;
+    int64_t fp64_fallback_solves; /* FP32 3x3 solves redone in FP64 (cumulative) */
+    int64_t failed_solves;        /* solves that fell back to the gradient step (cumulative) */
+    int64_t device_bytes;         /* device memory owned by the handle */
+    double autotune_ms_per_iteration; /* best measured sweep time per iteration (0 if not tuned) */
+} gaia_vbd_stats;
+
+/* ---- life cycle ------------------------------------------------------------
+ * gaia_vbd_create: VBDPhysics::loadRunningparameters (VBD/VBDPhysics.cpp:90-97)
+ * followed by VBDPhysics::initialize (VBD/VBDPhysics.cpp:208-454) and
+ * initializeGPU (:563-651). Reads Models.json and Parameters.json with the
+ * reference's keys and defaults, substitutes ${REPO_ROOT} in paths
+ * (Parser/InputHandler.h:128-185), loads the .t meshes and vertex colorings
+ * (computing the reference's OrderedGreedy coloring when a model gives no
+ * coloring file), precomputes the rest shape in FP64, merges colors into
+ * parallel groups and uploads everything. repo_root may be NULL.
+ * Extra PhysicsParams keys: "gpuPrecision" ("fp32" | "fp64"),
+ * "lanesPerVertex", "blockSize" (0 = autotune), "autotune" (bool).
+ */
+int gaia_vbd_create(const char* models_json, const char* params_json, const char* repo_root, gaia_vbd** out);
+/* The two halves of gaia_vbd_create. gaia_vbd_load is host-only (no GPU needed):
+ * VBDPhysics::loadRunningparameters plus the host part of initialize (meshes,
+ * colorings, rest shape, parallel groups); the introspection calls below work on a
+ * loaded handle. gaia_vbd_initialize builds the device layout and CUDA graphs
+ * (VBDPhysics::initializeGPU, VBD/VBDPhysics.cpp:563-651). */
+int gaia_vbd_load(const char* models_json, const char* params_json, const char* repo_root, gaia_vbd** out);
+int gaia_vbd_initialize(gaia_vbd* h);
+/* ~VBDPhysics. Safe on NULL. */
+void gaia_vbd_destroy(gaia_vbd* h);
+/* Message of the last failed call on this handle ("" if none). */
+const char* gaia_vbd_last_error(const gaia_vbd* h);
+/* Message of the last failed gaia_vbd_create or tool call on this thread. */
+const char* gaia_vbd_last_global_error(void);
+
+/* ---- stepping --------------------------------------------------------------
+ * gaia_vbd_run_step: VBDPhysics::runStep -> runStepGPU (VBD/VBDPhysics.cpp:809-969),
+ * n_steps times; each step runs numSubsteps substeps of: initial step +
+ * deformers, `iterations` color sweeps of the per-vertex block solve
+ * (VBDPhysicsCompute.cu:803-908 / VBDPhysics.cpp:2402-2483), velocity update.
+ * Asynchronous on the handle's stream; errors of device work surface on the
+ * next synchronizing call. */
+int gaia_vbd_run_step(gaia_vbd* h, int32_t n_steps);
+int gaia_vbd_synchronize(gaia_vbd* h);
+/* Runs n_steps and times them with CUDA events on the handle's stream:
+ * total_ms = all device work, sweep_ms = the color sweeps (solve kernels) only. */
+int gaia_vbd_run_step_timed(gaia_vbd* h, int32_t n_steps, float* total_ms, float* sweep_ms);
+/* Restore the state gaia_vbd_initialize produced: rest positions, initial velocities,
+ * substep clock at 0 (counters are kept). The reference recovers a saved state with
+ * BasePhysicFramework::recoverFromState (Framework/BasePhysicsFramework.cpp:264-282). */
+int gaia_vbd_reset(gaia_vbd* h);
+/* Re-run the autotuner (lanes per vertex x block size) on the current state;
+ * the state is restored afterwards. */
+int gaia_vbd_autotune(gaia_vbd* h);
+
+/* ---- state access (TetMeshFEM positions()/velocities(); VBDPhysics::syncAllToCPU / syncAllToGPU,
+ * VBD/VBDPhysics.h:266-299). Arrays are 3*num_vertices(mesh), x,y,z per vertex. Synchronous. */
+int gaia_vbd_num_meshes(const gaia_vbd* h);
+int64_t gaia_vbd_num_vertices(const gaia_vbd* h, int32_t mesh);
+int64_t gaia_vbd_num_tets(const gaia_vbd* h, int32_t mesh);
+int gaia_vbd_get_positions(gaia_vbd* h, int32_t mesh, double* out);
+int gaia_vbd_set_positions(gaia_vbd* h, int32_t mesh, const double* in);
+int gaia_vbd_get_velocities(gaia_vbd* h, int32_t mesh, double* out);
+int gaia_vbd_set_velocities(gaia_vbd* h, int32_t mesh, const double* in);
+/* Whole-scene FP32 state, meshes concatenated in Models.json order (3 floats per vertex).
+ * set_state copies host->device and scatters on the device; get_positions gathers on the
+ * device and copies device->host. Pass page-locked buffers for full copy bandwidth. */
+int gaia_vbd_set_state_f32(gaia_vbd* h, const float* x, const float* v);
+int gaia_vbd_get_positions_f32(gaia_vbd* h, float* x);
+int gaia_vbd_get_velocities_f32(gaia_vbd* h, float* v);
+
+/* ---- introspection ----------------------------------------------------------
+ * Parallel groups (VBDPhysics::vertexParallelGroups, VBD/VBDPhysics.cpp:235-274):
+ * group g holds size pairs (mesh, vertex), in the reference's order. */
+int gaia_vbd_num_groups(const gaia_vbd* h);
+int64_t gaia_vbd_group_size(const gaia_vbd* h, int32_t g);
+int gaia_vbd_get_group(const gaia_vbd* h, int32_t g, int32_t* out_pairs);
+/* Per-vertex color index (position in the size-sorted color list, TetMeshFEM.cpp:122-134). */
+int gaia_vbd_get_coloring(const gaia_vbd* h, int32_t mesh, int32_t* colors);
+/* FP64 rest shape: DmInv 9 per tet (column-major), rest volume per tet, lumped mass per vertex. */
+int gaia_vbd_get_rest_shape(const gaia_vbd* h, int32_t mesh, double* dminv, double* vol, double* mass);
+/* Total Neo-Hookean elastic energy (rest energy removed) plus inertia energy
+ * (VBDPhysicsCompute.cu:1223-1237, 1775-1810; VBD_BaseMaterial.h:223-241), evaluated on
+ * the device and reduced in FP64. */
+int gaia_vbd_energy(gaia_vbd* h, double* out);
+/* Per-vertex force and 3x3 Hessian (material + inertia + ground) at the current state,
+ * computed by the solve kernel without moving the vertex: f3 = 3 values, h9 = 9 (row-major). */
+int gaia_vbd_vertex_force_hessian(gaia_vbd* h, int32_t mesh, int32_t vertex, int32_t apply_friction,
+                                  double* f3, double* h9);
+int gaia_vbd_get_stats(gaia_vbd* h, gaia_vbd_stats* out);
+
+/* ---- tools -------------------------------------------------------------------
+ * GraphColoring tool (GraphColoring/GraphColoring.cpp:157-196) on a tet list:
+ * MCS (Modules/GraphColoring/mcs.cpp:14-168) and OrderedGreedy (gready.cpp:15-117),
+ * bit-exact with the reference. Return the number of colors, or -1 on error. */
+int32_t gaia_vbd_color_mcs(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
+int32_t gaia_vbd_color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
+/* Write a coloring as the reference's JSON list of lists (ColoringAlgorithms.cpp:200-211). */
+int gaia_vbd_write_coloring(const char* path, int32_t nv, const int32_t* colors);
+/* Write a .t mesh ("Vertex id x y z" / "Tet id a b c d"). */
+int gaia_vbd_write_t(const char* path, int32_t nv, const double* X, int32_t ntet, const int32_t* tets);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GAIA_VBD_H */

@@ -1,0 +1,275 @@
+"""ctypes front end of the CPU oracle — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and ``bench.py`` (its cpu_baseline and
+``--impl reference`` legs) may import this module. It restates the reference's
+CPU VBD path (Simulator/Modules/VBD/VBDPhysics.cpp:1580-1632, 2402-2483) and
+coloring tools (GraphColoring/mcs.cpp:14-168, gready.cpp:15-117); the product
+library never calls it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "liboracle.so")
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++, no GPU needed)."""
+    src = os.path.join(_HERE, "vbd_oracle.cpp")
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
+    return _LIB
+
+
+class OracleMesh(C.Structure):
+    _fields_ = [
+        ("nv", C.c_int32), ("ntet", C.c_int32),
+        ("X", C.POINTER(C.c_double)), ("V0", C.POINTER(C.c_double)),
+        ("tets", C.POINTER(C.c_int32)), ("fixed", C.POINTER(C.c_int8)),
+        ("ncolors", C.c_int32), ("color_offsets", C.POINTER(C.c_int32)),
+        ("color_verts", C.POINTER(C.c_int32)),
+        ("miu", C.c_double), ("lmbd", C.c_double), ("density", C.c_double),
+        ("damping_hydrostatic", C.c_double), ("damping_deviatoric", C.c_double),
+        ("exp_vel_damping", C.c_double), ("const_vel_damping", C.c_double),
+        ("friction_dynamic", C.c_double), ("friction_eps_v", C.c_double),
+        ("init_type", C.c_int32), ("active", C.c_int32),
+    ]
+
+
+class OracleParams(C.Structure):
+    _fields_ = [
+        ("time_step", C.c_double), ("num_substeps", C.c_int32), ("iterations", C.c_int32),
+        ("gravity", C.c_double * 3), ("world_lo", C.c_double * 3), ("world_hi", C.c_double * 3),
+        ("use_plane_ground", C.c_int32),
+        ("boundary_stiffness", C.c_double), ("boundary_friction_mu", C.c_double),
+        ("boundary_friction_eps_v", C.c_double),
+        ("step_size", C.c_double), ("step_size_gd", C.c_double),
+        ("friction_start_iter", C.c_int32), ("associate_gravity", C.c_int32),
+        ("use_accelerator", C.c_int32), ("accelerator_rho", C.c_double),
+    ]
+
+
+class OracleDeformer(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32), ("center", C.c_double * 3), ("axis", C.c_double * 3),
+        ("angular_velocity", C.c_double), ("end_time", C.c_double), ("speed", C.c_double * 3),
+        ("nsel", C.c_int32), ("sel_mesh", C.POINTER(C.c_int32)), ("sel_vert", C.POINTER(C.c_int32)),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        L = _lib
+        L.oracle_read_t.restype = C.c_int32
+        L.oracle_read_t.argtypes = [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p, C.c_void_p]
+        L.oracle_color_mcs.restype = C.c_int32
+        L.oracle_color_greedy.restype = C.c_int32
+        L.oracle_create.restype = C.c_void_p
+        L.oracle_create.argtypes = [C.c_int32, C.c_int32, C.POINTER(OracleMesh), C.POINTER(OracleParams),
+                                    C.c_int32, C.POINTER(OracleDeformer), C.c_int32]
+        for name in ("oracle_destroy",):
+            getattr(L, name).argtypes = [C.c_void_p]
+        L.oracle_step.argtypes = [C.c_void_p, C.c_int32]
+        L.oracle_substep_sample.argtypes = [C.c_void_p, C.c_int32]
+        for name in ("oracle_get_positions", "oracle_get_velocities", "oracle_set_positions",
+                     "oracle_set_velocities"):
+            getattr(L, name).argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+        L.oracle_get_rest.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_num_groups.argtypes = [C.c_void_p]
+        L.oracle_group_size.argtypes = [C.c_void_p, C.c_int32]
+        L.oracle_group.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+        L.oracle_vertex_force_hessian.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                                  C.c_void_p, C.c_void_p]
+        L.oracle_energy.argtypes = [C.c_void_p]
+        L.oracle_energy.restype = C.c_double
+        L.oracle_solve_failures.argtypes = [C.c_void_p]
+    return _lib
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def read_t(path: str) -> tuple[np.ndarray, np.ndarray]:
+    """.t mesh (vertex ids in file order) -> positions (nv, 3) float64, tets (ntet, 4) int32."""
+    L = lib()
+    nv, nt = C.c_int32(), C.c_int32()
+    if L.oracle_read_t(path.encode(), C.byref(nv), C.byref(nt), None, None) != 0:
+        raise FileNotFoundError(path)
+    X = np.empty((nv.value, 3), np.float64)
+    T = np.empty((nt.value, 4), np.int32)
+    L.oracle_read_t(path.encode(), C.byref(nv), C.byref(nt), X.ctypes.data, T.ctypes.data)
+    return X, T
+
+
+def color_mcs(nv: int, tets: np.ndarray) -> np.ndarray:
+    tets = np.ascontiguousarray(tets, dtype=np.int32)
+    out = np.empty(nv, dtype=np.int32)
+    n = lib().oracle_color_mcs(nv, len(tets), _ptr(tets, C.c_int32), _ptr(out, C.c_int32))
+    if n < 0:
+        raise RuntimeError("oracle MCS coloring failed")
+    return out
+
+
+def color_greedy(nv: int, tets: np.ndarray) -> np.ndarray:
+    tets = np.ascontiguousarray(tets, dtype=np.int32)
+    out = np.empty(nv, dtype=np.int32)
+    n = lib().oracle_color_greedy(nv, len(tets), _ptr(tets, C.c_int32), _ptr(out, C.c_int32))
+    if n < 0:
+        raise RuntimeError("oracle greedy coloring failed")
+    return out
+
+
+def colors_to_categories(colors: np.ndarray) -> list[list[int]]:
+    """GraphColoring/ColoringAlgorithms.cpp:69-80: category c lists its nodes in index order."""
+    n = int(colors.max()) + 1 if len(colors) else 0
+    cats: list[list[int]] = [[] for _ in range(n)]
+    for v, c in enumerate(colors.tolist()):
+        cats[c].append(v)
+    return cats
+
+
+class OracleScene:
+    """A scene in the oracle. `scene` is the dict produced by
+    ``gaia_gb300.scene_io.load_scene`` (meshes, params, deformers)."""
+
+    def __init__(self, scene: dict, precision: int = 64, nthreads: int = 0):
+        L = lib()
+        self._keep = []
+        meshes = (OracleMesh * len(scene["meshes"]))()
+        for i, m in enumerate(scene["meshes"]):
+            X = np.ascontiguousarray(m["X"], dtype=np.float64).reshape(-1)
+            V0 = np.ascontiguousarray(m["V0"], dtype=np.float64).reshape(-1)
+            tets = np.ascontiguousarray(m["tets"], dtype=np.int32).reshape(-1)
+            fixed = np.ascontiguousarray(m["fixed"], dtype=np.int8)
+            cats = m["colors"]
+            offs = np.zeros(len(cats) + 1, dtype=np.int32)
+            offs[1:] = np.cumsum([len(c) for c in cats])
+            cverts = np.ascontiguousarray(np.concatenate([np.asarray(c, np.int32) for c in cats])
+                                          if cats else np.zeros(0, np.int32), dtype=np.int32)
+            self._keep += [X, V0, tets, fixed, offs, cverts]
+            mm = meshes[i]
+            mm.nv, mm.ntet = len(X) // 3, len(tets) // 4
+            mm.X, mm.V0 = _ptr(X, C.c_double), _ptr(V0, C.c_double)
+            mm.tets, mm.fixed = _ptr(tets, C.c_int32), _ptr(fixed, C.c_int8)
+            mm.ncolors = len(cats)
+            mm.color_offsets, mm.color_verts = _ptr(offs, C.c_int32), _ptr(cverts, C.c_int32)
+            mat = m["material"]
+            mm.miu, mm.lmbd, mm.density = mat["miu"], mat["lmbd"], mat["density"]
+            mm.damping_hydrostatic = mat["dampingHydrostatic"]
+            mm.damping_deviatoric = mat["dampingDeviatoric"]
+            mm.exp_vel_damping = mat["exponentialVelDamping"]
+            mm.const_vel_damping = mat["constantVelDamping"]
+            mm.friction_dynamic = mat["frictionDynamic"]
+            mm.friction_eps_v = mat["frictionEpsV"]
+            mm.init_type = mat["initializationType"]
+            mm.active = 1
+        p = scene["params"]
+        op = OracleParams()
+        op.time_step, op.num_substeps, op.iterations = p["timeStep"], p["numSubsteps"], p["iterations"]
+        for k in range(3):
+            op.gravity[k] = p["gravity"][k]
+            op.world_lo[k] = p["worldBounds"][0][k]
+            op.world_hi[k] = p["worldBounds"][1][k]
+        op.use_plane_ground = int(p["usePlaneGround"])
+        op.boundary_stiffness = p["boundaryCollisionStiffness"]
+        op.boundary_friction_mu = p["boundaryFrictionDynamic"]
+        op.boundary_friction_eps_v = p["boundaryFrictionEpsV"]
+        op.step_size, op.step_size_gd = p["stepSize"], p["stepSizeGD"]
+        op.friction_start_iter = p["frictionStartIter"]
+        op.associate_gravity = int(p["associateGravityWithInertia"])
+        op.use_accelerator = int(p["useAccelerator"])
+        op.accelerator_rho = p["acceleratorRho"]
+        defs = (OracleDeformer * max(1, len(scene["deformers"])))()
+        for i, d in enumerate(scene["deformers"]):
+            dd = defs[i]
+            dd.type = 0 if d["DeformerName"] == "Rotator" else 1
+            for k in range(3):
+                dd.center[k] = d.get("center", [0, 0, 0])[k]
+                dd.axis[k] = d.get("axis", [1, 0, 0])[k]
+                dd.speed[k] = d.get("speed", [0, 0, 0])[k]
+            dd.angular_velocity = d.get("angularVelocity", 0.0)
+            dd.end_time = d.get("rotationEndTime", d.get("deformationEndTime", -1.0))
+            sm, sv = [], []
+            for mi, verts in zip(d["selectedMeshes"], d["selectedVertices"]):
+                sm += [mi] * len(verts)
+                sv += list(verts)
+            sm = np.asarray(sm, np.int32)
+            sv = np.asarray(sv, np.int32)
+            self._keep += [sm, sv]
+            dd.nsel = len(sm)
+            dd.sel_mesh, dd.sel_vert = _ptr(sm, C.c_int32), _ptr(sv, C.c_int32)
+        self._nv = [len(np.asarray(m["X"]).reshape(-1)) // 3 for m in scene["meshes"]]
+        self._ntet = [len(np.asarray(m["tets"]).reshape(-1)) // 4 for m in scene["meshes"]]
+        self.h = L.oracle_create(precision, len(scene["meshes"]), meshes, C.byref(op),
+                                 len(scene["deformers"]), defs, nthreads)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib().oracle_destroy(h)
+            self.h = None
+
+    def step(self, n: int = 1) -> None:
+        lib().oracle_step(self.h, n)
+
+    def substep_sample(self, iterations: int) -> None:
+        lib().oracle_substep_sample(self.h, iterations)
+
+    def positions(self, mesh: int = 0) -> np.ndarray:
+        out = np.empty((self._nv[mesh], 3), np.float64)
+        lib().oracle_get_positions(self.h, mesh, out.ctypes.data)
+        return out
+
+    def velocities(self, mesh: int = 0) -> np.ndarray:
+        out = np.empty((self._nv[mesh], 3), np.float64)
+        lib().oracle_get_velocities(self.h, mesh, out.ctypes.data)
+        return out
+
+    def set_positions(self, mesh: int, x: np.ndarray) -> None:
+        x = np.ascontiguousarray(x, np.float64)
+        lib().oracle_set_positions(self.h, mesh, x.ctypes.data)
+
+    def set_velocities(self, mesh: int, v: np.ndarray) -> None:
+        v = np.ascontiguousarray(v, np.float64)
+        lib().oracle_set_velocities(self.h, mesh, v.ctypes.data)
+
+    def rest(self, mesh: int = 0):
+        nt, nv = self._ntet[mesh], self._nv[mesh]
+        dminv = np.empty((nt, 9), np.float64)
+        vol = np.empty(nt, np.float64)
+        mass = np.empty(nv, np.float64)
+        lib().oracle_get_rest(self.h, mesh, dminv.ctypes.data, vol.ctypes.data, mass.ctypes.data)
+        return dminv, vol, mass
+
+    def groups(self) -> list[np.ndarray]:
+        L = lib()
+        out = []
+        for g in range(L.oracle_num_groups(self.h)):
+            n = L.oracle_group_size(self.h, g)
+            a = np.empty(2 * n, np.int32)
+            L.oracle_group(self.h, g, a.ctypes.data)
+            out.append(a.reshape(-1, 2))
+        return out
+
+    def vertex_force_hessian(self, mesh: int, v: int, apply_friction: bool = True):
+        f = np.empty(3, np.float64)
+        H = np.empty(9, np.float64)
+        lib().oracle_vertex_force_hessian(self.h, mesh, v, int(apply_friction), f.ctypes.data, H.ctypes.data)
+        return f, H.reshape(3, 3)
+
+    def energy(self) -> float:
+        return float(lib().oracle_energy(self.h))
+
+    def solve_failures(self) -> int:
+        return int(lib().oracle_solve_failures(self.h))

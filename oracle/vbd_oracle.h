@@ -1,0 +1,101 @@
+/*
+ * CPU oracle for the VBD step — TEST INFRASTRUCTURE ONLY.
+ *
+ * This library restates, on the CPU and in plain C++, the reference's own
+ * algorithm for Gaia's Vertex Block Descent step so that the CUDA path can be
+ * checked against it. Only tests/, __graft_entry__.smoke() and bench.py's
+ * cpu_baseline / --impl reference legs may load it. The product library
+ * (libgaia_vbd.so) never links, loads or calls anything here.
+ *
+ * Parity anchors:
+ *   - vertex coloring (MCS, OrderedGreedy): pinned bit-exactly against the
+ *     reference's 18 shipped *.t.vertexColoring.json fixtures;
+ *   - the VBD step: restated from the reference's CPU path
+ *     (Simulator/Modules/VBD/VBDPhysics.cpp:1580-1632, 2402-2483;
+ *      VBD_NeoHookean.cpp:379-581). The reference cannot be built here
+ *     (its CuMatrix / MeshFrame2 submodules are empty), so per-step
+ *     trajectories are "parity unpinned" beyond this restatement.
+ */
+#ifndef GAIA_VBD_ORACLE_H
+#define GAIA_VBD_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int32_t nv, ntet;
+    const double* X;            /* 3*nv initial positions (x,y,z per vertex) */
+    const double* V0;           /* 3*nv initial velocities, or NULL = zero */
+    const int32_t* tets;        /* 4*ntet vertex ids */
+    const int8_t* fixed;        /* nv fixed flags, or NULL */
+    int32_t ncolors;            /* vertex color categories as read from JSON (unsorted) */
+    const int32_t* color_offsets; /* ncolors+1 */
+    const int32_t* color_verts;
+    double miu, lmbd, density;
+    double damping_hydrostatic, damping_deviatoric;
+    double exp_vel_damping, const_vel_damping;   /* raw JSON values */
+    double friction_dynamic, friction_eps_v;
+    int32_t init_type;
+    int32_t active;             /* activeForMaterialSolve */
+} OracleMesh;
+
+typedef struct {
+    double time_step;
+    int32_t num_substeps, iterations;
+    double gravity[3];
+    double world_lo[3], world_hi[3];
+    int32_t use_plane_ground;
+    double boundary_stiffness, boundary_friction_mu, boundary_friction_eps_v;
+    double step_size, step_size_gd;
+    int32_t friction_start_iter;
+    int32_t associate_gravity;
+    int32_t use_accelerator;
+    double accelerator_rho;
+} OracleParams;
+
+typedef struct {
+    int32_t type;               /* 0 = Rotator, 1 = Translator */
+    double center[3], axis[3];
+    double angular_velocity, end_time;
+    double speed[3];
+    int32_t nsel;               /* number of (mesh, vertex) pairs */
+    const int32_t* sel_mesh;
+    const int32_t* sel_vert;
+} OracleDeformer;
+
+/* .t reader: call with X == NULL to get the counts. Returns 0, or -1 if unreadable. */
+int32_t oracle_read_t(const char* path, int32_t* nv, int32_t* ntet, double* X, int32_t* tets);
+
+/* Graph coloring restatements (return number of colors, -1 on error). */
+int32_t oracle_color_mcs(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
+int32_t oracle_color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
+
+/* Simulation. precision = 64 (double) or 32 (float). nthreads <= 0: all cores. */
+void* oracle_create(int32_t precision, int32_t nmesh, const OracleMesh* meshes,
+                    const OracleParams* params, int32_t ndef, const OracleDeformer* defs,
+                    int32_t nthreads);
+void oracle_destroy(void* h);
+int32_t oracle_step(void* h, int32_t nsteps);
+/* Run only `iterations` solver iterations of one substep (a bounded timing sample). */
+int32_t oracle_substep_sample(void* h, int32_t iterations);
+void oracle_get_positions(void* h, int32_t mesh, double* out);
+void oracle_get_velocities(void* h, int32_t mesh, double* out);
+void oracle_set_positions(void* h, int32_t mesh, const double* in);
+void oracle_set_velocities(void* h, int32_t mesh, const double* in);
+void oracle_get_rest(void* h, int32_t mesh, double* dminv, double* vol, double* mass);
+int32_t oracle_num_groups(void* h);
+int32_t oracle_group_size(void* h, int32_t g);          /* number of (mesh, vertex) pairs */
+void oracle_group(void* h, int32_t g, int32_t* out);    /* 2*size ints: mesh, vertex */
+/* Force and 3x3 Hessian of one vertex at the current state (material+inertia+boundary). */
+void oracle_vertex_force_hessian(void* h, int32_t mesh, int32_t v, int32_t apply_friction,
+                                 double* f3, double* h9);
+/* Total elastic (Neo-Hookean, rest energy removed) + inertia energy, in double. */
+double oracle_energy(void* h);
+int32_t oracle_solve_failures(void* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
