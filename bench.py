@@ -210,6 +210,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32", "fp64"])
+    ap.add_argument("--lanes", type=int, default=0, help="lanes per vertex (0 = autotune)")
+    ap.add_argument("--block", type=int, default=0, help="solve block size (0 = autotune)")
+    ap.add_argument("--param", action="append", default=[],
+                    help="PhysicsParams override key=json_value (e.g. usePDL=false)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -225,6 +229,14 @@ def main():
     tmp = tempfile.TemporaryDirectory()
     d = tmp.name
     mp, pp = make_scene(args.workload, d, args.precision, args.size, args.iterations)
+    overrides = {}
+    if args.lanes or args.block:
+        overrides.update(lanesPerVertex=args.lanes, blockSize=args.block, autotune=False)
+    for kv in args.param:
+        k, v = kv.split("=", 1)
+        overrides[k] = json.loads(v)
+    if overrides:
+        pp = scenes.set_precision(pp, args.precision, **overrides)
 
     # ---- FP32-mixed engine: device-resident timing ---------------------------------
     phys = VBDPhysics()

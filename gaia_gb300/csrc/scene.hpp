@@ -42,6 +42,8 @@ struct PhysicsParams {
     int lanesPerVertex = 0;              // 0 = autotune
     int blockSize = 0;                   // 0 = autotune
     bool autotune = true;
+    bool usePDL = true;                  // programmatic dependent launch between color kernels
+    int smallColorVertices = 16384;      // colors up to this size use one warp per vertex
 };
 
 // ObjectParams (Materials/Materials.h:12-75) + ObjectParamsVBD

@@ -110,8 +110,10 @@ public:
         block_ = sc_.p.blockSize;
         if (lanes_ != 0 && lanes_ != 2 && lanes_ != 4 && lanes_ != 8 && lanes_ != 16 && lanes_ != 32)
             throw std::runtime_error("lanesPerVertex must be 2, 4, 8, 16 or 32");
-        if (block_ != 0 && (block_ < 64 || block_ > 512 || block_ % 32))
-            throw std::runtime_error("blockSize must be a multiple of 32 in [64, 512]");
+        if (block_ != 0 && (block_ < 64 || block_ > 256 || block_ % 32))
+            throw std::runtime_error("blockSize must be a multiple of 32 in [64, 256]");
+        use_pdl_ = sc_.p.usePDL;
+        small_color_ = sc_.p.smallColorVertices;
         if (lanes_ == 0 || block_ == 0) {
             if (sc_.p.autotune) autotune_impl();
             if (lanes_ == 0) lanes_ = 4;
@@ -267,10 +269,14 @@ public:
         c_.inv_dt = R(1.0 / p.dt);
         c_.dt2inv = R(p.dtSqrReciprocal);
         c_.dt_d = p.dt;
+        c_.dt_f = float(p.dt);
         for (int k = 0; k < 3; ++k) {
             c_.g[k] = p.gravity[k];
             c_.lo[k] = p.worldLo[k];
             c_.hi[k] = p.worldHi[k];
+            c_.g_f[k] = float(p.gravity[k]);
+            c_.lo_f[k] = float(p.worldLo[k]);
+            c_.hi_f[k] = float(p.worldHi[k]);
         }
         c_.kb = R(p.boundaryCollisionStiffness);
         c_.fr_mu = R(p.boundaryFrictionDynamic);
@@ -348,20 +354,41 @@ public:
     }
 
     // ---- kernels ----------------------------------------------------------------
+    // Launch of one color's solve. pdl: launched as a programmatic dependent of
+    // the previous kernel in the stream (its static-data prologue overlaps that
+    // kernel's tail; k_solve waits on griddepcontrol before reading positions).
+    template <bool PROBE, int L>
+    void launch_solve_l(int grid, int B, int beg, int end, int friction, double* probe, bool pdl) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(B);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st_;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = pdl ? attr : nullptr;
+        cfg.numAttrs = pdl ? 1 : 0;
+        GAIA_CUDA(cudaLaunchKernelEx(&cfg, dev::k_solve<L, ST, R, PROBE>, ptrs(), c_, beg, end, friction, probe));
+    }
+
     template <bool PROBE>
-    void launch_solve(int L, int B, int beg, int end, int friction, double* probe) {
+    void launch_solve(int L, int B, int beg, int end, int friction, double* probe, bool pdl = false) {
         if (end <= beg) return;
         int grid = div_up(int64_t(end - beg) * L, B);
-        auto P = ptrs();
         switch (L) {
-            case 2: dev::k_solve<2, ST, R, PROBE><<<grid, B, 0, st_>>>(P, c_, beg, end, friction, probe); break;
-            case 4: dev::k_solve<4, ST, R, PROBE><<<grid, B, 0, st_>>>(P, c_, beg, end, friction, probe); break;
-            case 8: dev::k_solve<8, ST, R, PROBE><<<grid, B, 0, st_>>>(P, c_, beg, end, friction, probe); break;
-            case 16: dev::k_solve<16, ST, R, PROBE><<<grid, B, 0, st_>>>(P, c_, beg, end, friction, probe); break;
-            default: dev::k_solve<32, ST, R, PROBE><<<grid, B, 0, st_>>>(P, c_, beg, end, friction, probe); break;
+            case 2: launch_solve_l<PROBE, 2>(grid, B, beg, end, friction, probe, pdl); break;
+            case 4: launch_solve_l<PROBE, 4>(grid, B, beg, end, friction, probe, pdl); break;
+            case 8: launch_solve_l<PROBE, 8>(grid, B, beg, end, friction, probe, pdl); break;
+            case 16: launch_solve_l<PROBE, 16>(grid, B, beg, end, friction, probe, pdl); break;
+            default: launch_solve_l<PROBE, 32>(grid, B, beg, end, friction, probe, pdl); break;
         }
-        GAIA_CUDA(cudaGetLastError());
     }
+
+    // Lanes per vertex for one color: small colors cannot fill the GPU with the
+    // tuned lane count, so they use one warp per vertex (one incidence per lane,
+    // the shortest dependent-load chain).
+    int lanes_for(int n) const { return n <= small_color_ ? 32 : lanes_cur_; }
 
     void enqueue_init() {
         auto P = ptrs();
@@ -392,8 +419,16 @@ public:
             *omega = order == 1 ? 1.0 : (order == 2 ? 2.0 / (2.0 - rho * rho) : 4.0 / (4.0 - rho * rho * *omega));
             GAIA_CUDA(cudaMemcpyAsync(d_acc_prev_.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
         }
-        for (size_t g = 0; g < group_beg_.size(); ++g)
-            launch_solve<false>(L, B, group_beg_[g], group_end_[g], friction, nullptr);
+        lanes_cur_ = L;
+        // programmatic launch only directly after another solve kernel in the stream
+        bool after_solve = it > 0 && !accel;
+        for (size_t g = 0; g < group_beg_.size(); ++g) {
+            const int n = group_end_[g] - group_beg_[g];
+            if (n <= 0) continue;
+            launch_solve<false>(lanes_for(n), B, group_beg_[g], group_end_[g], friction, nullptr,
+                                use_pdl_ && after_solve);
+            after_solve = true;
+        }
         if (accel) {
             dev::k_accel_apply<ST><<<div_up(nactive_, 256), 256, 0, st_>>>(d_pos_.p, d_acc_pp_.p, d_acc_prev_.p, nactive_, *omega);
             GAIA_CUDA(cudaGetLastError());
@@ -493,7 +528,7 @@ public:
         save.alloc(nslots_, nullptr);
         GAIA_CUDA(cudaMemcpyAsync(save.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
         const int Ls[] = {2, 4, 8, 16, 32};
-        const int Bs[] = {128, 256, 512};
+        const int Bs[] = {128, 256};
         float best = 1e30f;
         int bestL = 4, bestB = 256;
         double omega = 1.0;
@@ -505,7 +540,7 @@ public:
                     launch_solve<false>(L, B, group_beg_[g], group_end_[g], 1, nullptr);
                 GAIA_CUDA(cudaEventRecord(ev_a_, st_));
                 const int reps = 3;
-                for (int r = 0; r < reps; ++r) enqueue_iteration(1, L, B, &omega, false);
+                for (int r = 0; r < reps; ++r) enqueue_iteration(0, L, B, &omega, false);
                 GAIA_CUDA(cudaEventRecord(ev_b_, st_));
                 GAIA_CUDA(cudaEventSynchronize(ev_b_));
                 float ms = 0.f;
@@ -714,7 +749,9 @@ private:
     int nmesh_ = 0;
     int64_t nslots_ = 0;
     int32_t nactive_ = 0, ninc_ = 0;
-    int lanes_ = 0, block_ = 0;
+    int lanes_ = 0, block_ = 0, lanes_cur_ = 4;
+    bool use_pdl_ = true;
+    int small_color_ = 16384;
     double tuned_ms_ = 0.0;
     int64_t launches_per_substep_ = 0;
     size_t bytes_ = 0;

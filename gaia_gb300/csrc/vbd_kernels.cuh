@@ -66,8 +66,23 @@ struct Consts {
     double dt_d;
     double g[3];
     double lo[3], hi[3];
+    float dt_f, g_f[3], lo_f[3], hi_f[3];  // the same constants for FP32 state arithmetic
     int32_t plane, assoc_grav;
 };
+
+// The FP64 or FP32 copy of a constant, matching the state scalar type.
+template <typename Sc>
+__device__ __forceinline__ Sc pick(double d, float f);
+template <>
+__device__ __forceinline__ float pick<float>(double, float f) { return f; }
+template <>
+__device__ __forceinline__ double pick<double>(double d, float) { return d; }
+
+// Programmatic dependent launch: let the next grid in the stream start its
+// prologue now, and wait for the previous grid's results (no-ops when the
+// kernel was not launched as a programmatic dependent).
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // Counter slots in device memory.
 enum { CNT_FP64_SOLVES = 0, CNT_FAILED_SOLVES = 1, CNT_NONFINITE = 2, CNT_N = 4 };
@@ -159,34 +174,47 @@ __device__ __forceinline__ bool solve3<double>(const double* H, const double* b,
     return ldlt3<double>(H, b, x, 1e-12);
 }
 
+// One incidence record as loaded from HBM (streaming loads: each record is
+// read once per iteration). load() issues the loads; the fields are decoded
+// where they are used, so a record can be in flight while the previous one
+// is being computed.
 template <typename R>
-__device__ __forceinline__ void load_record(const int4* rec_n, const R4<R>* rec_a, const R4<R>* rec_b, const R* rec_c,
-                                            int r, int& n0, int& n1, int& n2, R* m0, R* m1, R* m2);
+struct RecRaw;
 template <>
-__device__ __forceinline__ void load_record<float>(const int4* rec_n, const R4<float>* rec_a, const R4<float>* rec_b,
-                                                   const float*, int r, int& n0, int& n1, int& n2, float* m0,
-                                                   float* m1, float* m2) {
-    int4 n = __ldcs(rec_n + r);
-    float4 a = __ldcs(reinterpret_cast<const float4*>(rec_a) + r);
-    float4 b = __ldcs(reinterpret_cast<const float4*>(rec_b) + r);
-    n0 = n.x; n1 = n.y; n2 = n.z;
-    m0[0] = a.x; m0[1] = a.y; m0[2] = a.z;
-    m1[0] = a.w; m1[1] = b.x; m1[2] = b.y;
-    m2[0] = b.z; m2[1] = b.w; m2[2] = f_bits(n.w);
-}
+struct RecRaw<float> {
+    int4 n;
+    float4 a, b;
+    __device__ __forceinline__ void load(const int4* rec_n, const R4<float>* rec_a, const R4<float>* rec_b,
+                                         const float*, int r) {
+        n = __ldcs(rec_n + r);
+        a = __ldcs(reinterpret_cast<const float4*>(rec_a) + r);
+        b = __ldcs(reinterpret_cast<const float4*>(rec_b) + r);
+    }
+    __device__ __forceinline__ void rows(float* m0, float* m1, float* m2) const {
+        m0[0] = a.x; m0[1] = a.y; m0[2] = a.z;
+        m1[0] = a.w; m1[1] = b.x; m1[2] = b.y;
+        m2[0] = b.z; m2[1] = b.w; m2[2] = f_bits(n.w);
+    }
+};
 template <>
-__device__ __forceinline__ void load_record<double>(const int4* rec_n, const R4<double>* rec_a,
-                                                    const R4<double>* rec_b, const double* rec_c, int r, int& n0,
-                                                    int& n1, int& n2, double* m0, double* m1, double* m2) {
-    int4 n = __ldcs(rec_n + r);
-    const double2* pa = reinterpret_cast<const double2*>(rec_a + r);
-    const double2* pb = reinterpret_cast<const double2*>(rec_b + r);
-    double2 a0 = __ldcs(pa), a1 = __ldcs(pa + 1), b0 = __ldcs(pb), b1 = __ldcs(pb + 1);
-    n0 = n.x; n1 = n.y; n2 = n.z;
-    m0[0] = a0.x; m0[1] = a0.y; m0[2] = a1.x;
-    m1[0] = a1.y; m1[1] = b0.x; m1[2] = b0.y;
-    m2[0] = b1.x; m2[1] = b1.y; m2[2] = __ldcs(rec_c + r);
-}
+struct RecRaw<double> {
+    int4 n;
+    double2 a0, a1, b0, b1;
+    double c;
+    __device__ __forceinline__ void load(const int4* rec_n, const R4<double>* rec_a, const R4<double>* rec_b,
+                                         const double* rec_c, int r) {
+        n = __ldcs(rec_n + r);
+        const double2* pa = reinterpret_cast<const double2*>(rec_a + r);
+        const double2* pb = reinterpret_cast<const double2*>(rec_b + r);
+        a0 = __ldcs(pa); a1 = __ldcs(pa + 1); b0 = __ldcs(pb); b1 = __ldcs(pb + 1);
+        c = __ldcs(rec_c + r);
+    }
+    __device__ __forceinline__ void rows(double* m0, double* m1, double* m2) const {
+        m0[0] = a0.x; m0[1] = a0.y; m0[2] = a1.x;
+        m1[0] = a1.y; m1[1] = b0.x; m1[2] = b0.y;
+        m2[0] = b1.x; m2[1] = b1.y; m2[2] = c;
+    }
+};
 
 // Accumulator of one vertex: force (3), lambda-part of the Hessian (6, upper
 // triangle), and S = sum A mu |m_o|^2 (the isotropic part).
@@ -285,10 +313,19 @@ __device__ __forceinline__ void axis_friction(int d, const R* dx, R mu, R lambda
 // [beg, end). PROBE = write force/Hessian of the single vertex `beg` to
 // probe_out instead of moving it.
 // ---------------------------------------------------------------------------
+// Minimum resident blocks of 256 threads: caps FP32-compute kernels at 64
+// registers (32 warps per SM, no spills); the FP64 kernel keeps its registers.
+template <typename R>
+struct SolveOcc {
+    static constexpr int kMinBlocks = sizeof(R) == 8 ? 2 : 4;
+};
+
 template <int L, typename ST, typename R, bool PROBE>
-__global__ void __launch_bounds__(512) k_solve(Ptrs<ST, R> P, Consts<R> c, int beg, int end, int friction,
-                                               double* probe_out) {
+__global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
+    k_solve(Ptrs<ST, R> P, Consts<R> c, int beg, int end, int friction, double* probe_out) {
     using U = typename ST::U;
+    using Sc = typename ST::Sc;
+    pdl_launch_dependents();
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = tid & (L - 1);
     const int v = beg + tid / L;
@@ -296,20 +333,34 @@ __global__ void __launch_bounds__(512) k_solve(Ptrs<ST, R> P, Consts<R> c, int b
     Acc<R> acc = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     U uo{};
     MeshMat<R> mat;
+    int r = 0, e = 0;
+    RecRaw<R> cur;
+    // prologue on static data (records, CSR offsets, materials): overlaps the
+    // previous color's tail when launched as a programmatic dependent
+    if (valid) {
+        mat = P.mats[P.slot_mesh[v]];
+        r = P.inc_ofs[v] + lane;
+        e = P.inc_ofs[v + 1];
+        if (r < e) cur.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r);
+    }
+    pdl_wait();
     if (valid) {
         uo = P.u[v];
-        mat = P.mats[P.slot_mesh[v]];
-        const int s = P.inc_ofs[v], e = P.inc_ofs[v + 1];
-        for (int r = s + lane; r < e; r += L) {
-            int n0, n1, n2;
+        while (r < e) {
+            // two-stage pipeline: the next record is in flight during this incidence
+            const int rn = r + L;
+            RecRaw<R> nxt;
+            if (rn < e) nxt.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, rn);
+            const U q0 = ST::ldg(P.u, cur.n.x), q1 = ST::ldg(P.u, cur.n.y), q2 = ST::ldg(P.u, cur.n.z);
             R m0[3], m1[3], m2[3];
-            load_record<R>(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r, n0, n1, n2, m0, m1, m2);
-            const U q0 = ST::ldg(P.u, n0), q1 = ST::ldg(P.u, n1), q2 = ST::ldg(P.u, n2);
+            cur.rows(m0, m1, m2);
             R e0[3], e1[3], e2[3];
             ST::diff(q0, uo, e0);
             ST::diff(q1, uo, e1);
             ST::diff(q2, uo, e2);
             incidence<R>(e0, e1, e2, m0, m1, m2, mat.mu, mat.lmbd, acc);
+            cur = nxt;
+            r = rn;
         }
     }
     reduce_group<L, R>(acc);
@@ -351,13 +402,13 @@ __global__ void __launch_bounds__(512) k_solve(Ptrs<ST, R> P, Consts<R> c, int b
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             // below = lo - x, above = x - hi (x = X + u)
-            R below = ST::template sub_from<R>(c.lo[d], Xc[d], uo, d);
+            R below = ST::template sub_from<R>(pick<Sc>(c.lo[d], c.lo_f[d]), Xc[d], uo, d);
             R depth;
             if (below > R(0)) {
                 depth = below;
                 f[d] += depth * c.kb;
             } else {
-                R above = -ST::template sub_from<R>(c.hi[d], Xc[d], uo, d);
+                R above = -ST::template sub_from<R>(pick<Sc>(c.hi[d], c.hi_f[d]), Xc[d], uo, d);
                 if (!(above > R(0))) continue;
                 depth = above;
                 f[d] -= depth * c.kb;
@@ -383,7 +434,6 @@ __global__ void __launch_bounds__(512) k_solve(Ptrs<ST, R> P, Consts<R> c, int b
         step = c.step_gd;
         d3[0] = f[0]; d3[1] = f[1]; d3[2] = f[2];
     }
-    using Sc = typename ST::Sc;
     const Sc s0 = Sc(step * d3[0]), s1 = Sc(step * d3[1]), s2 = Sc(step * d3[2]);
     if (!(isfinite(s0) && isfinite(s1) && isfinite(s2))) {
         atomicAdd(&P.counters[CNT_NONFINITE], 1ull);
@@ -402,7 +452,7 @@ __global__ void k_initial_step(Ptrs<ST, R> P, Consts<R> c) {
     using Sc = typename ST::Sc;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= P.nslots) return;
-    const Sc dt = Sc(c.dt_d);
+    const Sc dt = pick<Sc>(c.dt_d, c.dt_f);
     const U x = P.u[s];
     V v = P.vel[s];
     P.xprev[s] = x;
@@ -411,9 +461,9 @@ __global__ void k_initial_step(Ptrs<ST, R> P, Consts<R> c) {
     if (init_type == 2 || init_type == 4) P.vprev[s] = v;
     const V vp = v;
     if (c.assoc_grav) {
-        v.x += dt * Sc(c.g[0]);
-        v.y += dt * Sc(c.g[1]);
-        v.z += dt * Sc(c.g[2]);
+        v.x += dt * pick<Sc>(c.g[0], c.g_f[0]);
+        v.y += dt * pick<Sc>(c.g[1], c.g_f[1]);
+        v.z += dt * pick<Sc>(c.g[2], c.g_f[2]);
     }
     if (fixed) { v.x = 0; v.y = 0; v.z = 0; }
     const U yv = ST::add(x, dt * v.x, dt * v.y, dt * v.z);
@@ -426,7 +476,7 @@ __global__ void k_initial_step(Ptrs<ST, R> P, Consts<R> c) {
         case 3: xn = ST::add(x, Sc(0.5) * dt * v.x, Sc(0.5) * dt * v.y, Sc(0.5) * dt * v.z); break;
         case 4: {
             const Sc h = Sc(0.5) * dt * dt;
-            xn = ST::add(x, dt * vp.x + h * Sc(c.g[0]), dt * vp.y + h * Sc(c.g[1]), dt * vp.z + h * Sc(c.g[2]));
+            xn = ST::add(x, dt * vp.x + h * pick<Sc>(c.g[0], c.g_f[0]), dt * vp.y + h * pick<Sc>(c.g[1], c.g_f[1]), dt * vp.z + h * pick<Sc>(c.g[2], c.g_f[2]));
             break;
         }
         default: xn = yv; break;
@@ -479,7 +529,7 @@ __global__ void k_velocity(Ptrs<ST, R> P, Consts<R> c, double* time) {
     if (s >= P.nslots) return;
     V v{0, 0, 0, 0};
     if (s < P.nactive) {
-        const Sc dt = Sc(c.dt_d);
+        const Sc dt = pick<Sc>(c.dt_d, c.dt_f);
         Sc d[3];
         ST::diff(P.u[s], P.xprev[s], d);
         v.x = d[0] / dt;

@@ -51,7 +51,7 @@ struct StF32 {
         return U{float(x[0]), float(x[1]), float(x[2]), float(w)};
     }
     __device__ static void to_d(const U& u, double* x) { x[0] = u.x; x[1] = u.y; x[2] = u.z; }
-    __device__ static double mass(const U& u) { return u.w; }
+    __device__ static Sc mass(const U& u) { return u.w; }
     __device__ static U ldg(const U* p, int i) {
         float4 v = __ldg(reinterpret_cast<const float4*>(p) + i);
         return U{v.x, v.y, v.z, v.w};
@@ -66,8 +66,8 @@ struct StF32 {
     }
     __device__ static float comp(const U& u, int d) { return d == 0 ? u.x : (d == 1 ? u.y : u.z); }
     template <typename R>
-    __device__ static R sub_from(double c, float X, const U& u, int d) {
-        return R((float(c) - X) - comp(u, d));
+    __device__ static R sub_from(Sc c, float X, const U& u, int d) {
+        return R((c - X) - comp(u, d));
     }
 };
 
@@ -77,7 +77,7 @@ struct StF64 {
     using Sc = double;
     __host__ __device__ static U from_d(const double* x, double w) { return U{x[0], x[1], x[2], w}; }
     __device__ static void to_d(const U& u, double* x) { x[0] = u.x; x[1] = u.y; x[2] = u.z; }
-    __device__ static double mass(const U& u) { return u.w; }
+    __device__ static Sc mass(const U& u) { return u.w; }
     __device__ static U ldg(const U* p, int i) {
         const double2* q = reinterpret_cast<const double2*>(p + i);
         double2 a = __ldg(q), b = __ldg(q + 1);
@@ -93,7 +93,7 @@ struct StF64 {
     }
     __device__ static double comp(const U& u, int d) { return d == 0 ? u.x : (d == 1 ? u.y : u.z); }
     template <typename R>
-    __device__ static R sub_from(double c, float X, const U& u, int d) {
+    __device__ static R sub_from(Sc c, float X, const U& u, int d) {
         return R((c - double(X)) - comp(u, d));
     }
 };
@@ -116,7 +116,7 @@ struct StDF {
         x[1] = double(u.hy) + double(u.ly);
         x[2] = double(u.hz) + double(u.lz);
     }
-    __device__ static double mass(const U& u) { return u.w; }
+    __device__ static Sc mass(const U& u) { return u.w; }
     __device__ static U ldg(const U* p, int i) {
         const float4* q = reinterpret_cast<const float4*>(p + i);
         float4 a = __ldg(q), b = __ldg(q + 1);
@@ -136,10 +136,10 @@ struct StDF {
         return a;
     }
     template <typename R>
-    __device__ static R sub_from(double c, float X, const U& u, int d) {
+    __device__ static R sub_from(Sc c, float X, const U& u, int d) {
         float h = d == 0 ? u.hx : (d == 1 ? u.hy : u.hz);
         float l = d == 0 ? u.lx : (d == 1 ? u.ly : u.lz);
-        return R(__fsub_rn(__fsub_rn(__fsub_rn(float(c), X), h), l));
+        return R(__fsub_rn(__fsub_rn(__fsub_rn(c, X), h), l));
     }
 };
 
