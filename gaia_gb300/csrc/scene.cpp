@@ -444,6 +444,7 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         get(*pp, "autotune", p.autotune);
         get(*pp, "usePDL", p.usePDL);
         get(*pp, "smallColorVertices", p.smallColorVertices);
+        get(*pp, "solveVariant", p.solveVariant);
     }
     if (p.numSubsteps <= 0 || p.timeStep <= 0) throw std::runtime_error("timeStep and numSubsteps must be positive");
     if (p.iterations < 0) throw std::runtime_error("iterations must be >= 0");

@@ -44,6 +44,7 @@ struct PhysicsParams {
     bool autotune = true;
     bool usePDL = true;                  // programmatic dependent launch between color kernels
     int smallColorVertices = 16384;      // colors up to this size use one warp per vertex
+    int solveVariant = -1;               // -1 autotune, 0 register-pipelined, 1 TMA-staged records
 };
 
 // ObjectParams (Materials/Materials.h:12-75) + ObjectParamsVBD

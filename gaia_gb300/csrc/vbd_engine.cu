@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -114,7 +115,13 @@ public:
             throw std::runtime_error("blockSize must be a multiple of 32 in [64, 256]");
         use_pdl_ = sc_.p.usePDL;
         small_color_ = sc_.p.smallColorVertices;
-        if (lanes_ == 0 || block_ == 0) {
+        set_tma_smem_limits();
+        variant_fixed_ = sc_.p.solveVariant;
+        if (variant_fixed_ != -1 && variant_fixed_ != 0 && variant_fixed_ != 1)
+            throw std::runtime_error("solveVariant must be -1 (autotune), 0 (registers) or 1 (TMA-staged)");
+        if (variant_fixed_ == 1 && sizeof(R) != 4) variant_fixed_ = 0;  // the FP64 engine has no TMA variant
+        if (variant_fixed_ >= 0) variant_ = variant_fixed_;
+        if (lanes_ == 0 || block_ == 0 || variant_fixed_ < 0) {
             if (sc_.p.autotune) autotune_impl();
             if (lanes_ == 0) lanes_ = 4;
             if (block_ == 0) block_ = 256;
@@ -372,9 +379,66 @@ public:
         GAIA_CUDA(cudaLaunchKernelEx(&cfg, dev::k_solve<L, ST, R, PROBE>, ptrs(), c_, beg, end, friction, probe));
     }
 
+    // Largest record count of any block of vpb consecutive vertices in [beg, end).
+    int max_records(int beg, int end, int vpb) {
+        auto key = std::make_pair(beg, vpb);
+        auto it = maxrec_cache_.find(key);
+        if (it != maxrec_cache_.end()) return it->second;
+        int m = 0;
+        for (int v0 = beg; v0 < end; v0 += vpb) m = std::max(m, inc_ofs_[std::min(end, v0 + vpb)] - inc_ofs_[v0]);
+        maxrec_cache_[key] = m;
+        return m;
+    }
+
+    template <int L>
+    bool launch_solve_tma_l(int B, int beg, int end, int friction, bool pdl) {
+        if constexpr (sizeof(R) != 4) {
+            return false;
+        } else {
+            const int vpb = B / L;
+            const int mr = max_records(beg, end, vpb);
+            const size_t smem = 16 + 48 * size_t(mr);
+            if (smem > kTmaSmemMax) return false;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(div_up(end - beg, vpb));
+            cfg.blockDim = dim3(B);
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = st_;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = pdl ? attr : nullptr;
+            cfg.numAttrs = pdl ? 1 : 0;
+            GAIA_CUDA(cudaLaunchKernelEx(&cfg, dev::k_solve_tma<L, ST>, ptrs(), c_, beg, end, friction, mr));
+            return true;
+        }
+    }
+
+    // TMA-staged launch if this engine computes in FP32 and the block's records fit.
+    bool launch_solve_tma(int L, int B, int beg, int end, int friction, bool pdl) {
+        switch (L) {
+            case 2: return launch_solve_tma_l<2>(B, beg, end, friction, pdl);
+            case 4: return launch_solve_tma_l<4>(B, beg, end, friction, pdl);
+            case 8: return launch_solve_tma_l<8>(B, beg, end, friction, pdl);
+            case 16: return launch_solve_tma_l<16>(B, beg, end, friction, pdl);
+            default: return launch_solve_tma_l<32>(B, beg, end, friction, pdl);
+        }
+    }
+
+    void set_tma_smem_limits() {
+        if constexpr (sizeof(R) == 4) {
+            GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_tma<2, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
+            GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_tma<4, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
+            GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_tma<8, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
+            GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_tma<16, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
+            GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_tma<32, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
+        }
+    }
+
     template <bool PROBE>
     void launch_solve(int L, int B, int beg, int end, int friction, double* probe, bool pdl = false) {
         if (end <= beg) return;
+        if (!PROBE && variant_ == 1 && launch_solve_tma(L, B, beg, end, friction, pdl)) return;
         int grid = div_up(int64_t(end - beg) * L, B);
         switch (L) {
             case 2: launch_solve_l<PROBE, 2>(grid, B, beg, end, friction, probe, pdl); break;
@@ -530,34 +594,40 @@ public:
         const int Ls[] = {2, 4, 8, 16, 32};
         const int Bs[] = {128, 256};
         float best = 1e30f;
-        int bestL = 4, bestB = 256;
+        int bestL = 4, bestB = 256, bestV = 0;
         double omega = 1.0;
-        for (int L : Ls) {
-            if (lanes_ && L != lanes_) continue;
-            for (int B : Bs) {
-                if (block_ && B != block_) continue;
-                for (size_t g = 0; g < group_beg_.size(); ++g)  // warm-up
-                    launch_solve<false>(L, B, group_beg_[g], group_end_[g], 1, nullptr);
-                GAIA_CUDA(cudaEventRecord(ev_a_, st_));
-                const int reps = 3;
-                for (int r = 0; r < reps; ++r) enqueue_iteration(0, L, B, &omega, false);
-                GAIA_CUDA(cudaEventRecord(ev_b_, st_));
-                GAIA_CUDA(cudaEventSynchronize(ev_b_));
-                float ms = 0.f;
-                GAIA_CUDA(cudaEventElapsedTime(&ms, ev_a_, ev_b_));
-                ms /= reps;
-                if (ms < best) {
-                    best = ms;
-                    bestL = L;
-                    bestB = B;
+        const int nvar = sizeof(R) == 4 ? 2 : 1;
+        for (int var = 0; var < nvar; ++var) {
+            if (variant_fixed_ >= 0 && var != variant_fixed_) continue;
+            variant_ = var;
+            for (int L : Ls) {
+                if (lanes_ && L != lanes_) continue;
+                for (int B : Bs) {
+                    if (block_ && B != block_) continue;
+                    enqueue_iteration(0, L, B, &omega, false);  // warm-up
+                    GAIA_CUDA(cudaEventRecord(ev_a_, st_));
+                    const int reps = 3;
+                    for (int r = 0; r < reps; ++r) enqueue_iteration(0, L, B, &omega, false);
+                    GAIA_CUDA(cudaEventRecord(ev_b_, st_));
+                    GAIA_CUDA(cudaEventSynchronize(ev_b_));
+                    float ms = 0.f;
+                    GAIA_CUDA(cudaEventElapsedTime(&ms, ev_a_, ev_b_));
+                    ms /= reps;
+                    if (ms < best) {
+                        best = ms;
+                        bestL = L;
+                        bestB = B;
+                        bestV = var;
+                    }
+                    GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
                 }
-                GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
             }
         }
         GAIA_CUDA(cudaMemsetAsync(d_counters_.p, 0, dev::CNT_N * sizeof(unsigned long long), st_));
         GAIA_CUDA(cudaStreamSynchronize(st_));
         lanes_ = bestL;
         block_ = bestB;
+        variant_ = bestV;
         tuned_ms_ = best;
     }
 
@@ -739,6 +809,7 @@ public:
         s->failed_solves = int64_t(h[dev::CNT_FAILED_SOLVES]);
         s->device_bytes = int64_t(bytes_);
         s->autotune_ms_per_iteration = tuned_ms_;
+        s->solve_variant = variant_;
     }
 
 private:
@@ -752,6 +823,10 @@ private:
     int lanes_ = 0, block_ = 0, lanes_cur_ = 4;
     bool use_pdl_ = true;
     int small_color_ = 16384;
+    int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma
+    int variant_fixed_ = -1;   // from PhysicsParams solveVariant (-1 = autotune)
+    std::map<std::pair<int, int>, int> maxrec_cache_;
+    static constexpr size_t kTmaSmemMax = 200 * 1024;
     double tuned_ms_ = 0.0;
     int64_t launches_per_substep_ = 0;
     size_t bytes_ = 0;

@@ -313,6 +313,11 @@ __device__ __forceinline__ void axis_friction(int d, const R* dx, R mu, R lambda
 // [beg, end). PROBE = write force/Hessian of the single vertex `beg` to
 // probe_out instead of moving it.
 // ---------------------------------------------------------------------------
+template <typename ST, typename R, bool PROBE>
+__device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R>& c, int v, const typename ST::U& uo,
+                                            const MeshMat<R>& mat, const Acc<R>& acc, int friction,
+                                            double* probe_out);
+
 // Minimum resident blocks of 256 threads: caps FP32-compute kernels at 64
 // registers (32 warps per SM, no spills); the FP64 kernel keeps its registers.
 template <typename R>
@@ -365,8 +370,17 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
     }
     reduce_group<L, R>(acc);
     if (!valid || lane != 0) return;
+    vertex_tail<ST, R, PROBE>(P, c, v, uo, mat, acc, friction, probe_out);
+}
 
-    // ---- per-vertex tail (lane 0 of the group) --------------------------------
+// ---- per-vertex tail (lane 0 of a vertex group): damping, inertia, ground and
+// friction, 3x3 solve, update ------------------------------------------------------
+template <typename ST, typename R, bool PROBE>
+__device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R>& c, int v, const typename ST::U& uo,
+                                            const MeshMat<R>& mat, const Acc<R>& acc, int friction,
+                                            double* probe_out) {
+    using U = typename ST::U;
+    using Sc = typename ST::Sc;
     R f[3] = {acc.f0, acc.f1, acc.f2};
     R H[6] = {acc.h00 + acc.S, acc.h01, acc.h02, acc.h11 + acc.S, acc.h12, acc.h22 + acc.S};
     const U xp = P.xprev[v];
@@ -440,6 +454,120 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
         return;
     }
     P.u[v] = ST::add(uo, s0, s1, s2);
+}
+
+// ---------------------------------------------------------------------------
+// TMA-staged solve (FP32 compute). Each block owns vpb = blockDim / L
+// consecutive vertices of the color; their incidence records are one
+// contiguous range [inc_ofs[v0], inc_ofs[v0 + vpb]). Thread 0 stages the range
+// into shared memory with three bulk copies (cp.async.bulk, one per record
+// array) completing on an mbarrier, issued before the programmatic-dependency
+// wait: a block's whole record range is in flight at once, overlapping the
+// previous color's tail, at no register cost. Neighbour positions are gathered
+// as in k_solve. max_rec bounds the records of any block of this launch (the
+// host sizes the dynamic shared memory from it).
+// ---------------------------------------------------------------------------
+enum { CNT_TIMEOUT = 3 };
+constexpr int kMbarSpinLimit = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Bounded wait on an mbarrier phase; false if the phase did not complete within the limit.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int i = 0; i < kMbarSpinLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <int L, typename ST>
+__global__ void __launch_bounds__(256, 4)
+    k_solve_tma(Ptrs<ST, float> P, Consts<float> c, int beg, int end, int friction, int max_rec) {
+    using U = typename ST::U;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t bar = smem_u32(smem);
+    int4* s_n = reinterpret_cast<int4*>(smem + 16);
+    float4* s_a = reinterpret_cast<float4*>(smem + 16 + 16 * size_t(max_rec));
+    float4* s_b = reinterpret_cast<float4*>(smem + 16 + 32 * size_t(max_rec));
+    pdl_launch_dependents();
+    const int vpb = blockDim.x / L;
+    const int v0 = beg + blockIdx.x * vpb;
+    const int v1 = min(end, v0 + vpb);
+    const int r0 = P.inc_ofs[v0];
+    const int nrec = min(P.inc_ofs[v1] - r0, max_rec);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t bytes = uint32_t(nrec) * 16u;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(3u * bytes) : "memory");
+        if (bytes) {
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_u32(s_n)),
+                "l"(P.rec_n + r0), "r"(bytes), "r"(bar)
+                : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_u32(s_a)),
+                "l"(P.rec_a + r0), "r"(bytes), "r"(bar)
+                : "memory");
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_u32(s_b)),
+                "l"(P.rec_b + r0), "r"(bytes), "r"(bar)
+                : "memory");
+        }
+    }
+    const int lane = threadIdx.x & (L - 1);
+    const int v = v0 + int(threadIdx.x) / L;
+    const bool valid = v < v1;
+    MeshMat<float> mat;
+    int rb = 0, re = 0;
+    if (valid) {
+        mat = P.mats[P.slot_mesh[v]];
+        rb = P.inc_ofs[v] - r0 + lane;
+        re = min(P.inc_ofs[v + 1] - r0, nrec);
+    }
+    pdl_wait();
+    U uo{};
+    if (valid) uo = P.u[v];
+    const bool ok = mbar_wait(bar, 0);
+    Acc<float> acc = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (valid && ok) {
+        for (int r = rb; r < re; r += L) {
+            const int4 n = s_n[r];
+            const float4 a = s_a[r], b = s_b[r];
+            const U q0 = ST::ldg(P.u, n.x), q1 = ST::ldg(P.u, n.y), q2 = ST::ldg(P.u, n.z);
+            const float m0[3] = {a.x, a.y, a.z}, m1[3] = {a.w, b.x, b.y}, m2[3] = {b.z, b.w, f_bits(n.w)};
+            float e0[3], e1[3], e2[3];
+            ST::diff(q0, uo, e0);
+            ST::diff(q1, uo, e1);
+            ST::diff(q2, uo, e2);
+            incidence<float>(e0, e1, e2, m0, m1, m2, mat.mu, mat.lmbd, acc);
+        }
+    }
+    if (!ok && threadIdx.x == 0) {
+        // the copies did not land within the limit: record it, give them one more bounded
+        // wait so no copy is left writing into this block's shared memory, and skip the update
+        atomicAdd(&P.counters[CNT_TIMEOUT], 1ull);
+        mbar_wait(bar, 0);
+    }
+    reduce_group<L, float>(acc);
+    if (!valid || lane != 0 || !ok) return;
+    vertex_tail<ST, float, false>(P, c, v, uo, mat, acc, friction, nullptr);
 }
 
 // Initial step of a substep over all slots: VBD_BaseMaterial.h:201-259 and

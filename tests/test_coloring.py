@@ -1,0 +1,100 @@
+"""Coloring parity (CPU): the reference's shipped MCS colorings are reproduced
+bit-exactly by the oracle's restatement (GraphColoring/mcs.cpp:14-168) and by
+the library's O(E log V) implementation; the library's OrderedGreedy matches
+the oracle's restatement of gready.cpp:15-117."""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_MODELS = "/root/reference/Data/mesh_models"
+
+
+def _fixtures():
+    d = np.load(os.path.join(HERE, "golden", "coloring_fixtures.npz"))
+    for name in d["names"]:
+        name = str(name)
+        yield name, d[name + "__tets"], d[name + "__colors"]
+
+
+FIXTURES = list(_fixtures())
+
+
+def test_fixture_count():
+    assert len(FIXTURES) == 11
+
+
+@pytest.mark.parametrize("name,tets,colors", FIXTURES, ids=[f[0] for f in FIXTURES])
+def test_mcs_matches_reference_fixture(name, tets, colors, oracle_lib, gaia_lib):
+    nv = len(colors)
+    assert np.array_equal(oracle_lib.color_mcs(nv, tets), colors)
+    assert np.array_equal(gaia_lib.color_mcs(nv, tets), colors)
+
+
+@pytest.mark.parametrize("name,tets,colors", FIXTURES, ids=[f[0] for f in FIXTURES])
+def test_greedy_library_matches_oracle(name, tets, colors, oracle_lib, gaia_lib):
+    nv = len(colors)
+    g_lib = gaia_lib.color_greedy(nv, tets)
+    g_orc = oracle_lib.color_greedy(nv, tets)
+    assert np.array_equal(g_lib, g_orc)
+    # a valid coloring: no tet has two vertices of one color
+    c = g_lib[tets]
+    for i in range(4):
+        for j in range(i + 1, 4):
+            assert not np.any(c[:, i] == c[:, j])
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_MODELS), reason="reference tree not mounted")
+def test_all_reference_fixtures(oracle_lib, gaia_lib):
+    """Every *.t.vertexColoring.json shipped with a .t mesh (18 of them), from the reference tree."""
+    from oracle import scene_io
+
+    n = 0
+    for f in sorted(glob.glob(os.path.join(REF_MODELS, "**", "*.t.vertexColoring.json"), recursive=True)):
+        t = f[: -len(".vertexColoring.json")]
+        if not os.path.exists(t):
+            continue
+        X, T = scene_io.load_t(t)
+        cats = json.load(open(f))
+        colors = gaia_lib.color_mcs(len(X), T)
+        got = [np.flatnonzero(colors == c).tolist() for c in range(int(colors.max()) + 1)]
+        assert got == cats, t
+        n += 1
+    assert n == 18
+
+
+@pytest.mark.parametrize("n", [(2, 2, 2), (3, 4, 5), (7, 7, 7), (12, 5, 3)])
+def test_greedy_and_mcs_on_lattices(n, oracle_lib, gaia_lib):
+    from gaia_gb300 import scenes
+
+    X, T = scenes.lattice_cube(n, 0.01, jitter=1e-4, seed=3)
+    assert np.array_equal(gaia_lib.color_greedy(len(X), T), oracle_lib.color_greedy(len(X), T))
+    assert np.array_equal(gaia_lib.color_mcs(len(X), T), oracle_lib.color_mcs(len(X), T))
+
+
+def test_random_tet_soups(oracle_lib, gaia_lib):
+    """Arbitrary (non-manifold) tet lists: ties and degree orders are exercised."""
+    rng = np.random.Generator(np.random.PCG64(9))
+    for trial in range(20):
+        nv = int(rng.integers(5, 60))
+        nt = int(rng.integers(1, 80))
+        T = np.stack([rng.choice(nv, 4, replace=False) for _ in range(nt)]).astype(np.int32)
+        assert np.array_equal(gaia_lib.color_greedy(nv, T), oracle_lib.color_greedy(nv, T)), trial
+        assert np.array_equal(gaia_lib.color_mcs(nv, T), oracle_lib.color_mcs(nv, T)), trial
+
+
+def test_isolated_vertices(oracle_lib, gaia_lib):
+    T = np.array([[0, 1, 2, 3]], np.int32)
+    nv = 7  # vertices 4..6 belong to no tet
+    assert np.array_equal(gaia_lib.color_greedy(nv, T), oracle_lib.color_greedy(nv, T))
+    assert np.array_equal(gaia_lib.color_mcs(nv, T), oracle_lib.color_mcs(nv, T))
+
+
+def test_coloring_file_roundtrip(tmp_path, gaia_lib):
+    colors = np.array([0, 1, 2, 3, 0, 1], np.int32)
+    p = tmp_path / "c.json"
+    gaia_lib.write_coloring(str(p), colors)
+    assert json.load(open(p)) == [[0, 4], [1, 5], [2], [3]]

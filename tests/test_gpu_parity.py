@@ -80,6 +80,20 @@ def test_lanes_per_vertex_agree(drop_scene, drop_ref, lanes):
     assert _rel(xs[0], drop_ref[0], x0[0]) <= TOL["fp64"]
 
 
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("lanes", [4, 32])
+@pytest.mark.parametrize("precision", ["mixed", "fp32"])
+def test_solve_variants_agree(drop_scene, drop_ref, variant, lanes, precision):
+    """Register-pipelined (0) and TMA-staged (1) solve kernels, with and without
+    programmatic dependent launch, give the oracle's result."""
+    mp, pp = drop_scene
+    for pdl in (True, False):
+        x0, xs, st = _run_gpu(mp, pp, precision, 40, lanesPerVertex=lanes, blockSize=128, autotune=False,
+                              solveVariant=variant, usePDL=pdl, smallColorVertices=0)
+        assert st["solve_variant"] == variant
+        assert _rel(xs[0], drop_ref[0], x0[0]) <= TOL[precision], (variant, lanes, precision, pdl)
+
+
 def test_twist(tmp_path, gaia_lib, oracle_lib):
     """Twist test (both x faces Dirichlet, one rotating at 2 rad/s), 10^3 lattice, 20 steps x 20 iterations."""
     from gaia_gb300 import scenes
