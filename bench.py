@@ -35,6 +35,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "VBD vertex-solves/s & steps/s, FP32-mixed vs plain FP64 at <=1e-5 rel pos err"
+# dram__bytes_read.sum + dram__bytes_write.sum per solved incidence of k_solve, measured by
+# ncu on colors 0-2 of the 60^3 twist (2,354,128 incidences; see profiles/)
+TRAFFIC_BYTES_PER_INCIDENCE = {"fp32": 55.8, "mixed": 62.0}
 
 
 def load_peaks() -> tuple[float, str]:
@@ -214,6 +217,7 @@ def measure_mode(args, mp, pp, precision, overrides, world, local, xref=None):
     phys.loadRunningparameters(mp, ppm)
     phys.initialize()
     st = phys.stats()
+    ccfg = phys.colorConfigs()
     nact, ninc, n = st["num_active_vertices"], st["num_incidences"], st["num_vertices"]
     x0 = np.concatenate([phys.positions(m) for m in range(phys.numMeshes())])
     err = None
@@ -255,7 +259,7 @@ def measure_mode(args, mp, pp, precision, overrides, world, local, xref=None):
         "precision": precision, "value": world * solves * args.steps / (total_ms / 1e3),
         "steps_per_s": args.steps / (total_ms / 1e3), "ms_per_step": total_ms / args.steps, "sweep_ms": sweep_ms,
         "e2e_value": world * solves * e2e_steps / e2e_s, "e2e_steps": e2e_steps, "error": err, "clocks": clocks,
-        "stats": st, "nact": nact, "ninc": ninc, "n": n,
+        "stats": st, "nact": nact, "ninc": ninc, "n": n, "ccfg": ccfg,
     }
 
 
@@ -349,8 +353,13 @@ def main():
         launches_solve = st["num_groups"] * args.iterations * args.steps
         alg_bytes_iter = 64.0 * nact + 61.0 * ninc
         achieved = alg_bytes_iter * args.iterations * args.steps / (head["sweep_ms"] / 1e3) / 1e9
+        # DRAM bytes per solved incidence (records + per-vertex data) from the ncu capture of the
+        # 60^3 twist (profiles/k_solve_twist60_*_full.md), scaled to one average launch here
+        per_inc = TRAFFIC_BYTES_PER_INCIDENCE.get(head["precision"])
+        traffic = per_inc * ninc / st["num_groups"] if per_inc else None
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                    "traffic": None, "peak_kind": peak_kind, "kernel": "k_solve",
+                    "traffic": traffic, "traffic_source": "60^3 ncu capture, scaled per incidence",
+                    "peak_kind": peak_kind, "kernel": "k_solve",
                     "algorithmic_bytes_per_launch": alg_bytes_iter / st["num_groups"],
                     "avg_launch_us": 1e3 * head["sweep_ms"] / launches_solve}
         if fp64:
@@ -366,6 +375,7 @@ def main():
                        "precision": head["precision"], "colors": st["num_groups"],
                        "lanes_per_vertex": st["lanes_per_vertex"], "block": st["block_size"],
                        "solve_variant": st.get("solve_variant"), "overrides": overrides,
+                       "color_configs": [[c["lanes"], c["block"], c["variant"]] for c in head["ccfg"]],
                        "l2": f"inputs larger than L2 (incidence records {48 * ninc / 1e9:.2f} GB per iteration)"},
             "e2e": {"value": head["e2e_value"], "unit": "vertex-solves/s", "h2d_bytes_per_step": 24 * n,
                     "d2h_bytes_per_step": 24 * n, "steps": head["e2e_steps"]},

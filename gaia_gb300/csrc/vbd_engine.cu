@@ -90,6 +90,7 @@ public:
     virtual void vertex_force_hessian(int mesh, int v, int friction, double* f3, double* h9) = 0;
     virtual void stats(gaia_vbd_stats* s) = 0;
     virtual void sync() = 0;
+    virtual void color_config(int g, int32_t* L, int32_t* B, int32_t* variant, float* ms) const = 0;
 };
 
 template <typename ST, typename R>
@@ -121,12 +122,17 @@ public:
             throw std::runtime_error("solveVariant must be -1 (autotune), 0 (registers) or 1 (TMA-staged)");
         if (variant_fixed_ == 1 && sizeof(R) != 4) variant_fixed_ = 0;  // the FP64 engine has no TMA variant
         if (variant_fixed_ >= 0) variant_ = variant_fixed_;
-        if (lanes_ == 0 || block_ == 0 || variant_fixed_ < 0) {
-            if (sc_.p.autotune) autotune_impl();
-            if (lanes_ == 0) lanes_ = 4;
-            if (block_ == 0) block_ = 256;
-        }
+        if ((lanes_ == 0 || block_ == 0 || variant_fixed_ < 0) && sc_.p.autotune) autotune_impl();
+        finalize_cfg();
         capture();
+    }
+
+    void color_config(int g, int32_t* L, int32_t* B, int32_t* variant, float* ms) const override {
+        if (g < 0 || size_t(g) >= ccfg_.size()) throw std::invalid_argument("color index out of range");
+        if (L) *L = ccfg_[g].L;
+        if (B) *B = ccfg_[g].B;
+        if (variant) *variant = ccfg_[g].variant;
+        if (ms) *ms = ccfg_[g].ms;
     }
 
     ~Engine() override {
@@ -436,9 +442,10 @@ public:
     }
 
     template <bool PROBE>
-    void launch_solve(int L, int B, int beg, int end, int friction, double* probe, bool pdl = false) {
+    void launch_solve(int L, int B, int beg, int end, int friction, double* probe, bool pdl = false,
+                      int variant = 0) {
         if (end <= beg) return;
-        if (!PROBE && variant_ == 1 && launch_solve_tma(L, B, beg, end, friction, pdl)) return;
+        if (!PROBE && variant == 1 && launch_solve_tma(L, B, beg, end, friction, pdl)) return;
         int grid = div_up(int64_t(end - beg) * L, B);
         switch (L) {
             case 2: launch_solve_l<PROBE, 2>(grid, B, beg, end, friction, probe, pdl); break;
@@ -449,10 +456,24 @@ public:
         }
     }
 
-    // Lanes per vertex for one color: small colors cannot fill the GPU with the
-    // tuned lane count, so they use one warp per vertex (one incidence per lane,
-    // the shortest dependent-load chain).
-    int lanes_for(int n) const { return n <= small_color_ ? 32 : lanes_cur_; }
+    // Launch configuration of every merged color. Colors differ in size and in
+    // vertex degree (on a 5-tet lattice the largest color holds the vertices with
+    // 8 incident tets, the next ones those with 32), so the autotuner picks lanes
+    // per vertex, block size and kernel variant per color.
+    struct ColorCfg {
+        int L = 4, B = 128, variant = 0;
+        float ms = 0.f;
+    };
+
+    // One configuration for all colors; small colors, which cannot fill the GPU,
+    // use one warp per vertex (one incidence per lane, the shortest load chain).
+    void uniform_cfg(int L, int B, int variant) {
+        ccfg_.assign(group_beg_.size(), ColorCfg{});
+        for (size_t g = 0; g < group_beg_.size(); ++g) {
+            const int n = group_end_[g] - group_beg_[g];
+            ccfg_[g] = ColorCfg{n <= small_color_ ? 32 : L, B, variant, 0.f};
+        }
+    }
 
     void enqueue_init() {
         auto P = ptrs();
@@ -474,7 +495,7 @@ public:
     }
 
     // One iteration's color sweep: VBDPhysics.cpp:879-953 (graph of per-color kernels).
-    void enqueue_iteration(int it, int L, int B, double* omega, bool accel) {
+    void enqueue_iteration(int it, double* omega, bool accel) {
         int friction = it >= sc_.p.frictionStartIter ? 1 : 0;
         if (accel) {
             // getAcceleratorOmega (VBDPhysics.cpp:3558-3574)
@@ -483,14 +504,14 @@ public:
             *omega = order == 1 ? 1.0 : (order == 2 ? 2.0 / (2.0 - rho * rho) : 4.0 / (4.0 - rho * rho * *omega));
             GAIA_CUDA(cudaMemcpyAsync(d_acc_prev_.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
         }
-        lanes_cur_ = L;
         // programmatic launch only directly after another solve kernel in the stream
         bool after_solve = it > 0 && !accel;
         for (size_t g = 0; g < group_beg_.size(); ++g) {
             const int n = group_end_[g] - group_beg_[g];
             if (n <= 0) continue;
-            launch_solve<false>(lanes_for(n), B, group_beg_[g], group_end_[g], friction, nullptr,
-                                use_pdl_ && after_solve);
+            const ColorCfg& cc = ccfg_[g];
+            launch_solve<false>(cc.L, cc.B, group_beg_[g], group_end_[g], friction, nullptr,
+                                use_pdl_ && after_solve, cc.variant);
             after_solve = true;
         }
         if (accel) {
@@ -537,7 +558,7 @@ public:
         g_init_ = capture_one([&] { enqueue_init(); });
         g_sweep_ = capture_one([&] {
             double omega = 1.0;
-            for (int it = 0; it < sc_.p.iterations; ++it) enqueue_iteration(it, lanes_, block_, &omega, sc_.p.useAccelerator);
+            for (int it = 0; it < sc_.p.iterations; ++it) enqueue_iteration(it, &omega, sc_.p.useAccelerator);
         });
         g_vel_ = capture_one([&] { enqueue_velocity(); });
         launches_per_substep_ = 1 + (h_def_slot_.empty() ? 0 : 1) + 1;
@@ -584,8 +605,11 @@ public:
         if (sweep_ms) *sweep_ms = sw;
     }
 
-    // Autotuner: lanes per vertex x block size, timed over full color sweeps on
-    // the current state (positions restored afterwards).
+    // Autotuner: per merged color, every (kernel variant, lanes per vertex, block
+    // size) is timed on that color's kernel alone (CUDA events around repeated
+    // launches on the current state, positions restored afterwards) and the
+    // fastest is kept. Fixed lanesPerVertex / blockSize / solveVariant
+    // parameters restrict the search.
     void autotune_impl() {
         if (nactive_ == 0) return;
         DevBuf<S4> save;
@@ -593,42 +617,55 @@ public:
         GAIA_CUDA(cudaMemcpyAsync(save.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
         const int Ls[] = {2, 4, 8, 16, 32};
         const int Bs[] = {128, 256};
-        float best = 1e30f;
-        int bestL = 4, bestB = 256, bestV = 0;
-        double omega = 1.0;
         const int nvar = sizeof(R) == 4 ? 2 : 1;
-        for (int var = 0; var < nvar; ++var) {
-            if (variant_fixed_ >= 0 && var != variant_fixed_) continue;
-            variant_ = var;
-            for (int L : Ls) {
-                if (lanes_ && L != lanes_) continue;
-                for (int B : Bs) {
-                    if (block_ && B != block_) continue;
-                    enqueue_iteration(0, L, B, &omega, false);  // warm-up
-                    GAIA_CUDA(cudaEventRecord(ev_a_, st_));
-                    const int reps = 3;
-                    for (int r = 0; r < reps; ++r) enqueue_iteration(0, L, B, &omega, false);
-                    GAIA_CUDA(cudaEventRecord(ev_b_, st_));
-                    GAIA_CUDA(cudaEventSynchronize(ev_b_));
-                    float ms = 0.f;
-                    GAIA_CUDA(cudaEventElapsedTime(&ms, ev_a_, ev_b_));
-                    ms /= reps;
-                    if (ms < best) {
-                        best = ms;
-                        bestL = L;
-                        bestB = B;
-                        bestV = var;
+        const int reps = 4;
+        ccfg_.assign(group_beg_.size(), ColorCfg{});
+        double total = 0.0;
+        for (size_t g = 0; g < group_beg_.size(); ++g) {
+            const int beg = group_beg_[g], end = group_end_[g];
+            if (end <= beg) continue;
+            ColorCfg best;
+            best.ms = 1e30f;
+            for (int var = 0; var < nvar; ++var) {
+                if (variant_fixed_ >= 0 && var != variant_fixed_) continue;
+                for (int L : Ls) {
+                    if (lanes_ && L != lanes_) continue;
+                    for (int B : Bs) {
+                        if (block_ && B != block_) continue;
+                        launch_solve<false>(L, B, beg, end, 1, nullptr, false, var);  // warm-up
+                        GAIA_CUDA(cudaEventRecord(ev_a_, st_));
+                        for (int r = 0; r < reps; ++r) launch_solve<false>(L, B, beg, end, 1, nullptr, false, var);
+                        GAIA_CUDA(cudaEventRecord(ev_b_, st_));
+                        GAIA_CUDA(cudaEventSynchronize(ev_b_));
+                        float ms = 0.f;
+                        GAIA_CUDA(cudaEventElapsedTime(&ms, ev_a_, ev_b_));
+                        ms /= reps;
+                        if (ms < best.ms) best = ColorCfg{L, B, var, ms};
                     }
-                    GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
                 }
             }
+            ccfg_[g] = best;
+            total += best.ms;
+            GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
         }
         GAIA_CUDA(cudaMemsetAsync(d_counters_.p, 0, dev::CNT_N * sizeof(unsigned long long), st_));
         GAIA_CUDA(cudaStreamSynchronize(st_));
-        lanes_ = bestL;
-        block_ = bestB;
-        variant_ = bestV;
-        tuned_ms_ = best;
+        tuned_ms_ = total;
+        tuned_ = true;
+    }
+
+    // After construction or a re-tune: per-color configurations in place, and the
+    // configuration of the largest color reported as the engine's.
+    void finalize_cfg() {
+        if (!tuned_) uniform_cfg(lanes_ ? lanes_ : 4, block_ ? block_ : 128, variant_);
+        size_t big = 0;
+        for (size_t g = 0; g < group_beg_.size(); ++g)
+            if (group_end_[g] - group_beg_[g] > group_end_[big] - group_beg_[big]) big = g;
+        if (!ccfg_.empty()) {
+            lanes_ = ccfg_[big].L;
+            block_ = ccfg_[big].B;
+            variant_ = ccfg_[big].variant;
+        }
     }
 
     void reset() override {
@@ -642,12 +679,11 @@ public:
     }
 
     void autotune() override {
-        int keepL = sc_.p.lanesPerVertex, keepB = sc_.p.blockSize;
-        lanes_ = keepL;
-        block_ = keepB;
+        lanes_ = sc_.p.lanesPerVertex;
+        block_ = sc_.p.blockSize;
+        tuned_ = false;
         autotune_impl();
-        if (lanes_ == 0) lanes_ = 4;
-        if (block_ == 0) block_ = 256;
+        finalize_cfg();
         capture();
     }
 
@@ -820,7 +856,9 @@ private:
     int nmesh_ = 0;
     int64_t nslots_ = 0;
     int32_t nactive_ = 0, ninc_ = 0;
-    int lanes_ = 0, block_ = 0, lanes_cur_ = 4;
+    int lanes_ = 0, block_ = 0;
+    std::vector<ColorCfg> ccfg_;
+    bool tuned_ = false;
     bool use_pdl_ = true;
     int small_color_ = 16384;
     int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma
@@ -1095,6 +1133,12 @@ int gaia_vbd_vertex_force_hessian(gaia_vbd* h, int32_t mesh, int32_t vertex, int
     GAIA_NEED(h);
     if (!f3 || !h9) return GAIA_VBD_E_INVALID_ARG;
     return guarded(h, [&] { h->eng->vertex_force_hessian(mesh, vertex, apply_friction, f3, h9); });
+}
+
+int gaia_vbd_get_color_config(gaia_vbd* h, int32_t g, int32_t* lanes, int32_t* block, int32_t* variant,
+                              float* tuned_ms) {
+    GAIA_NEED(h);
+    return guarded(h, [&] { h->eng->color_config(g, lanes, block, variant, tuned_ms); });
 }
 
 int gaia_vbd_get_stats(gaia_vbd* h, gaia_vbd_stats* out) {

@@ -181,6 +181,16 @@ class VBDPhysics:
                                                    H.ctypes.data), self.handle)
         return f, H.reshape(3, 3)
 
+    def colorConfigs(self) -> list[dict]:
+        """Per merged color: lanes per vertex, block size, kernel variant, tuned ms per launch."""
+        out = []
+        for g in range(lib().gaia_vbd_num_groups(self.handle)):
+            L, B, V, ms = C.c_int32(), C.c_int32(), C.c_int32(), C.c_float()
+            _check(lib().gaia_vbd_get_color_config(self.handle, g, C.byref(L), C.byref(B), C.byref(V), C.byref(ms)),
+                   self.handle)
+            out.append({"lanes": L.value, "block": B.value, "variant": V.value, "ms": ms.value})
+        return out
+
     def stats(self) -> dict:
         s = Stats()
         _check(lib().gaia_vbd_get_stats(self.handle, C.byref(s)), self.handle)

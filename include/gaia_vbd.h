@@ -139,6 +139,13 @@ int gaia_vbd_energy(gaia_vbd* h, double* out);
 int gaia_vbd_vertex_force_hessian(gaia_vbd* h, int32_t mesh, int32_t vertex, int32_t apply_friction,
                                   double* f3, double* h9);
 int gaia_vbd_get_stats(gaia_vbd* h, gaia_vbd_stats* out);
+/* Launch configuration the autotuner chose for merged color g (parallel group g):
+ * lanes per vertex, block size, kernel variant (0 registers, 1 TMA-staged), and the
+ * measured time of one launch in ms (0 when not tuned). Any pointer may be NULL.
+ * The reference launches every color with one 32-thread block per vertex
+ * (VBDPhysicsCompute.cu:114-123). */
+int gaia_vbd_get_color_config(gaia_vbd* h, int32_t g, int32_t* lanes, int32_t* block, int32_t* variant,
+                              float* tuned_ms);
 
 /* ---- tools -------------------------------------------------------------------
  * GraphColoring tool (GraphColoring/GraphColoring.cpp:157-196) on a tet list:

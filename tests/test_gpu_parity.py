@@ -75,7 +75,8 @@ def test_drop_cube_trajectory(drop_scene, drop_ref, precision):
 def test_lanes_per_vertex_agree(drop_scene, drop_ref, lanes):
     """Every lanes-per-vertex variant of the solve kernel gives the oracle's result."""
     mp, pp = drop_scene
-    x0, xs, st = _run_gpu(mp, pp, "fp64", 40, lanesPerVertex=lanes, blockSize=128, autotune=False)
+    x0, xs, st = _run_gpu(mp, pp, "fp64", 40, lanesPerVertex=lanes, blockSize=128, autotune=False,
+                          smallColorVertices=0)
     assert st["lanes_per_vertex"] == lanes
     assert _rel(xs[0], drop_ref[0], x0[0]) <= TOL["fp64"]
 
