@@ -74,6 +74,9 @@ _SIGNATURES = {
     "gaia_vbd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "gaia_vbd_get_color_config": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                             C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
+    "gaia_vbd_energy_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_void_p,
+                                          C.c_void_p]),
     "gaia_vbd_color_mcs": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "gaia_vbd_color_greedy": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "gaia_vbd_write_coloring": (C.c_int, [C.c_char_p, C.c_int32, C.c_void_p]),

@@ -18,8 +18,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgaia_vbd.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["scene.cpp", "vbd_engine.cu"]
-HEADERS = ["scene.hpp", "json_lite.hpp", "vbd_kernels.cuh"]
+SOURCES = ["scene.cpp", "vbd_engine.cu", "vbd_energy_noalloc.cu"]
+HEADERS = ["scene.hpp", "json_lite.hpp", "vbd_kernels.cuh", "vbd_state.cuh"]
 
 
 def nvcc() -> str:

@@ -68,6 +68,9 @@ inline int div_up(int64_t a, int64_t b) { return int((a + b - 1) / b); }
 
 }  // namespace
 
+// Message for gaia_vbd_last_global_error from entry points defined in other files.
+void set_last_global_error(const std::string& msg) { g_last_error = msg; }
+
 // One incidence record (layout in vbd_kernels.cuh).
 template <typename R>
 void make_record(int4& n, dev::R4<R>& a, dev::R4<R>& b, R* c, const int* nb, double mv[3][3]);

@@ -147,6 +147,29 @@ int gaia_vbd_get_stats(gaia_vbd* h, gaia_vbd_stats* out);
 int gaia_vbd_get_color_config(gaia_vbd* h, int32_t g, int32_t* lanes, int32_t* block, int32_t* variant,
                               float* tuned_ms);
 
+/* ---- energy without device allocation -----------------------------------------
+ * This entry point has no counterpart in the reference. It is for callers that
+ * cannot call cudaMalloc: hosts that give all device memory to their own arena at
+ * start-up, and real-time or plugin hosts that forbid allocation after start-up
+ * because cudaMalloc / cudaFree synchronize the device. It returns the same total
+ * as gaia_vbd_energy (Neo-Hookean energy with the rest energy removed, plus the
+ * inertia energy when y is given) for one mesh held in caller-owned DEVICE arrays,
+ * and allocates nothing:
+ *   x 3*nv positions, y 3*nv inertia targets or NULL (then mass may be NULL too),
+ *   mass nv lumped masses, tets 4*ntet, dminv 9*ntet (column-major), vol ntet,
+ *   out 1 double (device); stream = cudaStream_t or NULL.
+ * Its only scratch is a fixed array of 4096 partial sums (32 KiB) compiled into the
+ * library, which every GPU that loads the library holds until the process exits.
+ * Limits: nv and ntet each at most 2^24; larger calls fail with GAIA_VBD_E_INVALID_ARG
+ * and a message in gaia_vbd_last_global_error. The first call on a device looks up
+ * the scratch array's device address for that device; make that first call before
+ * any stream capture. The call is asynchronous on `stream`. All calls share the one
+ * scratch array: calls whose kernels overlap on the GPU (different streams or
+ * threads) race and must be serialized by the caller. */
+int gaia_vbd_energy_noalloc(const double* x, const double* y, const double* mass, int32_t nv,
+                            const int32_t* tets, const double* dminv, const double* vol, int32_t ntet,
+                            double mu, double lmbd, double dt, double* out, void* stream);
+
 /* ---- tools -------------------------------------------------------------------
  * GraphColoring tool (GraphColoring/GraphColoring.cpp:157-196) on a tet list:
  * MCS (Modules/GraphColoring/mcs.cpp:14-168) and OrderedGreedy (gready.cpp:15-117),
