@@ -263,6 +263,45 @@ def measure_mode(args, mp, pp, precision, overrides, world, local, xref=None):
     }
 
 
+def measure_scene_loop(args, mp, pp, precision, d):
+    """The batching comparison: every scene of the batch as its own handle (its own
+    layout, graphs and stream), stepped one after another in a host loop. Returns
+    scenes-steps/s over `args.loop_steps` steps, timed on the host around a full
+    device synchronisation."""
+    from gaia_gb300 import VBDPhysics, scenes
+
+    models = json.load(open(mp))["Models"]
+    params = json.load(open(pp))["PhysicsParams"]
+    params = dict(params, gpuPrecision=precision, autotune=False)
+    handles = []
+    for i, m in enumerate(models):
+        sd = os.path.join(d, f"scene{i}")
+        os.makedirs(sd, exist_ok=True)
+        smp, spp = scenes._write_json(sd, [m], params)
+        h = VBDPhysics()
+        h.loadRunningparameters(smp, spp)
+        h.initialize()
+        handles.append(h)
+    for _ in range(args.warmup):
+        for h in handles:
+            h.runStep(1)
+    for h in handles:
+        h.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.loop_steps):
+        for h in handles:
+            h.runStep(1)
+    for h in handles:
+        h.synchronize()
+    dt = time.perf_counter() - t0
+    for h in handles:
+        h.close()
+    return {"scenes_steps_per_s": len(models) * args.loop_steps / dt, "ms_per_step": 1e3 * dt / args.loop_steps,
+            "steps": args.loop_steps, "scenes": len(models),
+            "how": "one handle per scene (own graphs and stream, fixed lanes/block, no autotune), "
+                   "stepped in a host loop; host-timed around a full synchronisation"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -270,8 +309,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gaia", choices=["gaia", "reference"])
     ap.add_argument("--workload", default="twist", choices=["twist", "drop", "batch"])
-    ap.add_argument("--size", type=int, default=100)
-    ap.add_argument("--iterations", type=int, default=50)
+    ap.add_argument("--size", type=int, default=0,
+                    help="vertices per cube edge (0 = the workload's own: twist 100, drop 10)")
+    ap.add_argument("--iterations", type=int, default=0,
+                    help="VBD iterations per step (0 = the workload's own: twist 50, drop 20, batch 20)")
+    ap.add_argument("--loop-steps", type=int, default=5,
+                    help="batch workload: steps of the one-handle-per-scene loop it is compared with")
     ap.add_argument("--error-steps", type=int, default=100)
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--ref-iters", type=int, default=2)
@@ -286,6 +329,10 @@ def main():
     ap.add_argument("--param", action="append", default=[],
                     help="PhysicsParams override key=json_value (e.g. usePDL=false)")
     args = ap.parse_args()
+    if args.iterations <= 0:
+        args.iterations = 50 if args.workload == "twist" else 20
+    if args.size <= 0:
+        args.size = 10 if args.workload == "drop" else 100
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
@@ -337,6 +384,16 @@ def main():
     ok = [r for r in runs if r["error"] is None or r["error"]["rel"] <= args.tolerance]
     head = max(ok, key=lambda r: r["value"]) if ok else min(runs, key=lambda r: r["error"]["rel"])
 
+    # ---- batching: the merged step against one handle per scene in a host loop -----------
+    batching = None
+    if args.workload == "batch" and args.loop_steps > 0:
+        nsc = len(json.load(open(mp))["Models"])
+        loop = measure_scene_loop(args, mp, pp, head["precision"], d)
+        merged = world * nsc * head["steps_per_s"]
+        batching = {"scenes_steps_per_s": merged, "scenes": world * nsc,
+                    "per_scene_loop": dict(loop, scenes_steps_per_s=world * loop["scenes_steps_per_s"]),
+                    "speedup_over_loop": merged / (world * loop["scenes_steps_per_s"])}
+
     # ---- CPU baseline: the oracle on a bounded sample of the same workload ------------------
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -379,7 +436,7 @@ def main():
                        "l2": f"inputs larger than L2 (incidence records {48 * ninc / 1e9:.2f} GB per iteration)"},
             "e2e": {"value": head["e2e_value"], "unit": "vertex-solves/s", "h2d_bytes_per_step": 24 * n,
                     "d2h_bytes_per_step": 24 * n, "steps": head["e2e_steps"]},
-            "error_vs_fp64": head["error"], "fp64": fp64,
+            "error_vs_fp64": head["error"], "fp64": fp64, "batching": batching,
             "modes": {r["precision"]: {"value": r["value"], "ms_per_step": r["ms_per_step"],
                                        "error_vs_fp64": r["error"]["rel"] if r["error"] else None,
                                        "e2e": r["e2e_value"]} for r in runs},
