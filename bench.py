@@ -302,13 +302,176 @@ def measure_scene_loop(args, mp, pp, precision, d):
                    "stepped in a host loop; host-timed around a full synchronisation"}
 
 
+# ---------------------------------------------------------------- cloth workload
+CLOTH_METRIC = "cloth VBD vertex-solves/s & steps/s (StVK + bending + VF/EE contact), FP32 vs plain FP64"
+
+
+def cloth_scene(args, d: str, precision: str):
+    from gaia_gb300 import scenes
+
+    return scenes.cloth_on_sphere(d, n=args.size, iterations=args.iterations, precision=precision)
+
+
+def cloth_algorithmic_bytes(c) -> tuple[float, dict]:
+    """Algorithmic HBM bytes of one sweep of the cloth solve (all colors), FP32 layout:
+    per vertex 89 B (x, x_prev, y, x_next 16 B each, mass 4, fixed 1, mesh/local ids 8,
+    three CSR offsets 12, VF contact count 4), per face incidence 48 B (list entry 8, face
+    ids 16, DmInv 16, area 4, FV link count 4), per bending incidence 40 B (list entry 8,
+    edge ids 16, row of Q 16), per edge incidence 12 B (list entry 8, EE count 4).
+    Positions of neighbours are L2-resident and not counted."""
+    e6, fe = c.topology(0)
+    nv, nf, ne = c.numVertices(0), c.numFaces(0), c.numEdges(0)
+    interior = int((e6[:, 5] >= 0).sum())
+    # bending incidences: the two vertices on each interior edge plus the two across it
+    b = nv * 89.0 + 3 * nf * 48.0 + 4 * interior * 40.0 + 2 * ne * 12.0
+    return b, {"vertices": nv, "faces": nf, "edges": ne, "interior_edges": interior}
+
+
+def cloth_engine(mp, pp, precision):
+    from gaia_gb300 import VBDClothSimulationFramework, scenes
+
+    c = VBDClothSimulationFramework()
+    c.loadRunningparameters(mp, scenes.set_precision(pp, precision))
+    c.initialize()
+    return c
+
+
+def cloth_cpu_sample(mp, pp, iters: int, reps: int) -> dict:
+    """The cloth oracle (FP64 solve, FP32 contact detection, all host threads) on
+    `reps` samples of one substep with `iters` iterations (contact detection included)."""
+    from oracle import cloth as oc
+
+    sc = oc.load_scene(mp, pp)
+    sc["params"]["iterations"] = iters
+    sc["params"]["numSubsteps"] = 1
+    o = oc.ClothOracle(sc, nthreads=0)
+    nv = len(sc["meshes"][0]["X"])
+    t0 = time.perf_counter()
+    o.step(reps)
+    dt = time.perf_counter() - t0
+    return {"value": nv * iters * reps / dt, "seconds": dt, "cores": os.cpu_count() or 1, "vertices": nv}
+
+
+def run_cloth(args, world, rank, local):
+    import numpy as np
+
+    peak, peak_kind = load_peaks()
+    tmp = tempfile.TemporaryDirectory()
+    d = tmp.name
+    mp, pp = cloth_scene(args, d, "fp32")
+    # plain FP64 engine: the reference trajectory for the error, and its speed
+    fp64, xref = None, None
+    if not args.no_fp64:
+        c64 = cloth_engine(mp, pp, "fp64")
+        x0 = c64.positions(0)
+        c64.runStep(args.error_steps)
+        xref = c64.positions(0)
+        t64 = c64.run_steps_timed(args.fp64_steps)
+        st64 = c64.stats()
+        c64.close()
+        fp64 = {"value": st64["num_sim_vertices"] * args.iterations * args.fp64_steps / (t64 / 1e3),
+                "unit": "vertex-solves/s", "ms_per_step": t64 / args.fp64_steps}
+    err = None
+    if xref is not None:
+        ce = cloth_engine(mp, pp, "fp32")
+        ce.runStep(args.error_steps)
+        x = ce.positions(0)
+        ce.close()
+        err = {"steps": args.error_steps, "rel": float(np.linalg.norm(x - xref) / np.linalg.norm(xref - x0)),
+               "max_abs_m": float(np.abs(x - xref).max()), "reference": "fp64 engine, same kernels"}
+    c = cloth_engine(mp, pp, "fp32")
+    nv = c.numVertices(0)
+    for _ in range(args.warmup):
+        c.runStep(1)
+    c.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    barrier(world)
+    total_ms = c.run_steps_timed(args.steps)
+    clocks = clk.stop()
+    total_ms = allmax(world, total_ms)
+    st = c.stats()
+    sweep_ms = c.time_solve(5)
+    alg, counts = cloth_algorithmic_bytes(c)
+    # e2e through the C ABI with host buffers: per step the positions and velocities of
+    # the cloth go host -> device, the step runs, positions and velocities come back
+    xh, vh = c.positions(0), c.velocities(0)
+    e2e_steps = max(3, args.steps // 3)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        c.setPositions(0, xh)
+        c.setVelocities(0, vh)
+        c.runStep(1)
+        xh = c.positions(0)
+        vh = c.velocities(0)
+    e2e_s = allmax(world, time.perf_counter() - t0)
+    c.close()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        s = cloth_cpu_sample(mp, pp, args.ref_iters, args.cpu_reps)
+        cpu = {"value": s["value"], "unit": "vertex-solves/s", "cores": s["cores"], "kind": "port",
+               "sample": f"{args.cpu_reps} x one substep with {args.ref_iters} iterations (contact detection "
+                         f"included) over {s['vertices']} vertices ({s['seconds']:.1f} s), CPU restatement of the "
+                         "reference cloth step"}
+    tmp.cleanup()
+    if rank != 0:
+        return
+    solves = world * nv * args.iterations
+    ngroups = st["num_groups"]
+    achieved = alg / (sweep_ms / 1e3) / 1e9
+    line = {
+        "metric": CLOTH_METRIC, "value": solves * args.steps / (total_ms / 1e3), "unit": "vertex-solves/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "steps_per_s": args.steps / (total_ms / 1e3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG64 height noise)",
+        "config": {"workload": f"cloth_on_sphere {args.size}x{args.size} (1 m, icosphere r=0.3 collider), "
+                               f"{args.iterations} iterations/step, dt=1/600, contact radius 2e-3",
+                   **counts, "colors": ngroups, "detections": st["detections"], "truncations": st["truncations"],
+                   "l2": "inputs larger than L2 (per-sweep records %.0f MB)" % (alg / 1e6)},
+        "e2e": {"value": solves * e2e_steps / e2e_s, "unit": "vertex-solves/s", "h2d_bytes_per_step": 48 * nv,
+                "d2h_bytes_per_step": 48 * nv, "steps": e2e_steps},
+        "error_vs_fp64": err, "fp64": fp64,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind, "kernel": "cloth k_solve + k_commit (all colors)",
+                     "algorithmic_bytes_per_launch": alg / max(ngroups, 1),
+                     "avg_launch_us": 1e3 * sweep_ms / max(ngroups, 1)},
+        "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": st["kernel_launches_per_step"] * args.steps,
+        "fp64_fallback_solves": st["fp64_fallback_solves"], "failed_solves": st["failed_solves"],
+        "overflow": {k: st[k] for k in ("vf_overflow", "ee_overflow", "fv_overflow", "candidate_overflow",
+                                        "stack_overflow")},
+    }
+    if fp64:
+        fp64["speedup_over_fp64"] = line["value"] / fp64["value"]
+    print(json.dumps(line), flush=True)
+
+
+def run_cloth_reference(args, world, rank):
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as d:
+        mp, pp = cloth_scene(args, d, "fp64")
+        s = cloth_cpu_sample(mp, pp, args.ref_iters, args.steps)
+    v = s["value"]
+    line = {
+        "impl": "reference", "metric": CLOTH_METRIC, "value": v, "unit": "vertex-solves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * s["seconds"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"cloth_on_sphere {args.size}x{args.size}", "vertices": s["vertices"],
+                   "sample": f"each step = one substep with {args.ref_iters} iterations"},
+        "cpu_baseline": {"value": v, "unit": "vertex-solves/s", "cores": s["cores"], "kind": "port",
+                         "sample": f"{args.steps} samples of one substep x {args.ref_iters} iterations"},
+        "e2e": {"value": v, "unit": "vertex-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gaia", choices=["gaia", "reference"])
-    ap.add_argument("--workload", default="twist", choices=["twist", "drop", "batch"])
+    ap.add_argument("--workload", default="twist", choices=["twist", "drop", "batch", "cloth"])
     ap.add_argument("--size", type=int, default=0,
                     help="vertices per cube edge (0 = the workload's own: twist 100, drop 10)")
     ap.add_argument("--iterations", type=int, default=0,
@@ -332,8 +495,16 @@ def main():
     if args.iterations <= 0:
         args.iterations = 50 if args.workload == "twist" else 20
     if args.size <= 0:
-        args.size = 10 if args.workload == "drop" else 100
+        args.size = {"drop": 10, "cloth": 512}.get(args.workload, 100)
     world, rank, local = dist_setup()
+    if args.workload == "cloth":
+        if args.error_steps == 100:
+            args.error_steps = 30
+        if args.impl == "reference":
+            run_cloth_reference(args, world, rank)
+        else:
+            run_cloth(args, world, rank, local)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
         return

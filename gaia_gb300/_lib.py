@@ -41,7 +41,21 @@ class Stats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
-# Every symbol the header declares, with its ctypes signature.
+class ClothStats(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int32), ("num_groups", C.c_int32), ("num_vertices", C.c_int64),
+        ("num_sim_vertices", C.c_int64), ("num_faces", C.c_int64), ("num_edges", C.c_int64),
+        ("kernel_launches_per_step", C.c_int64), ("detections", C.c_int64), ("truncations", C.c_int64),
+        ("vf_overflow", C.c_int64), ("ee_overflow", C.c_int64), ("fv_overflow", C.c_int64),
+        ("candidate_overflow", C.c_int64), ("stack_overflow", C.c_int64), ("fp64_fallback_solves", C.c_int64),
+        ("failed_solves", C.c_int64), ("device_bytes", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+# Every symbol the headers (gaia_vbd.h, gaia_cloth.h) declare, with its ctypes signature.
 _SIGNATURES = {
     "gaia_vbd_create": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
     "gaia_vbd_load": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
@@ -81,6 +95,38 @@ _SIGNATURES = {
     "gaia_vbd_color_greedy": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "gaia_vbd_write_coloring": (C.c_int, [C.c_char_p, C.c_int32, C.c_void_p]),
     "gaia_vbd_write_t": (C.c_int, [C.c_char_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
+    # cloth (gaia_cloth.h)
+    "gaia_cloth_load": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    "gaia_cloth_initialize": (C.c_int, [C.c_void_p]),
+    "gaia_cloth_create": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    "gaia_cloth_destroy": (None, [C.c_void_p]),
+    "gaia_cloth_last_error": (C.c_char_p, [C.c_void_p]),
+    "gaia_cloth_run_step": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gaia_cloth_run_step_timed": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
+    "gaia_cloth_synchronize": (C.c_int, [C.c_void_p]),
+    "gaia_cloth_num_meshes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "gaia_cloth_num_vertices": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "gaia_cloth_num_faces": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "gaia_cloth_num_edges": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "gaia_cloth_get_positions": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_cloth_set_positions": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_cloth_get_velocities": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_cloth_set_velocities": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_cloth_get_topology": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
+    "gaia_cloth_get_rest_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gaia_cloth_num_groups": (C.c_int, [C.c_void_p]),
+    "gaia_cloth_group_size": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "gaia_cloth_get_group": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_cloth_detect": (C.c_int, [C.c_void_p]),
+    "gaia_cloth_get_vf_contacts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "gaia_cloth_get_ee_contacts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "gaia_cloth_get_bounds": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_cloth_get_min_distances": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gaia_cloth_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ClothStats)]),
+    "gaia_cloth_vertex_force_hessian": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "gaia_cloth_time_solve": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
+    "gaia_cloth_color_greedy": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_cloth_color_mcs": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
 }
 
 _lib = None

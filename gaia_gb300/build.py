@@ -1,7 +1,8 @@
 """Build libgaia_vbd.so in-tree with nvcc for sm_103a.
 
-Two translation units compiled in parallel (host scene code, CUDA engine),
-one -gencode, no cmake. Output: gaia_gb300/libgaia_vbd.so.
+Translation units compiled in parallel (host scene code, the tet and cloth
+engines, the cloth contact detector), one -gencode, no cmake. Output:
+gaia_gb300/libgaia_vbd.so.
 """
 from __future__ import annotations
 
@@ -18,8 +19,12 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgaia_vbd.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["scene.cpp", "vbd_engine.cu", "vbd_energy_noalloc.cu"]
-HEADERS = ["scene.hpp", "json_lite.hpp", "vbd_kernels.cuh", "vbd_state.cuh"]
+SOURCES = ["scene.cpp", "vbd_engine.cu", "vbd_energy_noalloc.cu", "cloth_scene.cpp", "cloth_cd.cu", "cloth_engine.cu"]
+HEADERS = ["scene.hpp", "json_lite.hpp", "json_get.hpp", "vbd_kernels.cuh", "vbd_state.cuh", "cloth_scene.hpp",
+           "cloth_cd.hpp", "cloth_dev.cuh"]
+PUBLIC_HEADERS = ["gaia_vbd.h", "gaia_cloth.h"]
+# The contact detector's predicates must round like the CPU restatement: no FMA contraction.
+EXTRA_FLAGS = {"cloth_cd.cu": ["--fmad=false"]}
 
 
 def nvcc() -> str:
@@ -38,13 +43,14 @@ def _stale(target: str, deps: list[str]) -> bool:
 
 def _compile(src: str, verbose_ptxas: bool) -> str:
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
-    deps = [os.path.join(CSRC, src)] + [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "gaia_vbd.h")]
+    deps = ([os.path.join(CSRC, src)] + [os.path.join(CSRC, h) for h in HEADERS] +
+            [os.path.join(INCLUDE, h) for h in PUBLIC_HEADERS])
     if not _stale(obj, deps) and not verbose_ptxas:
         return obj
     cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj, "-O3", "-std=c++17", "-lineinfo",
            "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE, *ARCH]
     if src.endswith(".cu"):
-        cmd += ["--expt-relaxed-constexpr", "-Xptxas", "-O3"]
+        cmd += ["--expt-relaxed-constexpr", "-Xptxas", "-O3", *EXTRA_FLAGS.get(src, [])]
         if verbose_ptxas:
             cmd += ["-Xptxas", "-v"]
     else:

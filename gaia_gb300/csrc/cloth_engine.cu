@@ -1,0 +1,1432 @@
+// GB300 cloth VBD step: per-color block solve of the StVK membrane, quadratic
+// bending, inertia, world-box contact and the vertex-face / edge-edge contact
+// energies with lagged friction; conservative-bound step truncation; GPU
+// contact detection (cloth_cd.cu) re-run inside the iteration loop whenever a
+// vertex left its bound; the whole substep captured in one CUDA graph.
+//
+// Step semantics follow VBDClothSimulationFramework::runStep_CDEveryIter
+// (VBDCloth/VBDClothPhysics.cpp:389-518):
+//   per iteration: [detection if required or first iteration] -> [initial
+//   guess on the first iteration] -> per merged color: solve every vertex of the
+//   color into x_next from the current positions, then commit (the reference's
+//   vertexPositionNext copy, VBDClothPhysics.cpp:480-492) -> [Chebyshev step];
+//   then the velocity update.
+// The per-vertex solve is VBDStepWithExistingCollisions (VBDClothPhysics.cpp:1026-1154).
+//
+// Layout in HBM: all meshes' vertices concatenated (simulated meshes first,
+// then colliders), positions as 4-component vectors (FP32 or FP64), incidence
+// lists per simulated vertex (faces with the vertex's order, edges, bending
+// stencils) as CSR int2 arrays, per-face DmInv (2x2) and area, per-edge 4x4
+// bending form. The detector reads a float4 copy of the positions taken at the
+// last detection (the reference's positionsAtPrevCollisionDetection).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "cloth_cd.hpp"
+#include "cloth_dev.cuh"
+#include "cloth_scene.hpp"
+#include "gaia_cloth.h"
+#include "scene.hpp"
+#include "vbd_kernels.cuh"
+
+namespace gaia {
+void set_last_global_error(const std::string& msg);
+
+namespace cloth {
+namespace {
+
+struct CudaError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+#define CL_CUDA(call)                                                                                    \
+    do {                                                                                                 \
+        cudaError_t e__ = (call);                                                                        \
+        if (e__ != cudaSuccess)                                                                          \
+            throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e__) + " (" + __FILE__ + ":" + \
+                            std::to_string(__LINE__) + ")");                                             \
+    } while (0)
+
+template <typename T>
+struct Buf {
+    T* p = nullptr;
+    size_t n = 0;
+    Buf() = default;
+    Buf(const Buf&) = delete;
+    Buf& operator=(const Buf&) = delete;
+    ~Buf() {
+        if (p) cudaFree(p);
+    }
+    void alloc(size_t count, size_t* total) {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = count;
+        CL_CUDA(cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T)));
+        if (total) *total += std::max<size_t>(count, 1) * sizeof(T);
+    }
+    void upload(const std::vector<T>& h, size_t* total, cudaStream_t st) {
+        alloc(h.size(), total);
+        if (!h.empty()) CL_CUDA(cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    }
+};
+
+inline int nblk(int64_t n, int b) { return int((n + b - 1) / b); }
+
+}  // namespace
+
+template <typename R>
+struct alignas(4 * sizeof(R)) P4 {
+    R x, y, z, w;
+};
+template <typename R>
+struct Vec;
+template <>
+struct Vec<float> {
+    using T = float3;
+};
+template <>
+struct Vec<double> {
+    using T = double3;
+};
+
+template <typename R>
+struct ClothMat {
+    R miu, lambda, dampStVK, dampBend, kBend, fricMu, fricEps, expDamp, constDamp, maxVel, noGravThr;
+    int hasNoGrav, initType, pad;
+};
+
+template <typename R>
+struct Consts {
+    R dt, dtSqrRecip, stepSize, g[3], lo[3], hi[3], kb, muB, epsUB, kc, rc, thick, degThr2, relax, maxQ;
+    int nSimV, nV, assocGrav, handleCollision;
+};
+
+template <typename R>
+struct Args {
+    P4<R>* x;
+    P4<R>* xprev;
+    P4<R>* y;
+    P4<R>* xnext;
+    P4<R>* xcd;
+    P4<R>* v;
+    P4<R>* vprev;
+    P4<R>* accel;
+    P4<R>* xPrevIter;
+    R* bound;
+    const R* mass;
+    const uint8_t* fixed;
+    uint8_t* active;
+    const int2* vInfo;
+    const ClothMat<R>* mats;
+    const int4* faces;
+    const int4* edges;
+    const int* vfOfs;
+    const int2* vfList;
+    const int* veOfs;
+    const int2* veList;
+    const int* vbOfs;
+    const int2* vbList;
+    const P4<R>* faceDmInv;  // (m00, m10, m01, m11) column-major
+    const R* faceArea;
+    const R* bendQ;          // 16 per edge, row-major
+    float4* xf;
+    CDOut cd;
+    int* req;
+    int* state;              // [0] = completed initial steps
+    unsigned long long* counters;
+};
+
+namespace kern {
+
+template <typename R>
+__device__ __forceinline__ typename Vec<R>::T ld(const P4<R>* p, int i) {
+    const P4<R> q = p[i];
+    return typename Vec<R>::T{q.x, q.y, q.z};
+}
+template <typename R>
+__device__ __forceinline__ void st(P4<R>* p, int i, typename Vec<R>::T v) {
+    p[i] = P4<R>{v.x, v.y, v.z, R(0)};
+}
+template <typename V, typename R>
+__device__ __forceinline__ V normalized(V a) {
+    const R nn = dot(a, a);
+    return nn > R(0) ? mul(R(1) / sqrt(nn), a) : a;
+}
+template <typename R>
+__device__ __forceinline__ void add_outer(R* H, R s, R nx, R ny, R nz) {
+    H[0] += s * nx * nx;
+    H[1] += s * nx * ny;
+    H[2] += s * nx * nz;
+    H[3] += s * ny * ny;
+    H[4] += s * ny * nz;
+    H[5] += s * nz * nz;
+}
+
+// One vertex-face contact seen from vertex order `order` (3 = the vertex side, 0..2 =
+// a face vertex): accumulateVFContactForceAndHessian (VBDClothPhysics.cpp:1248-1321) with
+// the closest point recomputed from the current positions (updateVFContactPointInfo).
+template <typename R>
+__device__ void vf_term(const Args<R>& a, const Consts<R>& c, int u, int face, int order, R* f, R* H) {
+    using V = typename Vec<R>::T;
+    const int4 fv = a.faces[face];
+    const V xu = ld(a.x, u), A = ld(a.x, fv.x), B = ld(a.x, fv.y), C = ld(a.x, fv.z);
+    V bary, cp;
+    closest_point_triangle<V, R>(xu, A, B, C, bary, cp);
+    const V diff = sub(xu, cp);
+    const V n = normalized<V, R>(diff);
+    const R dis = dot(diff, n);
+    if (!(dis < c.rc + c.thick)) return;
+    const R b = order == 3 ? R(1) : -(order == 0 ? bary.x : (order == 1 ? bary.y : bary.z));
+    R dEdD, d2E;
+    contact_repulsion<R>(dis, c.thick, c.rc, c.kc, dEdD, d2E);
+    const R lambda = -dEdD;
+    f[0] += b * lambda * n.x;
+    f[1] += b * lambda * n.y;
+    f[2] += b * lambda * n.z;
+    add_outer(H, d2E * b * b, n.x, n.y, n.z);
+    const V dx3 = sub(xu, ld(a.xprev, u));
+    const V cprev = add(add(mul(bary.x, ld(a.xprev, fv.x)), mul(bary.y, ld(a.xprev, fv.y))), mul(bary.z, ld(a.xprev, fv.z)));
+    const V dx = sub(dx3, sub(cp, cprev));
+    const V e0 = normalized<V, R>(sub(B, A));
+    const V e1 = normalized<V, R>(cross(e0, n));
+    const ClothMat<R>& mf = a.mats[a.vInfo[fv.x].x];
+    const ClothMat<R>& mu_ = a.mats[a.vInfo[u].x];
+    const R mu = (mf.fricMu + mu_.fricMu) * R(0.5);
+    const R epsU = (mf.fricEps + mu_.fricEps) * R(0.5) * c.dt;
+    const R t0[3] = {e0.x, e0.y, e0.z}, t1[3] = {e1.x, e1.y, e1.z};
+    friction<R>(mu, lambda, t0, t1, dot(e0, dx), dot(e1, dx), epsU, b, f, H);
+}
+
+// One edge-edge contact of edge e (this vertex has order 0/1 on it) with edge e2:
+// accumulateEEContactForceAndHessian (VBDClothPhysics.cpp:1323-1399).
+template <typename R>
+__device__ void ee_term(const Args<R>& a, const Consts<R>& c, int e, int e2, int order, R* f, R* H) {
+    using V = typename Vec<R>::T;
+    const int4 E = a.edges[e], F = a.edges[e2];
+    const V p1 = ld(a.x, E.x), p2 = ld(a.x, E.y), q1 = ld(a.x, F.x), q2 = ld(a.x, F.y);
+    V c1, c2;
+    R s, t;
+    closest_points_segments(p1, p2, q1, q2, c1, c2, s, t);
+    const V diff = sub(c1, c2);
+    const R dis = sqrt(dot(diff, diff));
+    const V v1 = sub(p2, p1), v2 = sub(q2, q1);
+    const V cr = cross(v1, v2);
+    const R par = dot(cr, cr) / (sqrt(dot(v1, v1)) * sqrt(dot(v2, v2)));
+    if (!(dis < c.rc + c.thick && par > R(CMP_EPS))) return;
+    const V n = mul(R(1) / dis, diff);
+    const R b = order == 0 ? R(1) - s : (order == 1 ? s : (order == 2 ? R(-1) + t : -t));
+    R dEdD, d2E;
+    contact_repulsion<R>(dis, c.thick, c.rc, c.kc, dEdD, d2E);
+    const R lambda = -dEdD;
+    f[0] += b * lambda * n.x;
+    f[1] += b * lambda * n.y;
+    f[2] += b * lambda * n.z;
+    add_outer(H, d2E * b * b, n.x, n.y, n.z);
+    const V c1p = add(mul(R(1) - s, ld(a.xprev, E.x)), mul(s, ld(a.xprev, E.y)));
+    const V c2p = add(mul(R(1) - t, ld(a.xprev, F.x)), mul(t, ld(a.xprev, F.y)));
+    const V dx = sub(sub(c1, c1p), sub(c2, c2p));
+    const V e0 = normalized<V, R>(v1);
+    const V e1 = normalized<V, R>(cross(e0, n));
+    const ClothMat<R>& m1 = a.mats[a.vInfo[E.x].x];
+    const ClothMat<R>& m2 = a.mats[a.vInfo[F.x].x];
+    const R mu = (m1.fricMu + m2.fricMu) * R(0.5);
+    const R epsU = (m1.fricEps + m2.fricEps) * R(0.5) * c.dt;
+    const R t0[3] = {e0.x, e0.y, e0.z}, t1[3] = {e1.x, e1.y, e1.z};
+    friction<R>(mu, lambda, t0, t1, dot(e0, dx), dot(e1, dx), epsU, b, f, H);
+}
+
+template <typename R>
+__device__ __forceinline__ bool solve_block(const R* H, const R* b, R* x, unsigned long long* counters);
+template <>
+__device__ __forceinline__ bool solve_block<float>(const float* H, const float* b, float* x,
+                                                   unsigned long long* counters) {
+    if (gaia::dev::ldlt3<float>(H, b, x, 1e-5f)) return true;
+    double Hd[6], bd[3], xd[3];
+    for (int i = 0; i < 6; ++i) Hd[i] = H[i];
+    for (int i = 0; i < 3; ++i) bd[i] = b[i];
+    atomicAdd(&counters[CC_FP64_SOLVES], 1ull);
+    if (!gaia::dev::ldlt3<double>(Hd, bd, xd, 1e-12)) return false;
+    for (int i = 0; i < 3; ++i) x[i] = float(xd[i]);
+    return true;
+}
+template <>
+__device__ __forceinline__ bool solve_block<double>(const double* H, const double* b, double* x,
+                                                    unsigned long long*) {
+    return gaia::dev::ldlt3<double>(H, b, x, 1e-12);
+}
+
+// The block solve of one vertex of a color: VBDStepWithExistingCollisions
+// (VBDClothPhysics.cpp:1026-1154) with accumlateStVKForceAndHessian
+// (VBDTriMeshStVK.cpp:721-911) in closed form, accumlateBendingForceAndHessian
+// (:913-982), accumlateBoundaryForceAndHessian (VBDClothPhysics.cpp:1401-1463) and
+// applyConservativeBoundTruncation (:1223-1246). Writes x_next.
+// Force and Hessian (sym 00 01 02 11 12 22) of vertex v at the current positions.
+template <typename R>
+__device__ void accumulate(const Args<R>& a, const Consts<R>& c, int v, R* f, R* H) {
+    using V = typename Vec<R>::T;
+    const V x = ld(a.x, v);
+    const V xp = ld(a.xprev, v);
+    const ClothMat<R> mat = a.mats[a.vInfo[v].x];
+
+    // contacts: vertex side, face side (vertices linked to the incident faces), edges
+    const int nvf = min(a.cd.vfCount[v], VF_CAP);
+    for (int k = 0; k < nvf; ++k) vf_term(a, c, v, a.cd.vfFace[size_t(v) * VF_CAP + k], 3, f, H);
+    for (int k = a.vfOfs[v]; k < a.vfOfs[v + 1]; ++k) {
+        const int2 fo = a.vfList[k];
+        const int m = min(a.cd.fvCount[fo.x], FV_CAP);
+        for (int j = 0; j < m; ++j) vf_term(a, c, a.cd.fvVert[size_t(fo.x) * FV_CAP + j], fo.x, fo.y, f, H);
+    }
+    for (int k = a.veOfs[v]; k < a.veOfs[v + 1]; ++k) {
+        const int2 eo = a.veList[k];
+        const int m = min(a.cd.eeCount[eo.x], EE_CAP);
+        for (int j = 0; j < m; ++j) ee_term(a, c, eo.x, a.cd.eeOther[size_t(eo.x) * EE_CAP + j], eo.y, f, H);
+    }
+
+    // inertia (VBDBaseTriMesh.cpp:316-323)
+    const R mh = a.mass[v] * c.dtSqrRecip;
+    const V yv = ld(a.y, v);
+    f[0] += mh * (yv.x - x.x);
+    f[1] += mh * (yv.y - x.y);
+    f[2] += mh * (yv.z - x.z);
+    H[0] += mh;
+    H[3] += mh;
+    H[5] += mh;
+
+    // StVK membrane: with F = [f0 f1] = Ds DmInv, G = (F^T F - I) / 2,
+    // S = 2 mu G + lambda tr(G) I and m the vertex's row of dF/dx:
+    //   force -= A F S m,  H += A [ (m^T S m) I + mu |m|^2 F F^T + (mu + lambda) (F m)(F m)^T ]
+    // which equals the reference's 6x6 d2W/dF2 contracted with m (assembleMembraneHessian).
+    R Hm[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = a.vfOfs[v]; k < a.vfOfs[v + 1]; ++k) {
+        const int2 fo = a.vfList[k];
+        const int4 fv = a.faces[fo.x];
+        const V x0 = ld(a.x, fv.x), x1 = ld(a.x, fv.y), x2 = ld(a.x, fv.z);
+        const V d1 = sub(x1, x0), d2 = sub(x2, x0);
+        const P4<R> D = a.faceDmInv[fo.x];  // m00 m10 m01 m11
+        const V f0 = add(mul(D.x, d1), mul(D.y, d2));
+        const V f1 = add(mul(D.z, d1), mul(D.w, d2));
+        const R G00 = R(0.5) * (dot(f0, f0) - R(1)), G11 = R(0.5) * (dot(f1, f1) - R(1)), G01 = R(0.5) * dot(f0, f1);
+        const R tr = G00 + G11;
+        const R S00 = R(2) * mat.miu * G00 + mat.lambda * tr, S11 = R(2) * mat.miu * G11 + mat.lambda * tr;
+        const R S01 = R(2) * mat.miu * G01;
+        R m1, m2;
+        if (fo.y == 0) {
+            m1 = -D.x - D.y;
+            m2 = -D.z - D.w;
+        } else if (fo.y == 1) {
+            m1 = D.x;
+            m2 = D.z;
+        } else {
+            m1 = D.y;
+            m2 = D.w;
+        }
+        const R A = a.faceArea[fo.x];
+        const R Sm0 = S00 * m1 + S01 * m2, Sm1 = S01 * m1 + S11 * m2;
+        const V P = add(mul(Sm0, f0), mul(Sm1, f1));
+        f[0] -= A * P.x;
+        f[1] -= A * P.y;
+        f[2] -= A * P.z;
+        const R mSm = m1 * Sm0 + m2 * Sm1;
+        const R mm = m1 * m1 + m2 * m2;
+        const V g = add(mul(m1, f0), mul(m2, f1));
+        const R kF = A * mat.miu * mm, kg = A * (mat.miu + mat.lambda);
+        Hm[0] += A * mSm + kF * (f0.x * f0.x + f1.x * f1.x) + kg * g.x * g.x;
+        Hm[1] += kF * (f0.x * f0.y + f1.x * f1.y) + kg * g.x * g.y;
+        Hm[2] += kF * (f0.x * f0.z + f1.x * f1.z) + kg * g.x * g.z;
+        Hm[3] += A * mSm + kF * (f0.y * f0.y + f1.y * f1.y) + kg * g.y * g.y;
+        Hm[4] += kF * (f0.y * f0.z + f1.y * f1.z) + kg * g.y * g.z;
+        Hm[5] += A * mSm + kF * (f0.z * f0.z + f1.z * f1.z) + kg * g.z * g.z;
+    }
+    {
+        const R dmp = mat.dampStVK / c.dt;
+        const V du = sub(x, xp);
+        f[0] -= dmp * (Hm[0] * du.x + Hm[1] * du.y + Hm[2] * du.z);
+        f[1] -= dmp * (Hm[1] * du.x + Hm[3] * du.y + Hm[4] * du.z);
+        f[2] -= dmp * (Hm[2] * du.x + Hm[4] * du.y + Hm[5] * du.z);
+        for (int k = 0; k < 6; ++k) H[k] += Hm[k] * (R(1) + dmp);
+    }
+
+    // quadratic bending: E = k/2 X^T Q X over the 4 stencil vertices
+    if (mat.kBend != R(0)) {
+        const R db = mat.dampBend / c.dt;
+        for (int k = a.vbOfs[v]; k < a.vbOfs[v + 1]; ++k) {
+            const int2 eo = a.vbList[k];
+            const int4 E = a.edges[eo.x];
+            const V X0 = ld(a.x, E.x), X1 = ld(a.x, E.y), X2 = ld(a.x, E.z), X3 = ld(a.x, E.w);
+            const V n1 = cross(sub(X1, X0), sub(X2, X0));
+            const V n2 = cross(sub(X2, X3), sub(X1, X3));
+            if (dot(n1, n1) < c.degThr2 || dot(n2, n2) < c.degThr2) continue;
+            const R* Q = a.bendQ + size_t(eo.x) * 16 + 4 * eo.y;
+            const V gr = add(add(mul(Q[0], X0), mul(Q[1], X1)), add(mul(Q[2], X2), mul(Q[3], X3)));
+            const R hq = mat.kBend * Q[eo.y];
+            f[0] -= mat.kBend * gr.x + hq * (x.x - xp.x) * db;
+            f[1] -= mat.kBend * gr.y + hq * (x.y - xp.y) * db;
+            f[2] -= mat.kBend * gr.z + hq * (x.z - xp.z) * db;
+            const R hb = hq * (R(1) + db);
+            H[0] += hb;
+            H[3] += hb;
+            H[5] += hb;
+        }
+    }
+
+    // world box: penalty on each violated axis with friction in the other two
+    {
+        const R xs[3] = {x.x, x.y, x.z}, dxs[3] = {x.x - xp.x, x.y - xp.y, x.z - xp.z};
+        const int diag[3] = {0, 3, 5};
+        for (int d = 0; d < 3; ++d) {
+            R pen;
+            if (xs[d] < c.lo[d]) {
+                pen = c.lo[d] - xs[d];
+                f[d] += pen * c.kb;
+            } else if (xs[d] > c.hi[d]) {
+                pen = xs[d] - c.hi[d];
+                f[d] -= pen * c.kb;
+            } else {
+                continue;
+            }
+            H[diag[d]] += c.kb;
+            R t0[3] = {0, 0, 0}, t1[3] = {0, 0, 0};
+            const int a1 = (d + 1) % 3, a2 = (d + 2) % 3;
+            t0[a1] = R(1);
+            t1[a2] = R(1);
+            friction<R>(c.muB, pen * c.kb, t0, t1, dxs[a1], dxs[a2], c.epsUB, R(1), f, H);
+        }
+    }
+
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_solve(Args<R> a, Consts<R> c, const int* verts, int n) {
+    using V = typename Vec<R>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int v = verts[i];
+    if (a.fixed[v]) return;
+    R f[3] = {0, 0, 0}, H[6] = {0, 0, 0, 0, 0, 0};
+    accumulate(a, c, v, f, H);
+    const V x = ld(a.x, v);
+    R dx[3];
+    V xn = x;
+    if (solve_block<R>(H, f, dx, a.counters)) {
+        xn = V{x.x + c.stepSize * dx[0], x.y + c.stepSize * dx[1], x.z + c.stepSize * dx[2]};
+        const V xc = ld(a.xcd, v);
+        const V disp = sub(xn, xc);
+        const R s = sqrt(dot(disp, disp));
+        const R bnd = a.bound[v];
+        if (s > bnd) {
+            xn = add(xc, mul(bnd / s, disp));
+            *a.req = 1;
+            atomicAdd(&a.counters[CC_TRUNCATIONS], 1ull);
+        }
+        if (!(isfinite(xn.x) && isfinite(xn.y) && isfinite(xn.z))) {
+            atomicAdd(&a.counters[CC_NONFINITE], 1ull);
+            xn = x;
+        }
+    } else {
+        atomicAdd(&a.counters[CC_FAILED], 1ull);
+    }
+    st(a.xnext, v, xn);
+}
+
+// One vertex's force and Hessian, for parity tests of the accumulation.
+template <typename R>
+__global__ void k_probe(Args<R> a, Consts<R> c, int v, double* out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    R f[3] = {0, 0, 0}, H[6] = {0, 0, 0, 0, 0, 0};
+    accumulate(a, c, v, f, H);
+    for (int k = 0; k < 3; ++k) out[k] = double(f[k]);
+    for (int k = 0; k < 6; ++k) out[3 + k] = double(H[k]);
+}
+
+template <typename R>
+__global__ void k_commit(Args<R> a, const int* verts, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int v = verts[i];
+    if (!a.fixed[v]) a.x[v] = a.xnext[v];
+}
+
+// applyInitialStep + forwardStep_intertia (VBDCloth/VBDBaseTriMesh.cpp:55-178, 180-196).
+template <typename R>
+__global__ void k_init_step(Args<R> a, Consts<R> c) {
+    using V = typename Vec<R>::T;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= c.nSimV) return;
+    const bool hasPrev = a.state[0] > 0;
+    const V x = ld(a.x, v);
+    st(a.xprev, v, x);
+    V vel = ld(a.v, v);
+    if (hasPrev) st(a.accel, v, mul(R(1) / c.dt, sub(vel, ld(a.vprev, v))));
+    const V vp = vel;
+    st(a.vprev, v, vel);
+    if (c.assocGrav) vel = V{vel.x + c.dt * c.g[0], vel.y + c.dt * c.g[1], vel.z + c.dt * c.g[2]};
+    if (a.fixed[v]) vel = V{0, 0, 0};
+    st(a.v, v, vel);
+    const V y = add(x, mul(c.dt, vel));
+    st(a.y, v, y);
+    const int type = a.mats[a.vInfo[v].x].initType;
+    V xn = x;
+    if (type == 0) {
+        xn = y;
+    } else if (type == 1) {
+        if (hasPrev) {
+            const R gn = sqrt(c.g[0] * c.g[0] + c.g[1] * c.g[1] + c.g[2] * c.g[2]);
+            const V gd = V{c.g[0] / gn, c.g[1] / gn, c.g[2] / gn};
+            R ac = dot(ld(a.accel, v), gd);
+            ac = ac < gn ? ac : gn;
+            ac = ac > R(1e-5) ? ac : R(0);
+            xn = add(add(x, mul(c.dt, vp)), mul(c.dt * c.dt * ac, gd));
+        } else {
+            xn = y;
+        }
+    } else if (type == 3) {
+        V step = sub(y, x);
+        const R s = sqrt(dot(step, step));
+        const R bnd = a.bound[v];
+        if (c.handleCollision && s > bnd && s != R(0)) step = mul(bnd / s, step);
+        xn = add(x, step);
+    }
+    st(a.x, v, xn);
+}
+
+// updateVelocity (VBDClothPhysics.cpp:2318-2360).
+template <typename R>
+__global__ void k_velocity(Args<R> a, Consts<R> c) {
+    using V = typename Vec<R>::T;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v == 0) a.state[0] += 1;
+    if (v >= c.nSimV) return;
+    V vel = mul(R(1) / c.dt, sub(ld(a.x, v), ld(a.xprev, v)));
+    const ClothMat<R> m = a.mats[a.vInfo[v].x];
+    const R vm = sqrt(dot(vel, vel));
+    if (m.hasNoGrav && m.maxVel > R(0) && vel.y > m.noGravThr) {
+        if (vm > m.maxVel) vel = mul(m.maxVel / vm, vel);
+    } else if (vm > R(1e-6)) {
+        R vn = vm * m.expDamp - m.constDamp;
+        vn = vn > R(1e-6) ? vn : R(0);
+        vel = mul(vn / vm, vel);
+    } else {
+        vel = V{0, 0, 0};
+    }
+    if (a.fixed[v]) vel = V{0, 0, 0};
+    st(a.v, v, vel);
+}
+
+// applyAcceleration (VBDClothPhysics.cpp:893-915): Chebyshev step outside active contacts.
+template <typename R>
+__global__ void k_accel(Args<R> a, Consts<R> c, R omega) {
+    using V = typename Vec<R>::T;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= c.nSimV || a.active[v]) return;
+    const V pi = ld(a.xPrevIter, v);
+    V xn = add(mul(omega, sub(ld(a.x, v), pi)), pi);
+    const V xc = ld(a.xcd, v);
+    const V disp = sub(xn, xc);
+    const R s = sqrt(dot(disp, disp));
+    if (s > a.bound[v]) {
+        xn = add(xc, mul(a.bound[v] / s, disp));
+        *a.req = 1;
+    }
+    st(a.x, v, xn);
+}
+
+template <typename R>
+__global__ void k_copy_positions(P4<R>* dst, const P4<R>* src, int n) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) dst[v] = src[v];
+}
+
+__global__ void k_set_int(int* p, int val) { *p = val; }
+
+template <typename R>
+__global__ void k_reset_active(Args<R> a, int n) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) a.active[v] = 0;
+}
+
+// positions of the simulated vertices at this detection: float copy for the
+// detector, working-precision copy for the bound truncation
+template <typename R>
+__global__ void k_snapshot(Args<R> a, int n, const int* req) {
+    if (req && *req == 0) return;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    const P4<R> p = a.x[v];
+    a.xcd[v] = p;
+    a.xf[v] = make_float4(float(p.x), float(p.y), float(p.z), 0.f);
+}
+
+// conservative bounds and active-contact mask (VBDClothPhysics.cpp:780-814)
+template <typename R>
+__global__ void k_bounds(Args<R> a, Consts<R> c, const int* req) {
+    if (*req == 0) return;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= c.nSimV) return;
+    float dMin = float(c.maxQ);
+    dMin = fminf(dMin, a.cd.vfMinDis[v]);
+    bool act = a.cd.vfCount[v] > 0;
+    for (int k = a.vfOfs[v]; k < a.vfOfs[v + 1]; ++k) {
+        const int f = a.vfList[k].x;
+        dMin = fminf(dMin, __int_as_float(a.cd.fMinDisBits[f]));
+        act = act || a.cd.fvCount[f] > 0;
+    }
+    for (int k = a.veOfs[v]; k < a.veOfs[v + 1]; ++k) {
+        const int e = a.veList[k].x;
+        dMin = fminf(dMin, a.cd.eeMinDis[e]);
+        act = act || a.cd.eeCount[e] > 0;
+    }
+    dMin = fmaxf(0.f, dMin - float(c.thick));
+    a.bound[v] = R(dMin * float(c.relax));
+    if (act) a.active[v] = 1;
+}
+
+template <typename R>
+__global__ void k_bounds_inf(Args<R> a, int n) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) a.bound[v] = R(std::numeric_limits<float>::max());
+}
+
+}  // namespace kern
+
+class ClothEngineBase {
+public:
+    virtual ~ClothEngineBase() {}
+    virtual void run_steps(int n) = 0;
+    virtual float run_steps_timed(int n) = 0;
+    virtual void sync() = 0;
+    virtual void get_positions(int mesh, double* out) = 0;
+    virtual void set_positions(int mesh, const double* in) = 0;
+    virtual void get_velocities(int mesh, double* out) = 0;
+    virtual void set_velocities(int mesh, const double* in) = 0;
+    virtual void detect() = 0;
+    virtual void vf_contacts(std::vector<int32_t>& rows) = 0;
+    virtual void ee_contacts(std::vector<int32_t>& rows) = 0;
+    virtual void bounds(int mesh, double* out) = 0;
+    virtual void min_distances(int mesh, float* vf, float* fv, float* ee) = 0;
+    virtual void stats(gaia_cloth_stats* s) = 0;
+    virtual void vertex_force_hessian(int mesh, int v, double* f3, double* h9) = 0;
+    virtual float time_solve(int reps) = 0;
+};
+
+template <typename R>
+class ClothEngine : public ClothEngineBase {
+public:
+    explicit ClothEngine(const Scene& s) : sc_(s) {
+        CL_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+        CL_CUDA(cudaEventCreate(&ev0_));
+        CL_CUDA(cudaEventCreate(&ev1_));
+        build();
+        capture();
+    }
+    ~ClothEngine() override {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        cudaEventDestroy(ev0_);
+        cudaEventDestroy(ev1_);
+        cudaStreamDestroy(st_);
+    }
+
+    void run_steps(int n) override {
+        for (int i = 0; i < n; ++i) {
+            if (sc_.p.handleCollision && sc_.p.contactBVHReconstructionSteps > 0 &&
+                frame_ % sc_.p.contactBVHReconstructionSteps == 0)
+                rebuild_bvh();
+            for (int s = 0; s < sc_.p.numSubsteps; ++s) CL_CUDA(cudaGraphLaunch(graph_, st_));
+            ++frame_;
+        }
+    }
+    float run_steps_timed(int n) override {
+        CL_CUDA(cudaEventRecord(ev0_, st_));
+        run_steps(n);
+        CL_CUDA(cudaEventRecord(ev1_, st_));
+        CL_CUDA(cudaEventSynchronize(ev1_));
+        float ms = 0.f;
+        CL_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+        check_nonfinite();
+        return ms;
+    }
+    void sync() override {
+        CL_CUDA(cudaStreamSynchronize(st_));
+        check_nonfinite();
+    }
+
+    void get_positions(int mesh, double* out) override { copy_out(x_.p, mesh, out); }
+    void get_velocities(int mesh, double* out) override {
+        if (mesh >= sc_.numSim) {
+            std::fill(out, out + 3 * size_t(sc_.meshes[mesh].nv), 0.0);
+            return;
+        }
+        copy_out(v_.p, mesh, out);
+    }
+    void set_positions(int mesh, const double* in) override {
+        copy_in(x_.p, mesh, in);
+        if (mesh >= sc_.numSim) {  // colliders: their previous positions and the detector copy too
+            copy_in(xprev_.p, mesh, in);
+            std::vector<float4> h(sc_.meshes[mesh].nv);
+            for (size_t i = 0; i < h.size(); ++i)
+                h[i] = make_float4(float(in[3 * i]), float(in[3 * i + 1]), float(in[3 * i + 2]), 0.f);
+            CL_CUDA(cudaMemcpyAsync(xf_.p + vbase_[mesh], h.data(), h.size() * sizeof(float4), cudaMemcpyHostToDevice, st_));
+            CL_CUDA(cudaStreamSynchronize(st_));
+        }
+    }
+    void set_velocities(int mesh, const double* in) override {
+        if (mesh >= sc_.numSim) throw std::invalid_argument("colliders have no velocities");
+        copy_in(v_.p, mesh, in);
+    }
+
+    void detect() override {
+        if (sc_.numSim == 0) return;
+        rebuild_bvh();
+        kern::k_set_int<<<1, 1, 0, st_>>>(req_.p, 1);
+        enqueue_detection();
+        CL_CUDA(cudaStreamSynchronize(st_));
+        CL_CUDA(cudaGetLastError());
+    }
+    void vf_contacts(std::vector<int32_t>& rows) override {
+        const CDOut& o = cd_.out();
+        const int nV = cdt_.nV;
+        std::vector<int> cnt(nV), face(size_t(nV) * VF_CAP);
+        CL_CUDA(cudaMemcpyAsync(cnt.data(), o.vfCount, nV * sizeof(int), cudaMemcpyDeviceToHost, st_));
+        CL_CUDA(cudaMemcpyAsync(face.data(), o.vfFace, face.size() * sizeof(int), cudaMemcpyDeviceToHost, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+        rows.clear();
+        for (int v = 0; v < nV; ++v)
+            for (int k = 0; k < std::min(cnt[v], VF_CAP); ++k) {
+                const int f = face[size_t(v) * VF_CAP + k];
+                rows.insert(rows.end(), {vmesh_[v], vlocal_[v], fmesh_[f], f - fbase_[fmesh_[f]]});
+            }
+    }
+    void ee_contacts(std::vector<int32_t>& rows) override {
+        const CDOut& o = cd_.out();
+        const int nE = cdt_.nSimE;
+        std::vector<int> cnt(nE), other(size_t(nE) * EE_CAP);
+        CL_CUDA(cudaMemcpyAsync(cnt.data(), o.eeCount, nE * sizeof(int), cudaMemcpyDeviceToHost, st_));
+        CL_CUDA(cudaMemcpyAsync(other.data(), o.eeOther, other.size() * sizeof(int), cudaMemcpyDeviceToHost, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+        rows.clear();
+        for (int e = 0; e < nE; ++e)
+            for (int k = 0; k < std::min(cnt[e], EE_CAP); ++k) {
+                const int e2 = other[size_t(e) * EE_CAP + k];
+                rows.insert(rows.end(), {emesh_[e], e - ebase_[emesh_[e]], emesh_[e2], e2 - ebase_[emesh_[e2]]});
+            }
+    }
+    void bounds(int mesh, double* out) override {
+        if (mesh < 0 || mesh >= sc_.numSim) throw std::invalid_argument("bounds exist for simulated meshes only");
+        const int nv = sc_.meshes[mesh].nv;
+        std::vector<R> h(nv);
+        CL_CUDA(cudaMemcpyAsync(h.data(), bound_.p + vbase_[mesh], nv * sizeof(R), cudaMemcpyDeviceToHost, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+        for (int i = 0; i < nv; ++i) out[i] = double(h[i]);
+    }
+    void min_distances(int mesh, float* vf, float* fv, float* ee) override {
+        const CDOut& o = cd_.out();
+        const TriMesh& m = sc_.meshes[mesh];
+        if (vf) CL_CUDA(cudaMemcpyAsync(vf, o.vfMinDis + vbase_[mesh], m.nv * sizeof(float), cudaMemcpyDeviceToHost, st_));
+        if (fv) CL_CUDA(cudaMemcpyAsync(fv, o.fMinDisBits + fbase_[mesh], m.nf * sizeof(float), cudaMemcpyDeviceToHost, st_));
+        if (ee) {
+            if (mesh >= sc_.numSim) throw std::invalid_argument("edge-edge distances exist for simulated meshes only");
+            CL_CUDA(cudaMemcpyAsync(ee, o.eeMinDis + ebase_[mesh], m.ne * sizeof(float), cudaMemcpyDeviceToHost, st_));
+        }
+        CL_CUDA(cudaStreamSynchronize(st_));
+    }
+    // Milliseconds of one sweep of the per-color solve and commit kernels over all
+    // colors (CUDA events around `reps` sweeps on the current state); positions,
+    // the detection flag and the counters are restored afterwards.
+    float time_solve(int reps) override {
+        if (reps <= 0) throw std::invalid_argument("reps must be positive");
+        Buf<P4<R>> save;
+        save.alloc(x_.n, nullptr);
+        Buf<unsigned long long> csave;
+        csave.alloc(CC_N, nullptr);
+        Buf<int> rsave;
+        rsave.alloc(1, nullptr);
+        CL_CUDA(cudaMemcpyAsync(save.p, x_.p, x_.n * sizeof(P4<R>), cudaMemcpyDeviceToDevice, st_));
+        CL_CUDA(cudaMemcpyAsync(csave.p, counters_.p, CC_N * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st_));
+        CL_CUDA(cudaMemcpyAsync(rsave.p, req_.p, sizeof(int), cudaMemcpyDeviceToDevice, st_));
+        const int B = sc_.p.blockSize;
+        auto sweep = [&] {
+            for (auto& g : groups_) {
+                const int n = int(g->n);
+                if (n == 0) continue;
+                kern::k_solve<R><<<nblk(n, B), B, 0, st_>>>(a_, c_, g->p, n);
+                kern::k_commit<R><<<nblk(n, 256), 256, 0, st_>>>(a_, g->p, n);
+            }
+        };
+        sweep();  // warm-up
+        CL_CUDA(cudaEventRecord(ev0_, st_));
+        for (int r = 0; r < reps; ++r) sweep();
+        CL_CUDA(cudaEventRecord(ev1_, st_));
+        CL_CUDA(cudaEventSynchronize(ev1_));
+        float ms = 0.f;
+        CL_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+        CL_CUDA(cudaMemcpyAsync(x_.p, save.p, x_.n * sizeof(P4<R>), cudaMemcpyDeviceToDevice, st_));
+        CL_CUDA(cudaMemcpyAsync(counters_.p, csave.p, CC_N * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st_));
+        CL_CUDA(cudaMemcpyAsync(req_.p, rsave.p, sizeof(int), cudaMemcpyDeviceToDevice, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+        CL_CUDA(cudaGetLastError());
+        return ms / reps;
+    }
+    void vertex_force_hessian(int mesh, int v, double* f3, double* h9) override {
+        if (mesh < 0 || mesh >= sc_.numSim || v < 0 || v >= sc_.meshes[mesh].nv)
+            throw std::invalid_argument("vertex out of range");
+        Buf<double> out;
+        out.alloc(9, nullptr);
+        kern::k_probe<R><<<1, 32, 0, st_>>>(a_, c_, vbase_[mesh] + v, out.p);
+        double h[9];
+        CL_CUDA(cudaMemcpyAsync(h, out.p, sizeof(h), cudaMemcpyDeviceToHost, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+        for (int k = 0; k < 3; ++k) f3[k] = h[k];
+        const int idx[9] = {3, 4, 5, 4, 6, 7, 5, 7, 8};
+        for (int k = 0; k < 9; ++k) h9[k] = h[idx[k]];
+    }
+    void stats(gaia_cloth_stats* s) override {
+        unsigned long long h[CC_N];
+        CL_CUDA(cudaMemcpyAsync(h, counters_.p, sizeof(h), cudaMemcpyDeviceToHost, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+        std::memset(s, 0, sizeof(*s));
+        s->precision = sizeof(R) == 4 ? 32 : 64;
+        s->num_groups = int32_t(groups_.size());
+        s->num_vertices = cdt_.nV;
+        s->num_sim_vertices = cdt_.nSimV;
+        s->num_faces = cdt_.nF;
+        s->num_edges = cdt_.nE;
+        s->kernel_launches_per_step = launches_per_substep_ * sc_.p.numSubsteps;
+        s->detections = int64_t(h[CC_DETECTIONS]);
+        s->truncations = int64_t(h[CC_TRUNCATIONS]);
+        s->vf_overflow = int64_t(h[CC_VF_OVERFLOW]);
+        s->ee_overflow = int64_t(h[CC_EE_OVERFLOW]);
+        s->fv_overflow = int64_t(h[CC_FV_OVERFLOW]);
+        s->candidate_overflow = int64_t(h[CC_CAND_OVERFLOW]);
+        s->stack_overflow = int64_t(h[CC_STACK_OVERFLOW]);
+        s->fp64_fallback_solves = int64_t(h[CC_FP64_SOLVES]);
+        s->failed_solves = int64_t(h[CC_FAILED]);
+        s->device_bytes = int64_t(bytes_ + cd_.device_bytes());
+    }
+
+private:
+    void check_nonfinite() {
+        unsigned long long h = 0;
+        CL_CUDA(cudaMemcpyAsync(&h, counters_.p + CC_NONFINITE, sizeof(h), cudaMemcpyDeviceToHost, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+        if (h) throw std::domain_error("a cloth vertex solve produced a non-finite position");
+    }
+    void copy_out(const P4<R>* src, int mesh, double* out) {
+        const int nv = sc_.meshes.at(mesh).nv;
+        std::vector<P4<R>> h(nv);
+        CL_CUDA(cudaMemcpyAsync(h.data(), src + vbase_[mesh], nv * sizeof(P4<R>), cudaMemcpyDeviceToHost, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+        for (int i = 0; i < nv; ++i) {
+            out[3 * i] = double(h[i].x);
+            out[3 * i + 1] = double(h[i].y);
+            out[3 * i + 2] = double(h[i].z);
+        }
+    }
+    void copy_in(P4<R>* dst, int mesh, const double* in) {
+        const int nv = sc_.meshes.at(mesh).nv;
+        std::vector<P4<R>> h(nv);
+        for (int i = 0; i < nv; ++i) h[i] = P4<R>{R(in[3 * i]), R(in[3 * i + 1]), R(in[3 * i + 2]), R(0)};
+        CL_CUDA(cudaMemcpyAsync(dst + vbase_[mesh], h.data(), nv * sizeof(P4<R>), cudaMemcpyHostToDevice, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    void build() {
+        const int nm = int(sc_.meshes.size());
+        vbase_.assign(nm + 1, 0);
+        fbase_.assign(nm + 1, 0);
+        ebase_.assign(nm + 1, 0);
+        for (int m = 0; m < nm; ++m) {
+            vbase_[m + 1] = vbase_[m] + sc_.meshes[m].nv;
+            fbase_[m + 1] = fbase_[m] + sc_.meshes[m].nf;
+            ebase_[m + 1] = ebase_[m] + sc_.meshes[m].ne;
+        }
+        const int nV = vbase_[nm], nF = fbase_[nm], nE = ebase_[nm];
+        const int ns = sc_.numSim;
+        const int nSimV = vbase_[ns], nSimF = fbase_[ns], nSimE = ebase_[ns];
+        if (int64_t(nV) * std::max(VF_CAP, 1) > (int64_t(1) << 31) || int64_t(nF) * FV_CAP > (int64_t(1) << 31))
+            throw std::runtime_error("scene too large for 32-bit contact indexing");
+
+        std::vector<P4<R>> hx(nV);
+        std::vector<int2> vInfo(nV);
+        std::vector<uint8_t> fixed(nV, 1);
+        std::vector<R> mass(std::max(nSimV, 1), R(0));
+        std::vector<int4> faces(nF), faceEdges(nF), edges(nE), edgeInfo(nE);
+        std::vector<int> nbrVOfs(nV + 1, 0), nbrV;
+        std::vector<int> vfOfs(nSimV + 1, 0), veOfs(nSimV + 1, 0), vbOfs(nSimV + 1, 0);
+        std::vector<int2> vfList, veList, vbList;
+        std::vector<P4<R>> dminv(std::max(nSimF, 1));
+        std::vector<R> area(std::max(nSimF, 1)), bendQ(16 * size_t(std::max(nSimE, 1)), R(0));
+        vmesh_.assign(nV, 0);
+        vlocal_.assign(nV, 0);
+        fmesh_.assign(nF, 0);
+        emesh_.assign(nE, 0);
+        for (int m = 0; m < nm; ++m) {
+            const TriMesh& M = sc_.meshes[m];
+            const int vb = vbase_[m], fb = fbase_[m], eb = ebase_[m];
+            for (int i = 0; i < M.nv; ++i) {
+                hx[vb + i] = P4<R>{R(M.X[3 * i]), R(M.X[3 * i + 1]), R(M.X[3 * i + 2]), R(0)};
+                vInfo[vb + i] = make_int2(m, i);
+                vmesh_[vb + i] = m;
+                vlocal_[vb + i] = i;
+                if (m < ns) {
+                    fixed[vb + i] = M.fixed[i];
+                    mass[vb + i] = R(M.mass[i]);
+                }
+                for (int k = M.nbrVOfs[i]; k < M.nbrVOfs[i + 1]; ++k) nbrV.push_back(vb + M.nbrV[k]);
+                nbrVOfs[vb + i + 1] = int(nbrV.size());
+            }
+            for (int f = 0; f < M.nf; ++f) {
+                faces[fb + f] = make_int4(vb + M.faces[3 * f], vb + M.faces[3 * f + 1], vb + M.faces[3 * f + 2], m);
+                faceEdges[fb + f] = make_int4(eb + M.faceEdges[3 * f], eb + M.faceEdges[3 * f + 1], eb + M.faceEdges[3 * f + 2], f);
+                fmesh_[fb + f] = m;
+                if (m < ns) {
+                    const double* d = &M.dminv[4 * f];
+                    dminv[fb + f] = P4<R>{R(d[0]), R(d[1]), R(d[2]), R(d[3])};
+                    area[fb + f] = R(M.area[f]);
+                }
+            }
+            for (int e = 0; e < M.ne; ++e) {
+                const Edge& E = M.edges[e];
+                edges[eb + e] = make_int4(vb + E.v1, vb + E.v2, vb + E.v12next, E.v21next < 0 ? -1 : vb + E.v21next);
+                edgeInfo[eb + e] = make_int4(fb + E.f1, E.f2 < 0 ? -1 : fb + E.f2, m, e);
+                emesh_[eb + e] = m;
+                if (m < ns)
+                    for (int k = 0; k < 16; ++k) bendQ[16 * size_t(eb + e) + k] = R(M.bendQ[16 * size_t(e) + k]);
+            }
+            if (m < ns) {
+                for (int i = 0; i < M.nv; ++i) {
+                    for (int k = M.nbrFOfs[i]; k < M.nbrFOfs[i + 1]; ++k) vfList.push_back(make_int2(fb + M.nbrF[k], M.nbrFOrder[k]));
+                    vfOfs[vb + i + 1] = int(vfList.size());
+                    for (int k = M.nbrEOfs[i]; k < M.nbrEOfs[i + 1]; ++k) veList.push_back(make_int2(eb + M.nbrE[k], M.nbrEOrder[k]));
+                    veOfs[vb + i + 1] = int(veList.size());
+                    for (int k = M.bendOfs[i]; k < M.bendOfs[i + 1]; ++k) vbList.push_back(make_int2(eb + M.bendE[k], M.bendOrder[k]));
+                    vbOfs[vb + i + 1] = int(vbList.size());
+                }
+            }
+        }
+        std::vector<ClothMat<R>> mats(nm);
+        for (int m = 0; m < nm; ++m) {
+            ClothMat<R> M{};
+            if (m < ns) {
+                const ObjectParams& o = sc_.objs[m];
+                M.miu = R(o.miu);
+                M.lambda = R(o.lambda);
+                M.dampStVK = R(o.dampingStVK);
+                M.dampBend = R(o.dampingBending);
+                M.kBend = R(o.bendingStiffness);
+                M.fricMu = R(o.frictionDynamic);
+                M.fricEps = R(o.frictionEpsV);
+                M.expDamp = R(o.exponentialVelDamping);
+                M.constDamp = R(o.constantVelDamping);
+                M.maxVel = R(o.maxVelocityMagnitude);
+                M.noGravThr = R(o.noGravZoneThreshold);
+                M.hasNoGrav = o.hasNoGravZone ? 1 : 0;
+                M.initType = o.initializationType;
+            } else {
+                const int c = m - ns;
+                M.fricMu = R(sc_.colliderFriction[2 * c]);
+                M.fricEps = R(sc_.colliderFriction[2 * c + 1]);
+            }
+            mats[m] = M;
+        }
+
+        const PhysicsParams& p = sc_.p;
+        Consts<R>& c = c_;
+        c.dt = R(p.dt);
+        c.dtSqrRecip = R(p.dtSqrReciprocal);
+        c.stepSize = R(p.stepSize);
+        for (int k = 0; k < 3; ++k) {
+            c.g[k] = R(p.gravity[k]);
+            c.lo[k] = R(p.worldLo[k]);
+            c.hi[k] = R(p.worldHi[k]);
+        }
+        c.kb = R(p.boundaryContactStiffness);
+        c.muB = R(p.boundaryFrictionDynamic);
+        c.epsUB = R(p.boundaryFrictionEpsValue * p.dt);
+        c.kc = R(p.contactStiffness);
+        c.rc = R(p.contactRadius);
+        c.thick = R(p.thickness);
+        c.degThr2 = R(p.degenerateTriangleThres * p.degenerateTriangleThres);
+        c.relax = R(p.conservativeStepRelaxation);
+        c.maxQ = R(float(p.maxQueryDis));
+        c.nSimV = nSimV;
+        c.nV = nV;
+        c.assocGrav = p.associateGravityWithInertia ? 1 : 0;
+        c.handleCollision = p.handleCollision ? 1 : 0;
+
+        size_t* tb = &bytes_;
+        x_.upload(hx, tb, st_);
+        xprev_.upload(hx, tb, st_);
+        y_.upload(hx, tb, st_);
+        xnext_.upload(hx, tb, st_);
+        xcd_.upload(hx, tb, st_);
+        xPrevIter_.upload(hx, tb, st_);
+        std::vector<P4<R>> zeros(nV, P4<R>{0, 0, 0, 0});
+        v_.upload(zeros, tb, st_);
+        vprev_.upload(zeros, tb, st_);
+        accel_.upload(zeros, tb, st_);
+        bound_.upload(std::vector<R>(std::max(nSimV, 1), R(std::numeric_limits<float>::max())), tb, st_);
+        mass_.upload(mass, tb, st_);
+        fixed_.upload(fixed, tb, st_);
+        active_.upload(std::vector<uint8_t>(std::max(nSimV, 1), 0), tb, st_);
+        vInfo_.upload(vInfo, tb, st_);
+        mats_.upload(mats, tb, st_);
+        faces_.upload(faces, tb, st_);
+        faceEdges_.upload(faceEdges, tb, st_);
+        edges_.upload(edges, tb, st_);
+        edgeInfo_.upload(edgeInfo, tb, st_);
+        nbrVOfs_.upload(nbrVOfs, tb, st_);
+        nbrV_.upload(nbrV, tb, st_);
+        vfOfs_.upload(vfOfs, tb, st_);
+        vfList_.upload(vfList, tb, st_);
+        veOfs_.upload(veOfs, tb, st_);
+        veList_.upload(veList, tb, st_);
+        vbOfs_.upload(vbOfs, tb, st_);
+        vbList_.upload(vbList, tb, st_);
+        dminv_.upload(dminv, tb, st_);
+        area_.upload(area, tb, st_);
+        bendQ_.upload(bendQ, tb, st_);
+        std::vector<float4> hf(nV);
+        for (int i = 0; i < nV; ++i) hf[i] = make_float4(float(hx[i].x), float(hx[i].y), float(hx[i].z), 0.f);
+        xf_.upload(hf, tb, st_);
+        req_.upload(std::vector<int>{0}, tb, st_);
+        state_.upload(std::vector<int>{0, 0}, tb, st_);
+        counters_.upload(std::vector<unsigned long long>(CC_N, 0ull), tb, st_);
+
+        groups_.clear();
+        for (const auto& g : sc_.groups) {
+            std::vector<int> gv;
+            for (size_t k = 0; k + 1 < g.size(); k += 2) gv.push_back(vbase_[g[k]] + g[k + 1]);
+            groups_.emplace_back(new Buf<int>());
+            groups_.back()->upload(gv, tb, st_);
+        }
+
+        cdt_.nV = nV;
+        cdt_.nF = nF;
+        cdt_.nE = nE;
+        cdt_.nSimV = nSimV;
+        cdt_.nSimF = nSimF;
+        cdt_.nSimE = nSimE;
+        cdt_.numSimMeshes = ns;
+        cdt_.faces = faces_.p;
+        cdt_.faceEdges = faceEdges_.p;
+        cdt_.edges = edges_.p;
+        cdt_.edgeInfo = edgeInfo_.p;
+        cdt_.vInfo = vInfo_.p;
+        cdt_.nbrVOfs = nbrVOfs_.p;
+        cdt_.nbrV = nbrV_.p;
+        cd_.init(cdt_, counters_.p, st_);
+        CL_CUDA(cudaStreamSynchronize(st_));
+
+        Args<R>& a = a_;
+        a.x = x_.p;
+        a.xprev = xprev_.p;
+        a.y = y_.p;
+        a.xnext = xnext_.p;
+        a.xcd = xcd_.p;
+        a.v = v_.p;
+        a.vprev = vprev_.p;
+        a.accel = accel_.p;
+        a.xPrevIter = xPrevIter_.p;
+        a.bound = bound_.p;
+        a.mass = mass_.p;
+        a.fixed = fixed_.p;
+        a.active = active_.p;
+        a.vInfo = vInfo_.p;
+        a.mats = mats_.p;
+        a.faces = faces_.p;
+        a.edges = edges_.p;
+        a.vfOfs = vfOfs_.p;
+        a.vfList = vfList_.p;
+        a.veOfs = veOfs_.p;
+        a.veList = veList_.p;
+        a.vbOfs = vbOfs_.p;
+        a.vbList = vbList_.p;
+        a.faceDmInv = dminv_.p;
+        a.faceArea = area_.p;
+        a.bendQ = bendQ_.p;
+        a.xf = xf_.p;
+        a.cd = cd_.out();
+        a.req = req_.p;
+        a.state = state_.p;
+        a.counters = counters_.p;
+    }
+
+    void rebuild_bvh() {
+        if (cdt_.nSimV > 0) kern::k_snapshot<R><<<nblk(cdt_.nSimV, 256), 256, 0, st_>>>(a_, cdt_.nSimV, nullptr);
+        cd_.rebuild(xf_.p, st_);
+    }
+
+    // snapshot -> refit + queries -> bounds, each gated on the device flag
+    int enqueue_detection() {
+        const int ns = cdt_.nSimV;
+        kern::k_snapshot<R><<<nblk(std::max(ns, 1), 256), 256, 0, st_>>>(a_, ns, req_.p);
+        cd_.enqueue_detect(xf_.p, float(sc_.p.maxQueryDis), req_.p, st_);
+        kern::k_bounds<R><<<nblk(std::max(ns, 1), 256), 256, 0, st_>>>(a_, c_, req_.p);
+        return 9;
+    }
+
+    // One substep: the iteration loop of runStep_CDEveryIter, captured once.
+    void capture() {
+        const PhysicsParams& p = sc_.p;
+        const int ns = cdt_.nSimV;
+        const int B = p.blockSize;
+        CL_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+        int launches = 0;
+        R omega = R(1);
+        for (int it = 0; it < p.iterations; ++it) {
+            if (it == 0) {
+                kern::k_reset_active<R><<<nblk(std::max(ns, 1), 256), 256, 0, st_>>>(a_, ns);
+                ++launches;
+            }
+            if (p.handleCollision) {
+                if (it == 0 || p.contactDetectionEveryIteration) {
+                    kern::k_set_int<<<1, 1, 0, st_>>>(req_.p, 1);
+                    ++launches;
+                }
+                launches += enqueue_detection();
+                kern::k_set_int<<<1, 1, 0, st_>>>(req_.p, 0);
+                ++launches;
+            } else if (it == 0) {
+                kern::k_bounds_inf<R><<<nblk(std::max(ns, 1), 256), 256, 0, st_>>>(a_, ns);
+                ++launches;
+            }
+            if (p.applyAcceleration) {
+                kern::k_copy_positions<R><<<nblk(std::max(ns, 1), 256), 256, 0, st_>>>(xPrevIter_.p, x_.p, ns);
+                ++launches;
+            }
+            if (it == 0) {
+                kern::k_init_step<R><<<nblk(std::max(ns, 1), 256), 256, 0, st_>>>(a_, c_);
+                ++launches;
+            }
+            for (auto& g : groups_) {
+                const int n = int(g->n);
+                if (n == 0) continue;
+                kern::k_solve<R><<<nblk(n, B), B, 0, st_>>>(a_, c_, g->p, n);
+                kern::k_commit<R><<<nblk(n, 256), 256, 0, st_>>>(a_, g->p, n);
+                launches += 2;
+            }
+            if (p.applyAcceleration) {
+                // ChebysevAccelerator::getAcceleratorOmega (SolverUtils/ChebysevAccelerator.h:15-35)
+                const R rho = R(float(p.acceleratorRho));
+                const int order = it + 1;
+                if (rho == R(0)) omega = R(1);
+                else if (order == 1) omega = R(1);
+                else if (order == 2) omega = R(2) / (R(2) - rho * rho);
+                else omega = R(4) / (R(4) - rho * rho * omega);
+                if (omega > R(1)) {
+                    kern::k_accel<R><<<nblk(std::max(ns, 1), 256), 256, 0, st_>>>(a_, c_, omega);
+                    ++launches;
+                }
+            }
+        }
+        kern::k_velocity<R><<<nblk(std::max(ns, 1), 256), 256, 0, st_>>>(a_, c_);
+        ++launches;
+        cudaGraph_t g = nullptr;
+        CL_CUDA(cudaStreamEndCapture(st_, &g));
+        CL_CUDA(cudaGraphInstantiate(&graph_, g, 0));
+        cudaGraphDestroy(g);
+        launches_per_substep_ = launches;
+    }
+
+    Scene sc_;
+    cudaStream_t st_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    cudaGraphExec_t graph_ = nullptr;
+    int64_t frame_ = 0;
+    int launches_per_substep_ = 0;
+    size_t bytes_ = 0;
+    std::vector<int> vbase_, fbase_, ebase_, vmesh_, vlocal_, fmesh_, emesh_;
+    Buf<P4<R>> x_, xprev_, y_, xnext_, xcd_, xPrevIter_, v_, vprev_, accel_;
+    Buf<R> bound_, mass_, area_, bendQ_;
+    Buf<uint8_t> fixed_, active_;
+    Buf<int2> vInfo_, vfList_, veList_, vbList_;
+    Buf<ClothMat<R>> mats_;
+    Buf<int4> faces_, faceEdges_, edges_, edgeInfo_;
+    Buf<int> nbrVOfs_, nbrV_, vfOfs_, veOfs_, vbOfs_, req_, state_;
+    Buf<P4<R>> dminv_;
+    Buf<float4> xf_;
+    Buf<unsigned long long> counters_;
+    std::vector<std::unique_ptr<Buf<int>>> groups_;
+    CDTopo cdt_;
+    ContactDetector cd_;
+    Args<R> a_{};
+    Consts<R> c_{};
+};
+
+}  // namespace cloth
+}  // namespace gaia
+
+// ---- C ABI ---------------------------------------------------------------------
+
+struct gaia_cloth {
+    gaia::cloth::Scene scene;
+    std::unique_ptr<gaia::cloth::ClothEngineBase> eng;
+    std::string err;
+};
+
+namespace {
+
+template <typename Fn>
+int cguard(gaia_cloth* h, Fn&& fn) {
+    try {
+        fn();
+        if (h) h->err.clear();
+        return GAIA_VBD_OK;
+    } catch (const gaia::cloth::CudaError& e) {
+        if (h) h->err = e.what();
+        gaia::set_last_global_error(e.what());
+        return GAIA_VBD_E_CUDA;
+    } catch (const std::invalid_argument& e) {
+        if (h) h->err = e.what();
+        gaia::set_last_global_error(e.what());
+        return GAIA_VBD_E_INVALID_ARG;
+    } catch (const std::domain_error& e) {
+        if (h) h->err = e.what();
+        gaia::set_last_global_error(e.what());
+        return GAIA_VBD_E_NONFINITE;
+    } catch (const std::exception& e) {
+        if (h) h->err = e.what();
+        gaia::set_last_global_error(e.what());
+        std::string m = e.what();
+        if (m.find("coloring") != std::string::npos) return GAIA_VBD_E_COLORING;
+        if (m.find("degenerate") != std::string::npos || m.find("out of range") != std::string::npos ||
+            m.find("manifold") != std::string::npos || m.find("oriented") != std::string::npos)
+            return GAIA_VBD_E_MESH;
+        if (m.find("not supported") != std::string::npos || m.find("only static") != std::string::npos ||
+            m.find("not part of") != std::string::npos)
+            return GAIA_VBD_E_UNSUPPORTED;
+        return GAIA_VBD_E_INPUT;
+    }
+}
+
+bool mesh_ok(gaia_cloth* h, int32_t mesh) {
+    return h && h->eng && mesh >= 0 && size_t(mesh) < h->scene.meshes.size();
+}
+
+}  // namespace
+
+extern "C" {
+
+int gaia_cloth_load(const char* models_json, const char* params_json, const char* repo_root, gaia_cloth** out) {
+    if (!out || !models_json || !params_json) return GAIA_VBD_E_INVALID_ARG;
+    *out = nullptr;
+    std::unique_ptr<gaia_cloth> h(new gaia_cloth());
+    int rc = cguard(nullptr, [&] {
+        gaia::cloth::load_scene(models_json, params_json, repo_root ? repo_root : "", h->scene);
+    });
+    if (rc) return rc;
+    *out = h.release();
+    return GAIA_VBD_OK;
+}
+
+int gaia_cloth_initialize(gaia_cloth* h) {
+    if (!h) return GAIA_VBD_E_INVALID_ARG;
+    if (h->eng) return GAIA_VBD_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        h->err = "no CUDA device is visible";
+        gaia::set_last_global_error(h->err);
+        return GAIA_VBD_E_NO_DEVICE;
+    }
+    return cguard(h, [&] {
+        if (h->scene.p.gpuPrecision == "fp64") h->eng.reset(new gaia::cloth::ClothEngine<double>(h->scene));
+        else h->eng.reset(new gaia::cloth::ClothEngine<float>(h->scene));
+    });
+}
+
+int gaia_cloth_create(const char* models_json, const char* params_json, const char* repo_root, gaia_cloth** out) {
+    gaia_cloth* h = nullptr;
+    int rc = gaia_cloth_load(models_json, params_json, repo_root, &h);
+    if (rc) return rc;
+    rc = gaia_cloth_initialize(h);
+    if (rc) {
+        gaia::set_last_global_error(h->err);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GAIA_VBD_OK;
+}
+
+void gaia_cloth_destroy(gaia_cloth* h) { delete h; }
+
+const char* gaia_cloth_last_error(gaia_cloth* h) { return h ? h->err.c_str() : ""; }
+
+int gaia_cloth_run_step(gaia_cloth* h, int32_t n) {
+    if (!h || !h->eng || n < 0) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->run_steps(n); });
+}
+
+int gaia_cloth_run_step_timed(gaia_cloth* h, int32_t n, float* total_ms) {
+    if (!h || !h->eng || n < 0) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] {
+        float ms = h->eng->run_steps_timed(n);
+        if (total_ms) *total_ms = ms;
+    });
+}
+
+int gaia_cloth_synchronize(gaia_cloth* h) {
+    if (!h || !h->eng) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->sync(); });
+}
+
+int gaia_cloth_num_meshes(gaia_cloth* h, int32_t* num_sim, int32_t* num_colliders) {
+    if (!h) return GAIA_VBD_E_INVALID_ARG;
+    if (num_sim) *num_sim = h->scene.numSim;
+    if (num_colliders) *num_colliders = int32_t(h->scene.meshes.size()) - h->scene.numSim;
+    return GAIA_VBD_OK;
+}
+
+int64_t gaia_cloth_num_vertices(gaia_cloth* h, int32_t mesh) {
+    return (h && mesh >= 0 && size_t(mesh) < h->scene.meshes.size()) ? h->scene.meshes[mesh].nv : -1;
+}
+int64_t gaia_cloth_num_faces(gaia_cloth* h, int32_t mesh) {
+    return (h && mesh >= 0 && size_t(mesh) < h->scene.meshes.size()) ? h->scene.meshes[mesh].nf : -1;
+}
+int64_t gaia_cloth_num_edges(gaia_cloth* h, int32_t mesh) {
+    return (h && mesh >= 0 && size_t(mesh) < h->scene.meshes.size()) ? h->scene.meshes[mesh].ne : -1;
+}
+
+int gaia_cloth_get_positions(gaia_cloth* h, int32_t mesh, double* xyz) {
+    if (!mesh_ok(h, mesh) || !xyz) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->get_positions(mesh, xyz); });
+}
+int gaia_cloth_set_positions(gaia_cloth* h, int32_t mesh, const double* xyz) {
+    if (!mesh_ok(h, mesh) || !xyz) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->set_positions(mesh, xyz); });
+}
+int gaia_cloth_get_velocities(gaia_cloth* h, int32_t mesh, double* xyz) {
+    if (!mesh_ok(h, mesh) || !xyz) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->get_velocities(mesh, xyz); });
+}
+int gaia_cloth_set_velocities(gaia_cloth* h, int32_t mesh, const double* xyz) {
+    if (!mesh_ok(h, mesh) || !xyz) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->set_velocities(mesh, xyz); });
+}
+
+int gaia_cloth_get_topology(gaia_cloth* h, int32_t mesh, int32_t* edges6, int32_t* face_edges3) {
+    if (!h || mesh < 0 || size_t(mesh) >= h->scene.meshes.size()) return GAIA_VBD_E_INVALID_ARG;
+    const gaia::cloth::TriMesh& m = h->scene.meshes[mesh];
+    if (edges6)
+        for (int e = 0; e < m.ne; ++e) {
+            const gaia::cloth::Edge& E = m.edges[e];
+            int32_t* r = edges6 + 6 * size_t(e);
+            r[0] = E.v1;
+            r[1] = E.v2;
+            r[2] = E.v12next;
+            r[3] = E.v21next;
+            r[4] = E.f1;
+            r[5] = E.f2;
+        }
+    if (face_edges3) std::memcpy(face_edges3, m.faceEdges.data(), m.faceEdges.size() * sizeof(int32_t));
+    return GAIA_VBD_OK;
+}
+
+int gaia_cloth_get_rest_shape(gaia_cloth* h, int32_t mesh, double* dminv4, double* area, double* mass) {
+    if (!h || mesh < 0 || mesh >= h->scene.numSim) return GAIA_VBD_E_INVALID_ARG;
+    const gaia::cloth::TriMesh& m = h->scene.meshes[mesh];
+    if (dminv4) std::memcpy(dminv4, m.dminv.data(), m.dminv.size() * sizeof(double));
+    if (area) std::memcpy(area, m.area.data(), m.area.size() * sizeof(double));
+    if (mass) std::memcpy(mass, m.mass.data(), m.mass.size() * sizeof(double));
+    return GAIA_VBD_OK;
+}
+
+int gaia_cloth_num_groups(gaia_cloth* h) { return h ? int(h->scene.groups.size()) : -1; }
+
+int64_t gaia_cloth_group_size(gaia_cloth* h, int32_t g) {
+    if (!h || g < 0 || size_t(g) >= h->scene.groups.size()) return -1;
+    return int64_t(h->scene.groups[g].size() / 2);
+}
+
+int gaia_cloth_get_group(gaia_cloth* h, int32_t g, int32_t* pairs) {
+    if (!h || !pairs || g < 0 || size_t(g) >= h->scene.groups.size()) return GAIA_VBD_E_INVALID_ARG;
+    std::memcpy(pairs, h->scene.groups[g].data(), h->scene.groups[g].size() * sizeof(int32_t));
+    return GAIA_VBD_OK;
+}
+
+int gaia_cloth_detect(gaia_cloth* h) {
+    if (!h || !h->eng) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->detect(); });
+}
+
+int gaia_cloth_get_vf_contacts(gaia_cloth* h, int32_t* rows4, int64_t cap, int64_t* n) {
+    if (!h || !h->eng || !n || cap < 0 || (cap > 0 && !rows4)) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] {
+        std::vector<int32_t> r;
+        h->eng->vf_contacts(r);
+        *n = int64_t(r.size() / 4);
+        std::memcpy(rows4, r.data(), size_t(std::min<int64_t>(cap, *n)) * 4 * sizeof(int32_t));
+    });
+}
+
+int gaia_cloth_get_ee_contacts(gaia_cloth* h, int32_t* rows4, int64_t cap, int64_t* n) {
+    if (!h || !h->eng || !n || cap < 0 || (cap > 0 && !rows4)) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] {
+        std::vector<int32_t> r;
+        h->eng->ee_contacts(r);
+        *n = int64_t(r.size() / 4);
+        std::memcpy(rows4, r.data(), size_t(std::min<int64_t>(cap, *n)) * 4 * sizeof(int32_t));
+    });
+}
+
+int gaia_cloth_get_bounds(gaia_cloth* h, int32_t mesh, double* bounds) {
+    if (!mesh_ok(h, mesh) || !bounds) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->bounds(mesh, bounds); });
+}
+
+int gaia_cloth_get_min_distances(gaia_cloth* h, int32_t mesh, float* vertex_face, float* face_vertex, float* edge_edge) {
+    if (!mesh_ok(h, mesh)) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->min_distances(mesh, vertex_face, face_vertex, edge_edge); });
+}
+
+int gaia_cloth_vertex_force_hessian(gaia_cloth* h, int32_t mesh, int32_t v, double* f3, double* h9) {
+    if (!h || !h->eng || !f3 || !h9) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->vertex_force_hessian(mesh, v, f3, h9); });
+}
+
+int gaia_cloth_time_solve(gaia_cloth* h, int32_t reps, float* ms_per_sweep) {
+    if (!h || !h->eng || !ms_per_sweep || reps <= 0) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { *ms_per_sweep = h->eng->time_solve(reps); });
+}
+
+int gaia_cloth_get_stats(gaia_cloth* h, gaia_cloth_stats* out) {
+    if (!h || !h->eng || !out) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->stats(out); });
+}
+
+static int32_t color_tri(int32_t nv, int32_t nf, const int32_t* faces, int32_t bending, int32_t* colors, bool mcs) {
+    if (nv <= 0 || nf < 0 || !faces || !colors) return -1;
+    try {
+        gaia::cloth::TriMesh m;
+        m.X.assign(3 * size_t(nv), 0.f);
+        m.faces.assign(faces, faces + 3 * size_t(nf));
+        for (int32_t v : m.faces)
+            if (v < 0 || v >= nv) return -1;
+        gaia::cloth::build_topology(m);
+        std::vector<int64_t> ofs;
+        std::vector<int32_t> adj;
+        gaia::cloth::tri_vertex_graph(m, bending != 0, ofs, adj);
+        return mcs ? gaia::color_mcs_graph(nv, ofs, adj, colors) : gaia::color_greedy_graph(nv, ofs, adj, colors);
+    } catch (const std::exception& e) {
+        gaia::set_last_global_error(e.what());
+        return -1;
+    }
+}
+
+int32_t gaia_cloth_color_greedy(int32_t nv, int32_t nf, const int32_t* faces, int32_t bending, int32_t* colors) {
+    return color_tri(nv, nf, faces, bending, colors, false);
+}
+
+int32_t gaia_cloth_color_mcs(int32_t nv, int32_t nf, const int32_t* faces, int32_t bending, int32_t* colors) {
+    return color_tri(nv, nf, faces, bending, colors, true);
+}
+
+}  // extern "C"

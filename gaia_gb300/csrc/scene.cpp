@@ -11,69 +11,14 @@
 #include <sstream>
 #include <stdexcept>
 
+#include "json_get.hpp"
 #include "json_lite.hpp"
 
 namespace gaia {
 
 namespace {
 
-std::string read_file(const std::string& path) {
-    std::ifstream f(path, std::ios::binary);
-    if (!f) throw std::runtime_error("cannot open file: " + path);
-    std::ostringstream ss;
-    ss << f.rdbuf();
-    return ss.str();
-}
-
-std::string replace_all(std::string s, const std::string& from, const std::string& to) {
-    if (from.empty()) return s;
-    size_t pos = 0;
-    while ((pos = s.find(from, pos)) != std::string::npos) {
-        s.replace(pos, from.size(), to);
-        pos += to.size();
-    }
-    return s;
-}
-
-// EXTRACT_FROM_JSON semantics: read the key if present, keep the default otherwise.
-void get(const json::Value& o, const char* k, double& out) {
-    if (auto* v = o.find(k)) {
-        if (v->type == json::Value::Number) out = v->num;
-        else if (v->type == json::Value::Bool) out = v->b ? 1.0 : 0.0;
-        else throw std::runtime_error(std::string("key '") + k + "' is not a number");
-    }
-}
-void get(const json::Value& o, const char* k, int& out) {
-    double d = out;
-    get(o, k, d);
-    out = int(d);
-}
-void get(const json::Value& o, const char* k, bool& out) {
-    if (auto* v = o.find(k)) {
-        if (v->type == json::Value::Bool) out = v->b;
-        else if (v->type == json::Value::Number) out = v->num != 0.0;
-        else throw std::runtime_error(std::string("key '") + k + "' is not a bool");
-    }
-}
-void get(const json::Value& o, const char* k, std::string& out) {
-    if (auto* v = o.find(k)) {
-        if (v->type == json::Value::String) out = v->str;
-        else throw std::runtime_error(std::string("key '") + k + "' is not a string");
-    }
-}
-void get3(const json::Value& o, const char* k, double* out) {
-    if (auto* v = o.find(k)) {
-        if (!v->is_array() || v->arr.size() != 3) throw std::runtime_error(std::string("key '") + k + "' is not a 3-vector");
-        for (int i = 0; i < 3; ++i) out[i] = v->arr[i].num;
-    }
-}
-void get_ints(const json::Value& o, const char* k, std::vector<int32_t>& out) {
-    if (auto* v = o.find(k)) {
-        if (!v->is_array()) throw std::runtime_error(std::string("key '") + k + "' is not an array");
-        out.clear();
-        for (auto& e : v->arr) out.push_back(int32_t(e.num));
-    }
-}
+using namespace jsonio;
 
 // Vertex graph of a tet mesh as CSR with sorted unique neighbours
 // (GraphColoring/TetMeshVertexGraph.h:14-41: all vertex pairs sharing a tet).
@@ -132,6 +77,10 @@ int32_t color_mcs(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors
     std::vector<int64_t> ofs;
     std::vector<int32_t> adj;
     vertex_graph(nv, ntet, tets, ofs, adj);
+    return color_mcs_graph(nv, ofs, adj, colors);
+}
+
+int32_t color_mcs_graph(int32_t nv, const std::vector<int64_t>& ofs, const std::vector<int32_t>& adj, int32_t* colors) {
     std::vector<int32_t> weight(nv, 0), order;
     std::vector<uint8_t> done(nv, 0);
     order.reserve(nv);
@@ -170,6 +119,10 @@ int32_t color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* col
     std::vector<int64_t> ofs;
     std::vector<int32_t> adj;
     vertex_graph(nv, ntet, tets, ofs, adj);
+    return color_greedy_graph(nv, ofs, adj, colors);
+}
+
+int32_t color_greedy_graph(int32_t nv, const std::vector<int64_t>& ofs, const std::vector<int32_t>& adj, int32_t* colors) {
     std::vector<int32_t> deg(nv);
     using E = std::pair<int32_t, int32_t>;  // (degree, index), min-heap
     std::priority_queue<E, std::vector<E>, std::greater<E>> pq;

@@ -119,6 +119,10 @@ void validate_coloring(const TetMesh& m);  // every vertex exactly once; no two 
 // Colorings (bit-exact with GraphColoring/mcs.cpp and gready.cpp, in O(E log V)).
 int32_t color_mcs(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
 int32_t color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
+// The same two algorithms on a vertex graph given as CSR with sorted unique
+// neighbours (ofs has nv + 1 entries).
+int32_t color_mcs_graph(int32_t nv, const std::vector<int64_t>& ofs, const std::vector<int32_t>& adj, int32_t* colors);
+int32_t color_greedy_graph(int32_t nv, const std::vector<int64_t>& ofs, const std::vector<int32_t>& adj, int32_t* colors);
 std::vector<std::vector<int32_t>> colors_to_categories(int32_t nv, const int32_t* colors);
 
 void write_t(const std::string& path, int32_t nv, const double* X, int32_t ntet, const int32_t* tets);

@@ -220,3 +220,119 @@ def set_precision(params_json: str, precision: str, out_path: str | None = None,
     with open(out, "w") as f:
         json.dump(P, f, indent=1)
     return out
+
+
+# ---------------------------------------------------------------- cloth scenes
+def write_obj(path: str, X: np.ndarray, faces: np.ndarray) -> None:
+    """Wavefront .obj with 1-based faces (the reference's cloth and collider format)."""
+    with open(path, "w") as f:
+        for x in np.asarray(X, np.float64):
+            f.write(f"v {x[0]:.9g} {x[1]:.9g} {x[2]:.9g}\n")
+        for t in np.asarray(faces, np.int64):
+            f.write(f"f {t[0] + 1} {t[1] + 1} {t[2] + 1}\n")
+
+
+def cloth_grid(n: int, side: float = 1.0, height: float = 0.0, noise: float = 0.0, seed: int = 1):
+    """A square cloth of n x n vertices in the xz plane at y = height, centred on the y
+    axis; each cell split into two triangles along alternating diagonals, faces wound
+    so their normals point up (+y). Vertex (i, j) has index i + n * j. Heights get
+    U(-noise, +noise) from numpy's PCG64 with `seed`."""
+    h = side / (n - 1)
+    i, j = np.meshgrid(np.arange(n), np.arange(n), indexing="xy")
+    X = np.stack([i.ravel() * h - 0.5 * side, np.full(n * n, height), j.ravel() * h - 0.5 * side], 1)
+    if noise > 0:
+        rng = np.random.Generator(np.random.PCG64(seed))
+        X[:, 1] += rng.uniform(-noise, noise, size=n * n)
+    ci, cj = np.meshgrid(np.arange(n - 1), np.arange(n - 1), indexing="xy")
+    ci, cj = ci.ravel(), cj.ravel()
+    a = ci + n * cj
+    b = a + 1
+    c = a + n
+    d = c + 1
+    even = ((ci + cj) & 1) == 0
+    # winding (a, c, b) has normal +y for this layout (x right, z down the rows)
+    t1 = np.where(even[:, None], np.stack([a, c, d], 1), np.stack([a, c, b], 1))
+    t2 = np.where(even[:, None], np.stack([a, d, b], 1), np.stack([b, c, d], 1))
+    F = np.concatenate([t1, t2], 0).astype(np.int32)
+    return X, F
+
+
+def icosphere(level: int, radius: float = 1.0, center=(0.0, 0.0, 0.0)):
+    """Subdivided icosahedron with outward-wound faces."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    V = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    V = [np.asarray(v, np.float64) / np.linalg.norm(v) for v in V]
+    F = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+         (8, 6, 7), (9, 8, 1)]
+    for _ in range(level):
+        cache = {}
+
+        def mid(a, b):
+            k = (min(a, b), max(a, b))
+            if k not in cache:
+                m = V[a] + V[b]
+                V.append(m / np.linalg.norm(m))
+                cache[k] = len(V) - 1
+            return cache[k]
+
+        F2 = []
+        for a, b, c in F:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            F2 += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        F = F2
+    X = np.asarray(V) * radius + np.asarray(center, np.float64)
+    return X, np.asarray(F, np.int32)
+
+
+def cloth_params(timeStep: float, iterations: int, contact_radius: float, max_query: float,
+                 contact_stiffness: float = 1e5, gravity=(0.0, -9.8, 0.0), precision: str = "fp32", **extra) -> dict:
+    p = {
+        "timeStep": timeStep, "numSubsteps": 1, "iterations": iterations, "gravity": list(gravity),
+        "worldBounds": [[-1e7, -1e7, -1e7], [1e7, 1e7, 1e7]], "boundaryFrictionDynamic": 0.1,
+        "handleCollision": True, "contactStiffness": contact_stiffness, "contactRadius": contact_radius,
+        "thickness": 0.0, "conservativeStepRelaxation": 0.45, "useNewton": False, "useLineSearch": False,
+        "evaluateConvergence": False, "gpuPrecision": precision, "saveOutputs": False,
+    }
+    p.update(extra)
+    return p
+
+
+def cloth_on_sphere(dirname: str, n: int = 512, side: float = 1.0, sphere_radius: float = 0.3, sphere_level: int = 5,
+                    gap: float = 0.01, iterations: int = 20, dt: float = 1.0 / 600.0, contact_radius: float = 2e-3,
+                    max_query: float | None = None, noise: float = 1e-3, seed: int = 1, precision: str = "fp32",
+                    mu: float = 1e4, lmbd: float = 1e4, bending: float = 1e-5, density: float = 0.2,
+                    contact_stiffness: float = 1e5, friction: float = 0.1, init_type: int = 2,
+                    **param_overrides) -> tuple[str, str]:
+    """Cloth drape: an n x n vertex cloth (`side` metres, StVK mu/lambda, quadratic bending,
+    areal density) `gap` above a static icosphere collider of `sphere_radius` centred at the
+    origin; heights jittered by U(+-noise) (PCG64, `seed`); self and cloth-sphere VF/EE
+    contact at `contact_radius`, query radius `max_query` (default 1.5 x contact radius)."""
+    os.makedirs(dirname, exist_ok=True)
+    X, F = cloth_grid(n, side, sphere_radius + gap, noise, seed)
+    cpath = os.path.join(dirname, f"cloth{n}.obj")
+    write_obj(cpath, X, F)
+    from .cloth import color_trimesh
+    from .physics import write_coloring
+    colpath = cpath + ".vertexColoring.json"
+    write_coloring(colpath, color_trimesh(len(X), F, "greedy"))
+    SX, SF = icosphere(sphere_level, sphere_radius)
+    spath = os.path.join(dirname, f"sphere{sphere_level}.obj")
+    write_obj(spath, SX, SF)
+    model = {"path": cpath, "verticesColoringCategoriesPath": colpath, "materialName": "StVK_triMesh",
+             "miu": mu, "lambda": lmbd, "bendingStiffness": bending, "density": density, "frictionDynamic": friction,
+             "frictionEpsV": 0.01, "initializationType": init_type, "fixedPoints": []}
+    mq = max_query if max_query is not None else 1.5 * contact_radius
+    params = cloth_params(dt, iterations, contact_radius, mq, contact_stiffness, precision=precision, **param_overrides)
+    mp = os.path.join(dirname, "Models.json")
+    pp = os.path.join(dirname, "Parameters.json")
+    with open(mp, "w") as f:
+        json.dump({"Models": [model]}, f, indent=1)
+    P = {"PhysicsParams": params, "ContactDetectorParams": {"maxQueryDis": mq},
+         "ColliderParams": {"ColliderMeshes": [{"colliderType": "TriMeshSequence", "meshFiles": [spath],
+                                                "frictionDynamic": friction, "frictionEpsV": 0.01}]},
+         "SceneInfo": {"workload": f"cloth_on_sphere_{n}", "seed": seed}}
+    with open(pp, "w") as f:
+        json.dump(P, f, indent=1)
+    return mp, pp

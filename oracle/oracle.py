@@ -20,8 +20,8 @@ _LIB = os.path.join(_HERE, "liboracle.so")
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (g++, no GPU needed)."""
-    src = os.path.join(_HERE, "vbd_oracle.cpp")
-    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("vbd_oracle.cpp", "vbd_oracle.h", "cloth_oracle.cpp", "cloth_oracle.h")]
+    if force or not os.path.exists(_LIB) or any(os.path.getmtime(_LIB) < os.path.getmtime(s) for s in srcs):
         subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
     return _LIB
 

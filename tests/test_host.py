@@ -12,8 +12,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _header_symbols():
-    text = open(os.path.join(ROOT, "include", "gaia_vbd.h")).read()
-    return sorted(set(re.findall(r"\b(gaia_vbd_[a-z0-9_]+)\s*\(", text)))
+    syms = set()
+    for h in ("gaia_vbd.h", "gaia_cloth.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        syms |= set(re.findall(r"\b(gaia_(?:vbd|cloth)_[a-z0-9_]+)\s*\(", text))
+    return sorted(syms)
 
 
 def test_library_exports_every_declared_symbol(gaia_lib):
