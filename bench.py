@@ -383,6 +383,8 @@ def run_cloth(args, world, rank, local):
     nv = c.numVertices(0)
     for _ in range(args.warmup):
         c.runStep(1)
+    c.autotune()  # lanes per vertex re-timed on a state with the drape's contacts
+    c.runStep(1)
     c.synchronize()
     clk = ClockSampler(local)
     clk.start()
@@ -392,6 +394,7 @@ def run_cloth(args, world, rank, local):
     total_ms = allmax(world, total_ms)
     st = c.stats()
     sweep_ms = c.time_solve(5)
+    lanes = c.groupLanes()
     alg, counts = cloth_algorithmic_bytes(c)
     # e2e through the C ABI with host buffers: per step the positions and velocities of
     # the cloth go host -> device, the step runs, positions and velocities come back
@@ -426,7 +429,8 @@ def run_cloth(args, world, rank, local):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded PCG64 height noise)",
         "config": {"workload": f"cloth_on_sphere {args.size}x{args.size} (1 m, icosphere r=0.3 collider), "
                                f"{args.iterations} iterations/step, dt=1/600, contact radius 2e-3",
-                   **counts, "colors": ngroups, "detections": st["detections"], "truncations": st["truncations"],
+                   **counts, "colors": ngroups, "lanes_per_color": lanes, "detections": st["detections"],
+                   "truncations": st["truncations"],
                    "l2": "inputs larger than L2 (per-sweep records %.0f MB)" % (alg / 1e6)},
         "e2e": {"value": solves * e2e_steps / e2e_s, "unit": "vertex-solves/s", "h2d_bytes_per_step": 48 * nv,
                 "d2h_bytes_per_step": 48 * nv, "steps": e2e_steps},

@@ -125,6 +125,8 @@ _SIGNATURES = {
     "gaia_cloth_get_stats": (C.c_int, [C.c_void_p, C.POINTER(ClothStats)]),
     "gaia_cloth_vertex_force_hessian": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "gaia_cloth_time_solve": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float)]),
+    "gaia_cloth_autotune": (C.c_int, [C.c_void_p]),
+    "gaia_cloth_get_group_lanes": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gaia_cloth_color_greedy": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
     "gaia_cloth_color_mcs": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
 }

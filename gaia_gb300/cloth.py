@@ -159,6 +159,15 @@ class VBDClothSimulationFramework:
         self._check(lib().gaia_cloth_vertex_force_hessian(self.h, mesh, v, _ptr(f), _ptr(h)))
         return f, h.reshape(3, 3)
 
+    def autotune(self) -> None:
+        """Re-time the solve's lanes per vertex per color on the current state."""
+        self._check(lib().gaia_cloth_autotune(self.h))
+
+    def groupLanes(self) -> list[int]:
+        out = np.empty(lib().gaia_cloth_num_groups(self.h), np.int32)
+        self._check(lib().gaia_cloth_get_group_lanes(self.h, _ptr(out)))
+        return out.tolist()
+
     def time_solve(self, reps: int = 5) -> float:
         """Milliseconds per sweep of the per-color solve kernels (state restored)."""
         ms = C.c_float()

@@ -120,6 +120,7 @@ struct Args {
     P4<R>* vprev;
     P4<R>* accel;
     P4<R>* xPrevIter;
+    const P4<R>* xrest;      // rest positions (the loaded, transformed mesh)
     R* bound;
     const R* mass;
     const uint8_t* fixed;
@@ -263,34 +264,151 @@ __device__ __forceinline__ bool solve_block<double>(const double* H, const doubl
     return gaia::dev::ldlt3<double>(H, b, x, 1e-12);
 }
 
-// The block solve of one vertex of a color: VBDStepWithExistingCollisions
-// (VBDClothPhysics.cpp:1026-1154) with accumlateStVKForceAndHessian
-// (VBDTriMeshStVK.cpp:721-911) in closed form, accumlateBendingForceAndHessian
-// (:913-982), accumlateBoundaryForceAndHessian (VBDClothPhysics.cpp:1401-1463) and
-// applyConservativeBoundTruncation (:1223-1246). Writes x_next.
-// Force and Hessian (sym 00 01 02 11 12 22) of vertex v at the current positions.
+// StVK membrane of one incident face: with F = [f0 f1] = Ds DmInv, G = (F^T F - I) / 2,
+// S = 2 mu G + lambda tr(G) I and m the vertex's row of dF/dx:
+//   force -= A F S m,  H += A [ (m^T S m) I + mu |m|^2 F F^T + (mu + lambda) (F m)(F m)^T ]
+// which equals the reference's 6x6 d2W/dF2 contracted with m (accumlateStVKForceAndHessian,
+// VBDTriMeshStVK.cpp:721-911, and assembleMembraneHessian, VBDBaseTriMesh.h:149-160).
+// The strain is formed from displacements u = x - X: with Ds = Dr + dU (Dr the rest edges,
+// Dr^T Dr = Dm^T Dm), G = DmInv^T (Dr^T dU + dU^T Dr + dU^T dU) DmInv / 2, so FP32 keeps
+// the strain's own digits instead of those of F^T F - I.
 template <typename R>
-__device__ void accumulate(const Args<R>& a, const Consts<R>& c, int v, R* f, R* H) {
+__device__ __forceinline__ void membrane(const Args<R>& a, const ClothMat<R>& mat, int2 fo, R* f, R* Hm) {
     using V = typename Vec<R>::T;
-    const V x = ld(a.x, v);
-    const V xp = ld(a.xprev, v);
-    const ClothMat<R> mat = a.mats[a.vInfo[v].x];
-
-    // contacts: vertex side, face side (vertices linked to the incident faces), edges
-    const int nvf = min(a.cd.vfCount[v], VF_CAP);
-    for (int k = 0; k < nvf; ++k) vf_term(a, c, v, a.cd.vfFace[size_t(v) * VF_CAP + k], 3, f, H);
-    for (int k = a.vfOfs[v]; k < a.vfOfs[v + 1]; ++k) {
-        const int2 fo = a.vfList[k];
-        const int m = min(a.cd.fvCount[fo.x], FV_CAP);
-        for (int j = 0; j < m; ++j) vf_term(a, c, a.cd.fvVert[size_t(fo.x) * FV_CAP + j], fo.x, fo.y, f, H);
+    const int4 fv = a.faces[fo.x];
+    const V x0 = ld(a.x, fv.x), x1 = ld(a.x, fv.y), x2 = ld(a.x, fv.z);
+    const V X0 = ld(a.xrest, fv.x), X1 = ld(a.xrest, fv.y), X2 = ld(a.xrest, fv.z);
+    const V u0 = sub(x0, X0);
+    const V e1 = sub(X1, X0), e2 = sub(X2, X0);                 // rest edges
+    const V w1 = sub(sub(x1, X1), u0), w2 = sub(sub(x2, X2), u0);  // edge displacements
+    const P4<R> D = a.faceDmInv[fo.x];  // m00 m10 m01 m11
+    const V d1 = add(e1, w1), d2 = add(e2, w2);
+    const V f0 = add(mul(D.x, d1), mul(D.y, d2));
+    const V f1 = add(mul(D.z, d1), mul(D.w, d2));
+    // M = Dr^T dU + dU^T Dr + dU^T dU (2x2 symmetric)
+    const R M00 = R(2) * dot(e1, w1) + dot(w1, w1);
+    const R M11 = R(2) * dot(e2, w2) + dot(w2, w2);
+    const R M01 = dot(e1, w2) + dot(w1, e2) + dot(w1, w2);
+    // G = DmInv^T M DmInv / 2
+    const R a0 = M00 * D.x + M01 * D.y, a1 = M01 * D.x + M11 * D.y;  // M * col0(DmInv)
+    const R b0 = M00 * D.z + M01 * D.w, b1 = M01 * D.z + M11 * D.w;  // M * col1(DmInv)
+    const R G00 = R(0.5) * (D.x * a0 + D.y * a1), G11 = R(0.5) * (D.z * b0 + D.w * b1);
+    const R G01 = R(0.5) * (D.x * b0 + D.y * b1);
+    const R tr = G00 + G11;
+    const R S00 = R(2) * mat.miu * G00 + mat.lambda * tr, S11 = R(2) * mat.miu * G11 + mat.lambda * tr;
+    const R S01 = R(2) * mat.miu * G01;
+    R m1, m2;
+    if (fo.y == 0) {
+        m1 = -D.x - D.y;
+        m2 = -D.z - D.w;
+    } else if (fo.y == 1) {
+        m1 = D.x;
+        m2 = D.z;
+    } else {
+        m1 = D.y;
+        m2 = D.w;
     }
-    for (int k = a.veOfs[v]; k < a.veOfs[v + 1]; ++k) {
-        const int2 eo = a.veList[k];
-        const int m = min(a.cd.eeCount[eo.x], EE_CAP);
-        for (int j = 0; j < m; ++j) ee_term(a, c, eo.x, a.cd.eeOther[size_t(eo.x) * EE_CAP + j], eo.y, f, H);
-    }
+    const R A = a.faceArea[fo.x];
+    const R Sm0 = S00 * m1 + S01 * m2, Sm1 = S01 * m1 + S11 * m2;
+    const V P = add(mul(Sm0, f0), mul(Sm1, f1));
+    f[0] -= A * P.x;
+    f[1] -= A * P.y;
+    f[2] -= A * P.z;
+    const R mSm = m1 * Sm0 + m2 * Sm1;
+    const R mm = m1 * m1 + m2 * m2;
+    const V g = add(mul(m1, f0), mul(m2, f1));
+    const R kF = A * mat.miu * mm, kg = A * (mat.miu + mat.lambda);
+    Hm[0] += A * mSm + kF * (f0.x * f0.x + f1.x * f1.x) + kg * g.x * g.x;
+    Hm[1] += kF * (f0.x * f0.y + f1.x * f1.y) + kg * g.x * g.y;
+    Hm[2] += kF * (f0.x * f0.z + f1.x * f1.z) + kg * g.x * g.z;
+    Hm[3] += A * mSm + kF * (f0.y * f0.y + f1.y * f1.y) + kg * g.y * g.y;
+    Hm[4] += kF * (f0.y * f0.z + f1.y * f1.z) + kg * g.y * g.z;
+    Hm[5] += A * mSm + kF * (f0.z * f0.z + f1.z * f1.z) + kg * g.z * g.z;
+}
 
-    // inertia (VBDBaseTriMesh.cpp:316-323)
+// Quadratic bending of one stencil (accumlateBendingForceAndHessian,
+// VBDTriMeshStVK.cpp:913-982): E = k/2 X^T Q X over its 4 vertices, Rayleigh damping.
+template <typename R>
+__device__ __forceinline__ void bending(const Args<R>& a, const Consts<R>& c, const ClothMat<R>& mat,
+                                        typename Vec<R>::T x, typename Vec<R>::T xp, int2 eo, R* f, R* H) {
+    using V = typename Vec<R>::T;
+    const int4 E = a.edges[eo.x];
+    const V X0 = ld(a.x, E.x), X1 = ld(a.x, E.y), X2 = ld(a.x, E.z), X3 = ld(a.x, E.w);
+    const V n1 = cross(sub(X1, X0), sub(X2, X0));
+    const V n2 = cross(sub(X2, X3), sub(X1, X3));
+    if (dot(n1, n1) < c.degThr2 || dot(n2, n2) < c.degThr2) return;
+    const R db = mat.dampBend / c.dt;
+    const R* Q = a.bendQ + size_t(eo.x) * 16 + 4 * eo.y;
+    const V gr = add(add(mul(Q[0], X0), mul(Q[1], X1)), add(mul(Q[2], X2), mul(Q[3], X3)));
+    const R hq = mat.kBend * Q[eo.y];
+    f[0] -= mat.kBend * gr.x + hq * (x.x - xp.x) * db;
+    f[1] -= mat.kBend * gr.y + hq * (x.y - xp.y) * db;
+    f[2] -= mat.kBend * gr.z + hq * (x.z - xp.z) * db;
+    const R hb = hq * (R(1) + db);
+    H[0] += hb;
+    H[3] += hb;
+    H[5] += hb;
+}
+
+// Lane `lane` of an L-lane group's share of vertex v's incident terms: membrane (into Hm,
+// for the Rayleigh term), bending, vertex-side VF contacts, face-side VF contacts (the
+// vertices linked to each incident face, flattened over faces) and EE contacts (flattened
+// over the incident edges). Lane k takes items k, k + L, ...
+template <int L, typename R>
+__device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, const ClothMat<R>& mat, int v, int lane,
+                                        typename Vec<R>::T x, typename Vec<R>::T xp, R* f, R* H, R* Hm) {
+    const int fa = a.vfOfs[v], nF = a.vfOfs[v + 1] - fa;
+    const int ba = a.vbOfs[v], nB = mat.kBend != R(0) ? a.vbOfs[v + 1] - ba : 0;
+    const int nVF = min(a.cd.vfCount[v], VF_CAP);
+    for (int k = lane; k < nF + nB + nVF; k += L) {
+        if (k < nF) membrane(a, mat, a.vfList[fa + k], f, Hm);
+        else if (k < nF + nB) bending(a, c, mat, x, xp, a.vbList[ba + k - nF], f, H);
+        else vf_term(a, c, v, a.cd.vfFace[size_t(v) * VF_CAP + (k - nF - nB)], 3, f, H);
+    }
+    {   // face side: items (incident face i, link j) in face order
+        int i = 0, base = 0;
+        int cnt = nF > 0 ? min(a.cd.fvCount[a.vfList[fa].x], FV_CAP) : 0;
+        for (int t = lane;; t += L) {
+            while (i < nF && t >= base + cnt) {
+                base += cnt;
+                ++i;
+                cnt = i < nF ? min(a.cd.fvCount[a.vfList[fa + i].x], FV_CAP) : 0;
+            }
+            if (i >= nF) break;
+            const int2 fo = a.vfList[fa + i];
+            vf_term(a, c, a.cd.fvVert[size_t(fo.x) * FV_CAP + (t - base)], fo.x, fo.y, f, H);
+        }
+    }
+    {   // edges: items (incident edge i, contact j) in edge order
+        const int ea = a.veOfs[v], nE = a.veOfs[v + 1] - ea;
+        int i = 0, base = 0;
+        int cnt = nE > 0 ? min(a.cd.eeCount[a.veList[ea].x], EE_CAP) : 0;
+        for (int t = lane;; t += L) {
+            while (i < nE && t >= base + cnt) {
+                base += cnt;
+                ++i;
+                cnt = i < nE ? min(a.cd.eeCount[a.veList[ea + i].x], EE_CAP) : 0;
+            }
+            if (i >= nE) break;
+            const int2 eo = a.veList[ea + i];
+            ee_term(a, c, eo.x, a.cd.eeOther[size_t(eo.x) * EE_CAP + (t - base)], eo.y, f, H);
+        }
+    }
+}
+
+// Per-vertex terms: the membrane's Rayleigh damping on its own Hessian, inertia
+// (VBDBaseTriMesh.cpp:316-323) and the world box (accumlateBoundaryForceAndHessian,
+// VBDClothPhysics.cpp:1401-1463).
+template <typename R>
+__device__ __forceinline__ void vertex_terms(const Args<R>& a, const Consts<R>& c, const ClothMat<R>& mat, int v,
+                                             typename Vec<R>::T x, typename Vec<R>::T xp, R* f, R* H, const R* Hm) {
+    using V = typename Vec<R>::T;
+    const R dmp = mat.dampStVK / c.dt;
+    const V du = sub(x, xp);
+    f[0] -= dmp * (Hm[0] * du.x + Hm[1] * du.y + Hm[2] * du.z);
+    f[1] -= dmp * (Hm[1] * du.x + Hm[3] * du.y + Hm[4] * du.z);
+    f[2] -= dmp * (Hm[2] * du.x + Hm[4] * du.y + Hm[5] * du.z);
+    for (int k = 0; k < 6; ++k) H[k] += Hm[k] * (R(1) + dmp);
     const R mh = a.mass[v] * c.dtSqrRecip;
     const V yv = ld(a.y, v);
     f[0] += mh * (yv.x - x.x);
@@ -299,120 +417,71 @@ __device__ void accumulate(const Args<R>& a, const Consts<R>& c, int v, R* f, R*
     H[0] += mh;
     H[3] += mh;
     H[5] += mh;
-
-    // StVK membrane: with F = [f0 f1] = Ds DmInv, G = (F^T F - I) / 2,
-    // S = 2 mu G + lambda tr(G) I and m the vertex's row of dF/dx:
-    //   force -= A F S m,  H += A [ (m^T S m) I + mu |m|^2 F F^T + (mu + lambda) (F m)(F m)^T ]
-    // which equals the reference's 6x6 d2W/dF2 contracted with m (assembleMembraneHessian).
-    R Hm[6] = {0, 0, 0, 0, 0, 0};
-    for (int k = a.vfOfs[v]; k < a.vfOfs[v + 1]; ++k) {
-        const int2 fo = a.vfList[k];
-        const int4 fv = a.faces[fo.x];
-        const V x0 = ld(a.x, fv.x), x1 = ld(a.x, fv.y), x2 = ld(a.x, fv.z);
-        const V d1 = sub(x1, x0), d2 = sub(x2, x0);
-        const P4<R> D = a.faceDmInv[fo.x];  // m00 m10 m01 m11
-        const V f0 = add(mul(D.x, d1), mul(D.y, d2));
-        const V f1 = add(mul(D.z, d1), mul(D.w, d2));
-        const R G00 = R(0.5) * (dot(f0, f0) - R(1)), G11 = R(0.5) * (dot(f1, f1) - R(1)), G01 = R(0.5) * dot(f0, f1);
-        const R tr = G00 + G11;
-        const R S00 = R(2) * mat.miu * G00 + mat.lambda * tr, S11 = R(2) * mat.miu * G11 + mat.lambda * tr;
-        const R S01 = R(2) * mat.miu * G01;
-        R m1, m2;
-        if (fo.y == 0) {
-            m1 = -D.x - D.y;
-            m2 = -D.z - D.w;
-        } else if (fo.y == 1) {
-            m1 = D.x;
-            m2 = D.z;
+    const R xs[3] = {x.x, x.y, x.z}, dxs[3] = {x.x - xp.x, x.y - xp.y, x.z - xp.z};
+    const int diag[3] = {0, 3, 5};
+    for (int d = 0; d < 3; ++d) {
+        R pen;
+        if (xs[d] < c.lo[d]) {
+            pen = c.lo[d] - xs[d];
+            f[d] += pen * c.kb;
+        } else if (xs[d] > c.hi[d]) {
+            pen = xs[d] - c.hi[d];
+            f[d] -= pen * c.kb;
         } else {
-            m1 = D.y;
-            m2 = D.w;
+            continue;
         }
-        const R A = a.faceArea[fo.x];
-        const R Sm0 = S00 * m1 + S01 * m2, Sm1 = S01 * m1 + S11 * m2;
-        const V P = add(mul(Sm0, f0), mul(Sm1, f1));
-        f[0] -= A * P.x;
-        f[1] -= A * P.y;
-        f[2] -= A * P.z;
-        const R mSm = m1 * Sm0 + m2 * Sm1;
-        const R mm = m1 * m1 + m2 * m2;
-        const V g = add(mul(m1, f0), mul(m2, f1));
-        const R kF = A * mat.miu * mm, kg = A * (mat.miu + mat.lambda);
-        Hm[0] += A * mSm + kF * (f0.x * f0.x + f1.x * f1.x) + kg * g.x * g.x;
-        Hm[1] += kF * (f0.x * f0.y + f1.x * f1.y) + kg * g.x * g.y;
-        Hm[2] += kF * (f0.x * f0.z + f1.x * f1.z) + kg * g.x * g.z;
-        Hm[3] += A * mSm + kF * (f0.y * f0.y + f1.y * f1.y) + kg * g.y * g.y;
-        Hm[4] += kF * (f0.y * f0.z + f1.y * f1.z) + kg * g.y * g.z;
-        Hm[5] += A * mSm + kF * (f0.z * f0.z + f1.z * f1.z) + kg * g.z * g.z;
+        H[diag[d]] += c.kb;
+        R t0[3] = {0, 0, 0}, t1[3] = {0, 0, 0};
+        const int a1 = (d + 1) % 3, a2 = (d + 2) % 3;
+        t0[a1] = R(1);
+        t1[a2] = R(1);
+        friction<R>(c.muB, pen * c.kb, t0, t1, dxs[a1], dxs[a2], c.epsUB, R(1), f, H);
     }
-    {
-        const R dmp = mat.dampStVK / c.dt;
-        const V du = sub(x, xp);
-        f[0] -= dmp * (Hm[0] * du.x + Hm[1] * du.y + Hm[2] * du.z);
-        f[1] -= dmp * (Hm[1] * du.x + Hm[3] * du.y + Hm[4] * du.z);
-        f[2] -= dmp * (Hm[2] * du.x + Hm[4] * du.y + Hm[5] * du.z);
-        for (int k = 0; k < 6; ++k) H[k] += Hm[k] * (R(1) + dmp);
-    }
-
-    // quadratic bending: E = k/2 X^T Q X over the 4 stencil vertices
-    if (mat.kBend != R(0)) {
-        const R db = mat.dampBend / c.dt;
-        for (int k = a.vbOfs[v]; k < a.vbOfs[v + 1]; ++k) {
-            const int2 eo = a.vbList[k];
-            const int4 E = a.edges[eo.x];
-            const V X0 = ld(a.x, E.x), X1 = ld(a.x, E.y), X2 = ld(a.x, E.z), X3 = ld(a.x, E.w);
-            const V n1 = cross(sub(X1, X0), sub(X2, X0));
-            const V n2 = cross(sub(X2, X3), sub(X1, X3));
-            if (dot(n1, n1) < c.degThr2 || dot(n2, n2) < c.degThr2) continue;
-            const R* Q = a.bendQ + size_t(eo.x) * 16 + 4 * eo.y;
-            const V gr = add(add(mul(Q[0], X0), mul(Q[1], X1)), add(mul(Q[2], X2), mul(Q[3], X3)));
-            const R hq = mat.kBend * Q[eo.y];
-            f[0] -= mat.kBend * gr.x + hq * (x.x - xp.x) * db;
-            f[1] -= mat.kBend * gr.y + hq * (x.y - xp.y) * db;
-            f[2] -= mat.kBend * gr.z + hq * (x.z - xp.z) * db;
-            const R hb = hq * (R(1) + db);
-            H[0] += hb;
-            H[3] += hb;
-            H[5] += hb;
-        }
-    }
-
-    // world box: penalty on each violated axis with friction in the other two
-    {
-        const R xs[3] = {x.x, x.y, x.z}, dxs[3] = {x.x - xp.x, x.y - xp.y, x.z - xp.z};
-        const int diag[3] = {0, 3, 5};
-        for (int d = 0; d < 3; ++d) {
-            R pen;
-            if (xs[d] < c.lo[d]) {
-                pen = c.lo[d] - xs[d];
-                f[d] += pen * c.kb;
-            } else if (xs[d] > c.hi[d]) {
-                pen = xs[d] - c.hi[d];
-                f[d] -= pen * c.kb;
-            } else {
-                continue;
-            }
-            H[diag[d]] += c.kb;
-            R t0[3] = {0, 0, 0}, t1[3] = {0, 0, 0};
-            const int a1 = (d + 1) % 3, a2 = (d + 2) % 3;
-            t0[a1] = R(1);
-            t1[a2] = R(1);
-            friction<R>(c.muB, pen * c.kb, t0, t1, dxs[a1], dxs[a2], c.epsUB, R(1), f, H);
-        }
-    }
-
 }
 
+// Sum over the L lanes of a group (L divides 32; groups are aligned in the warp).
+template <int L, typename R>
+__device__ __forceinline__ void group_sum(R* v, int n, unsigned mask) {
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1)
+        for (int k = 0; k < n; ++k) v[k] += __shfl_xor_sync(mask, v[k], off, L);
+}
+
+// Force and Hessian (sym 00 01 02 11 12 22) of vertex v at the current positions
+// (one thread): VBDStepWithExistingCollisions up to its solve.
 template <typename R>
+__device__ void accumulate(const Args<R>& a, const Consts<R>& c, int v, R* f, R* H) {
+    using V = typename Vec<R>::T;
+    const V x = ld(a.x, v), xp = ld(a.xprev, v);
+    const ClothMat<R> mat = a.mats[a.vInfo[v].x];
+    R Hm[6] = {0, 0, 0, 0, 0, 0};
+    partial<1, R>(a, c, mat, v, 0, x, xp, f, H, Hm);
+    vertex_terms(a, c, mat, v, x, xp, f, H, Hm);
+}
+
+// The block solve of the vertices of one color, L lanes per vertex:
+// VBDStepWithExistingCollisions (VBDClothPhysics.cpp:1026-1154) with the conservative
+// bound truncation (applyConservativeBoundTruncation, :1223-1246). Writes x_next.
+template <int L, typename R>
 __global__ void __launch_bounds__(128) k_solve(Args<R> a, Consts<R> c, const int* verts, int n) {
     using V = typename Vec<R>::T;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = gid / L, lane = gid % L;
     if (i >= n) return;
     const int v = verts[i];
     if (a.fixed[v]) return;
-    R f[3] = {0, 0, 0}, H[6] = {0, 0, 0, 0, 0, 0};
-    accumulate(a, c, v, f, H);
-    const V x = ld(a.x, v);
+    const unsigned mask = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1)));
+    const V x = ld(a.x, v), xp = ld(a.xprev, v);
+    const ClothMat<R> mat = a.mats[a.vInfo[v].x];
+    R acc[15];  // f[3], H[6], Hm[6]
+#pragma unroll
+    for (int k = 0; k < 15; ++k) acc[k] = R(0);
+    partial<L, R>(a, c, mat, v, lane, x, xp, acc, acc + 3, acc + 9);
+    if (L > 1) group_sum<L, R>(acc, 15, mask);
+    if (lane != 0) return;
+    R* f = acc;
+    R* H = acc + 3;
+    vertex_terms(a, c, mat, v, x, xp, f, H, acc + 9);
     R dx[3];
     V xn = x;
     if (solve_block<R>(H, f, dx, a.counters)) {
@@ -614,6 +683,8 @@ public:
     virtual void stats(gaia_cloth_stats* s) = 0;
     virtual void vertex_force_hessian(int mesh, int v, double* f3, double* h9) = 0;
     virtual float time_solve(int reps) = 0;
+    virtual void autotune() = 0;
+    virtual void lanes(std::vector<int>& out) const = 0;
 };
 
 template <typename R>
@@ -624,6 +695,7 @@ public:
         CL_CUDA(cudaEventCreate(&ev0_));
         CL_CUDA(cudaEventCreate(&ev1_));
         build();
+        tune_lanes();
         capture();
     }
     ~ClothEngine() override {
@@ -736,6 +808,16 @@ public:
         }
         CL_CUDA(cudaStreamSynchronize(st_));
     }
+    // Re-time the lanes per vertex of every color on the current state (its contacts
+    // detected afresh) and capture the substep graph again.
+    void autotune() override {
+        tune_lanes(true);
+        if (graph_) cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+        capture();
+    }
+    void lanes(std::vector<int>& out) const override { out = groupL_; }
+
     // Milliseconds of one sweep of the per-color solve and commit kernels over all
     // colors (CUDA events around `reps` sweeps on the current state); positions,
     // the detection flag and the counters are restored afterwards.
@@ -750,13 +832,12 @@ public:
         CL_CUDA(cudaMemcpyAsync(save.p, x_.p, x_.n * sizeof(P4<R>), cudaMemcpyDeviceToDevice, st_));
         CL_CUDA(cudaMemcpyAsync(csave.p, counters_.p, CC_N * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st_));
         CL_CUDA(cudaMemcpyAsync(rsave.p, req_.p, sizeof(int), cudaMemcpyDeviceToDevice, st_));
-        const int B = sc_.p.blockSize;
         auto sweep = [&] {
-            for (auto& g : groups_) {
-                const int n = int(g->n);
+            for (size_t gi = 0; gi < groups_.size(); ++gi) {
+                const int n = int(groups_[gi]->n);
                 if (n == 0) continue;
-                kern::k_solve<R><<<nblk(n, B), B, 0, st_>>>(a_, c_, g->p, n);
-                kern::k_commit<R><<<nblk(n, 256), 256, 0, st_>>>(a_, g->p, n);
+                launch_solve(groupL_[gi], groups_[gi]->p, n);
+                kern::k_commit<R><<<nblk(n, 256), 256, 0, st_>>>(a_, groups_[gi]->p, n);
             }
         };
         sweep();  // warm-up
@@ -967,6 +1048,7 @@ private:
         xnext_.upload(hx, tb, st_);
         xcd_.upload(hx, tb, st_);
         xPrevIter_.upload(hx, tb, st_);
+        xrest_.upload(hx, tb, st_);
         std::vector<P4<R>> zeros(nV, P4<R>{0, 0, 0, 0});
         v_.upload(zeros, tb, st_);
         vprev_.upload(zeros, tb, st_);
@@ -1034,6 +1116,7 @@ private:
         a.vprev = vprev_.p;
         a.accel = accel_.p;
         a.xPrevIter = xPrevIter_.p;
+        a.xrest = xrest_.p;
         a.bound = bound_.p;
         a.mass = mass_.p;
         a.fixed = fixed_.p;
@@ -1056,6 +1139,64 @@ private:
         a.req = req_.p;
         a.state = state_.p;
         a.counters = counters_.p;
+    }
+
+    void launch_solve(int L, const int* verts, int n) {
+        const int B = sc_.p.blockSize;
+        const int64_t threads = int64_t(n) * L;
+        switch (L) {
+            case 1: kern::k_solve<1, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 2: kern::k_solve<2, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 4: kern::k_solve<4, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 8: kern::k_solve<8, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 16: kern::k_solve<16, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 32: kern::k_solve<32, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            default: throw std::invalid_argument("lanesPerVertex must be 1, 2, 4, 8, 16 or 32");
+        }
+    }
+
+    // Lanes per vertex of each color's solve: fixed by lanesPerVertex, or the fastest of
+    // 1..32 timed on the color's kernel alone (CUDA events over repeated launches on the
+    // initial state with its contacts detected; positions and counters restored).
+    void tune_lanes(bool force = false) {
+        groupL_.assign(groups_.size(), sc_.p.lanesPerVertex > 0 ? sc_.p.lanesPerVertex : 16);
+        if ((sc_.p.lanesPerVertex > 0 && !force) || cdt_.nSimV == 0) return;
+        Buf<P4<R>> save;
+        save.alloc(x_.n, nullptr);
+        Buf<unsigned long long> csave;
+        csave.alloc(CC_N, nullptr);
+        CL_CUDA(cudaMemcpyAsync(save.p, x_.p, x_.n * sizeof(P4<R>), cudaMemcpyDeviceToDevice, st_));
+        CL_CUDA(cudaMemcpyAsync(csave.p, counters_.p, CC_N * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st_));
+        if (sc_.p.handleCollision) {
+            rebuild_bvh();
+            kern::k_set_int<<<1, 1, 0, st_>>>(req_.p, 1);
+            enqueue_detection();
+        }
+        const int Ls[] = {1, 2, 4, 8, 16, 32};
+        for (size_t gi = 0; gi < groups_.size(); ++gi) {
+            const int n = int(groups_[gi]->n);
+            if (n == 0) continue;
+            float best = 1e30f;
+            for (int L : Ls) {
+                launch_solve(L, groups_[gi]->p, n);  // warm-up
+                CL_CUDA(cudaEventRecord(ev0_, st_));
+                for (int r = 0; r < 3; ++r) launch_solve(L, groups_[gi]->p, n);
+                CL_CUDA(cudaEventRecord(ev1_, st_));
+                CL_CUDA(cudaEventSynchronize(ev1_));
+                float ms = 0.f;
+                CL_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+                if (ms < best) {
+                    best = ms;
+                    groupL_[gi] = L;
+                }
+            }
+        }
+        // back to the state before tuning (positions, counters, the detection flag); the
+        // contact sets and bounds are recomputed by the detection that opens the next step
+        CL_CUDA(cudaMemcpyAsync(x_.p, save.p, x_.n * sizeof(P4<R>), cudaMemcpyDeviceToDevice, st_));
+        CL_CUDA(cudaMemcpyAsync(counters_.p, csave.p, CC_N * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st_));
+        CL_CUDA(cudaMemsetAsync(req_.p, 0, sizeof(int), st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
     }
 
     void rebuild_bvh() {
@@ -1105,11 +1246,11 @@ private:
                 kern::k_init_step<R><<<nblk(std::max(ns, 1), 256), 256, 0, st_>>>(a_, c_);
                 ++launches;
             }
-            for (auto& g : groups_) {
-                const int n = int(g->n);
+            for (size_t gi = 0; gi < groups_.size(); ++gi) {
+                const int n = int(groups_[gi]->n);
                 if (n == 0) continue;
-                kern::k_solve<R><<<nblk(n, B), B, 0, st_>>>(a_, c_, g->p, n);
-                kern::k_commit<R><<<nblk(n, 256), 256, 0, st_>>>(a_, g->p, n);
+                launch_solve(groupL_[gi], groups_[gi]->p, n);
+                kern::k_commit<R><<<nblk(n, 256), 256, 0, st_>>>(a_, groups_[gi]->p, n);
                 launches += 2;
             }
             if (p.applyAcceleration) {
@@ -1143,7 +1284,7 @@ private:
     int launches_per_substep_ = 0;
     size_t bytes_ = 0;
     std::vector<int> vbase_, fbase_, ebase_, vmesh_, vlocal_, fmesh_, emesh_;
-    Buf<P4<R>> x_, xprev_, y_, xnext_, xcd_, xPrevIter_, v_, vprev_, accel_;
+    Buf<P4<R>> x_, xprev_, y_, xnext_, xcd_, xPrevIter_, xrest_, v_, vprev_, accel_;
     Buf<R> bound_, mass_, area_, bendQ_;
     Buf<uint8_t> fixed_, active_;
     Buf<int2> vInfo_, vfList_, veList_, vbList_;
@@ -1154,6 +1295,7 @@ private:
     Buf<float4> xf_;
     Buf<unsigned long long> counters_;
     std::vector<std::unique_ptr<Buf<int>>> groups_;
+    std::vector<int> groupL_;
     CDTopo cdt_;
     ContactDetector cd_;
     Args<R> a_{};
@@ -1390,6 +1532,20 @@ int gaia_cloth_get_min_distances(gaia_cloth* h, int32_t mesh, float* vertex_face
 int gaia_cloth_vertex_force_hessian(gaia_cloth* h, int32_t mesh, int32_t v, double* f3, double* h9) {
     if (!h || !h->eng || !f3 || !h9) return GAIA_VBD_E_INVALID_ARG;
     return cguard(h, [&] { h->eng->vertex_force_hessian(mesh, v, f3, h9); });
+}
+
+int gaia_cloth_autotune(gaia_cloth* h) {
+    if (!h || !h->eng) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { h->eng->autotune(); });
+}
+
+int gaia_cloth_get_group_lanes(gaia_cloth* h, int32_t* lanes) {
+    if (!h || !h->eng || !lanes) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] {
+        std::vector<int> L;
+        h->eng->lanes(L);
+        std::memcpy(lanes, L.data(), L.size() * sizeof(int32_t));
+    });
 }
 
 int gaia_cloth_time_solve(gaia_cloth* h, int32_t reps, float* ms_per_sweep) {

@@ -376,6 +376,7 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         get(*pp, "gpuPrecision", p.gpuPrecision);
         get(*pp, "contactDetectionEveryIteration", p.contactDetectionEveryIteration);
         get(*pp, "blockSize", p.blockSize);
+        get(*pp, "lanesPerVertex", p.lanesPerVertex);
     }
     if (const json::Value* cp = params.find("ContactDetectorParams")) get(*cp, "maxQueryDis", p.maxQueryDis);
     if (p.numSubsteps <= 0 || p.timeStep <= 0) throw std::runtime_error("timeStep and numSubsteps must be positive");
@@ -383,8 +384,11 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
     if (p.useNewton) throw std::runtime_error("useNewton = true (Newton solver) is not part of the VBD cloth step");
     if (p.gpuPrecision != "fp32" && p.gpuPrecision != "fp64")
         throw std::runtime_error("cloth gpuPrecision must be \"fp32\" or \"fp64\"");
-    if (p.blockSize < 32 || p.blockSize > 1024 || p.blockSize % 32)
-        throw std::runtime_error("blockSize must be a multiple of 32 in [32, 1024]");
+    if (p.blockSize < 32 || p.blockSize > 128 || p.blockSize % 32)
+        throw std::runtime_error("blockSize must be 32, 64, 96 or 128");
+    if (p.lanesPerVertex != 0 && p.lanesPerVertex != 1 && p.lanesPerVertex != 2 && p.lanesPerVertex != 4 &&
+        p.lanesPerVertex != 8 && p.lanesPerVertex != 16 && p.lanesPerVertex != 32)
+        throw std::runtime_error("lanesPerVertex must be 0 (autotune), 1, 2, 4, 8, 16 or 32");
     if (!(p.maxQueryDis > 0)) throw std::runtime_error("maxQueryDis must be positive");
     p.dt = p.timeStep / p.numSubsteps;
     p.dtSqrReciprocal = 1.0 / (p.dt * p.dt);

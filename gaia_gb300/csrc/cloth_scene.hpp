@@ -48,6 +48,7 @@ struct PhysicsParams {
     std::string gpuPrecision = "fp32";     // "fp32" or "fp64" (the FP64 engine is the error reference)
     bool contactDetectionEveryIteration = false;  // also run detection when no vertex was truncated
     int blockSize = 128;
+    int lanesPerVertex = 0;                // lanes per vertex of the solve; 0 = autotune per color
 };
 
 // ObjectParams (Materials/Materials.h:12-75) + TriMeshParams (TriMesh/TriMesh.h:27-50)

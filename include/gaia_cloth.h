@@ -104,6 +104,11 @@ int gaia_cloth_get_min_distances(gaia_cloth* h, int32_t mesh, float* vertex_face
  * solve (VBDClothPhysics.cpp:1026-1124). */
 int gaia_cloth_vertex_force_hessian(gaia_cloth* h, int32_t mesh, int32_t v, double* f3, double* h9);
 
+/* Re-time the lanes per vertex of every color's solve kernel on the current state and
+ * capture the substep graph again (the simulation itself is unchanged). */
+int gaia_cloth_autotune(gaia_cloth* h);
+/* Lanes per vertex of each merged color's solve (num_groups entries). */
+int gaia_cloth_get_group_lanes(gaia_cloth* h, int32_t* lanes);
 /* Milliseconds of one sweep of the per-color solve kernels over all colors, timed with
  * CUDA events over `reps` sweeps on the current state; the state is restored. For
  * roofline accounting of the solve kernel. */

@@ -5,9 +5,10 @@
   its per-primitive minimum distances and the conservative bounds equal the oracle's
   bit for bit (both evaluate the FP32 predicates in the same order without FMA).
 * Per-vertex force and Hessian (contacts with the collider and with the cloth itself,
-  inertia, membrane, bending) equal the oracle's to 1e-9 (FP64 engine) / 1e-3 of the
-  state's largest entry (FP32: the membrane strain (F^T F - I) / 2 of a nearly
-  unstretched face keeps about 4 FP32 digits, as in the reference's FP32 arithmetic).
+  inertia, membrane, bending) equal the oracle's to 1e-9 (FP64 engine) / 5e-3 of the
+  state's largest entry (FP32: a contact distance is the difference of two FP32
+  positions, so a contact force carries about k * ulp(x) = 1e5 * 7e-9 N of rounding,
+  as in the reference's FP32 arithmetic).
 * Trajectories: the FP64 engine follows the FP64 oracle to 1e-8 relative position
   error (rel = |x - x_ref| / |x_ref - x_0| over all vertices) and the FP32 engine
   to 1e-4 over the same steps. Two properties of the reference's model make
@@ -106,9 +107,9 @@ def test_contact_pairs_bit_exact(tmp_path, gaia_lib, oracle_lib):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_vertex_force_hessian(precision, tmp_path, gaia_lib, oracle_lib):
-    """Per-vertex force and Hessian (contacts, inertia, membrane, bending) in a folded,
-    jittered state full of vertex-face and edge-edge contacts: FP64 engine within 1e-10
-    of the FP64 oracle, FP32 within 1e-4 (relative to the largest entry)."""
+    """Per-vertex force and Hessian (contacts, inertia, membrane, bending) in a state draped
+    on the collider and in a folded, jittered state full of vertex-face and edge-edge
+    contacts, against the FP64 oracle (tolerances in the module docstring)."""
     from oracle import cloth as oc
 
     mp, pp = _scene(tmp_path, precision=precision)
@@ -119,7 +120,7 @@ def test_vertex_force_hessian(precision, tmp_path, gaia_lib, oracle_lib):
     draped = walk.positions(0)
     rng = np.random.Generator(np.random.PCG64(5))
     folded = _folded(x0, 0.004) + rng.uniform(-2e-3, 2e-3, size=x0.shape)
-    tol = 1e-9 if precision == "fp64" else 1e-3
+    tol = 1e-9 if precision == "fp64" else 5e-3
     for name, x in (("draped", draped), ("folded", folded)):
         o = oc.ClothOracle(sc, nthreads=4)
         c = _engine(mp, pp)
