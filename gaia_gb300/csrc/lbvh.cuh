@@ -1,0 +1,290 @@
+// Linear BVH on the GPU: 30-bit Morton codes of primitive box centres in the scene box,
+// a CUB radix sort of (code, index) keys, Karras' parallel hierarchy ("Maximizing
+// parallelism in the construction of BVHs, octrees and k-d trees", HPG 2012), a
+// bottom-up refit in which the second thread to reach a node forms its box, and a
+// stack traversal that visits every primitive whose box is within a radius of a point.
+// Used by the cloth contact detector and the tet-mesh collision detector; each
+// including translation unit gets its own copy (anonymous namespace).
+#pragma once
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <stdexcept>
+#include <string>
+
+#include "cloth_dev.cuh"
+
+namespace gaia {
+namespace bvh {
+namespace {
+
+using cloth::ld3;
+using cloth::v3;
+using cloth::CC_STACK_OVERFLOW;
+
+inline void check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define BVH_CUDA(x) ::gaia::bvh::check((x), #x)
+
+template <typename T>
+T* dalloc(size_t n, size_t& bytes) {
+    T* p = nullptr;
+    if (n == 0) n = 1;
+    BVH_CUDA(cudaMalloc(&p, n * sizeof(T)));
+    bytes += n * sizeof(T);
+    return p;
+}
+
+inline int blocks(int n, int b) { return (n + b - 1) / b; }
+
+// Order-preserving int encoding of a float (for atomicMin / atomicMax on floats).
+__device__ __forceinline__ int ford(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float fdec(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__device__ __forceinline__ unsigned int expand_bits(unsigned int v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+// Primitives: an int4 of vertex ids per primitive, of which the first k (2 = edge,
+// 3 = triangle, 4 = tet) are used.
+struct Prims {
+    const int4* idx;
+    int k;
+};
+
+__device__ __forceinline__ void prim_box(const Prims& P, const float4* xf, int p, float3& lo, float3& hi) {
+    const int4 q = P.idx[p];
+    const float3 a = ld3(xf, q.x), b = ld3(xf, q.y);
+    lo = v3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z));
+    hi = v3(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z));
+    if (P.k >= 3) {
+        const float3 c = ld3(xf, q.z);
+        lo = v3(fminf(lo.x, c.x), fminf(lo.y, c.y), fminf(lo.z, c.z));
+        hi = v3(fmaxf(hi.x, c.x), fmaxf(hi.y, c.y), fmaxf(hi.z, c.z));
+    }
+    if (P.k >= 4) {
+        const float3 d = ld3(xf, q.w);
+        lo = v3(fminf(lo.x, d.x), fminf(lo.y, d.y), fminf(lo.z, d.z));
+        hi = v3(fmaxf(hi.x, d.x), fmaxf(hi.y, d.y), fmaxf(hi.z, d.z));
+    }
+}
+
+struct MinOp {
+    __device__ __forceinline__ float operator()(float a, float b) const { return fminf(a, b); }
+};
+
+__global__ void k_centroid_bounds(Prims t, const float4* xf, int n, int* bounds) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float3 lo = v3(3.4e38f, 3.4e38f, 3.4e38f), hi = v3(-3.4e38f, -3.4e38f, -3.4e38f);
+    if (i < n) {
+        float3 a, b;
+        prim_box(t, xf, i, a, b);
+        lo = v3(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z));
+        hi = lo;
+    }
+    using BR = cub::BlockReduce<float, 256>;
+    __shared__ typename BR::TempStorage tmp;
+    float vals[6] = {lo.x, lo.y, lo.z, -hi.x, -hi.y, -hi.z};
+    for (int k = 0; k < 6; ++k) {
+        float m = BR(tmp).Reduce(vals[k], MinOp());
+        __syncthreads();
+        if (threadIdx.x == 0) atomicMin(&bounds[k], ford(m));
+    }
+}
+
+__global__ void k_bounds_init(int* bounds) {
+    if (threadIdx.x < 6) bounds[threadIdx.x] = ford(3.4e38f);
+}
+
+__global__ void k_morton(Prims t, const float4* xf, int n, const int* bounds, unsigned long long* keys) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 a, b;
+    prim_box(t, xf, i, a, b);
+    const float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
+    unsigned int code = 0;
+    for (int k = 0; k < 3; ++k) {
+        const float lo = fdec(bounds[k]), hi = -fdec(bounds[3 + k]);
+        const float ext = hi - lo;
+        float u = ext > 0.f ? (c[k] - lo) / ext : 0.f;
+        u = fminf(fmaxf(u * 1024.f, 0.f), 1023.f);
+        code |= expand_bits((unsigned int)u) << (2 - k);
+    }
+    keys[i] = (static_cast<unsigned long long>(code) << 32) | static_cast<unsigned int>(i);
+}
+
+__device__ __forceinline__ int delta(const unsigned long long* k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    return __clzll(k[i] ^ k[j]);
+}
+
+// Karras 2012, "Maximizing parallelism in the construction of BVHs, octrees and k-d
+// trees": internal node i spans a key range found by binary search; keys are unique.
+__global__ void k_karras(const unsigned long long* keys, int n, int2* child, int* parent) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int l = 0;
+    for (int s = lmax / 2; s >= 1; s /= 2)
+        if (delta(keys, n, i, i + (l + s) * d) > dmin) l += s;
+    const int j = i + l * d;
+    const int dnode = delta(keys, n, i, j);
+    int s = 0, tt = l;
+    do {
+        tt = (tt + 1) >> 1;
+        if (delta(keys, n, i, i + (s + tt) * d) > dnode) s += tt;
+    } while (tt > 1);
+    const int gamma = i + s * d + min(d, 0);
+    const int left = (min(i, j) == gamma) ? (n - 1) + gamma : gamma;
+    const int right = (max(i, j) == gamma + 1) ? (n - 1) + gamma + 1 : gamma + 1;
+    child[i] = make_int2(left, right);
+    parent[left] = i;
+    parent[right] = i;
+    if (i == 0) parent[0] = -1;
+}
+
+// Leaf boxes from the current positions, then bottom-up unions: the second thread to
+// reach an internal node computes its box (the first returns) and resets its flag.
+__global__ void k_refit(Prims t, const float4* xf, int n, const unsigned long long* keys, const int2* child,
+                        const int* parent, float4* bmin, float4* bmax, int* flags, const int* req) {
+    if (req && *req == 0) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int node = (n - 1) + i;
+    float3 lo, hi;
+    prim_box(t, xf, int(keys[i] & 0xffffffffull), lo, hi);
+    bmin[node] = make_float4(lo.x, lo.y, lo.z, 0.f);
+    bmax[node] = make_float4(hi.x, hi.y, hi.z, 0.f);
+    if (n == 1) return;
+    __threadfence();
+    int p = parent[node];
+    while (p >= 0) {
+        if (atomicAdd(&flags[p], 1) == 0) return;
+        flags[p] = 0;
+        __threadfence();
+        const int2 c = child[p];
+        const float4 l0 = __ldcg(&bmin[c.x]), l1 = __ldcg(&bmax[c.x]);
+        const float4 r0 = __ldcg(&bmin[c.y]), r1 = __ldcg(&bmax[c.y]);
+        bmin[p] = make_float4(fminf(l0.x, r0.x), fminf(l0.y, r0.y), fminf(l0.z, r0.z), 0.f);
+        bmax[p] = make_float4(fmaxf(l1.x, r1.x), fmaxf(l1.y, r1.y), fmaxf(l1.z, r1.z), 0.f);
+        __threadfence();
+        p = parent[p];
+    }
+}
+
+struct LbvhDev {
+    int n;
+    const unsigned long long* keys;
+    const int2* child;
+    const float4* bmin;
+    const float4* bmax;
+};
+
+__device__ __forceinline__ bool sphere_box(float3 p, float r2, float4 lo, float4 hi) {
+    const float dx = fmaxf(fmaxf(lo.x - p.x, 0.f), p.x - hi.x);
+    const float dy = fmaxf(fmaxf(lo.y - p.y, 0.f), p.y - hi.y);
+    const float dz = fmaxf(fmaxf(lo.z - p.z, 0.f), p.z - hi.z);
+    return dx * dx + dy * dy + dz * dz <= r2;
+}
+
+// Visits every primitive whose box is within sqrt(r2) of p (stack traversal).
+template <typename F>
+__device__ __forceinline__ void traverse(const LbvhDev& b, float3 p, float r2, unsigned long long* counters, F&& leaf) {
+    if (b.n <= 0) return;
+    int stack[64];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const int node = stack[--sp];
+        if (!sphere_box(p, r2, b.bmin[node], b.bmax[node])) continue;
+        if (node >= b.n - 1) {
+            leaf(int(b.keys[node - (b.n - 1)] & 0xffffffffull));
+        } else {
+            if (sp + 2 > 64) {
+                atomicAdd(&counters[CC_STACK_OVERFLOW], 1ull);
+                continue;
+            }
+            const int2 c = b.child[node];
+            stack[sp++] = c.y;
+            stack[sp++] = c.x;
+        }
+    }
+}
+
+class Lbvh {
+public:
+    int n = 0;
+    Prims prims{nullptr, 0};
+    unsigned long long* keys = nullptr;
+    unsigned long long* keysTmp = nullptr;
+    int2* child = nullptr;
+    int* parent = nullptr;
+    float4* bmin = nullptr;
+    float4* bmax = nullptr;
+    int* flags = nullptr;
+    int* bounds = nullptr;
+    void* temp = nullptr;
+    size_t tempBytes = 0;
+
+    void alloc(int n_, Prims p, size_t& bytes) {
+        n = n_;
+        prims = p;
+        if (n == 0) return;
+        keys = dalloc<unsigned long long>(n, bytes);
+        keysTmp = dalloc<unsigned long long>(n, bytes);
+        child = dalloc<int2>(std::max(n - 1, 1), bytes);
+        parent = dalloc<int>(2 * n - 1, bytes);
+        bmin = dalloc<float4>(2 * n - 1, bytes);
+        bmax = dalloc<float4>(2 * n - 1, bytes);
+        flags = dalloc<int>(std::max(n - 1, 1), bytes);
+        bounds = dalloc<int>(6, bytes);
+        BVH_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, tempBytes, keysTmp, keys, n, 0, 62));
+        temp = dalloc<char>(tempBytes, bytes);
+        BVH_CUDA(cudaMemset(flags, 0, sizeof(int) * std::max(n - 1, 1)));
+        BVH_CUDA(cudaMemset(parent, 0xff, sizeof(int) * (2 * n - 1)));
+    }
+    void release() {
+        for (void* p : {(void*)keys, (void*)keysTmp, (void*)child, (void*)parent, (void*)bmin, (void*)bmax,
+                        (void*)flags, (void*)bounds, temp})
+            if (p) cudaFree(p);
+        keys = keysTmp = nullptr;
+        child = nullptr;
+        parent = flags = bounds = nullptr;
+        bmin = bmax = nullptr;
+        temp = nullptr;
+    }
+    // Morton codes of the primitive box centres, sorted (code, index) keys, hierarchy, boxes.
+    void build(const float4* xf, cudaStream_t st) {
+        if (n == 0) return;
+        k_bounds_init<<<1, 32, 0, st>>>(bounds);
+        k_centroid_bounds<<<blocks(n, 256), 256, 0, st>>>(prims, xf, n, bounds);
+        k_morton<<<blocks(n, 256), 256, 0, st>>>(prims, xf, n, bounds, keysTmp);
+        size_t tb = tempBytes;
+        BVH_CUDA(cub::DeviceRadixSort::SortKeys(temp, tb, keysTmp, keys, n, 0, 62, st));
+        if (n > 1) k_karras<<<blocks(n - 1, 256), 256, 0, st>>>(keys, n, child, parent);
+        refit(xf, nullptr, st);
+        BVH_CUDA(cudaGetLastError());
+    }
+    // Boxes from the current positions (when *req != 0, or always when req is null).
+    void refit(const float4* xf, const int* req, cudaStream_t st) {
+        if (n == 0) return;
+        k_refit<<<blocks(n, 256), 256, 0, st>>>(prims, xf, n, keys, child, parent, bmin, bmax, flags, req);
+    }
+    LbvhDev dev() const { return LbvhDev{n, keys, child, bmin, bmax}; }
+};
+
+
+}  // namespace
+}  // namespace bvh
+}  // namespace gaia
