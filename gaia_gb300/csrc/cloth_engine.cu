@@ -1177,19 +1177,20 @@ private:
             const int n = int(groups_[gi]->n);
             if (n == 0) continue;
             float best = 1e30f;
-            for (int L : Ls) {
-                launch_solve(L, groups_[gi]->p, n);  // warm-up
-                CL_CUDA(cudaEventRecord(ev0_, st_));
-                for (int r = 0; r < 3; ++r) launch_solve(L, groups_[gi]->p, n);
-                CL_CUDA(cudaEventRecord(ev1_, st_));
-                CL_CUDA(cudaEventSynchronize(ev1_));
-                float ms = 0.f;
-                CL_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
-                if (ms < best) {
-                    best = ms;
-                    groupL_[gi] = L;
+            for (int round = 0; round < 2; ++round)  // two interleaved rounds, best of both
+                for (int L : Ls) {
+                    launch_solve(L, groups_[gi]->p, n);  // warm-up
+                    CL_CUDA(cudaEventRecord(ev0_, st_));
+                    for (int r = 0; r < 4; ++r) launch_solve(L, groups_[gi]->p, n);
+                    CL_CUDA(cudaEventRecord(ev1_, st_));
+                    CL_CUDA(cudaEventSynchronize(ev1_));
+                    float ms = 0.f;
+                    CL_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
+                    if (ms < best) {
+                        best = ms;
+                        groupL_[gi] = L;
+                    }
                 }
-            }
         }
         // back to the state before tuning (positions, counters, the detection flag); the
         // contact sets and bounds are recomputed by the detection that opens the next step
