@@ -59,6 +59,13 @@ class VBDClothSimulationFramework:
     def synchronize(self) -> None:
         self._check(lib().gaia_cloth_synchronize(self.h))
 
+    # ---- PhysicsState recovery files (Framework/BasePhysicsFramework.h:127-319) -------
+    def saveState(self, path: str, binary: bool = False) -> None:
+        self._check(lib().gaia_cloth_save_state(self.h, path.encode(), int(binary)))
+
+    def recoverFromState(self, path: str) -> None:
+        self._check(lib().gaia_cloth_load_state(self.h, path.encode()))
+
     def run_steps_timed(self, n: int) -> float:
         ms = C.c_float()
         self._check(lib().gaia_cloth_run_step_timed(self.h, n, C.byref(ms)))

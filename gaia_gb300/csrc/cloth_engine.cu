@@ -35,6 +35,7 @@
 #include "cloth_scene.hpp"
 #include "gaia_cloth.h"
 #include "scene.hpp"
+#include "state_io.hpp"
 #include "vbd_kernels.cuh"
 
 namespace gaia {
@@ -1312,6 +1313,8 @@ struct gaia_cloth {
     gaia::cloth::Scene scene;
     std::unique_ptr<gaia::cloth::ClothEngineBase> eng;
     std::string err;
+    int64_t frame = 0;     // runStep calls since initialize / the last loaded state
+    double time = 0.0;     // simulated time (timeStep per runStep)
 };
 
 namespace {
@@ -1405,7 +1408,49 @@ const char* gaia_cloth_last_error(gaia_cloth* h) { return h ? h->err.c_str() : "
 
 int gaia_cloth_run_step(gaia_cloth* h, int32_t n) {
     if (!h || !h->eng || n < 0) return GAIA_VBD_E_INVALID_ARG;
-    return cguard(h, [&] { h->eng->run_steps(n); });
+    return cguard(h, [&] {
+        h->eng->run_steps(n);
+        h->frame += n;
+        h->time += n * h->scene.p.timeStep;
+    });
+}
+
+int gaia_cloth_save_state(gaia_cloth* h, const char* path, int32_t binary) {
+    if (!h || !h->eng || !path) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] {
+        gaia::PhysicsStateFile st;
+        st.frameId = int(h->frame);
+        st.curTime = h->time;
+        for (int m = 0; m < h->scene.numSim; ++m) {
+            const size_t nv = size_t(h->scene.meshes[m].nv);
+            std::vector<double> x(3 * nv), v(3 * nv);
+            h->eng->get_positions(m, x.data());
+            h->eng->get_velocities(m, v.data());
+            st.position.emplace_back(x.begin(), x.end());
+            st.velocity.emplace_back(v.begin(), v.end());
+        }
+        gaia::write_physics_state(path, st, binary != 0);
+    });
+}
+
+int gaia_cloth_load_state(gaia_cloth* h, const char* path) {
+    if (!h || !h->eng || !path) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] {
+        gaia::PhysicsStateFile st = gaia::read_physics_state(path);
+        for (int m = 0; m < h->scene.numSim && size_t(m) < st.position.size(); ++m) {
+            const size_t nv = size_t(h->scene.meshes[m].nv);
+            if (st.position[m].size() != 3 * nv)
+                throw std::invalid_argument("state file mesh " + std::to_string(m) + " has " +
+                                            std::to_string(st.position[m].size() / 3) + " vertices, the scene " +
+                                            std::to_string(nv));
+            std::vector<double> x(st.position[m].begin(), st.position[m].end());
+            std::vector<double> v(st.velocity[m].begin(), st.velocity[m].end());
+            h->eng->set_positions(m, x.data());
+            h->eng->set_velocities(m, v.data());
+        }
+        h->frame = st.frameId;
+        h->time = st.curTime;
+    });
 }
 
 int gaia_cloth_run_step_timed(gaia_cloth* h, int32_t n, float* total_ms) {

@@ -54,10 +54,13 @@ __device__ __forceinline__ unsigned int expand_bits(unsigned int v) {
 }
 
 // Primitives: an int4 of vertex ids per primitive, of which the first k (2 = edge,
-// 3 = triangle, 4 = tet) are used.
+// 3 = triangle, 4 = tet) are used. swept != 0: the box also covers the same vertices at
+// id + swept (a second set of positions in the same array, e.g. those at the start of a
+// time step), which bounds the primitive's linear motion between the two.
 struct Prims {
     const int4* idx;
     int k;
+    int swept = 0;
 };
 
 __device__ __forceinline__ void prim_box(const Prims& P, const float4* xf, int p, float3& lo, float3& hi) {
@@ -74,6 +77,14 @@ __device__ __forceinline__ void prim_box(const Prims& P, const float4* xf, int p
         const float3 d = ld3(xf, q.w);
         lo = v3(fminf(lo.x, d.x), fminf(lo.y, d.y), fminf(lo.z, d.z));
         hi = v3(fmaxf(hi.x, d.x), fmaxf(hi.y, d.y), fmaxf(hi.z, d.z));
+    }
+    if (P.swept) {
+        const int ids[4] = {q.x, q.y, q.z, q.w};
+        for (int j = 0; j < P.k; ++j) {
+            const float3 e = ld3(xf, ids[j] + P.swept);
+            lo = v3(fminf(lo.x, e.x), fminf(lo.y, e.y), fminf(lo.z, e.z));
+            hi = v3(fmaxf(hi.x, e.x), fmaxf(hi.y, e.y), fmaxf(hi.z, e.z));
+        }
     }
 }
 

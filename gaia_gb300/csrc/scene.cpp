@@ -245,6 +245,94 @@ void validate_coloring(const TetMesh& m) {
                     throw std::runtime_error("invalid coloring: tet " + std::to_string(t) + " has two vertices of one color");
 }
 
+void extract_surface(TetMesh& m) {
+    static const int kFace[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
+    struct Key {
+        int32_t a, b, c, id;  // sorted vertex ids, 4 * tet + local face
+    };
+    std::vector<Key> keys(4 * size_t(m.ntet));
+    for (int32_t t = 0; t < m.ntet; ++t)
+        for (int k = 0; k < 4; ++k) {
+            int32_t v[3] = {m.tets[4 * size_t(t) + kFace[k][0]], m.tets[4 * size_t(t) + kFace[k][1]],
+                            m.tets[4 * size_t(t) + kFace[k][2]]};
+            std::sort(v, v + 3);
+            keys[4 * size_t(t) + k] = Key{v[0], v[1], v[2], 4 * t + k};
+        }
+    auto less3 = [](const Key& x, const Key& y) {
+        return x.a != y.a ? x.a < y.a : (x.b != y.b ? x.b < y.b : x.c < y.c);
+    };
+    std::sort(keys.begin(), keys.end(), [&](const Key& x, const Key& y) { return less3(x, y) || (!less3(y, x) && x.id < y.id); });
+    std::vector<char> boundary(4 * size_t(m.ntet), 0);
+    for (size_t i = 0; i < keys.size();) {
+        size_t j = i + 1;
+        while (j < keys.size() && !less3(keys[i], keys[j])) ++j;
+        if (j - i == 1) boundary[size_t(keys[i].id)] = 1;
+        i = j;
+    }
+    m.sfaces.clear();
+    std::vector<char> on(size_t(m.nv), 0);
+    for (int32_t t = 0; t < m.ntet; ++t) {
+        const int32_t* tv = &m.tets[4 * size_t(t)];
+        double e[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int d = 0; d < 3; ++d) e[i][d] = double(m.X[3 * size_t(tv[i + 1]) + d]) - double(m.X[3 * size_t(tv[0]) + d]);
+        const double vol = e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) - e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
+                           e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
+        for (int k = 0; k < 4; ++k) {
+            if (!boundary[4 * size_t(t) + k]) continue;
+            int32_t f[3] = {tv[kFace[k][0]], tv[kFace[k][1]], tv[kFace[k][2]]};
+            if (vol < 0) std::swap(f[1], f[2]);
+            for (int i = 0; i < 3; ++i) {
+                m.sfaces.push_back(f[i]);
+                on[size_t(f[i])] = 1;
+            }
+        }
+    }
+    m.sverts.clear();
+    for (int32_t v = 0; v < m.nv; ++v)
+        if (on[size_t(v)]) m.sverts.push_back(v);
+    // face across each edge, and the surface ring of every vertex
+    const size_t nf = m.sfaces.size() / 3;
+    struct Edge {
+        int32_t lo, hi, face, k;
+    };
+    std::vector<Edge> edges;
+    edges.reserve(3 * nf);
+    for (size_t f = 0; f < nf; ++f)
+        for (int k = 0; k < 3; ++k) {
+            const int32_t a = m.sfaces[3 * f + k], b = m.sfaces[3 * f + (k + 1) % 3];
+            edges.push_back(Edge{std::min(a, b), std::max(a, b), int32_t(f), k});
+        }
+    std::sort(edges.begin(), edges.end(), [](const Edge& x, const Edge& y) {
+        return x.lo != y.lo ? x.lo < y.lo : (x.hi != y.hi ? x.hi < y.hi : x.face < y.face);
+    });
+    m.sface_nbr.assign(3 * nf, -1);
+    std::vector<std::vector<int32_t>> ring(static_cast<size_t>(m.nv));
+    for (size_t i = 0; i < edges.size();) {
+        size_t j = i;
+        while (j < edges.size() && edges[j].lo == edges[i].lo && edges[j].hi == edges[i].hi) ++j;
+        // each face takes the first other face on the edge
+        for (size_t a = i; a < j; ++a)
+            for (size_t b = i; b < j; ++b)
+                if (edges[b].face != edges[a].face) {
+                    m.sface_nbr[3 * size_t(edges[a].face) + size_t(edges[a].k)] = edges[b].face;
+                    break;
+                }
+        ring[size_t(edges[i].lo)].push_back(edges[i].hi);
+        ring[size_t(edges[i].hi)].push_back(edges[i].lo);
+        i = j;
+    }
+    m.sring_ofs.assign(size_t(m.nv) + 1, 0);
+    m.sring.clear();
+    for (int32_t v = 0; v < m.nv; ++v) {
+        auto& r = ring[size_t(v)];
+        std::sort(r.begin(), r.end());
+        r.erase(std::unique(r.begin(), r.end()), r.end());
+        m.sring.insert(m.sring.end(), r.begin(), r.end());
+        m.sring_ofs[size_t(v) + 1] = int32_t(m.sring.size());
+    }
+}
+
 // Rest shape (TetMesh/TetMeshFEM.cpp:332-443): rotation (axis-angle), scale,
 // translation; Dm = [x1-x0, x2-x0, x3-x0], DmInv = Dm^-1, volume = det/6,
 // lumped mass. DmInv/volume/mass are computed in FP64 from the FP32 positions.
@@ -388,6 +476,8 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         get(*pp, "useGPU", p.useGPU);
         get(*pp, "handleCollision", p.handleCollision);
         get(*pp, "collisionStiffness", p.collisionStiffness);
+        get(*pp, "collisionOffHeight", p.collisionOffHeight);
+        get(*pp, "intermediateCollisionIterations", p.intermediateCollisionIterations);
         get(*pp, "numThreadsVBDSolve", p.numThreadsVBDSolve);
         get(*pp, "useDouble3x3", p.useDouble3x3);
         get(*pp, "evaluateConvergence", p.evaluateConvergence);
@@ -398,6 +488,13 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         get(*pp, "usePDL", p.usePDL);
         get(*pp, "smallColorVertices", p.smallColorVertices);
         get(*pp, "solveVariant", p.solveVariant);
+    }
+    if (const json::Value* cp = params.find("CollisionParams")) {
+        get(*cp, "allowCCD", p.allowCCD);
+        get(*cp, "allowDCD", p.allowDCD);
+        get(*cp, "handleSelfCollision", p.handleSelfCollision);
+        get(*cp, "checkFeasibleRegion", p.checkFeasibleRegion);
+        get(*cp, "feasibleRegionEpsilon", p.feasibleRegionEpsilon);
     }
     if (p.numSubsteps <= 0 || p.timeStep <= 0) throw std::runtime_error("timeStep and numSubsteps must be positive");
     if (p.iterations < 0) throw std::runtime_error("iterations must be >= 0");
@@ -447,6 +544,7 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         TetMesh& m = s.meshes[i];
         load_t(s.objs[i].path, m.X, m.tets);
         prepare_mesh(p, s.objs[i], m);
+        extract_surface(m);
         if (!s.objs[i].verticesColoringCategoriesPath.empty()) {
             m.colors = load_coloring(s.objs[i].verticesColoringCategoriesPath);
         } else {

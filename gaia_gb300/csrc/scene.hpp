@@ -32,6 +32,15 @@ struct PhysicsParams {
     bool useGPU = true;
     bool handleCollision = false;
     double collisionStiffness = 1e5;
+    double collisionOffHeight = 1e7;          // contact detection only below this height (y)
+    int intermediateCollisionIterations = -1; // re-detect every n iterations (n > 0)
+    // CollisionDetectionParamters (CollisionDetector/CollisionDetertionParameters.h:41-78),
+    // "CollisionParams" in Parameters.json: the keys the VBD step uses
+    bool allowCCD = true;
+    bool allowDCD = true;
+    bool handleSelfCollision = true;
+    bool checkFeasibleRegion = true;
+    double feasibleRegionEpsilon = 1e-2;
     int numThreadsVBDSolve = 16;
     bool useDouble3x3 = false;
     bool evaluateConvergence = false;
@@ -97,6 +106,11 @@ struct TetMesh {
     std::vector<uint8_t> fixed;    // nv
     std::vector<std::vector<int32_t>> colors;  // sorted by size, large to small
     std::vector<int32_t> nbr_ofs, nbr_tet, nbr_order;  // CSR vertex -> incident tets
+    // surface (see extract_surface)
+    std::vector<int32_t> sfaces;               // 3 per boundary face, outward
+    std::vector<int32_t> sverts;               // boundary vertices, ascending
+    std::vector<int32_t> sface_nbr;            // 3 per face: face across edge AB, BC, CA (-1: none)
+    std::vector<int32_t> sring_ofs, sring;     // per vertex: surface neighbours, ascending
 };
 
 struct Scene {
@@ -114,6 +128,11 @@ void load_t(const std::string& path, std::vector<float>& X, std::vector<int32_t>
 std::vector<std::vector<int32_t>> load_coloring(const std::string& path);
 void prepare_mesh(const PhysicsParams& p, const ObjectParams& o, TetMesh& m);  // rest shape, CSR, fixed
 void build_parallel_groups(Scene& scene);
+// Boundary faces (faces of exactly one tet) in ascending (tet, local face) order; the
+// face opposite local vertex k is (1,2,3), (0,3,2), (0,1,3), (0,2,1) for k = 0..3, which
+// points out of a tet of positive rest volume, and is reversed for a negative one. Also
+// the surface vertices, the face across each face edge and each vertex's surface ring.
+void extract_surface(TetMesh& m);
 void validate_coloring(const TetMesh& m);  // every vertex exactly once; no two tet-neighbours share a color
 
 // Colorings (bit-exact with GraphColoring/mcs.cpp and gready.cpp, in O(E log V)).

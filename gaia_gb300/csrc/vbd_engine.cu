@@ -19,6 +19,8 @@
 
 #include "../../include/gaia_vbd.h"
 #include "scene.hpp"
+#include "state_io.hpp"
+#include "tet_cd.hpp"
 #include "vbd_kernels.cuh"
 
 namespace gaia {
@@ -94,6 +96,12 @@ public:
     virtual void stats(gaia_vbd_stats* s) = 0;
     virtual void sync() = 0;
     virtual void color_config(int g, int32_t* L, int32_t* B, int32_t* variant, float* ms) const = 0;
+    virtual double get_time() = 0;
+    virtual void set_time(double t) = 0;
+    // tet-mesh contact
+    virtual void set_prev_positions(int mesh, const double* in) = 0;
+    virtual int collide() = 0;
+    virtual void contacts(std::vector<int32_t>& rows) = 0;
 };
 
 template <typename ST, typename R>
@@ -111,6 +119,7 @@ public:
         GAIA_CUDA(cudaEventCreate(&ev_c_));
         build_layout();
         upload();
+        setup_contact();
         lanes_ = sc_.p.lanesPerVertex;
         block_ = sc_.p.blockSize;
         if (lanes_ != 0 && lanes_ != 2 && lanes_ != 4 && lanes_ != 8 && lanes_ != 16 && lanes_ != 32)
@@ -295,6 +304,7 @@ public:
             c_.hi_f[k] = float(p.worldHi[k]);
         }
         c_.kb = R(p.boundaryCollisionStiffness);
+        c_.kc = R(p.collisionStiffness);
         c_.fr_mu = R(p.boundaryFrictionDynamic);
         c_.fr_epsU = R(p.boundaryFrictionEpsV * p.dt);
         c_.step = R(p.stepSize);
@@ -366,7 +376,88 @@ public:
         P.counters = d_counters_.p;
         P.nactive = nactive_;
         P.nslots = int32_t(nslots_);
+        const tetcd::Records rc = cd_.records();
+        P.col_info = rc.info;
+        P.col_own = rc.own;
+        P.col_rel = rc.rel;
+        P.usnap = d_usnap_.p;
+        P.mesh_fric = d_mesh_fric_.p;
         return P;
+    }
+
+    // ---- tet-mesh contact -----------------------------------------------------------
+    // Surface faces / vertices, surface rings and tets of all meshes in slot terms for
+    // the detector, the detector itself, and the first hierarchies.
+    void setup_contact() {
+        const PhysicsParams& p = sc_.p;
+        tetcd::Params prm;
+        prm.ccd = p.allowCCD;
+        prm.dcd = p.allowDCD;
+        prm.handle_self = p.handleSelfCollision;
+        prm.check_feasible = p.checkFeasibleRegion;
+        prm.feasible_eps = float(p.feasibleRegionEpsilon);
+        prm.off_height = float(p.collisionOffHeight);
+        tetcd::Topo t;
+        t.nslots = int32_t(nslots_);
+        t.face_ofs.assign(nmesh_ + 1, 0);
+        std::vector<std::vector<int32_t>> ring(static_cast<size_t>(nslots_));
+        for (int m = 0; m < nmesh_; ++m) {
+            const TetMesh& M = sc_.meshes[m];
+            auto slot = [&](int32_t v) { return slot_of_[mesh_off_[m] + v]; };
+            const int32_t f0 = int32_t(t.faces.size());
+            const size_t nf = M.sfaces.size() / 3;
+            t.face_ofs[m + 1] = f0 + int32_t(nf);
+            for (size_t f = 0; f < nf; ++f) {
+                t.faces.push_back(make_int4(slot(M.sfaces[3 * f]), slot(M.sfaces[3 * f + 1]), slot(M.sfaces[3 * f + 2]), m));
+                int32_t nb[3];
+                for (int k = 0; k < 3; ++k) nb[k] = M.sface_nbr[3 * f + k] < 0 ? -1 : f0 + M.sface_nbr[3 * f + k];
+                t.face_nbr.push_back(make_int4(nb[0], nb[1], nb[2], 0));
+            }
+            for (int32_t v : M.sverts) t.verts.push_back(make_int2(slot(v), m));
+            for (int32_t v = 0; v < M.nv; ++v)
+                for (int32_t r = M.sring_ofs[v]; r < M.sring_ofs[v + 1]; ++r) ring[slot(v)].push_back(slot(M.sring[r]));
+            for (int32_t k = 0; k < M.ntet; ++k) {
+                const int32_t* tv = &M.tets[4 * size_t(k)];
+                t.tets.push_back(make_int4(slot(tv[0]), slot(tv[1]), slot(tv[2]), slot(tv[3])));
+                t.tet_mesh.push_back(m);
+            }
+        }
+        t.ring_ofs.assign(size_t(nslots_) + 1, 0);
+        for (int64_t s = 0; s < nslots_; ++s) {
+            t.ring.insert(t.ring.end(), ring[s].begin(), ring[s].end());
+            t.ring_ofs[s + 1] = int32_t(t.ring.size());
+        }
+        cd_.init(t, prm, bytes_);
+        if (!cd_.enabled()) return;
+        std::vector<float2> fr(nmesh_);
+        for (int m = 0; m < nmesh_; ++m) fr[m] = make_float2(float(sc_.objs[m].frictionDynamic), float(sc_.objs[m].frictionEpsV));
+        d_mesh_fric_.upload(fr, &bytes_, st_);
+        d_xf_.alloc(2 * size_t(nslots_), &bytes_);
+        d_usnap_.alloc(nslots_, &bytes_);
+        GAIA_CUDA(cudaMemcpyAsync(d_usnap_.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+        enqueue_gather();
+        cd_.build(d_xf_.p, st_);
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    void enqueue_gather() {
+        dev::k_gather_xf<ST><<<div_up(nslots_, 256), 256, 0, st_>>>(d_pos_.p, d_xprev_.p, d_rest_.p, d_xf_.p, int32_t(nslots_));
+        GAIA_CUDA(cudaGetLastError());
+    }
+
+    // One detection pass on the current and start-of-substep positions.
+    void enqueue_detection(bool intermediate, bool rebuild) {
+        if (!cd_.enabled()) return;
+        enqueue_gather();
+        cd_.enqueue(d_xf_.p, intermediate, rebuild, st_);
+    }
+
+    void enqueue_snapshot() {
+        if (!cd_.enabled()) return;
+        const tetcd::Records rc = cd_.records();
+        if (rc.inv_cap <= 0) return;
+        dev::k_snapshot_contacts<ST><<<div_up(rc.inv_cap, 256), 256, 0, st_>>>(rc.inv, rc.ninv, rc.inv_cap, d_pos_.p, d_usnap_.p);
+        GAIA_CUDA(cudaGetLastError());
     }
 
     // ---- kernels ----------------------------------------------------------------
@@ -478,10 +569,13 @@ public:
         }
     }
 
-    void enqueue_init() {
+    void enqueue_init(bool rebuild) {
         auto P = ptrs();
         dev::k_initial_step<ST, R><<<div_up(nslots_, 256), 256, 0, st_>>>(P, c_);
         GAIA_CUDA(cudaGetLastError());
+        // contacts: DCD on the start-of-substep positions, CCD on the trajectories to the
+        // initial guess, before the deformers move their vertices (VBDPhysics.cpp:846-859)
+        enqueue_detection(false, rebuild);
         if (!h_def_slot_.empty()) {
             dev::DeformVerts D;
             D.slot = d_def_slot_.p;
@@ -500,6 +594,10 @@ public:
     // One iteration's color sweep: VBDPhysics.cpp:879-953 (graph of per-color kernels).
     void enqueue_iteration(int it, double* omega, bool accel) {
         int friction = it >= sc_.p.frictionStartIter ? 1 : 0;
+        // intermediateCollisionDetection (VBDPhysics.cpp:878-884)
+        const int ici = sc_.p.intermediateCollisionIterations;
+        if (ici > 0 && it % ici == 0 && it) enqueue_detection(true, false);
+        enqueue_snapshot();
         if (accel) {
             // getAcceleratorOmega (VBDPhysics.cpp:3558-3574)
             double rho = sc_.p.acceleratorRho;
@@ -508,6 +606,8 @@ public:
             GAIA_CUDA(cudaMemcpyAsync(d_acc_prev_.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
         }
         // programmatic launch only directly after another solve kernel in the stream
+        // (with contacts the previous kernel is the snapshot kernel; k_solve reads no
+        // dynamic data before its griddepcontrol.wait either way)
         bool after_solve = it > 0 && !accel;
         for (size_t g = 0; g < group_beg_.size(); ++g) {
             const int n = group_end_[g] - group_beg_[g];
@@ -518,7 +618,8 @@ public:
             after_solve = true;
         }
         if (accel) {
-            dev::k_accel_apply<ST><<<div_up(nactive_, 256), 256, 0, st_>>>(d_pos_.p, d_acc_pp_.p, d_acc_prev_.p, nactive_, *omega);
+            dev::k_accel_apply<ST><<<div_up(nactive_, 256), 256, 0, st_>>>(d_pos_.p, d_acc_pp_.p, d_acc_prev_.p, nactive_,
+                                                                          *omega, cd_.records().info);
             GAIA_CUDA(cudaGetLastError());
         }
     }
@@ -530,7 +631,7 @@ public:
 
     // ---- graphs -----------------------------------------------------------------
     void destroy_graphs() {
-        for (auto* g : {&g_init_, &g_sweep_, &g_vel_})
+        for (auto* g : {&g_init_, &g_init_rb_, &g_sweep_, &g_vel_})
             if (*g) {
                 cudaGraphExecDestroy(*g);
                 *g = nullptr;
@@ -538,7 +639,7 @@ public:
     }
 
     template <typename Fn>
-    cudaGraphExec_t capture_one(Fn&& fn) {
+    cudaGraphExec_t capture_one(Fn&& fn, int64_t* kernels = nullptr) {
         cudaGraph_t graph = nullptr;
         GAIA_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
         try {
@@ -549,6 +650,20 @@ public:
             throw;
         }
         GAIA_CUDA(cudaStreamEndCapture(st_, &graph));
+        if (kernels) {
+            // kernel nodes of the captured work: the launches one replay makes
+            size_t n = 0;
+            GAIA_CUDA(cudaGraphGetNodes(graph, nullptr, &n));
+            std::vector<cudaGraphNode_t> nodes(n);
+            if (n) GAIA_CUDA(cudaGraphGetNodes(graph, nodes.data(), &n));
+            int64_t k = 0;
+            for (auto nd : nodes) {
+                cudaGraphNodeType t;
+                GAIA_CUDA(cudaGraphNodeGetType(nd, &t));
+                k += t == cudaGraphNodeTypeKernel ? 1 : 0;
+            }
+            *kernels = k;
+        }
         cudaGraphExec_t exec = nullptr;
         cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
@@ -558,22 +673,29 @@ public:
 
     void capture() {
         destroy_graphs();
-        g_init_ = capture_one([&] { enqueue_init(); });
-        g_sweep_ = capture_one([&] {
-            double omega = 1.0;
-            for (int it = 0; it < sc_.p.iterations; ++it) enqueue_iteration(it, &omega, sc_.p.useAccelerator);
-        });
-        g_vel_ = capture_one([&] { enqueue_velocity(); });
-        launches_per_substep_ = 1 + (h_def_slot_.empty() ? 0 : 1) + 1;
-        int64_t ng = 0;
-        for (size_t g = 0; g < group_beg_.size(); ++g) ng += group_end_[g] > group_beg_[g] ? 1 : 0;
-        launches_per_substep_ += int64_t(sc_.p.iterations) * (ng + (sc_.p.useAccelerator ? 1 : 0));
+        int64_t k_init = 0, k_init_rb = 0, k_sweep = 0, k_vel = 0;
+        g_init_ = capture_one([&] { enqueue_init(false); }, &k_init);
+        g_init_rb_ = cd_.enabled() ? capture_one([&] { enqueue_init(true); }, &k_init_rb) : nullptr;
+        g_sweep_ = capture_one(
+            [&] {
+                double omega = 1.0;
+                for (int it = 0; it < sc_.p.iterations; ++it) enqueue_iteration(it, &omega, sc_.p.useAccelerator);
+            },
+            &k_sweep);
+        g_vel_ = capture_one([&] { enqueue_velocity(); }, &k_vel);
+        const int64_t nsub = sc_.p.numSubsteps;
+        launches_per_step_ = nsub * (k_init + k_sweep + k_vel) + (g_init_rb_ ? k_init_rb - k_init : 0);
+        launches_per_substep_ = (launches_per_step_ + nsub - 1) / nsub;
     }
+
+    // The face hierarchy of the contact detector is rebuilt at the first substep of a
+    // step and refitted in the others.
+    cudaGraphExec_t init_graph(int sub) const { return sub == 0 && g_init_rb_ ? g_init_rb_ : g_init_; }
 
     void run_steps(int n) override {
         for (int k = 0; k < n; ++k)
             for (int sub = 0; sub < sc_.p.numSubsteps; ++sub) {
-                GAIA_CUDA(cudaGraphLaunch(g_init_, st_));
+                GAIA_CUDA(cudaGraphLaunch(init_graph(sub), st_));
                 GAIA_CUDA(cudaGraphLaunch(g_sweep_, st_));
                 GAIA_CUDA(cudaGraphLaunch(g_vel_, st_));
             }
@@ -588,7 +710,7 @@ public:
         int q = 0;
         for (int k = 0; k < n; ++k)
             for (int sub = 0; sub < sc_.p.numSubsteps; ++sub, ++q) {
-                GAIA_CUDA(cudaGraphLaunch(g_init_, st_));
+                GAIA_CUDA(cudaGraphLaunch(init_graph(sub), st_));
                 GAIA_CUDA(cudaEventRecord(ev[2 * q], st_));
                 GAIA_CUDA(cudaGraphLaunch(g_sweep_, st_));
                 GAIA_CUDA(cudaEventRecord(ev[2 * q + 1], st_));
@@ -671,6 +793,17 @@ public:
         }
     }
 
+    double get_time() override {
+        double t = 0.0;
+        GAIA_CUDA(cudaMemcpyAsync(&t, d_time_.p, sizeof(double), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        return t;
+    }
+    void set_time(double t) override {
+        GAIA_CUDA(cudaMemcpyAsync(d_time_.p, &t, sizeof(double), cudaMemcpyHostToDevice, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
     void reset() override {
         GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, h_pos_.data(), nslots_ * sizeof(S4), cudaMemcpyHostToDevice, st_));
         GAIA_CUDA(cudaMemcpyAsync(d_vel_.p, h_vel_.data(), nslots_ * sizeof(V4), cudaMemcpyHostToDevice, st_));
@@ -678,6 +811,7 @@ public:
         GAIA_CUDA(cudaMemcpyAsync(d_xprev_.p, h_pos_.data(), nslots_ * sizeof(S4), cudaMemcpyHostToDevice, st_));
         GAIA_CUDA(cudaMemsetAsync(d_time_.p, 0, sizeof(double), st_));
         GAIA_CUDA(cudaMemsetAsync(d_counters_.p + dev::CNT_NONFINITE, 0, sizeof(unsigned long long), st_));
+        cd_.reset(st_);
         GAIA_CUDA(cudaStreamSynchronize(st_));
     }
 
@@ -740,6 +874,48 @@ public:
         GAIA_CUDA(cudaGetLastError());
         GAIA_CUDA(cudaStreamSynchronize(st_));
     }
+    void set_prev_positions(int mesh, const double* in) override {
+        int64_t off, n;
+        mesh_range(mesh, off, n);
+        if (n == 0) return;
+        GAIA_CUDA(cudaMemcpyAsync(d_stage_f64_.p, in, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st_));
+        dev::k_scatter_positions_f64<ST><<<div_up(n, 256), 256, 0, st_>>>(d_xprev_.p, d_rest_.p, d_stage_f64_.p,
+                                                                          d_slot_of_.p + off, int32_t(n));
+        GAIA_CUDA(cudaGetLastError());
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    // A substep-start detection pass on the current positions (trajectories from the
+    // start-of-substep positions); returns the number of vertices with a contact.
+    int collide() override {
+        if (!cd_.enabled()) return 0;
+        enqueue_detection(false, true);
+        std::vector<int32_t> rows;
+        cd_.contacts(rows, st_);
+        return int(rows.size() / 3);
+    }
+
+    // Rows of 8: mesh, vertex, face mesh, face vertices (3, mesh-local), surface face
+    // (mesh-local), kind (1 = CCD, 2 = DCD), in (mesh, surface vertex) order.
+    void contacts(std::vector<int32_t>& out) override {
+        out.clear();
+        if (!cd_.enabled()) return;
+        std::vector<int32_t> rows;
+        cd_.contacts(rows, st_);
+        std::vector<int32_t> face_ofs(nmesh_ + 1, 0);
+        for (int m = 0; m < nmesh_; ++m) face_ofs[m + 1] = face_ofs[m] + int32_t(sc_.meshes[m].sfaces.size() / 3);
+        for (size_t r = 0; r + 2 < rows.size(); r += 3) {
+            const int32_t gi = orig_of_[rows[r]];
+            const int m = int(std::upper_bound(mesh_off_.begin(), mesh_off_.end(), int64_t(gi)) - mesh_off_.begin()) - 1;
+            const int32_t g = rows[r + 1];
+            const int fm = int(std::upper_bound(face_ofs.begin(), face_ofs.end(), g) - face_ofs.begin()) - 1;
+            const int32_t f = g - face_ofs[fm];
+            const int32_t* fv = &sc_.meshes[fm].sfaces[3 * size_t(f)];
+            const int32_t row[8] = {m, gi - int32_t(mesh_off_[m]), fm, fv[0], fv[1], fv[2], f, rows[r + 2]};
+            out.insert(out.end(), row, row + 8);
+        }
+    }
+
     void set_velocities(int mesh, const double* in) override {
         int64_t off, n;
         mesh_range(mesh, off, n);
@@ -843,7 +1019,7 @@ public:
         s->num_vertices = nslots_;
         s->num_active_vertices = nactive_;
         s->num_incidences = ninc_;
-        s->kernel_launches_per_step = launches_per_substep_ * sc_.p.numSubsteps;
+        s->kernel_launches_per_step = launches_per_step_;
         s->fp64_fallback_solves = int64_t(h[dev::CNT_FP64_SOLVES]);
         s->failed_solves = int64_t(h[dev::CNT_FAILED_SOLVES]);
         s->device_bytes = int64_t(bytes_);
@@ -855,7 +1031,11 @@ private:
     const Scene& sc_;
     cudaStream_t st_ = nullptr;
     cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr, ev_c_ = nullptr;
-    cudaGraphExec_t g_init_ = nullptr, g_sweep_ = nullptr, g_vel_ = nullptr;
+    cudaGraphExec_t g_init_ = nullptr, g_init_rb_ = nullptr, g_sweep_ = nullptr, g_vel_ = nullptr;
+    tetcd::Detector cd_;
+    DevBuf<float4> d_xf_;
+    DevBuf<S4> d_usnap_;
+    DevBuf<float2> d_mesh_fric_;
     int nmesh_ = 0;
     int64_t nslots_ = 0;
     int32_t nactive_ = 0, ninc_ = 0;
@@ -869,7 +1049,7 @@ private:
     std::map<std::pair<int, int>, int> maxrec_cache_;
     static constexpr size_t kTmaSmemMax = 200 * 1024;
     double tuned_ms_ = 0.0;
-    int64_t launches_per_substep_ = 0;
+    int64_t launches_per_substep_ = 0, launches_per_step_ = 0;
     size_t bytes_ = 0;
     dev::Consts<R> c_{};
     std::vector<int64_t> mesh_off_;
@@ -925,6 +1105,7 @@ struct gaia_vbd {
     gaia::Scene scene;
     std::unique_ptr<gaia::EngineBase> eng;
     std::string err;
+    int64_t frame = 0;  // runStep calls since initialize / the last loaded state
 };
 
 namespace {
@@ -1024,7 +1205,52 @@ const char* gaia_vbd_last_global_error(void) { return gaia::g_last_error.c_str()
 int gaia_vbd_run_step(gaia_vbd* h, int32_t n_steps) {
     GAIA_NEED(h);
     if (n_steps < 0) return GAIA_VBD_E_INVALID_ARG;
-    return guarded(h, [&] { h->eng->run_steps(n_steps); });
+    return guarded(h, [&] {
+        h->eng->run_steps(n_steps);
+        h->frame += n_steps;
+    });
+}
+
+int gaia_vbd_save_state(gaia_vbd* h, const char* path, int32_t binary) {
+    GAIA_NEED(h);
+    if (!path) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] {
+        gaia::PhysicsStateFile st;
+        st.frameId = int(h->frame);
+        st.curTime = h->eng->get_time();
+        for (size_t m = 0; m < h->scene.meshes.size(); ++m) {
+            const size_t nv = size_t(h->scene.meshes[m].nv);
+            std::vector<double> x(3 * nv), v(3 * nv);
+            h->eng->get_positions(int(m), x.data());
+            h->eng->get_velocities(int(m), v.data());
+            st.position.emplace_back(x.begin(), x.end());
+            st.velocity.emplace_back(v.begin(), v.end());
+        }
+        gaia::write_physics_state(path, st, binary != 0);
+    });
+}
+
+int gaia_vbd_load_state(gaia_vbd* h, const char* path) {
+    GAIA_NEED(h);
+    if (!path) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] {
+        gaia::PhysicsStateFile st = gaia::read_physics_state(path);
+        // BasePhysicFramework::recoverFromState / PhysicsState::initializePhysics: meshes
+        // beyond the file's are left as they are
+        for (size_t m = 0; m < h->scene.meshes.size() && m < st.position.size(); ++m) {
+            const size_t nv = size_t(h->scene.meshes[m].nv);
+            if (st.position[m].size() != 3 * nv)
+                throw std::invalid_argument("state file mesh " + std::to_string(m) + " has " +
+                                            std::to_string(st.position[m].size() / 3) + " vertices, the scene " +
+                                            std::to_string(nv));
+            std::vector<double> x(st.position[m].begin(), st.position[m].end());
+            std::vector<double> v(st.velocity[m].begin(), st.velocity[m].end());
+            h->eng->set_positions(int(m), x.data());
+            h->eng->set_velocities(int(m), v.data());
+        }
+        h->frame = st.frameId;
+        h->eng->set_time(st.curTime);
+    });
 }
 
 int gaia_vbd_synchronize(gaia_vbd* h) {
@@ -1038,9 +1264,57 @@ int gaia_vbd_run_step_timed(gaia_vbd* h, int32_t n_steps, float* total_ms, float
     return guarded(h, [&] { h->eng->run_steps_timed(n_steps, total_ms, sweep_ms); });
 }
 
+int gaia_vbd_num_surface(gaia_vbd* h, int32_t mesh, int32_t* nfaces, int32_t* nverts) {
+    if (!h) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] {
+        if (mesh < 0 || size_t(mesh) >= h->scene.meshes.size()) throw std::invalid_argument("mesh index out of range");
+        const gaia::TetMesh& m = h->scene.meshes[mesh];
+        if (nfaces) *nfaces = int32_t(m.sfaces.size() / 3);
+        if (nverts) *nverts = int32_t(m.sverts.size());
+    });
+}
+
+int gaia_vbd_get_surface(gaia_vbd* h, int32_t mesh, int32_t* faces, int32_t* verts) {
+    if (!h) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] {
+        if (mesh < 0 || size_t(mesh) >= h->scene.meshes.size()) throw std::invalid_argument("mesh index out of range");
+        const gaia::TetMesh& m = h->scene.meshes[mesh];
+        if (faces) std::copy(m.sfaces.begin(), m.sfaces.end(), faces);
+        if (verts) std::copy(m.sverts.begin(), m.sverts.end(), verts);
+    });
+}
+
+int gaia_vbd_set_prev_positions(gaia_vbd* h, int32_t mesh, const double* xyz) {
+    GAIA_NEED(h);
+    if (!xyz) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->set_prev_positions(mesh, xyz); });
+}
+
+int gaia_vbd_collide(gaia_vbd* h, int32_t* n_contacts) {
+    GAIA_NEED(h);
+    return guarded(h, [&] {
+        const int n = h->eng->collide();
+        if (n_contacts) *n_contacts = n;
+    });
+}
+
+int gaia_vbd_get_contacts(gaia_vbd* h, int32_t* rows, int32_t cap, int32_t* n_rows) {
+    GAIA_NEED(h);
+    return guarded(h, [&] {
+        std::vector<int32_t> r;
+        h->eng->contacts(r);
+        const int32_t n = int32_t(r.size() / 8);
+        if (n_rows) *n_rows = n;
+        if (rows) std::copy(r.begin(), r.begin() + 8 * std::min(n, std::max(cap, 0)), rows);
+    });
+}
+
 int gaia_vbd_reset(gaia_vbd* h) {
     GAIA_NEED(h);
-    return guarded(h, [&] { h->eng->reset(); });
+    return guarded(h, [&] {
+        h->eng->reset();
+        h->frame = 0;
+    });
 }
 
 int gaia_vbd_autotune(gaia_vbd* h) {

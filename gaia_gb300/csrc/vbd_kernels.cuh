@@ -47,6 +47,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "cloth_dev.cuh"
 #include "vbd_state.cuh"
 
 namespace gaia {
@@ -62,6 +63,7 @@ template <typename R>
 struct Consts {
     R dt, inv_dt, dt2inv;
     R kb, fr_mu, fr_epsU;
+    R kc;  // collisionStiffness of the tet-mesh v-f contact
     R step, step_gd;
     double dt_d;
     double g[3];
@@ -104,6 +106,12 @@ struct Ptrs {
     const MeshMat<R>* mats;
     unsigned long long* counters;
     int32_t nactive, nslots;
+    // tet-mesh contact records (tet_cd.hpp; null when contact detection is off)
+    const uint8_t* col_info;
+    const int4* col_own;
+    const int32_t* col_rel;
+    const typename ST::U* usnap;   // contact-involved slots at the start of the iteration
+    const float2* mesh_fric;       // per mesh: frictionDynamic, frictionEpsV
 };
 
 struct DeformerDev {
@@ -316,7 +324,128 @@ __device__ __forceinline__ void axis_friction(int d, const R* dx, R mu, R lambda
 template <typename ST, typename R, bool PROBE>
 __device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R>& c, int v, const typename ST::U& uo,
                                             const MeshMat<R>& mat, const Acc<R>& acc, int friction,
-                                            double* probe_out);
+                                            double* probe_out, int beg, int end);
+
+// ---------------------------------------------------------------------------
+// Tet-mesh vertex-face contact (VBDPhysicsCompute.cu:1731-1773, 1812-1930)
+// ---------------------------------------------------------------------------
+template <typename R>
+struct V3T;
+template <>
+struct V3T<float> {
+    using type = float3;
+};
+template <>
+struct V3T<double> {
+    using type = double3;
+};
+
+// A contact partner's displacement: slots of the color being solved are read from the
+// snapshot taken at the start of the iteration, so that, as in the reference's
+// Jacobi-within-color update (positionsNew), no vertex sees a same-color partner's new
+// position; other slots are read live (their colors are complete).
+template <typename ST, typename R, bool PROBE>
+__device__ __forceinline__ typename ST::U contact_u(const Ptrs<ST, R>& P, int s, int beg, int end) {
+    return (!PROBE && s >= beg && s < end) ? P.usnap[s] : P.u[s];
+}
+
+// accumlateCollisionForceAndHessianPerCollision_v2: the contact of vertex sp with its
+// recorded face, at the current positions, on the contact vertex of index `order`
+// (3 = sp itself, 0..2 = a face vertex). Positions are taken relative to sp's: q - p =
+// (X_q - X_p) + (u_q - u_p). Penalty k * depth along the face normal (interior closest
+// point) or the closest-point direction oriented like the face normal, lagged IPC
+// friction in the frame (edge AB, AB x n); scaled by b = 1 (sp) or -barycentric.
+template <typename ST, typename R, bool PROBE>
+__device__ __forceinline__ void contact_term(const Ptrs<ST, R>& P, const Consts<R>& c, int sp, int order, int beg,
+                                             int end, R* f, R* H) {
+    using U = typename ST::U;
+    using V = typename V3T<R>::type;
+    const int4 fo = P.col_own[sp];
+    const U up = contact_u<ST, R, PROBE>(P, sp, beg, end);
+    const U uq[3] = {contact_u<ST, R, PROBE>(P, fo.x, beg, end), contact_u<ST, R, PROBE>(P, fo.y, beg, end),
+                     contact_u<ST, R, PROBE>(P, fo.z, beg, end)};
+    const int fs[3] = {fo.x, fo.y, fo.z};
+    const float4 Xp = P.rest[sp];
+    V q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float4 Xq = P.rest[fs[k]];
+        R d[3];
+        ST::diff(uq[k], up, d);
+        q[k] = V{R(Xq.x) - R(Xp.x) + d[0], R(Xq.y) - R(Xp.y) + d[1], R(Xq.z) - R(Xp.z) + d[2]};
+    }
+    const V o{R(0), R(0), R(0)};
+    V bary, cp;
+    const int type = cloth::closest_point_triangle<V, R>(o, q[0], q[1], q[2], bary, cp);
+    V fn = cloth::cross(cloth::sub(q[1], q[0]), cloth::sub(q[2], q[0]));
+    const R fl = sqrt(cloth::dot(fn, fn));
+    fn = V{fn.x / fl, fn.y / fl, fn.z / fl};
+    const V diff = cp;
+    V n;
+    if (type == cloth::AtInterior) {
+        n = fn;
+    } else {
+        const R inv = R(1) / sqrt(cloth::dot(diff, diff));
+        n = cloth::mul(inv, diff);
+        if (cloth::dot(n, fn) < R(0)) n = V{-n.x, -n.y, -n.z};
+    }
+    const R depth = cloth::dot(diff, n);
+    if (!(depth > R(0))) return;
+    const R bw[4] = {-bary.x, -bary.y, -bary.z, R(1)};
+    const R b = bw[order];
+    const R lambda = depth * c.kc;
+    const R nn[3] = {n.x, n.y, n.z};
+    const R s1 = b * lambda, s2 = b * b * c.kc;
+    f[0] += s1 * nn[0]; f[1] += s1 * nn[1]; f[2] += s1 * nn[2];
+    H[0] += s2 * nn[0] * nn[0]; H[1] += s2 * nn[0] * nn[1]; H[2] += s2 * nn[0] * nn[2];
+    H[3] += s2 * nn[1] * nn[1]; H[4] += s2 * nn[1] * nn[2]; H[5] += s2 * nn[2] * nn[2];
+    // relative tangential displacement over the substep: dx_p - sum_k bary_k dx_k
+    R dx[3];
+    ST::diff(up, P.xprev[sp], dx);
+    const R bk[3] = {bary.x, bary.y, bary.z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        R dk[3];
+        ST::diff(uq[k], P.xprev[fs[k]], dk);
+        dx[0] -= bk[k] * dk[0];
+        dx[1] -= bk[k] * dk[1];
+        dx[2] -= bk[k] * dk[2];
+    }
+    V t0 = cloth::sub(q[1], q[0]);
+    const R l0 = sqrt(cloth::dot(t0, t0));
+    t0 = V{t0.x / l0, t0.y / l0, t0.z / l0};
+    V t1 = cloth::cross(t0, n);
+    const R l1 = sqrt(cloth::dot(t1, t1));
+    t1 = V{t1.x / l1, t1.y / l1, t1.z / l1};
+    const R ta[3] = {t0.x, t0.y, t0.z}, tb[3] = {t1.x, t1.y, t1.z};
+    const R u0 = ta[0] * dx[0] + ta[1] * dx[1] + ta[2] * dx[2];
+    const R u1 = tb[0] * dx[0] + tb[1] * dx[1] + tb[2] * dx[2];
+    const float2 fp = P.mesh_fric[P.slot_mesh[sp]], ff = P.mesh_fric[fo.w];
+    const R mu = (R(fp.x) + R(ff.x)) * R(0.5);
+    const R epsU = (R(fp.y) + R(ff.y)) * R(0.5) * c.dt;
+    cloth::friction<R>(mu, lambda, ta, tb, u0, u1, epsU, b, f, H);
+}
+
+template <typename R>
+struct ContactSum {
+    R f[3], H[6];
+};
+
+// accumulateCollisionForceAndHessian: the vertex's own contact, then its relations.
+// Out of line and returning by value, so that the solve's force and Hessian stay in
+// registers on the common path (no contact).
+template <typename ST, typename R, bool PROBE>
+__device__ __forceinline__ ContactSum<R> contact_forces(const Ptrs<ST, R>& P, const Consts<R>& c, int v, int info,
+                                                     int beg, int end) {
+    ContactSum<R> s{};
+    if (info & 8) contact_term<ST, R, PROBE>(P, c, v, 3, beg, end, s.f, s.H);
+    const int nrel = info & 7;
+    for (int j = 0; j < nrel; ++j) {
+        const int e = P.col_rel[4 * v + j];
+        contact_term<ST, R, PROBE>(P, c, e >> 2, e & 3, beg, end, s.f, s.H);
+    }
+    return s;
+}
 
 // Minimum resident blocks of 256 threads: caps FP32-compute kernels at 64
 // registers (32 warps per SM, no spills); the FP64 kernel keeps its registers.
@@ -370,7 +499,7 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
     }
     reduce_group<L, R>(acc);
     if (!valid || lane != 0) return;
-    vertex_tail<ST, R, PROBE>(P, c, v, uo, mat, acc, friction, probe_out);
+    vertex_tail<ST, R, PROBE>(P, c, v, uo, mat, acc, friction, probe_out, beg, end);
 }
 
 // ---- per-vertex tail (lane 0 of a vertex group): damping, inertia, ground and
@@ -378,7 +507,7 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
 template <typename ST, typename R, bool PROBE>
 __device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R>& c, int v, const typename ST::U& uo,
                                             const MeshMat<R>& mat, const Acc<R>& acc, int friction,
-                                            double* probe_out) {
+                                            double* probe_out, int beg, int end) {
     using U = typename ST::U;
     using Sc = typename ST::Sc;
     R f[3] = {acc.f0, acc.f1, acc.f2};
@@ -408,6 +537,16 @@ __device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R
         f[1] += w * dy[1];
         f[2] += w * dy[2];
         H[0] += w; H[3] += w; H[5] += w;
+    }
+    // tet-mesh contact (between inertia and boundary, VBDPhysicsCompute.cu:893-895)
+    if (P.col_info) {
+        const int info = P.col_info[v];
+        if (info) {
+            const ContactSum<R> cs = contact_forces<ST, R, PROBE>(P, c, v, info, beg, end);
+            f[0] += cs.f[0]; f[1] += cs.f[1]; f[2] += cs.f[2];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) H[i] += cs.H[i];
+        }
     }
     // plane ground / world box with friction on each violated axis (VBDPhysics.cpp:2858-2953)
     if (c.plane) {
@@ -567,7 +706,7 @@ __global__ void __launch_bounds__(256, 4)
     }
     reduce_group<L, float>(acc);
     if (!valid || lane != 0 || !ok) return;
-    vertex_tail<ST, float, false>(P, c, v, uo, mat, acc, friction, nullptr);
+    vertex_tail<ST, float, false>(P, c, v, uo, mat, acc, friction, nullptr, beg, end);
 }
 
 // Initial step of a substep over all slots: VBD_BaseMaterial.h:201-259 and
@@ -681,10 +820,15 @@ __global__ void k_velocity(Ptrs<ST, R> P, Consts<R> c, double* time) {
 // x = pp + omega (x - pp), then pp = the iterate before this iteration's sweep.
 template <typename ST>
 __global__ void k_accel_apply(typename ST::U* u, typename ST::U* prevprev, const typename ST::U* prev_iter,
-                              int32_t nactive, double omega) {
+                              int32_t nactive, double omega, const uint8_t* col_info) {
     using Sc = typename ST::Sc;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nactive) return;
+    // vertices in contact are not extrapolated (VBDPhysicsCompute.cu:928, activeCollisionMask)
+    if (col_info && col_info[s]) {
+        prevprev[s] = prev_iter[s];
+        return;
+    }
     const typename ST::U x = u[s], pp = prevprev[s];
     Sc d[3];
     ST::diff(x, pp, d);
@@ -693,6 +837,31 @@ __global__ void k_accel_apply(typename ST::U* u, typename ST::U* prevprev, const
     r.w = x.w;
     u[s] = r;
     prevprev[s] = prev_iter[s];
+}
+
+// FP32 positions for contact detection: xf[s] = X + u (now), xf[nslots + s] = X + xprev
+// (start of the substep), each rounded once from FP64.
+template <typename ST>
+__global__ void k_gather_xf(const typename ST::U* u, const typename ST::U* xprev, const float4* rest, float4* xf,
+                            int32_t nslots) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots) return;
+    const float4 X = rest[s];
+    double a[3], b[3];
+    ST::to_d(u[s], a);
+    ST::to_d(xprev[s], b);
+    xf[s] = make_float4(float(double(X.x) + a[0]), float(double(X.y) + a[1]), float(double(X.z) + a[2]), 0.f);
+    xf[nslots + s] = make_float4(float(double(X.x) + b[0]), float(double(X.y) + b[1]), float(double(X.z) + b[2]), 0.f);
+}
+
+// Snapshot of the contact-involved slots' displacements at the start of an iteration.
+template <typename ST>
+__global__ void k_snapshot_contacts(const int32_t* inv, const int32_t* ninv, int32_t cap, const typename ST::U* u,
+                                    typename ST::U* usnap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cap || i >= *ninv) return;
+    const int s = inv[i];
+    usnap[s] = u[s];
 }
 
 // ---------------------------------------------------------------------------

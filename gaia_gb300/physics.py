@@ -8,6 +8,7 @@ library; this class only marshals arguments and raises on error codes.
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 
 import numpy as np
@@ -98,6 +99,49 @@ class VBDPhysics:
     def reset(self) -> None:
         """Back to the initial state (rest positions, initial velocities, t = 0)."""
         _check(lib().gaia_vbd_reset(self.handle), self.handle)
+        self.frameId = 0
+
+    # -- tet-mesh contact (VBDPhysics::dcd / ccd / prepareCollisionDataGPU)
+    def surface(self, mesh: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        """Boundary faces (nf, 3), outward, and surface vertices of a mesh."""
+        if not self._h:
+            raise RuntimeError("call loadRunningparameters first")
+        h = self._h
+        nf, nsv = C.c_int32(), C.c_int32()
+        _check(lib().gaia_vbd_num_surface(h, mesh, C.byref(nf), C.byref(nsv)), h)
+        F = np.empty((nf.value, 3), np.int32)
+        V = np.empty(nsv.value, np.int32)
+        _check(lib().gaia_vbd_get_surface(h, mesh, F.ctypes.data, V.ctypes.data), h)
+        return F, V
+
+    def setPrevPositions(self, mesh: int, x: np.ndarray) -> None:
+        x = np.ascontiguousarray(x, np.float64)
+        _check(lib().gaia_vbd_set_prev_positions(self.handle, mesh, x.ctypes.data), self.handle)
+
+    def collide(self) -> int:
+        n = C.c_int32()
+        _check(lib().gaia_vbd_collide(self.handle, C.byref(n)), self.handle)
+        return n.value
+
+    def contacts(self) -> np.ndarray:
+        """Rows (mesh, vertex, face mesh, face v0, v1, v2, surface face, kind)."""
+        n = C.c_int32()
+        _check(lib().gaia_vbd_get_contacts(self.handle, None, 0, C.byref(n)), self.handle)
+        rows = np.empty((n.value, 8), np.int32)
+        if n.value:
+            _check(lib().gaia_vbd_get_contacts(self.handle, rows.ctypes.data, n.value, C.byref(n)), self.handle)
+        return rows
+
+    # -- PhysicsState (Framework/BasePhysicsFramework.h:127-319): the recovery-state file
+    # writeOutputs produces (BasePhysicsFramework.cpp:495-503) and recoverFromState reads
+    # (BasePhysicsFramework.cpp:264-282). FP32 positions and velocities of every mesh.
+    def saveState(self, path: str, binary: bool = False) -> None:
+        _check(lib().gaia_vbd_save_state(self.handle, path.encode(), int(binary)), self.handle)
+
+    def recoverFromState(self, path: str) -> None:
+        _check(lib().gaia_vbd_load_state(self.handle, path.encode()), self.handle)
+        with open(path) as f:
+            self.frameId = int(json.load(f).get("frameId", -1))
 
     def autotune(self) -> None:
         _check(lib().gaia_vbd_autotune(self.handle), self.handle)

@@ -165,6 +165,29 @@ def drop_cube(dirname: str, n: int = 10, precision: str = "mixed", iterations: i
     return _write_json(dirname, models, params, meta={"workload": f"drop_cube_{n}", "seed": seed})
 
 
+def stack_drop(dirname: str, n_lower: int = 6, n_upper: int = 5, spacing: float = 0.01, gap: float = 0.004,
+               speed: float = 1.5, precision: str = "mixed", iterations: int = 10, timeStep: float = 1.0 / 300.0,
+               numSubsteps: int = 1, collision_stiffness: float = 1e5, offset=(0.013, 0.0, 0.011),
+               seed: int = 3, **extra) -> tuple[str, str]:
+    """Tet-mesh contact: a cube (n_upper^3 lattice) moving down at `speed` m/s onto
+    another (n_lower^3) resting on the ground plane y = 0, `gap` above it and shifted
+    by `offset` in x/z so that edges and vertices also meet faces. Both cubes are
+    Neo-Hookean E=1e6, nu=0.4; contact through the tet-surface CCD and the v-f
+    penalty (collisionStiffness)."""
+    Xa, Ta = lattice_cube((n_lower,) * 3, spacing, (0.0, 0.0, 0.0), jitter=1e-4, seed=seed)
+    top = spacing * (n_lower - 1)
+    Xb, Tb = lattice_cube((n_upper,) * 3, spacing * 0.97, (offset[0], top + gap, offset[2]), jitter=1e-4,
+                          seed=seed + 1)
+    ta, ca = _write_mesh(dirname, "lower", Xa, Ta)
+    tb, cb = _write_mesh(dirname, "upper", Xb, Tb, coloring="mcs")
+    models = [model_entry(ta, ca, frictionDynamic=0.2, frictionEpsV=0.01),
+              model_entry(tb, cb, density=800.0, frictionDynamic=0.3, frictionEpsV=0.02,
+                          initialVelocity=[0.0, -speed, 0.0])]
+    params = physics_params(timeStep, iterations, numSubsteps=numSubsteps, ground_y=0.0, precision=precision,
+                            collisionStiffness=collision_stiffness, **extra)
+    return _write_json(dirname, models, params)
+
+
 def twist_cube(dirname: str, n: int = 100, precision: str = "mixed", iterations: int = 50, seed: int = 1,
                spacing: float = 0.01, omega: float = 2.0) -> tuple[str, str]:
     """Twist test: an n^3 lattice cube with its long (x) axis on the world x axis;

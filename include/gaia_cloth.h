@@ -60,6 +60,10 @@ int gaia_cloth_run_step(gaia_cloth* h, int32_t n_steps);
 /* The same, timed on the handle's stream with CUDA events. */
 int gaia_cloth_run_step_timed(gaia_cloth* h, int32_t n_steps, float* total_ms);
 int gaia_cloth_synchronize(gaia_cloth* h);
+/* PhysicsState recovery file of the simulated meshes (same format as gaia_vbd_save_state). */
+int gaia_cloth_save_state(gaia_cloth* h, const char* path, int32_t binary);
+int gaia_cloth_load_state(gaia_cloth* h, const char* path);
+
 
 int gaia_cloth_num_meshes(gaia_cloth* h, int32_t* num_sim, int32_t* num_colliders);
 int64_t gaia_cloth_num_vertices(gaia_cloth* h, int32_t mesh);

@@ -93,6 +93,33 @@ const char* gaia_vbd_last_global_error(void);
  * next synchronizing call. */
 int gaia_vbd_run_step(gaia_vbd* h, int32_t n_steps);
 int gaia_vbd_synchronize(gaia_vbd* h);
+/* PhysicsState recovery file (Framework/BasePhysicsFramework.h:127-319; written by
+ * writeOutputs, read by recoverFromState, BasePhysicsFramework.cpp:264-282, 495-502):
+ * frameId, curTime and every mesh's positions and velocities, inline ("text") or in
+ * <name>.pos / <name>.vel FP32 files next to the JSON (binary != 0). Loading sets
+ * positions, velocities, the frame counter and the simulated time. */
+int gaia_vbd_save_state(gaia_vbd* h, const char* path, int32_t binary);
+int gaia_vbd_load_state(gaia_vbd* h, const char* path);
+
+/* Tet-mesh vertex-face contact (VBDPhysics::dcd / ccd / prepareCollisionDataGPU,
+ * VBD/VBDPhysics.cpp:1812-2156; DiscreteCollisionDetector / ContinuousCollisionDetector).
+ * The step runs contact detection at the start of every substep (and every
+ * intermediateCollisionIterations iterations) when CollisionParams allowCCD / allowDCD
+ * are set (the reference's defaults). These calls expose it on its own:
+ *   gaia_vbd_num_surface / gaia_vbd_get_surface: the boundary faces (3 ints each,
+ *     outward, mesh-local vertex ids) and surface vertices of a mesh (host data, no GPU);
+ *   gaia_vbd_set_prev_positions: the positions at the start of the substep (3 doubles
+ *     per vertex), the trajectory origins of the continuous test;
+ *   gaia_vbd_collide: one substep-start detection pass on the current positions;
+ *   gaia_vbd_get_contacts: rows of 8 ints per vertex in contact, in (mesh, surface
+ *     vertex) order: mesh, vertex, face mesh, face vertices 0..2, surface face, kind
+ *     (1 = continuous, 2 = discrete: the vertex lies inside a tet). */
+int gaia_vbd_num_surface(gaia_vbd* h, int32_t mesh, int32_t* nfaces, int32_t* nverts);
+int gaia_vbd_get_surface(gaia_vbd* h, int32_t mesh, int32_t* faces, int32_t* verts);
+int gaia_vbd_set_prev_positions(gaia_vbd* h, int32_t mesh, const double* xyz);
+int gaia_vbd_collide(gaia_vbd* h, int32_t* n_contacts);
+int gaia_vbd_get_contacts(gaia_vbd* h, int32_t* rows, int32_t cap, int32_t* n_rows);
+
 /* Runs n_steps and times them with CUDA events on the handle's stream:
  * total_ms = all device work, sweep_ms = the color sweeps (solve kernels) only. */
 int gaia_vbd_run_step_timed(gaia_vbd* h, int32_t n_steps, float* total_ms, float* sweep_ms);

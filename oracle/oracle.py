@@ -20,7 +20,8 @@ _LIB = os.path.join(_HERE, "liboracle.so")
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (g++, no GPU needed)."""
-    srcs = [os.path.join(_HERE, f) for f in ("vbd_oracle.cpp", "vbd_oracle.h", "cloth_oracle.cpp", "cloth_oracle.h")]
+    srcs = [os.path.join(_HERE, f) for f in ("vbd_oracle.cpp", "vbd_oracle.h", "cloth_oracle.cpp", "cloth_oracle.h",
+                                              "tet_contact.cpp", "tet_contact.h")]
     if force or not os.path.exists(_LIB) or any(os.path.getmtime(_LIB) < os.path.getmtime(s) for s in srcs):
         subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
     return _LIB
@@ -51,6 +52,11 @@ class OracleParams(C.Structure):
         ("step_size", C.c_double), ("step_size_gd", C.c_double),
         ("friction_start_iter", C.c_int32), ("associate_gravity", C.c_int32),
         ("use_accelerator", C.c_int32), ("accelerator_rho", C.c_double),
+        ("allow_ccd", C.c_int32), ("allow_dcd", C.c_int32),
+        ("collision_stiffness", C.c_double), ("collision_off_height", C.c_double),
+        ("intermediate_collision_iterations", C.c_int32),
+        ("handle_self_collision", C.c_int32), ("check_feasible_region", C.c_int32),
+        ("feasible_region_eps", C.c_double),
     ]
 
 
@@ -93,6 +99,18 @@ def lib():
         L.oracle_energy.argtypes = [C.c_void_p]
         L.oracle_energy.restype = C.c_double
         L.oracle_solve_failures.argtypes = [C.c_void_p]
+        L.oracle_set_prev_positions.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+        L.oracle_collide.argtypes = [C.c_void_p]
+        L.oracle_collide.restype = C.c_int32
+        L.oracle_get_contacts.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+        L.oracle_get_contacts.restype = C.c_int32
+        L.oracle_num_surface.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+        L.oracle_num_surface.restype = C.c_int32
+        fp = C.POINTER(C.c_float)
+        L.oracle_ccd_tri_point.argtypes = [fp] * 6
+        L.oracle_ccd_tri_point.restype = C.c_int32
+        L.oracle_tet_surface.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p]
     return _lib
 
 
@@ -110,6 +128,31 @@ def read_t(path: str) -> tuple[np.ndarray, np.ndarray]:
     T = np.empty((nt.value, 4), np.int32)
     L.oracle_read_t(path.encode(), C.byref(nv), C.byref(nt), X.ctypes.data, T.ctypes.data)
     return X, T
+
+
+def tet_surface(X: np.ndarray, tets: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Boundary faces (nf, 3), outward, in (tet, local face) order, and the surface vertices."""
+    X = np.ascontiguousarray(X, np.float64).reshape(-1)
+    tets = np.ascontiguousarray(tets, np.int32).reshape(-1)
+    nf, nsv = C.c_int32(), C.c_int32()
+    L = lib()
+    L.oracle_tet_surface(len(X) // 3, len(tets) // 4, tets.ctypes.data, X.ctypes.data, C.byref(nf), C.byref(nsv),
+                         None, None)
+    F = np.empty((nf.value, 3), np.int32)
+    V = np.empty(nsv.value, np.int32)
+    L.oracle_tet_surface(len(X) // 3, len(tets) // 4, tets.ctypes.data, X.ctypes.data, C.byref(nf), C.byref(nsv),
+                         F.ctypes.data, V.ctypes.data)
+    return F, V
+
+
+def ccd_tri_point(x0, x1, p0, p1):
+    """FP32 moving point / moving triangle test -> (hit, tt, barycentrics)."""
+    fp = C.POINTER(C.c_float)
+    a = [np.ascontiguousarray(v, np.float32).reshape(-1) for v in (x0, x1, p0, p1)]
+    tt = np.zeros(1, np.float32)
+    b = np.zeros(3, np.float32)
+    hit = lib().oracle_ccd_tri_point(*[v.ctypes.data_as(fp) for v in a], tt.ctypes.data_as(fp), b.ctypes.data_as(fp))
+    return int(hit), float(tt[0]), b
 
 
 def color_mcs(nv: int, tets: np.ndarray) -> np.ndarray:
@@ -190,6 +233,14 @@ class OracleScene:
         op.associate_gravity = int(p["associateGravityWithInertia"])
         op.use_accelerator = int(p["useAccelerator"])
         op.accelerator_rho = p["acceleratorRho"]
+        col = p.get("collision", {"allowCCD": True, "allowDCD": True})
+        op.allow_ccd, op.allow_dcd = int(col["allowCCD"]), int(col["allowDCD"])
+        op.collision_stiffness = p.get("collisionStiffness", 1e5)
+        op.collision_off_height = p.get("collisionOffHeight", 1e7)
+        op.intermediate_collision_iterations = p.get("intermediateCollisionIterations", -1)
+        op.handle_self_collision = int(col.get("handleSelfCollision", True))
+        op.check_feasible_region = int(col.get("checkFeasibleRegion", True))
+        op.feasible_region_eps = col.get("feasibleRegionEpsilon", 1e-2)
         defs = (OracleDeformer * max(1, len(scene["deformers"])))()
         for i, d in enumerate(scene["deformers"]):
             dd = defs[i]
@@ -270,6 +321,22 @@ class OracleScene:
 
     def energy(self) -> float:
         return float(lib().oracle_energy(self.h))
+
+    def set_prev_positions(self, mesh: int, x: np.ndarray) -> None:
+        x = np.ascontiguousarray(x, np.float64)
+        lib().oracle_set_prev_positions(self.h, mesh, x.ctypes.data)
+
+    def collide(self) -> int:
+        """Substep-start contact detection on the current / previous positions."""
+        return int(lib().oracle_collide(self.h))
+
+    def contacts(self) -> np.ndarray:
+        """Rows (mesh, vertex, face mesh, face v0, v1, v2, surface face, kind) of the vertices in contact."""
+        n = lib().oracle_get_contacts(self.h, None, 0)
+        rows = np.empty((n, 8), np.int32)
+        if n:
+            lib().oracle_get_contacts(self.h, rows.ctypes.data, n)
+        return rows
 
     def solve_failures(self) -> int:
         return int(lib().oracle_solve_failures(self.h))

@@ -23,7 +23,11 @@ PHYSICS_DEFAULTS = {
     "boundaryFrictionDynamic": 0.1, "boundaryFrictionEpsV": 1.0, "boundaryCollisionStiffness": 1e5,
     "stepSize": 1.0, "stepSizeGD": 1e-3, "frictionStartIter": 0, "associateGravityWithInertia": True,
     "useAccelerator": False, "acceleratorRho": 0.93,
+    "collisionStiffness": 1e5, "collisionOffHeight": 1e7, "intermediateCollisionIterations": -1,
 }
+# CollisionDetector/CollisionDetertionParameters.h:41-78 (the keys the VBD step reads)
+COLLISION_DEFAULTS = {"allowCCD": True, "allowDCD": True, "handleSelfCollision": True, "checkFeasibleRegion": True,
+                      "feasibleRegionEpsilon": 1e-2}
 MATERIAL_DEFAULTS = {
     "density": 1.0, "frictionDynamic": 0.1, "frictionEpsV": 0.01, "exponentialVelDamping": 1.0,
     "constantVelDamping": 0.0, "initializationType": 0, "miu": 1e4, "lmbd": 1e4,
@@ -114,4 +118,7 @@ def load_scene(models_json: str, params_json: str, repo_root: str | None = None,
     for d in deformers:
         for mi, verts in zip(d["selectedMeshes"], d["selectedVertices"]):
             meshes[mi]["fixed"][np.asarray(verts, np.int64)] = 1
+    cp = dict(COLLISION_DEFAULTS)
+    cp.update({k: v for k, v in params.get("CollisionParams", {}).items() if k in COLLISION_DEFAULTS})
+    pp["collision"] = cp
     return {"meshes": meshes, "params": pp, "deformers": deformers}

@@ -3,6 +3,7 @@
 // Each function cites the reference file:line it restates. Paths are relative
 // to the reference project's Simulator/Modules directory.
 #include "vbd_oracle.h"
+#include "tet_contact.h"
 
 #include <algorithm>
 #include <array>
@@ -181,6 +182,14 @@ struct Mesh {
     bool active = true;
     // accelerator buffers (VBDPhysicsCompute.cu:910-944)
     std::vector<R> prev_iter, prevprev_iter;
+    // contact: surface, detector results per surface vertex, and the per-vertex
+    // records of VBD_BaseMeshGPU.h:18-43 (v side: face mesh + face vertices; up to
+    // four relations to contacts whose face holds this vertex: mesh, vertex, order)
+    oracle_tc::Surface surf;
+    std::vector<oracle_tc::CcdHit> hits;
+    std::vector<char> penetrated;             // per surface vertex: DCD found it inside a tet
+    std::vector<char> col_active, col_mask;
+    std::vector<int32_t> col_fmesh, col_fv, col_face, col_kind, col_nrel, col_rel;
 };
 
 struct Deformer {
@@ -422,21 +431,269 @@ void inertia_force_hessian(const Scene<R>& s, const Mesh<R>& m, int iv, R* force
     H[0] += w; H[4] += w; H[8] += w;
 }
 
+// ---------------------------------------------------------------------------
+// Tet-mesh contact (v-f): detection at the start of a substep, the contact
+// records, and the per-contact force and Hessian.
+// ---------------------------------------------------------------------------
+
+// Closest point on triangle abc (VBD/VBD_GeneralCompute.h:180-268, the Voronoi
+// region walk of Ericson's "Real-Time Collision Detection" 5.1.5). 6 = interior.
+template <typename R>
+int closest_point_triangle(const R* p, const R* a, const R* b, const R* c, R* bary, R* cp) {
+    R ab[3], ac[3], ap[3], bp[3], cpv[3];
+    for (int d = 0; d < 3; ++d) {
+        ab[d] = b[d] - a[d];
+        ac[d] = c[d] - a[d];
+        ap[d] = p[d] - a[d];
+    }
+    auto dot = [](const R* u, const R* v) { return u[0] * v[0] + u[1] * v[1] + u[2] * v[2]; };
+    const R d1 = dot(ab, ap), d2 = dot(ac, ap);
+    auto set = [&](R u, R v, R w) {
+        bary[0] = u; bary[1] = v; bary[2] = w;
+        for (int d = 0; d < 3; ++d) cp[d] = u * a[d] + v * b[d] + w * c[d];
+    };
+    if (d1 <= 0 && d2 <= 0) { set(1, 0, 0); for (int d = 0; d < 3; ++d) cp[d] = a[d]; return 0; }
+    for (int d = 0; d < 3; ++d) bp[d] = p[d] - b[d];
+    const R d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= 0 && d4 <= d3) { set(0, 1, 0); for (int d = 0; d < 3; ++d) cp[d] = b[d]; return 1; }
+    for (int d = 0; d < 3; ++d) cpv[d] = p[d] - c[d];
+    const R d5 = dot(ab, cpv), d6 = dot(ac, cpv);
+    if (d6 >= 0 && d5 <= d6) { set(0, 0, 1); for (int d = 0; d < 3; ++d) cp[d] = c[d]; return 2; }
+    const R vc = d1 * d4 - d3 * d2;
+    if (vc <= 0 && d1 >= 0 && d3 <= 0) {
+        const R v = d1 / (d1 - d3);
+        bary[0] = 1 - v; bary[1] = v; bary[2] = 0;
+        for (int d = 0; d < 3; ++d) cp[d] = a[d] + v * ab[d];
+        return 3;
+    }
+    const R vb = d5 * d2 - d1 * d6;
+    if (vb <= 0 && d2 >= 0 && d6 <= 0) {
+        const R v = d2 / (d2 - d6);
+        bary[0] = 1 - v; bary[1] = 0; bary[2] = v;
+        for (int d = 0; d < 3; ++d) cp[d] = a[d] + v * ac[d];
+        return 5;
+    }
+    const R va = d3 * d6 - d5 * d4;
+    if (va <= 0 && (d4 - d3) >= 0 && (d5 - d6) >= 0) {
+        const R v = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        bary[0] = 0; bary[1] = 1 - v; bary[2] = v;
+        for (int d = 0; d < 3; ++d) cp[d] = b[d] + v * (c[d] - b[d]);
+        return 4;
+    }
+    const R denom = R(1) / (va + vb + vc);
+    const R v = vb * denom, w = vc * denom;
+    bary[0] = 1 - v - w; bary[1] = v; bary[2] = w;
+    for (int d = 0; d < 3; ++d) cp[d] = a[d] + v * ab[d] + w * ac[d];
+    return 6;
+}
+
+// accumlateCollisionForceAndHessianPerCollision_v2 (VBDPhysicsCompute.cu:1812-1930):
+// the contact of vertex qv of mesh qm with its recorded face, evaluated at the current
+// positions, acting on the vertex of that contact with index `order` (3 = the
+// colliding vertex, 0..2 = a face vertex): penalty k * depth along the face normal
+// (interior) or along the closest-point direction, with lagged IPC friction in the
+// frame (edge AB, edge x normal); force * b and Hessian * b^2 with b = 1 for the
+// vertex and -barycentric for a face vertex.
+template <typename R>
+void contact_term(const Scene<R>& s, int qm, int qv, int order, R* force, R* H) {
+    const Mesh<R>& Q = s.meshes[qm];
+    const Mesh<R>& F = s.meshes[Q.col_fmesh[qv]];
+    const int32_t* fv = &Q.col_fv[3 * size_t(qv)];
+    const R* p = &Q.x[3 * size_t(qv)];
+    const R* A = &F.x[3 * size_t(fv[0])];
+    const R* B = &F.x[3 * size_t(fv[1])];
+    const R* C = &F.x[3 * size_t(fv[2])];
+    R bary[3], cp[3];
+    const int type = closest_point_triangle<R>(p, A, B, C, bary, cp);
+    R e1[3], e2[3], fn[3], diff[3], n[3];
+    for (int d = 0; d < 3; ++d) {
+        e1[d] = B[d] - A[d];
+        e2[d] = C[d] - A[d];
+        diff[d] = cp[d] - p[d];
+    }
+    fn[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    fn[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    fn[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    const R fl = std::sqrt(fn[0] * fn[0] + fn[1] * fn[1] + fn[2] * fn[2]);
+    for (int d = 0; d < 3; ++d) fn[d] /= fl;
+    if (type == 6) {
+        for (int d = 0; d < 3; ++d) n[d] = fn[d];
+    } else {
+        const R inv = R(1) / std::sqrt(diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2]);
+        for (int d = 0; d < 3; ++d) n[d] = diff[d] * inv;
+        if (n[0] * fn[0] + n[1] * fn[1] + n[2] * fn[2] < 0)
+            for (int d = 0; d < 3; ++d) n[d] = -n[d];
+    }
+    const R depth = diff[0] * n[0] + diff[1] * n[1] + diff[2] * n[2];
+    if (!(depth > 0)) return;
+    const R b = order == 3 ? R(1) : -bary[order];
+    const R k = R(s.p.collision_stiffness);
+    const R lambda = depth * k;
+    R cf[3], cH[9];
+    for (int r = 0; r < 3; ++r) {
+        cf[r] = n[r] * lambda;
+        for (int c = 0; c < 3; ++c) cH[3 * r + c] = n[r] * n[c] * k;
+    }
+    R dx[3];
+    for (int d = 0; d < 3; ++d) {
+        const R d3 = p[d] - Q.xprev[3 * size_t(qv) + d];
+        const R d0 = A[d] - F.xprev[3 * size_t(fv[0]) + d];
+        const R d1 = B[d] - F.xprev[3 * size_t(fv[1]) + d];
+        const R d2 = C[d] - F.xprev[3 * size_t(fv[2]) + d];
+        dx[d] = d3 - (bary[0] * d0 + bary[1] * d1 + bary[2] * d2);
+    }
+    R t0[3] = {e1[0], e1[1], e1[2]};
+    const R l0 = std::sqrt(t0[0] * t0[0] + t0[1] * t0[1] + t0[2] * t0[2]);
+    for (int d = 0; d < 3; ++d) t0[d] /= l0;
+    R t1[3] = {t0[1] * n[2] - t0[2] * n[1], t0[2] * n[0] - t0[0] * n[2], t0[0] * n[1] - t0[1] * n[0]};
+    const R l1 = std::sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+    for (int d = 0; d < 3; ++d) t1[d] /= l1;
+    const R T[6] = {t0[0], t0[1], t0[2], t1[0], t1[1], t1[2]};
+    const R u[2] = {t0[0] * dx[0] + t0[1] * dx[1] + t0[2] * dx[2], t1[0] * dx[0] + t1[1] * dx[1] + t1[2] * dx[2]};
+    const R mu = (Q.fr_mu + F.fr_mu) * R(0.5);
+    const R epsV = (Q.fr_eps + F.fr_eps) * R(0.5);
+    vertex_friction<R>(mu, lambda, T, u, epsV * R(s.dt), cf, cH);
+    for (int r = 0; r < 3; ++r) force[r] += b * cf[r];
+    for (int i = 0; i < 9; ++i) H[i] += b * b * cH[i];
+}
+
+// accumulateCollisionForceAndHessian (VBDPhysicsCompute.cu:1731-1773): the vertex's
+// own contact, then its relations in record order.
+template <typename R>
+void collision_force_hessian(const Scene<R>& s, int im, int iv, R* force, R* H) {
+    const Mesh<R>& m = s.meshes[im];
+    if (m.col_active.empty()) return;
+    if (m.col_active[iv]) contact_term(s, im, iv, 3, force, H);
+    for (int j = 0; j < m.col_nrel[iv]; ++j) {
+        const int32_t* r = &m.col_rel[12 * size_t(iv) + 3 * j];
+        contact_term(s, r[0], r[1], r[2], force, H);
+    }
+}
+
+// prepareCollisionDataGPU (VBDPhysics.cpp:1812-1894): clear, then, mesh by mesh and
+// surface vertex by surface vertex, record every hit as the vertex's contact and
+// append a relation to each of the face's vertices that has fewer than four.
+template <typename R>
+void build_contact_records(Scene<R>& s) {
+    for (auto& m : s.meshes) {
+        m.col_active.assign(size_t(m.nv), 0);
+        m.col_mask.assign(size_t(m.nv), 0);
+        m.col_nrel.assign(size_t(m.nv), 0);
+        m.col_fmesh.assign(size_t(m.nv), -1);
+        m.col_face.assign(size_t(m.nv), -1);
+        m.col_kind.assign(size_t(m.nv), 0);
+        m.col_fv.assign(3 * size_t(m.nv), -1);
+        m.col_rel.assign(12 * size_t(m.nv), -1);
+    }
+    for (size_t im = 0; im < s.meshes.size(); ++im) {
+        auto& m = s.meshes[im];
+        for (size_t i = 0; i < m.surf.verts.size(); ++i) {
+            const oracle_tc::CcdHit& h = m.hits[i];
+            if (h.face < 0) continue;
+            const int v = m.surf.verts[i];
+            m.col_active[v] = 1;
+            m.col_mask[v] = 1;
+            m.col_fmesh[v] = h.fmesh;
+            m.col_face[v] = h.face;
+            m.col_kind[v] = h.tt < 0.f ? 2 : 1;
+            auto& F = s.meshes[h.fmesh];
+            for (int j = 0; j < 3; ++j) {
+                const int fv = F.surf.faces[3 * size_t(h.face) + j];
+                m.col_fv[3 * size_t(v) + j] = fv;
+                if (F.col_nrel[fv] < 4) {
+                    int32_t* r = &F.col_rel[12 * size_t(fv) + 3 * F.col_nrel[fv]];
+                    r[0] = int32_t(im);
+                    r[1] = v;
+                    r[2] = j;
+                    F.col_nrel[fv]++;
+                    F.col_mask[fv] = 1;
+                }
+            }
+        }
+    }
+}
+
+// Contact detection of one substep (VBDPhysics.cpp:1958-2035 dcd, 2078-2116 ccd) or of
+// an intermediate pass (:2037-2076, 2118-2156), on FP32 copies of the positions:
+//   substep start: DCD (run before the initial step, so on the previous positions) for
+//   the surface vertices below collisionOffHeight, marking the ones inside a tet as
+//   penetrated; without DCD all results are cleared; then CCD for the vertices below
+//   the height that DCD did not mark;
+//   intermediate: DCD (current positions) for the penetrated vertices, or for all when
+//   CCD is off; CCD as above on the current positions.
+// Entries the reference does not revisit keep their previous result.
+template <typename R>
+void detect_contacts(Scene<R>& s, bool intermediate) {
+    const bool ccd = s.p.allow_ccd != 0, dcd = s.p.allow_dcd != 0;
+    if (!ccd && !dcd) return;
+    const float off = float(s.p.collision_off_height);
+    oracle_tc::DcdParams dp;
+    dp.handle_self = s.p.handle_self_collision != 0;
+    dp.check_feasible = s.p.check_feasible_region != 0;
+    dp.feasible_eps = float(s.p.feasible_region_eps);
+    std::vector<std::vector<float>> xf(s.meshes.size()), pf(s.meshes.size());
+    std::vector<oracle_tc::CcdMesh> cm(s.meshes.size());
+    for (size_t im = 0; im < s.meshes.size(); ++im) {
+        auto& m = s.meshes[im];
+        xf[im].resize(m.x.size());
+        pf[im].resize(m.x.size());
+        for (size_t i = 0; i < m.x.size(); ++i) {
+            xf[im][i] = float(m.x[i]);
+            pf[im][i] = float(m.xprev[i]);
+        }
+        cm[im] = oracle_tc::CcdMesh{xf[im].data(), pf[im].data(), &m.surf, m.ntet, m.tets.data()};
+        if (m.hits.size() != m.surf.verts.size()) m.hits.assign(m.surf.verts.size(), oracle_tc::CcdHit{});
+        if (m.penetrated.size() != m.surf.verts.size()) m.penetrated.assign(m.surf.verts.size(), 0);
+    }
+    oracle_tc::Detector det(cm);
+    auto height = [&](size_t im, size_t i, bool prev) {
+        return (prev ? pf : xf)[im][3 * size_t(s.meshes[im].surf.verts[i]) + 1];
+    };
+    if (dcd) {
+        det.build_tets(!intermediate);
+        for (size_t im = 0; im < s.meshes.size(); ++im) {
+            auto& m = s.meshes[im];
+            if (!intermediate) std::fill(m.penetrated.begin(), m.penetrated.end(), 0);
+            for (size_t i = 0; i < m.surf.verts.size(); ++i) {
+                const bool query = intermediate ? (m.penetrated[i] || !ccd) : height(im, i, true) < off;
+                if (!query) continue;
+                oracle_tc::CcdHit h;
+                const bool inside = det.dcd(int(im), int(i), dp, h);
+                m.hits[i] = h;
+                if (inside && !intermediate) m.penetrated[i] = 1;
+            }
+        }
+    } else if (!intermediate) {
+        for (auto& m : s.meshes) std::fill(m.hits.begin(), m.hits.end(), oracle_tc::CcdHit{});
+    }
+    if (ccd) {
+        det.build_swept();
+        for (size_t im = 0; im < s.meshes.size(); ++im) {
+            auto& m = s.meshes[im];
+            for (size_t i = 0; i < m.surf.verts.size(); ++i)
+                if (height(im, i, false) < off && !m.penetrated[i]) m.hits[i] = det.ccd(int(im), int(i));
+        }
+    }
+    build_contact_records(s);
+}
+
 template <typename R>
 void vertex_force_hessian(const Scene<R>& s, const Mesh<R>& m, int iv, bool apply_friction, R* force, R* H) {
     for (int i = 0; i < 3; ++i) force[i] = 0;
     for (int i = 0; i < 9; ++i) H[i] = 0;
     material_force_hessian(m, iv, R(s.dt), force, H);
     inertia_force_hessian(s, m, iv, force, H);
+    collision_force_hessian(s, int(&m - s.meshes.data()), iv, force, H);
     boundary_force_hessian(s, m, iv, apply_friction, force, H);
 }
 
 // One block-descent update of one vertex: VBDPhysics.cpp:2402-2483
-// (VBDStepWithCollision without contact and without line search).
+// (VBDStepWithCollision without line search), written to out[3] (the new position).
 template <typename R>
-void vbd_vertex_step(Scene<R>& s, Mesh<R>& m, int iv, bool apply_friction) {
+void vbd_vertex_step(Scene<R>& s, Mesh<R>& m, int iv, bool apply_friction, R* out) {
     R force[3], H[9];
     vertex_force_hessian(s, m, iv, apply_friction, force, H);
+    for (int d = 0; d < 3; ++d) out[d] = m.x[3 * size_t(iv) + d];
     R n2 = force[0] * force[0] + force[1] * force[1] + force[2] * force[2];
     if (!(n2 > R(1e-10))) return;  // CMP_EPSILON2, Types/Types.h:20-21
     R dx[3];
@@ -449,7 +706,7 @@ void vbd_vertex_step(Scene<R>& s, Mesh<R>& m, int iv, bool apply_friction) {
         for (int d = 0; d < 3; ++d) dx[d] = force[d];
         s.failures.fetch_add(1);
     }
-    for (int d = 0; d < 3; ++d) m.x[3 * size_t(iv) + d] += step * dx[d];
+    for (int d = 0; d < 3; ++d) out[d] += step * dx[d];
 }
 
 // Parallel-group merge: VBDPhysics.cpp:99-122 (findSmallestParallelGroup) and
@@ -602,25 +859,42 @@ void substep(Scene<R>& s, int iterations) {
     s.cur_time += s.dt;
     for (auto& m : s.meshes)
         if (m.active) initial_step(s, m);
+    detect_contacts(s, false);
     apply_deformers(s);
     double omega = 1.0;
     if (s.p.use_accelerator)
         for (auto& m : s.meshes) m.prevprev_iter = m.x;
     for (int it = 0; it < iterations; ++it) {
         bool fric = it >= s.p.friction_start_iter;
+        // intermediateCollisionDetection (VBDPhysics.cpp:878-884, 2158-2172)
+        const int ici = s.p.intermediate_collision_iterations;
+        if (ici > 0 && it % ici == 0 && it) detect_contacts(s, true);
         if (s.p.use_accelerator) {
             omega = accel_omega(it + 1, s.p.accelerator_rho, omega);
             for (auto& m : s.meshes) m.prev_iter = m.x;
         }
+        // a group (merged color) is updated Jacobi-style, as the GPU path does
+        // (positionsNew, then commit: VBDPhysicsCompute.cu:803-908, 946-968): no vertex of
+        // a group sees another's new position. Tet neighbours are never in one group, so
+        // this only matters for contact partners.
+        std::vector<R> xnew;
         for (auto& g : s.groups) {
             int64_t n = int64_t(g.size() / 2);
+            xnew.resize(3 * size_t(n));
             s.pool->run(n, [&](int64_t b, int64_t e) {
                 for (int64_t i = b; i < e; ++i) {
                     auto& m = s.meshes[g[2 * i]];
                     int v = g[2 * i + 1];
-                    if (!m.fixed[v] && m.active) vbd_vertex_step(s, m, v, fric);
+                    R* out = &xnew[3 * size_t(i)];
+                    if (!m.fixed[v] && m.active) vbd_vertex_step(s, m, v, fric, out);
+                    else for (int d = 0; d < 3; ++d) out[d] = m.x[3 * size_t(v) + d];
                 }
             });
+            for (int64_t i = 0; i < n; ++i) {
+                auto& m = s.meshes[g[2 * i]];
+                int v = g[2 * i + 1];
+                for (int d = 0; d < 3; ++d) m.x[3 * size_t(v) + d] = xnew[3 * size_t(i) + d];
+            }
         }
         if (s.p.use_accelerator) {
             const R om = R(omega);
@@ -628,10 +902,13 @@ void substep(Scene<R>& s, int iterations) {
                 if (!m.active) continue;
                 for (int i = 0; i < m.nv; ++i) {
                     if (m.fixed[i]) continue;
+                    const bool colliding = !m.col_mask.empty() && m.col_mask[i];
                     for (int d = 0; d < 3; ++d) {
                         size_t k = 3 * size_t(i) + d;
-                        R diff = m.x[k] - m.prevprev_iter[k];
-                        m.x[k] = m.prevprev_iter[k] + om * diff;
+                        if (!colliding) {
+                            R diff = m.x[k] - m.prevprev_iter[k];
+                            m.x[k] = m.prevprev_iter[k] + om * diff;
+                        }
                         m.prevprev_iter[k] = m.prev_iter[k];
                     }
                 }
@@ -684,6 +961,8 @@ Scene<R>* create(int nmesh, const OracleMesh* meshes, const OracleParams* params
                   [](const std::vector<int32_t>& a, const std::vector<int32_t>& b) { return a.size() > b.size(); });
         rest_shape(m);
         build_adjacency(m);
+        m.surf = oracle_tc::extract_surface(m.nv, m.ntet, in.tets, in.X);
+        m.hits.assign(m.surf.verts.size(), oracle_tc::CcdHit{});
     }
     for (int i = 0; i < ndef; ++i) {
         Deformer d;
@@ -962,6 +1241,54 @@ double oracle_energy(void* h) {
 }
 int32_t oracle_solve_failures(void* h) {
     return dispatch(h, [&](auto& s) { return int32_t(s.failures.load()); });
+}
+
+void oracle_set_prev_positions(void* h, int32_t mesh, const double* in) {
+    dispatch(h, [&](auto& s) {
+        auto& m = s.meshes[mesh];
+        using R = typename std::decay_t<decltype(m.x)>::value_type;
+        for (size_t i = 0; i < m.xprev.size(); ++i) m.xprev[i] = R(in[i]);
+        return 0;
+    });
+}
+int32_t oracle_collide(void* h) {
+    return dispatch(h, [&](auto& s) {
+        detect_contacts(s, false);
+        int32_t n = 0;
+        for (auto& m : s.meshes)
+            for (char a : m.col_active) n += a ? 1 : 0;
+        return n;
+    });
+}
+int32_t oracle_get_contacts(void* h, int32_t* rows, int32_t cap) {
+    return dispatch(h, [&](auto& s) {
+        int32_t n = 0;
+        for (size_t im = 0; im < s.meshes.size(); ++im) {
+            auto& m = s.meshes[im];
+            if (m.col_active.empty()) continue;
+            for (int32_t v : m.surf.verts) {
+                if (!m.col_active[v]) continue;
+                if (n < cap) {
+                    int32_t* r = rows + 8 * size_t(n);
+                    r[0] = int32_t(im);
+                    r[1] = v;
+                    r[2] = m.col_fmesh[v];
+                    for (int j = 0; j < 3; ++j) r[3 + j] = m.col_fv[3 * size_t(v) + j];
+                    r[6] = m.col_face[v];
+                    r[7] = m.col_kind[v];
+                }
+                ++n;
+            }
+        }
+        return n;
+    });
+}
+int32_t oracle_num_surface(void* h, int32_t mesh, int32_t* nverts) {
+    return dispatch(h, [&](auto& s) {
+        auto& m = s.meshes[mesh];
+        if (nverts) *nverts = int32_t(m.surf.verts.size());
+        return int32_t(m.surf.faces.size() / 3);
+    });
 }
 
 }  // extern "C"

@@ -53,6 +53,13 @@ typedef struct {
     int32_t associate_gravity;
     int32_t use_accelerator;
     double accelerator_rho;
+    /* tet-mesh contact (CollisionParams allowCCD / allowDCD; PhysicsParams
+       collisionStiffness, collisionOffHeight, intermediateCollisionIterations) */
+    int32_t allow_ccd, allow_dcd;
+    double collision_stiffness, collision_off_height;
+    int32_t intermediate_collision_iterations;
+    int32_t handle_self_collision, check_feasible_region;
+    double feasible_region_eps;
 } OracleParams;
 
 typedef struct {
@@ -94,6 +101,17 @@ void oracle_vertex_force_hessian(void* h, int32_t mesh, int32_t v, int32_t apply
 /* Total elastic (Neo-Hookean, rest energy removed) + inertia energy, in double. */
 double oracle_energy(void* h);
 int32_t oracle_solve_failures(void* h);
+
+/* Tet-mesh contact. oracle_collide runs the substep-start detection on the current
+ * positions (trajectories from the previous positions) and builds the contact
+ * records the solve reads; it returns the number of vertices in contact (v side).
+ * oracle_get_contacts writes, per such vertex in (mesh, surface vertex) order,
+ * 8 ints: mesh, vertex, face mesh, face vertex 0..2, surface face index, kind
+ * (1 = CCD, 2 = DCD); it returns the row count (rows beyond cap are not written). */
+void oracle_set_prev_positions(void* h, int32_t mesh, const double* in);
+int32_t oracle_collide(void* h);
+int32_t oracle_get_contacts(void* h, int32_t* rows, int32_t cap);
+int32_t oracle_num_surface(void* h, int32_t mesh, int32_t* nverts);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,146 @@
+"""Tet-mesh contact, host side: the oracle's FP32 CCD restatement against the
+reference's own CCD test (golden vectors from the reference build, and the build
+itself where the reference tree is present), surface extraction of the product vs the
+oracle, and the oracle's contact behaviour on a stacked-cube scene."""
+import ctypes as C
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_TREE = "/root/reference/Simulator/Modules/CollisionDetector/CCDSolver.h"
+
+
+def _oracle_ccd(x0, x1, p0, p1):
+    from oracle import oracle as orc
+
+    fp = C.POINTER(C.c_float)
+    fn = orc.lib().oracle_ccd_tri_point
+    n = len(x0)
+    hit = np.zeros(n, np.int32)
+    tt = np.zeros(n, np.float32)
+    bary = np.zeros((n, 3), np.float32)
+    t = np.zeros(1, np.float32)
+    b = np.zeros(3, np.float32)
+    for k in range(n):
+        args = [np.ascontiguousarray(v[k], np.float32) for v in (x0, x1, p0, p1)]
+        hit[k] = fn(*[v.ctypes.data_as(fp) for v in args], t.ctypes.data_as(fp), b.ctypes.data_as(fp))
+        tt[k] = t[0]
+        bary[k] = b
+    return hit, tt, bary
+
+
+def _same(a_hit, a_tt, a_bary, b_hit, b_tt, b_bary):
+    assert np.array_equal(a_hit, b_hit)
+    h = a_hit == 1
+    assert a_tt[h].tobytes() == b_tt[h].tobytes()
+    assert a_bary[h].tobytes() == b_bary[h].tobytes()
+
+
+def test_ccd_matches_reference_golden_vectors():
+    """tests/golden/ccd_vectors.npz holds the reference CCDSolver.h's own outputs."""
+    g = np.load(os.path.join(HERE, "golden", "ccd_vectors.npz"))
+    hit, tt, bary = _oracle_ccd(g["x0"], g["x1"], g["p0"], g["p1"])
+    assert g["hit"].sum() > 500
+    _same(hit, tt, bary, g["hit"], g["tt"], g["bary"])
+
+
+@pytest.mark.skipif(not os.path.exists(REF_TREE), reason="reference tree not present")
+def test_ccd_matches_reference_build_fresh_cases():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("mk", os.path.join(HERE, "golden", "make_ccd_vectors.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "..", "oracle"), "ref"], check=True)
+    lib = C.CDLL(os.path.join(HERE, "..", "oracle", "_ref", "libccd_ref.so"))
+    fn = lib.ref_ccd_tri_point
+    fn.argtypes = [C.POINTER(C.c_float)] * 6
+    fn.restype = C.c_int32
+    x0, x1, p0, p1 = mk.cases(5000, seed=123)
+    _same(*_oracle_ccd(x0, x1, p0, p1), *mk.evaluate(fn, x0, x1, p0, p1))
+
+
+def _surface_invariants(X, tets, F, V):
+    # closed 2-manifold: every undirected edge in two faces, used once in each direction
+    e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]])
+    directed = {tuple(x) for x in e.tolist()}
+    assert len(directed) == len(e)
+    assert all((b, a) in directed for a, b in directed)
+    assert len(V) - len(directed) // 2 + len(F) == 2  # Euler characteristic of a sphere
+    assert np.array_equal(np.unique(F), V)
+    # outward: the surface encloses the tets' total volume (divergence theorem)
+    a, b, c = X[F[:, 0]], X[F[:, 1]], X[F[:, 2]]
+    enclosed = np.einsum("ij,ij->i", a, np.cross(b, c)).sum() / 6.0
+    d = X[tets[:, 1:]] - X[tets[:, :1]]
+    vol = np.abs(np.einsum("ij,ij->i", d[:, 0], np.cross(d[:, 1], d[:, 2]))).sum() / 6.0
+    assert enclosed == pytest.approx(vol, rel=1e-9)
+
+
+def test_surface_matches_oracle(tmp_path, gaia_lib):
+    from gaia_gb300 import VBDPhysics, scenes
+    from oracle import oracle as orc
+    from oracle import scene_io
+
+    mp, pp = scenes.stack_drop(str(tmp_path), n_lower=5, n_upper=4, spacing=0.02)
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, pp)  # host only
+    sc = scene_io.load_scene(mp, pp)
+    for m, mesh in enumerate(sc["meshes"]):
+        F, V = phys.surface(m)
+        Fo, Vo = orc.tet_surface(mesh["X"], mesh["tets"])
+        assert np.array_equal(F, Fo) and np.array_equal(V, Vo)
+        _surface_invariants(mesh["X"], mesh["tets"], F, V)
+    phys.close()
+
+
+def test_surface_of_mirrored_mesh_is_outward(tmp_path, gaia_lib):
+    """Negatively oriented tets (a mirrored mesh) still give outward faces."""
+    from gaia_gb300 import VBDPhysics, scenes
+    from oracle import oracle as orc
+
+    X, T = scenes.lattice_cube((4, 3, 5), 0.02, jitter=1e-3, seed=5)
+    T = T[:, [0, 2, 1, 3]]  # every tet negatively oriented
+    tp, cp = scenes._write_mesh(str(tmp_path), "m", X, T)
+    mp, pp = scenes._write_json(str(tmp_path), [scenes.model_entry(tp, cp)], scenes.physics_params(0.01, 2))
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, pp)
+    F, V = phys.surface(0)
+    Xf = X.astype(np.float32).astype(np.float64)
+    Fo, Vo = orc.tet_surface(Xf, T)
+    assert np.array_equal(F, Fo) and np.array_equal(V, Vo)
+    _surface_invariants(Xf, T, F, V)
+    phys.close()
+
+
+def _run_stack(tmp_path, spacing, steps):
+    from gaia_gb300 import scenes
+    from oracle import oracle as orc
+    from oracle import scene_io
+
+    mp, pp = scenes.stack_drop(str(tmp_path), spacing=spacing, gap=0.01, speed=1.0)
+    o = orc.OracleScene(scene_io.load_scene(mp, pp), 64, 0)
+    kinds = set()
+    for _ in range(steps):
+        o.step(1)
+        kinds |= set(o.contacts()[:, 7].tolist())
+    return o, kinds
+
+
+def test_oracle_stack_rests_on_contact(tmp_path):
+    """3 cm cells: the point-in-tet test is live (|6V| >= 1e-5), DCD holds the upper cube."""
+    o, kinds = _run_stack(tmp_path, 0.03, 40)
+    assert 2 in kinds
+    lower, upper = o.positions(0), o.positions(1)
+    assert upper[:, 1].min() > lower[:, 1].max() - 0.005
+
+
+def test_oracle_stack_small_cells_ccd_only(tmp_path):
+    """1 cm cells: |6V| < CMP_EPSILON = 1e-5 for every tet, so the reference's point-in-tet
+    test never fires and only CCD contacts occur (penalty contact cannot hold a body that
+    stays below the surface after a substep)."""
+    o, kinds = _run_stack(tmp_path, 0.01, 15)
+    assert kinds and kinds <= {1}
