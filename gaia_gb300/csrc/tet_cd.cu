@@ -17,6 +17,7 @@
 #include "tet_cd.hpp"
 
 #include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
 
 #include <algorithm>
 #include <stdexcept>
@@ -473,9 +474,8 @@ __global__ void k_ccd(Dev D, bvh::LbvhDev fb, const float4* xf, float off) {
     D.hit_tt[i] = besttt;
 }
 
-// Own contacts, relation keys (face vertex slot, surface vertex, order) and the list of
-// contact-involved slots.
-__global__ void k_own(Dev D, uint8_t* info, int4* own, unsigned long long* keys, int32_t* inv, int32_t* ninv) {
+// Own contacts and relation keys (face vertex slot, surface vertex, order).
+__global__ void k_own(Dev D, uint8_t* info, int4* own, unsigned long long* keys) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= D.nsv) return;
     const int g = D.hit[i];
@@ -491,11 +491,6 @@ __global__ void k_own(Dev D, uint8_t* info, int4* own, unsigned long long* keys,
 #pragma unroll
     for (int j = 0; j < 3; ++j)
         keys[3 * size_t(i) + j] = (static_cast<unsigned long long>(f[j]) << 32) | (static_cast<unsigned>(i) << 2) | j;
-    const int k = atomicAdd(ninv, 4);
-    inv[k] = slot;
-    inv[k + 1] = fv.x;
-    inv[k + 2] = fv.y;
-    inv[k + 3] = fv.z;
 }
 
 // The first four relations of each face vertex in (surface vertex) order.
@@ -530,12 +525,14 @@ struct Detector::Impl {
     uint8_t* info = nullptr;
     int4* own = nullptr;
     int32_t* rel = nullptr;
-    int32_t* inv = nullptr;
-    int32_t* ninv = nullptr;
+    int32_t* list = nullptr;
+    int32_t* nlist = nullptr;
     int* vol_flag = nullptr;
     unsigned long long *keys = nullptr, *keys_sorted = nullptr, *counters = nullptr;
     void* sort_tmp = nullptr;
     size_t sort_tmp_bytes = 0;
+    void* select_tmp = nullptr;
+    size_t select_tmp_bytes = 0;
     bvh::Lbvh face_bvh, tet_bvh;
 };
 
@@ -547,8 +544,9 @@ void Detector::release() {
     d_->tet_bvh.release();
     for (void* p : {(void*)d_->faces, (void*)d_->face_nbr, (void*)d_->sv, (void*)d_->ring_ofs, (void*)d_->ring,
                     (void*)d_->tet_mesh, (void*)d_->tets, (void*)d_->hit, (void*)d_->hit_tt, (void*)d_->pen,
-                    (void*)d_->info, (void*)d_->own, (void*)d_->rel, (void*)d_->inv, (void*)d_->ninv,
-                    (void*)d_->vol_flag, (void*)d_->keys, (void*)d_->keys_sorted, (void*)d_->counters, d_->sort_tmp})
+                    (void*)d_->info, (void*)d_->own, (void*)d_->rel, (void*)d_->list, (void*)d_->nlist,
+                    (void*)d_->vol_flag, (void*)d_->keys, (void*)d_->keys_sorted, (void*)d_->counters, d_->sort_tmp,
+                    d_->select_tmp})
         if (p) cudaFree(p);
     delete d_;
     d_ = nullptr;
@@ -584,8 +582,8 @@ void Detector::init(const Topo& t, const Params& prm, size_t& bytes) {
     I.info = dalloc<uint8_t>(nslots_, bytes);
     I.own = dalloc<int4>(nslots_, bytes);
     I.rel = dalloc<int32_t>(4 * size_t(nslots_), bytes);
-    I.inv = dalloc<int32_t>(4 * size_t(nsv_), bytes);
-    I.ninv = dalloc<int32_t>(1, bytes);
+    I.list = dalloc<int32_t>(nslots_, bytes);
+    I.nlist = dalloc<int32_t>(1, bytes);
     I.vol_flag = dalloc<int>(1, bytes);
     I.keys = dalloc<unsigned long long>(3 * size_t(nsv_), bytes);
     I.keys_sorted = dalloc<unsigned long long>(3 * size_t(nsv_), bytes);
@@ -593,10 +591,13 @@ void Detector::init(const Topo& t, const Params& prm, size_t& bytes) {
     TCD_CUDA(cudaMemset(I.hit, 0xff, sizeof(int32_t) * std::max(nsv_, 1)));
     TCD_CUDA(cudaMemset(I.pen, 0, std::max(nsv_, 1)));
     TCD_CUDA(cudaMemset(I.info, 0, std::max(nslots_, 1)));
-    TCD_CUDA(cudaMemset(I.ninv, 0, sizeof(int32_t)));
+    TCD_CUDA(cudaMemset(I.nlist, 0, sizeof(int32_t)));
     TCD_CUDA(cudaMemset(I.counters, 0, sizeof(unsigned long long) * cloth::CC_N));
     TCD_CUDA(cub::DeviceRadixSort::SortKeys(nullptr, I.sort_tmp_bytes, I.keys, I.keys_sorted, 3 * nsv_));
     I.sort_tmp = dalloc<char>(I.sort_tmp_bytes, bytes);
+    TCD_CUDA(cub::DeviceSelect::Flagged(nullptr, I.select_tmp_bytes, thrust::counting_iterator<int32_t>(0), I.info,
+                                        I.list, I.nlist, nslots_));
+    I.select_tmp = dalloc<char>(I.select_tmp_bytes, bytes);
     I.face_bvh.alloc(nf_, bvh::Prims{I.faces, 3, nslots_}, bytes);
     if (prm.dcd) I.tet_bvh.alloc(ntet_, bvh::Prims{I.tets, 4, 0}, bytes);
     Dev& D = I.D;
@@ -642,13 +643,15 @@ void Detector::enqueue(const float4* xf, bool intermediate, bool rebuild, cudaSt
         k_clear_hits<<<blocks(nsv_, 256), 256, 0, st>>>(D);
     }
     if (prm_.ccd) k_ccd<<<blocks(nsv_, 128), 128, 0, st>>>(D, I.face_bvh.dev(), xf, prm_.off_height);
-    // records
+    // records, and the ascending list of slots that have any
     TCD_CUDA(cudaMemsetAsync(I.info, 0, size_t(nslots_), st));
-    TCD_CUDA(cudaMemsetAsync(I.ninv, 0, sizeof(int32_t), st));
-    k_own<<<blocks(nsv_, 256), 256, 0, st>>>(D, I.info, I.own, I.keys, I.inv, I.ninv);
+    k_own<<<blocks(nsv_, 256), 256, 0, st>>>(D, I.info, I.own, I.keys);
     size_t tb = I.sort_tmp_bytes;
     TCD_CUDA(cub::DeviceRadixSort::SortKeys(I.sort_tmp, tb, I.keys, I.keys_sorted, 3 * nsv_, 0, 64, st));
     k_rel<<<blocks(3 * int64_t(nsv_), 256), 256, 0, st>>>(D, I.keys_sorted, 3 * nsv_, I.info, I.rel);
+    size_t sb = I.select_tmp_bytes;
+    TCD_CUDA(cub::DeviceSelect::Flagged(I.select_tmp, sb, thrust::counting_iterator<int32_t>(0), I.info, I.list,
+                                        I.nlist, nslots_, st));
     TCD_CUDA(cudaGetLastError());
 }
 
@@ -665,7 +668,7 @@ void Detector::reset(cudaStream_t st) {
     TCD_CUDA(cudaMemsetAsync(I.hit, 0xff, sizeof(int32_t) * std::max(nsv_, 1), st));
     TCD_CUDA(cudaMemsetAsync(I.pen, 0, std::max(nsv_, 1), st));
     TCD_CUDA(cudaMemsetAsync(I.info, 0, std::max(nslots_, 1), st));
-    TCD_CUDA(cudaMemsetAsync(I.ninv, 0, sizeof(int32_t), st));
+    TCD_CUDA(cudaMemsetAsync(I.nlist, 0, sizeof(int32_t), st));
 }
 
 Records Detector::records() const {
@@ -674,9 +677,8 @@ Records Detector::records() const {
     r.info = d_->info;
     r.own = d_->own;
     r.rel = d_->rel;
-    r.inv = d_->inv;
-    r.ninv = d_->ninv;
-    r.inv_cap = 4 * nsv_;
+    r.list = d_->list;
+    r.nlist = d_->nlist;
     return r;
 }
 

@@ -45,16 +45,14 @@ struct Params {
 //   info: bit 3 = the vertex has its own contact (own[slot]), bits 0-2 = number of
 //         relations (contacts whose face holds this vertex, at most 4);
 //   own:  the contact face's vertex slots (x, y, z) and mesh (w);
-//   rel:  4 per slot, (colliding vertex slot << 2) | vertex order in the face.
-// Contact-involved slots (every contact's vertex and face vertices, with repeats) are
-// listed in inv[0 .. *ninv) for the per-iteration snapshot of their positions.
+//   rel:  4 per slot, (colliding vertex slot << 2) | vertex order in the face;
+//   list: the slots with info != 0, ascending, list[0 .. *nlist).
 struct Records {
     const uint8_t* info = nullptr;
     const int4* own = nullptr;
     const int32_t* rel = nullptr;
-    const int32_t* inv = nullptr;
-    const int32_t* ninv = nullptr;
-    int32_t inv_cap = 0;
+    const int32_t* list = nullptr;
+    const int32_t* nlist = nullptr;
 };
 
 class Detector {

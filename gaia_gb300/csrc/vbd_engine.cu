@@ -380,8 +380,8 @@ public:
         P.col_info = rc.info;
         P.col_own = rc.own;
         P.col_rel = rc.rel;
-        P.usnap = d_usnap_.p;
         P.mesh_fric = d_mesh_fric_.p;
+        P.col_scratch = d_col_scratch_.p;
         return P;
     }
 
@@ -429,12 +429,11 @@ public:
         }
         cd_.init(t, prm, bytes_);
         if (!cd_.enabled()) return;
-        std::vector<float2> fr(nmesh_);
-        for (int m = 0; m < nmesh_; ++m) fr[m] = make_float2(float(sc_.objs[m].frictionDynamic), float(sc_.objs[m].frictionEpsV));
+        std::vector<double2> fr(nmesh_);
+        for (int m = 0; m < nmesh_; ++m) fr[m] = make_double2(sc_.objs[m].frictionDynamic, sc_.objs[m].frictionEpsV);
         d_mesh_fric_.upload(fr, &bytes_, st_);
         d_xf_.alloc(2 * size_t(nslots_), &bytes_);
-        d_usnap_.alloc(nslots_, &bytes_);
-        GAIA_CUDA(cudaMemcpyAsync(d_usnap_.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+        d_col_scratch_.alloc(9 * size_t(nslots_), &bytes_);
         enqueue_gather();
         cd_.build(d_xf_.p, st_);
         GAIA_CUDA(cudaStreamSynchronize(st_));
@@ -452,12 +451,19 @@ public:
         cd_.enqueue(d_xf_.p, intermediate, rebuild, st_);
     }
 
-    void enqueue_snapshot() {
-        if (!cd_.enabled()) return;
+    // Contact sums of the vertices with records in [beg, end), before that color's solve.
+    void launch_contact_color(int beg, int end, bool pdl) {
         const tetcd::Records rc = cd_.records();
-        if (rc.inv_cap <= 0) return;
-        dev::k_snapshot_contacts<ST><<<div_up(rc.inv_cap, 256), 256, 0, st_>>>(rc.inv, rc.ninv, rc.inv_cap, d_pos_.p, d_usnap_.p);
-        GAIA_CUDA(cudaGetLastError());
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kContactBlocks);
+        cfg.blockDim = dim3(128);
+        cfg.stream = st_;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = pdl ? attr : nullptr;
+        cfg.numAttrs = pdl ? 1 : 0;
+        GAIA_CUDA(cudaLaunchKernelEx(&cfg, dev::k_contact_color<ST, R>, ptrs(), c_, beg, end, rc.list, rc.nlist));
     }
 
     // ---- kernels ----------------------------------------------------------------
@@ -597,7 +603,6 @@ public:
         // intermediateCollisionDetection (VBDPhysics.cpp:878-884)
         const int ici = sc_.p.intermediateCollisionIterations;
         if (ici > 0 && it % ici == 0 && it) enqueue_detection(true, false);
-        enqueue_snapshot();
         if (accel) {
             // getAcceleratorOmega (VBDPhysics.cpp:3558-3574)
             double rho = sc_.p.acceleratorRho;
@@ -606,13 +611,17 @@ public:
             GAIA_CUDA(cudaMemcpyAsync(d_acc_prev_.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
         }
         // programmatic launch only directly after another solve kernel in the stream
-        // (with contacts the previous kernel is the snapshot kernel; k_solve reads no
-        // dynamic data before its griddepcontrol.wait either way)
+        // (k_contact_color and k_solve read no dynamic data before griddepcontrol.wait)
         bool after_solve = it > 0 && !accel;
+        const bool contacts = cd_.enabled();
         for (size_t g = 0; g < group_beg_.size(); ++g) {
             const int n = group_end_[g] - group_beg_[g];
             if (n <= 0) continue;
             const ColorCfg& cc = ccfg_[g];
+            if (contacts) {
+                launch_contact_color(group_beg_[g], group_end_[g], use_pdl_ && after_solve);
+                after_solve = true;
+            }
             launch_solve<false>(cc.L, cc.B, group_beg_[g], group_end_[g], friction, nullptr,
                                 use_pdl_ && after_solve, cc.variant);
             after_solve = true;
@@ -1000,6 +1009,7 @@ public:
         if (v < 0 || v >= n) throw std::invalid_argument("vertex index out of range");
         int32_t s = slot_of_[off + v];
         if (s >= nactive_) throw std::invalid_argument("vertex is fixed (not solved)");
+        if (cd_.enabled()) launch_contact_color(s, s + 1, false);
         launch_solve<true>(lanes_, block_, s, s + 1, friction, d_probe_.p);
         double h[12];
         GAIA_CUDA(cudaMemcpyAsync(h, d_probe_.p, sizeof(h), cudaMemcpyDeviceToHost, st_));
@@ -1034,8 +1044,8 @@ private:
     cudaGraphExec_t g_init_ = nullptr, g_init_rb_ = nullptr, g_sweep_ = nullptr, g_vel_ = nullptr;
     tetcd::Detector cd_;
     DevBuf<float4> d_xf_;
-    DevBuf<S4> d_usnap_;
-    DevBuf<float2> d_mesh_fric_;
+    DevBuf<double2> d_mesh_fric_;
+    DevBuf<R> d_col_scratch_;
     int nmesh_ = 0;
     int64_t nslots_ = 0;
     int32_t nactive_ = 0, ninc_ = 0;
@@ -1048,6 +1058,7 @@ private:
     int variant_fixed_ = -1;   // from PhysicsParams solveVariant (-1 = autotune)
     std::map<std::pair<int, int>, int> maxrec_cache_;
     static constexpr size_t kTmaSmemMax = 200 * 1024;
+    static constexpr int kContactBlocks = 64;
     double tuned_ms_ = 0.0;
     int64_t launches_per_substep_ = 0, launches_per_step_ = 0;
     size_t bytes_ = 0;

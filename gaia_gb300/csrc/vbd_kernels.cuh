@@ -110,8 +110,8 @@ struct Ptrs {
     const uint8_t* col_info;
     const int4* col_own;
     const int32_t* col_rel;
-    const typename ST::U* usnap;   // contact-involved slots at the start of the iteration
-    const float2* mesh_fric;       // per mesh: frictionDynamic, frictionEpsV
+    const double2* mesh_fric;      // per mesh: frictionDynamic, frictionEpsV
+    R* col_scratch;                // 9 per slot: contact force (3) and Hessian (6) of the solve
 };
 
 struct DeformerDev {
@@ -340,38 +340,27 @@ struct V3T<double> {
     using type = double3;
 };
 
-// A contact partner's displacement: slots of the color being solved are read from the
-// snapshot taken at the start of the iteration, so that, as in the reference's
-// Jacobi-within-color update (positionsNew), no vertex sees a same-color partner's new
-// position; other slots are read live (their colors are complete).
-template <typename ST, typename R, bool PROBE>
-__device__ __forceinline__ typename ST::U contact_u(const Ptrs<ST, R>& P, int s, int beg, int end) {
-    return (!PROBE && s >= beg && s < end) ? P.usnap[s] : P.u[s];
-}
-
 // accumlateCollisionForceAndHessianPerCollision_v2: the contact of vertex sp with its
 // recorded face, at the current positions, on the contact vertex of index `order`
 // (3 = sp itself, 0..2 = a face vertex). Positions are taken relative to sp's: q - p =
 // (X_q - X_p) + (u_q - u_p). Penalty k * depth along the face normal (interior closest
 // point) or the closest-point direction oriented like the face normal, lagged IPC
 // friction in the frame (edge AB, AB x n); scaled by b = 1 (sp) or -barycentric.
-template <typename ST, typename R, bool PROBE>
-__device__ __forceinline__ void contact_term(const Ptrs<ST, R>& P, const Consts<R>& c, int sp, int order, int beg,
-                                             int end, R* f, R* H) {
+template <typename ST, typename R>
+__device__ __forceinline__ void contact_term(const Ptrs<ST, R>& P, const Consts<R>& c, int sp, int order, R* f,
+                                             R* H) {
     using U = typename ST::U;
     using V = typename V3T<R>::type;
     const int4 fo = P.col_own[sp];
-    const U up = contact_u<ST, R, PROBE>(P, sp, beg, end);
-    const U uq[3] = {contact_u<ST, R, PROBE>(P, fo.x, beg, end), contact_u<ST, R, PROBE>(P, fo.y, beg, end),
-                     contact_u<ST, R, PROBE>(P, fo.z, beg, end)};
     const int fs[3] = {fo.x, fo.y, fo.z};
+    const U up = P.u[sp];
     const float4 Xp = P.rest[sp];
     V q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const float4 Xq = P.rest[fs[k]];
         R d[3];
-        ST::diff(uq[k], up, d);
+        ST::diff(P.u[fs[k]], up, d);
         q[k] = V{R(Xq.x) - R(Xp.x) + d[0], R(Xq.y) - R(Xp.y) + d[1], R(Xq.z) - R(Xp.z) + d[2]};
     }
     const V o{R(0), R(0), R(0)};
@@ -406,7 +395,7 @@ __device__ __forceinline__ void contact_term(const Ptrs<ST, R>& P, const Consts<
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         R dk[3];
-        ST::diff(uq[k], P.xprev[fs[k]], dk);
+        ST::diff(P.u[fs[k]], P.xprev[fs[k]], dk);
         dx[0] -= bk[k] * dk[0];
         dx[1] -= bk[k] * dk[1];
         dx[2] -= bk[k] * dk[2];
@@ -420,31 +409,51 @@ __device__ __forceinline__ void contact_term(const Ptrs<ST, R>& P, const Consts<
     const R ta[3] = {t0.x, t0.y, t0.z}, tb[3] = {t1.x, t1.y, t1.z};
     const R u0 = ta[0] * dx[0] + ta[1] * dx[1] + ta[2] * dx[2];
     const R u1 = tb[0] * dx[0] + tb[1] * dx[1] + tb[2] * dx[2];
-    const float2 fp = P.mesh_fric[P.slot_mesh[sp]], ff = P.mesh_fric[fo.w];
+    const double2 fp = P.mesh_fric[P.slot_mesh[sp]], ff = P.mesh_fric[fo.w];
     const R mu = (R(fp.x) + R(ff.x)) * R(0.5);
     const R epsU = (R(fp.y) + R(ff.y)) * R(0.5) * c.dt;
     cloth::friction<R>(mu, lambda, ta, tb, u0, u1, epsU, b, f, H);
 }
 
-template <typename R>
-struct ContactSum {
-    R f[3], H[6];
-};
-
-// accumulateCollisionForceAndHessian: the vertex's own contact, then its relations.
-// Out of line and returning by value, so that the solve's force and Hessian stay in
-// registers on the common path (no contact).
-template <typename ST, typename R, bool PROBE>
-__device__ __forceinline__ ContactSum<R> contact_forces(const Ptrs<ST, R>& P, const Consts<R>& c, int v, int info,
-                                                     int beg, int end) {
-    ContactSum<R> s{};
-    if (info & 8) contact_term<ST, R, PROBE>(P, c, v, 3, beg, end, s.f, s.H);
-    const int nrel = info & 7;
-    for (int j = 0; j < nrel; ++j) {
-        const int e = P.col_rel[4 * v + j];
-        contact_term<ST, R, PROBE>(P, c, e >> 2, e & 3, beg, end, s.f, s.H);
+// accumulateCollisionForceAndHessian (VBDPhysicsCompute.cu:1731-1773) for the vertices
+// with contact records in the slot range [beg, end) of one color, evaluated just before
+// that color's solve kernel: the vertex's own contact, then its relations, summed into
+// its 9 scratch values, which the solve adds between inertia and boundary. Running
+// before the color's solve, every read sees the positions of earlier colors updated and
+// those of this color not yet, which is the reference's Jacobi-within-color update
+// (positionsNew, VBDPhysicsCompute.cu:803-908). `list` holds the slots with records,
+// ascending, so a color's vertices are one sub-range.
+template <typename ST, typename R>
+__global__ void __launch_bounds__(128) k_contact_color(Ptrs<ST, R> P, Consts<R> c, int beg, int end,
+                                                       const int32_t* list, const int32_t* nlist) {
+    pdl_launch_dependents();
+    pdl_wait();
+    const int n = *nlist;
+    auto lower = [&](int key) {
+        int lo = 0, hi = n;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (list[mid] < key) lo = mid + 1;
+            else hi = mid;
+        }
+        return lo;
+    };
+    const int i0 = lower(beg), i1 = lower(end);
+    for (int i = i0 + int(blockIdx.x * blockDim.x + threadIdx.x); i < i1; i += int(gridDim.x * blockDim.x)) {
+        const int v = list[i];
+        const int info = P.col_info[v];
+        R f[3] = {R(0), R(0), R(0)}, H[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};
+        if (info & 8) contact_term<ST, R>(P, c, v, 3, f, H);
+        const int nrel = info & 7;
+        for (int j = 0; j < nrel; ++j) {
+            const int e = P.col_rel[4 * v + j];
+            contact_term<ST, R>(P, c, e >> 2, e & 3, f, H);
+        }
+        R* o = P.col_scratch + 9 * size_t(v);
+        o[0] = f[0]; o[1] = f[1]; o[2] = f[2];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) o[3 + k] = H[k];
     }
-    return s;
 }
 
 // Minimum resident blocks of 256 threads: caps FP32-compute kernels at 64
@@ -538,15 +547,13 @@ __device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R
         f[2] += w * dy[2];
         H[0] += w; H[3] += w; H[5] += w;
     }
-    // tet-mesh contact (between inertia and boundary, VBDPhysicsCompute.cu:893-895)
-    if (P.col_info) {
-        const int info = P.col_info[v];
-        if (info) {
-            const ContactSum<R> cs = contact_forces<ST, R, PROBE>(P, c, v, info, beg, end);
-            f[0] += cs.f[0]; f[1] += cs.f[1]; f[2] += cs.f[2];
+    // tet-mesh contact (between inertia and boundary, VBDPhysicsCompute.cu:893-895),
+    // evaluated by k_contact_color just before this color
+    if (P.col_info && P.col_info[v]) {
+        const R* cs = P.col_scratch + 9 * size_t(v);
+        f[0] += cs[0]; f[1] += cs[1]; f[2] += cs[2];
 #pragma unroll
-            for (int i = 0; i < 6; ++i) H[i] += cs.H[i];
-        }
+        for (int i = 0; i < 6; ++i) H[i] += cs[3 + i];
     }
     // plane ground / world box with friction on each violated axis (VBDPhysics.cpp:2858-2953)
     if (c.plane) {
@@ -852,16 +859,6 @@ __global__ void k_gather_xf(const typename ST::U* u, const typename ST::U* xprev
     ST::to_d(xprev[s], b);
     xf[s] = make_float4(float(double(X.x) + a[0]), float(double(X.y) + a[1]), float(double(X.z) + a[2]), 0.f);
     xf[nslots + s] = make_float4(float(double(X.x) + b[0]), float(double(X.y) + b[1]), float(double(X.z) + b[2]), 0.f);
-}
-
-// Snapshot of the contact-involved slots' displacements at the start of an iteration.
-template <typename ST>
-__global__ void k_snapshot_contacts(const int32_t* inv, const int32_t* ninv, int32_t cap, const typename ST::U* u,
-                                    typename ST::U* usnap) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= cap || i >= *ninv) return;
-    const int s = inv[i];
-    usnap[s] = u[s];
 }
 
 // ---------------------------------------------------------------------------
