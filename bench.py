@@ -143,6 +143,8 @@ def make_scene(workload: str, d: str, precision: str, size: int, iterations: int
         return scenes.drop_cube(d, n=size, iterations=iterations, precision=precision)
     if workload == "batch":
         return scenes.batch_cubes(d, n_scenes=512, iterations=iterations, precision=precision)
+    if workload == "collide":
+        return scenes.collision_drop(d, n_objects=32, iterations=iterations, precision=precision)
     raise ValueError(workload)
 
 
@@ -201,6 +203,9 @@ def run_reference(args, world, rank):
 def workload_name(args) -> str:
     if args.workload == "batch":
         return f"batch_cubes_512 (sides 4..24), {args.iterations} iterations/step, dt=1/300"
+    if args.workload == "collide":
+        return (f"collision_drop_32 (16 lattice cubes of 8..20 vertices per side, 16 tet balls r 0.05..0.15 m, "
+                f"1 m box, tet-surface CCD + DCD every substep), {args.iterations} iterations/step, dt=1/300")
     return f"{args.workload}_cube_{args.size}^3, {args.iterations} iterations/step, dt=1/300"
 
 
@@ -475,7 +480,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gaia", choices=["gaia", "reference"])
-    ap.add_argument("--workload", default="twist", choices=["twist", "drop", "batch", "cloth"])
+    ap.add_argument("--workload", default="twist", choices=["twist", "drop", "batch", "cloth", "collide"])
     ap.add_argument("--size", type=int, default=0,
                     help="vertices per cube edge (0 = the workload's own: twist 100, drop 10)")
     ap.add_argument("--iterations", type=int, default=0,
@@ -497,7 +502,9 @@ def main():
                     help="PhysicsParams override key=json_value (e.g. usePDL=false)")
     args = ap.parse_args()
     if args.iterations <= 0:
-        args.iterations = 50 if args.workload == "twist" else 20
+        args.iterations = {"twist": 50, "collide": 30}.get(args.workload, 20)
+    if args.workload == "collide" and args.error_steps == 100:
+        args.error_steps = 20  # contact sets change discretely; long horizons diverge chaotically
     if args.size <= 0:
         args.size = {"drop": 10, "cloth": 512}.get(args.workload, 100)
     world, rank, local = dist_setup()

@@ -136,13 +136,17 @@ def physics_params(timeStep: float, iterations: int, numSubsteps: int = 1, gravi
     return p
 
 
+# CollisionParams of scenes without contact between meshes (contact detection off)
+NO_CONTACT = {"allowCCD": False, "allowDCD": False}
+
+
 def _write_json(dirname: str, models: list[dict], params: dict, deformers: list[dict] | None = None,
-                meta: dict | None = None) -> tuple[str, str]:
+                meta: dict | None = None, collision: dict | None = None) -> tuple[str, str]:
     mp = os.path.join(dirname, "Models.json")
     pp = os.path.join(dirname, "Parameters.json")
     with open(mp, "w") as f:
         json.dump({"Models": models}, f, indent=1)
-    P = {"PhysicsParams": params, "CollisionParams": {}, "ViewerParams": {"enableViewer": False}}
+    P = {"PhysicsParams": params, "CollisionParams": dict(collision or {}), "ViewerParams": {"enableViewer": False}}
     if deformers:
         P["Deformers"] = deformers
     if meta:
@@ -192,7 +196,8 @@ def twist_cube(dirname: str, n: int = 100, precision: str = "mixed", iterations:
                spacing: float = 0.01, omega: float = 2.0) -> tuple[str, str]:
     """Twist test: an n^3 lattice cube with its long (x) axis on the world x axis;
     both x-end faces are Dirichlet and the x-max face rotates at `omega` rad/s about
-    the x axis (Rotator deformer). Same material, dt=1/300, `iterations` per step."""
+    the x axis (Rotator deformer). Same material, dt=1/300, `iterations` per step.
+    A single body without contact: CollisionParams turn contact detection off."""
     half = 0.5 * spacing * (n - 1)
     X, T = lattice_cube((n, n, n), spacing, (0.0, -half, -half), jitter=1e-4, seed=seed)
     tp, cp = _write_mesh(dirname, f"twist{n}", X, T)
@@ -204,14 +209,15 @@ def twist_cube(dirname: str, n: int = 100, precision: str = "mixed", iterations:
     params = physics_params(1.0 / 300.0, iterations, precision=precision)
     deformers = [{"DeformerName": "Rotator", "center": [0.0, 0.0, 0.0], "axis": [1.0, 0.0, 0.0],
                   "angularVelocity": omega, "selectedMeshes": [0], "selectedVertices": [right]}]
-    return _write_json(dirname, models, params, deformers, meta={"workload": f"twist_cube_{n}", "seed": seed})
+    return _write_json(dirname, models, params, deformers, meta={"workload": f"twist_cube_{n}", "seed": seed},
+                       collision=NO_CONTACT)
 
 
 def batch_cubes(dirname: str, n_scenes: int = 512, side_range=(4, 24), precision: str = "mixed",
                 iterations: int = 20, seed: int = 7, spacing: float = 0.01) -> tuple[str, str]:
     """Batching form: `n_scenes` independent lattice cubes, side drawn uniformly from
     side_range (vertices per edge), E ~ U(1e5, 1e7), nu ~ U(0.3, 0.45), laid out on a
-    grid above one ground plane (no inter-object contact), dt=1/300."""
+    grid above one ground plane (no inter-object contact, contact detection off), dt=1/300."""
     rng = np.random.Generator(np.random.PCG64(seed))
     sides = rng.integers(side_range[0], side_range[1] + 1, size=n_scenes)
     Es = rng.uniform(1e5, 1e7, size=n_scenes)
@@ -230,7 +236,77 @@ def batch_cubes(dirname: str, n_scenes: int = 512, side_range=(4, 24), precision
         models.append(model_entry(tp, cp, E=float(Es[s]), nu=float(nus[s]), translation=[tx, 0.1, tz]))
     params = physics_params(1.0 / 300.0, iterations, ground_y=0.0, precision=precision)
     return _write_json(dirname, models, params,
-                       meta={"workload": f"batch_cubes_{n_scenes}", "seed": seed, "sides": sides.tolist()})
+                       meta={"workload": f"batch_cubes_{n_scenes}", "seed": seed, "sides": sides.tolist()},
+                       collision=NO_CONTACT)
+
+
+def lattice_ball(radius: float, spacing: float, jitter: float = 0.0, seed: int = 1) -> tuple[np.ndarray, np.ndarray]:
+    """A tetrahedralised ball: the cells of a 5-tet lattice (see lattice_cube) whose
+    centres lie within `radius` of the origin, unused vertices dropped."""
+    n = int(np.ceil(2 * radius / spacing)) + 2
+    X, T = lattice_cube((n, n, n), spacing, (-(n - 1) * spacing / 2,) * 3, jitter=jitter, seed=seed)
+    c = X[T].mean(axis=1)
+    # a cell's 5 tets share its centre; keep cells, not single tets, so the surface stays manifold
+    cell_c = c.reshape(-1, 5, 3).mean(axis=1)
+    keep = np.repeat(np.linalg.norm(cell_c, axis=1) <= radius, 5)
+    T = T[keep]
+    used = np.unique(T)
+    remap = -np.ones(len(X), np.int64)
+    remap[used] = np.arange(len(used))
+    return X[used], remap[T].astype(np.int32)
+
+
+def collision_drop(dirname: str, n_objects: int = 32, precision: str = "mixed", iterations: int = 30,
+                   seed: int = 5, cube_sides=(8, 20), ball_radii=(0.05, 0.15), ball_tets=(5000, 40000),
+                   cube_spacing: float = 0.008, box: float = 1.0) -> tuple[str, str]:
+    """Collision-heavy drop: `n_objects` tet meshes, half lattice cubes (side drawn from
+    cube_sides vertices, `cube_spacing` apart) and half tetrahedralised balls (radius from
+    ball_radii, lattice spacing chosen for a tet count in ball_tets), at seeded random,
+    non-overlapping positions and random orientations in a `box`-metre world box with
+    walls, Neo-Hookean E=1e6, nu=0.4, rho=1000, gravity -9.8, dt=1/300, `iterations` per
+    step; vertex-face contact between and within objects (CCD and DCD)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    os.makedirs(dirname, exist_ok=True)
+    shapes = []
+    for k in range(n_objects):
+        if k % 2 == 0:
+            n = int(rng.integers(cube_sides[0], cube_sides[1] + 1))
+            X, T = lattice_cube((n, n, n), cube_spacing, (0.0, 0.0, 0.0), jitter=1e-4, seed=seed + k)
+            X = X - X.mean(axis=0)
+            name = f"cube{k}"
+        else:
+            r = float(rng.uniform(*ball_radii))
+            ntet = float(rng.uniform(*ball_tets))
+            h = (4.0 / 3.0 * np.pi * r ** 3 / (ntet / 5.0)) ** (1.0 / 3.0)
+            X, T = lattice_ball(r, h, jitter=1e-4 * h / 0.01, seed=seed + k)
+            name = f"ball{k}"
+        shapes.append((name, X, T, float(np.linalg.norm(X, axis=1).max())))
+    # place: largest first, rejection-sampled centres inside the box, no bounding-sphere overlap
+    order = sorted(range(n_objects), key=lambda k: -shapes[k][3])
+    centres = [None] * n_objects
+    placed = []
+    for k in order:
+        R = shapes[k][3]
+        for _ in range(20000):
+            c = rng.uniform(R + 0.01, box - R - 0.01, size=3)
+            if all(np.linalg.norm(c - pc) > R + pr + 0.01 for pc, pr in placed):
+                break
+        else:
+            raise RuntimeError("could not place all objects in the box")
+        centres[k] = c
+        placed.append((c, R))
+    models = []
+    for k, (name, X, T, R) in enumerate(shapes):
+        tp, cp = _write_mesh(dirname, name, X, T)
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        angle = float(rng.uniform(0, np.pi))
+        models.append(model_entry(tp, cp, rotation=(axis * angle).tolist(), translation=centres[k].tolist()))
+    params = physics_params(1.0 / 300.0, iterations, precision=precision,
+                            worldBounds=[[0.0, 0.0, 0.0], [box, box, box]], collisionStiffness=1e5)
+    nv = int(sum(len(s[1]) for s in shapes))
+    return _write_json(dirname, models, params,
+                       meta={"workload": f"collision_drop_{n_objects}", "seed": seed, "vertices": nv})
 
 
 def set_precision(params_json: str, precision: str, out_path: str | None = None, **overrides) -> str:
