@@ -72,6 +72,8 @@ _SIGNATURES = {
     "gaia_vbd_collide": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gaia_vbd_get_contacts": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     "gaia_vbd_load_state": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "gaia_vbd_write_ply": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32, C.c_int32]),
+    "gaia_vbd_write_binary": (C.c_int, [C.c_void_p, C.c_char_p]),
     "gaia_vbd_run_step_timed": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "gaia_vbd_autotune": (C.c_int, [C.c_void_p]),
     "gaia_vbd_reset": (C.c_int, [C.c_void_p]),
@@ -113,6 +115,8 @@ _SIGNATURES = {
     "gaia_cloth_synchronize": (C.c_int, [C.c_void_p]),
     "gaia_cloth_save_state": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
     "gaia_cloth_load_state": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "gaia_cloth_write_ply": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32, C.c_int32]),
+    "gaia_cloth_write_binary": (C.c_int, [C.c_void_p, C.c_char_p]),
     "gaia_cloth_num_meshes": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "gaia_cloth_num_vertices": (C.c_int64, [C.c_void_p, C.c_int32]),
     "gaia_cloth_num_faces": (C.c_int64, [C.c_void_p, C.c_int32]),

@@ -66,6 +66,12 @@ class VBDClothSimulationFramework:
     def recoverFromState(self, path: str) -> None:
         self._check(lib().gaia_cloth_load_state(self.h, path.encode()))
 
+    def writePLY(self, path: str, saveAllModelsTogether: bool = False, addModelName: bool = False) -> None:
+        self._check(lib().gaia_cloth_write_ply(self.h, path.encode(), int(saveAllModelsTogether), int(addModelName)))
+
+    def writeBinary(self, path: str) -> None:
+        self._check(lib().gaia_cloth_write_binary(self.h, path.encode()))
+
     def run_steps_timed(self, n: int) -> float:
         ms = C.c_float()
         self._check(lib().gaia_cloth_run_step_timed(self.h, n, C.byref(ms)))

@@ -1415,6 +1415,34 @@ int gaia_cloth_run_step(gaia_cloth* h, int32_t n) {
     });
 }
 
+namespace {
+// All vertices and faces of every simulated mesh (TriMeshFEM::saveAsPLY, writeAllToBinary).
+std::vector<gaia::FrameMesh> cloth_frame(gaia_cloth* h) {
+    std::vector<gaia::FrameMesh> out;
+    for (int m = 0; m < h->scene.numSim; ++m) {
+        const gaia::cloth::TriMesh& M = h->scene.meshes[m];
+        std::vector<double> x(3 * size_t(M.nv));
+        h->eng->get_positions(m, x.data());
+        gaia::FrameMesh fm;
+        fm.X.assign(x.begin(), x.end());
+        fm.faces = M.faces;
+        fm.model_path = h->scene.objs[m].path;
+        out.push_back(std::move(fm));
+    }
+    return out;
+}
+}  // namespace
+
+int gaia_cloth_write_ply(gaia_cloth* h, const char* path, int32_t all_in_one, int32_t add_model_name) {
+    if (!h || !h->eng || !path) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { gaia::write_frame_ply(path, cloth_frame(h), all_in_one != 0, add_model_name != 0, true); });
+}
+
+int gaia_cloth_write_binary(gaia_cloth* h, const char* path) {
+    if (!h || !h->eng || !path) return GAIA_VBD_E_INVALID_ARG;
+    return cguard(h, [&] { gaia::write_frame_binary(path, cloth_frame(h)); });
+}
+
 int gaia_cloth_save_state(gaia_cloth* h, const char* path, int32_t binary) {
     if (!h || !h->eng || !path) return GAIA_VBD_E_INVALID_ARG;
     return cguard(h, [&] {

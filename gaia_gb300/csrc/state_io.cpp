@@ -143,4 +143,60 @@ PhysicsStateFile read_physics_state(const std::string& path) {
     return s;
 }
 
+namespace {
+
+std::string ext_of(const std::string& path) {
+    const size_t k = path.find_last_of('/');
+    const std::string name = k == std::string::npos ? path : path.substr(k + 1);
+    const size_t d = name.find_last_of('.');
+    return d == std::string::npos ? std::string() : name.substr(d);
+}
+
+void save_ply(const std::string& path, const std::vector<float>& X, const std::vector<int32_t>& F) {
+    FILE* fp = std::fopen(path.c_str(), "w");
+    if (!fp) throw std::runtime_error("cannot write " + path);
+    const size_t nv = X.size() / 3, nf = F.size() / 3;
+    std::fprintf(fp, "ply\nformat ascii 1.0\ncomment Mocap generated\nelement vertex %zu\n", nv);
+    std::fprintf(fp, "property float x\nproperty float y\nproperty float z\n");
+    if (nf) std::fprintf(fp, "element face %zu \nproperty list uchar int vertex_indices\n", nf);
+    std::fprintf(fp, "end_header\n");
+    for (size_t i = 0; i < nv; ++i) std::fprintf(fp, "%f %f %f\n", double(X[3 * i]), double(X[3 * i + 1]), double(X[3 * i + 2]));
+    for (size_t i = 0; i < nf; ++i) std::fprintf(fp, "3 %d %d %d\n", F[3 * i], F[3 * i + 1], F[3 * i + 2]);
+    std::fclose(fp);
+}
+
+}  // namespace
+
+void write_frame_ply(const std::string& output, const std::vector<FrameMesh>& meshes, bool all_in_one,
+                     bool add_model_name, bool tri_mesh_naming) {
+    if (all_in_one) {
+        std::vector<float> X;
+        std::vector<int32_t> F;
+        int32_t off = 0;
+        for (const FrameMesh& m : meshes) {
+            X.insert(X.end(), m.X.begin(), m.X.end());
+            for (int32_t f : m.faces) F.push_back(f + off);
+            off += int32_t(m.X.size() / 3);
+        }
+        save_ply(output, X, F);
+        return;
+    }
+    const std::string dir = dir_of(output), stem = stem_of(output), ext = ext_of(output);
+    for (size_t i = 0; i < meshes.size(); ++i) {
+        char num[16];
+        std::snprintf(num, sizeof(num), tri_mesh_naming ? "%04d" : "%06d", int(i));
+        std::string name = dir + "/" + stem + (tri_mesh_naming ? "Model_" : "_Model_") + num;
+        if (add_model_name) name += "_" + stem_of(meshes[i].model_path);
+        name += tri_mesh_naming ? "_" + ext : ext;
+        save_ply(name, meshes[i].X, meshes[i].faces);
+    }
+}
+
+void write_frame_binary(const std::string& output, const std::vector<FrameMesh>& meshes) {
+    std::ofstream f(output, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot write " + output);
+    for (const FrameMesh& m : meshes)
+        f.write(reinterpret_cast<const char*>(m.X.data()), std::streamsize(m.X.size() * sizeof(float)));
+}
+
 }  // namespace gaia

@@ -1222,6 +1222,43 @@ int gaia_vbd_run_step(gaia_vbd* h, int32_t n_steps) {
     });
 }
 
+namespace {
+// Surface vertices (FP32 positions) and surface faces in surface-vertex numbering of every
+// mesh: what TetMeshFEM::saveAsPLY and writeAllToBinary write (surfaceVIds order here is
+// ascending vertex id).
+std::vector<gaia::FrameMesh> tet_frame(gaia_vbd* h) {
+    std::vector<gaia::FrameMesh> out;
+    for (size_t m = 0; m < h->scene.meshes.size(); ++m) {
+        const gaia::TetMesh& M = h->scene.meshes[m];
+        std::vector<double> x(3 * size_t(M.nv));
+        h->eng->get_positions(int(m), x.data());
+        gaia::FrameMesh fm;
+        std::vector<int32_t> local(size_t(M.nv), -1);
+        for (size_t i = 0; i < M.sverts.size(); ++i) {
+            const int32_t v = M.sverts[i];
+            local[size_t(v)] = int32_t(i);
+            for (int d = 0; d < 3; ++d) fm.X.push_back(float(x[3 * size_t(v) + d]));
+        }
+        for (int32_t v : M.sfaces) fm.faces.push_back(local[size_t(v)]);
+        fm.model_path = h->scene.objs[m].path;
+        out.push_back(std::move(fm));
+    }
+    return out;
+}
+}  // namespace
+
+int gaia_vbd_write_ply(gaia_vbd* h, const char* path, int32_t all_in_one, int32_t add_model_name) {
+    GAIA_NEED(h);
+    if (!path) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { gaia::write_frame_ply(path, tet_frame(h), all_in_one != 0, add_model_name != 0, false); });
+}
+
+int gaia_vbd_write_binary(gaia_vbd* h, const char* path) {
+    GAIA_NEED(h);
+    if (!path) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { gaia::write_frame_binary(path, tet_frame(h)); });
+}
+
 int gaia_vbd_save_state(gaia_vbd* h, const char* path, int32_t binary) {
     GAIA_NEED(h);
     if (!path) return GAIA_VBD_E_INVALID_ARG;

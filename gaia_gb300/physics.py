@@ -143,6 +143,14 @@ class VBDPhysics:
         with open(path) as f:
             self.frameId = int(json.load(f).get("frameId", -1))
 
+    # -- output frames (BasePhysicsFramework.cpp:442-489, IO/FileIO.cpp)
+    def writePLY(self, path: str, saveAllModelsTogether: bool = False, addModelName: bool = False) -> None:
+        _check(lib().gaia_vbd_write_ply(self.handle, path.encode(), int(saveAllModelsTogether), int(addModelName)),
+               self.handle)
+
+    def writeBinary(self, path: str) -> None:
+        _check(lib().gaia_vbd_write_binary(self.handle, path.encode()), self.handle)
+
     def autotune(self) -> None:
         _check(lib().gaia_vbd_autotune(self.handle), self.handle)
 

@@ -63,6 +63,11 @@ int gaia_cloth_synchronize(gaia_cloth* h);
 /* PhysicsState recovery file of the simulated meshes (same format as gaia_vbd_save_state). */
 int gaia_cloth_save_state(gaia_cloth* h, const char* path, int32_t binary);
 int gaia_cloth_load_state(gaia_cloth* h, const char* path);
+/* Output frames of the simulated meshes (BaseClothSimPhsicsFramework.cpp:130-160,
+ * IO/FileIO.cpp:86-117, 187-251): ASCII PLY of all vertices and faces, one file or one per
+ * mesh (<dir>/<stem>Model_<%04d>[_<model stem>]_<ext>), or raw FP32 xyz. */
+int gaia_cloth_write_ply(gaia_cloth* h, const char* path, int32_t all_in_one, int32_t add_model_name);
+int gaia_cloth_write_binary(gaia_cloth* h, const char* path);
 
 
 int gaia_cloth_num_meshes(gaia_cloth* h, int32_t* num_sim, int32_t* num_colliders);

@@ -100,6 +100,13 @@ int gaia_vbd_synchronize(gaia_vbd* h);
  * positions, velocities, the frame counter and the simulated time. */
 int gaia_vbd_save_state(gaia_vbd* h, const char* path, int32_t binary);
 int gaia_vbd_load_state(gaia_vbd* h, const char* path);
+/* Output frames as writeOutputs writes them (Framework/BasePhysicsFramework.cpp:442-489,
+ * IO/FileIO.cpp): the surface of every tet mesh as ASCII PLY, in one file (all_in_one)
+ * or one per mesh (<dir>/<stem>_Model_<%06d>[_<model stem>]<ext>), or the surface
+ * vertices of all meshes as raw FP32 xyz (the "bin" output). Surface vertices are in
+ * ascending vertex order. */
+int gaia_vbd_write_ply(gaia_vbd* h, const char* path, int32_t all_in_one, int32_t add_model_name);
+int gaia_vbd_write_binary(gaia_vbd* h, const char* path);
 
 /* Tet-mesh vertex-face contact (VBDPhysics::dcd / ccd / prepareCollisionDataGPU,
  * VBD/VBDPhysics.cpp:1812-2156; DiscreteCollisionDetector / ContinuousCollisionDetector).

@@ -146,3 +146,76 @@ def test_cloth_state_round_trip(tmp_path, gaia_lib):
     np.testing.assert_array_equal(ends[0], ends[1])
     motion = np.linalg.norm(x8 - x4)
     assert np.linalg.norm(ends[0] - x8) <= 1e-3 * motion, (np.linalg.norm(ends[0] - x8), motion)
+
+
+def _read_ply(path):
+    with open(path) as f:
+        lines = f.read().splitlines()
+    assert lines[0] == "ply" and lines[1] == "format ascii 1.0"
+    nv = int(next(l for l in lines if l.startswith("element vertex")).split()[2])
+    fl = [l for l in lines if l.startswith("element face")]
+    nf = int(fl[0].split()[2]) if fl else 0
+    body = lines[lines.index("end_header") + 1:]
+    X = np.array([[float(t) for t in l.split()] for l in body[:nv]]).reshape(-1, 3)
+    F = np.array([[int(t) for t in l.split()] for l in body[nv:nv + nf]], np.int64).reshape(-1, 4)
+    assert (F[:, 0] == 3).all()
+    return X, F[:, 1:]
+
+
+def test_tet_output_frames(tmp_path, gaia_lib):
+    """PLY (one per mesh, one for all) and raw FP32 frames of the tet surfaces."""
+    from gaia_gb300 import VBDPhysics, scenes
+
+    mp, pp = scenes.stack_drop(str(tmp_path / "s"), spacing=0.02, precision="fp64")
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, pp)
+    phys.initialize()
+    phys.runStep(3)
+    out = tmp_path / "out"
+    out.mkdir()
+    phys.writePLY(str(out / "A00000003.ply"))
+    phys.writePLY(str(out / "B00000003.ply"), saveAllModelsTogether=True)
+    phys.writePLY(str(out / "C00000003.ply"), addModelName=True)
+    phys.writeBinary(str(out / "A00000003.bin"))
+    allX, allF, off = [], [], 0
+    for m in range(2):
+        F, V = phys.surface(m)
+        x = phys.positions(m)[V]
+        local = -np.ones(phys.numVertices(m), np.int64)
+        local[V] = np.arange(len(V))
+        Xp, Fp = _read_ply(str(out / f"A00000003_Model_{m:06d}.ply"))
+        assert np.abs(Xp - x).max() <= 6e-7
+        np.testing.assert_array_equal(Fp, local[F])
+        name = ["lower", "upper"][m]
+        assert (out / f"C00000003_Model_{m:06d}_{name}.ply").exists()
+        allX.append(x)
+        allF.append(local[F] + off)
+        off += len(V)
+    Xa, Fa = _read_ply(str(out / "B00000003.ply"))
+    assert np.abs(Xa - np.concatenate(allX)).max() <= 6e-7
+    np.testing.assert_array_equal(Fa, np.concatenate(allF))
+    b = np.fromfile(str(out / "A00000003.bin"), np.float32).reshape(-1, 3)
+    np.testing.assert_array_equal(b, np.concatenate(allX).astype(np.float32))
+    phys.close()
+
+
+def test_cloth_output_frames(tmp_path, gaia_lib):
+    from gaia_gb300 import VBDClothSimulationFramework, scenes
+
+    mp, pp = scenes.cloth_on_sphere(str(tmp_path / "s"), n=10, side=0.3, sphere_radius=0.1, sphere_level=2,
+                                    contact_radius=0.01, iterations=4, dt=1.0 / 300.0, gap=0.004)
+    c = VBDClothSimulationFramework()
+    c.loadRunningparameters(mp, pp)
+    c.initialize()
+    c.runStep(2)
+    out = tmp_path / "out"
+    out.mkdir()
+    c.writePLY(str(out / "A00000002.ply"))
+    c.writeBinary(str(out / "A00000002.bin"))
+    x = c.positions(0)
+    Xp, Fp = _read_ply(str(out / "A00000002Model_0000_.ply"))
+    assert np.abs(Xp - x).max() <= 6e-7
+    assert Fp.shape[0] == c.numFaces(0)
+    b = np.fromfile(str(out / "A00000002.bin"), np.float32).reshape(-1, 3)
+    np.testing.assert_array_equal(b, x.astype(np.float32))
+    c.close()
