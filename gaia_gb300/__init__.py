@@ -8,7 +8,7 @@ points, the build recipe and the synthetic-scene writer.
 """
 from ._lib import GaiaError, lib  # noqa: F401
 from .cloth import VBDClothSimulationFramework, color_trimesh  # noqa: F401
-from .physics import VBDPhysics, color_greedy, color_mcs, write_coloring, write_t  # noqa: F401
+from .physics import VBDPhysics, color_gpu, color_greedy, color_mcs, write_coloring, write_t  # noqa: F401
 
-__all__ = ["VBDPhysics", "VBDClothSimulationFramework", "GaiaError", "lib", "color_greedy", "color_mcs",
+__all__ = ["VBDPhysics", "VBDClothSimulationFramework", "GaiaError", "lib", "color_greedy", "color_mcs", "color_gpu",
            "color_trimesh", "write_coloring", "write_t"]

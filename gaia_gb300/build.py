@@ -19,8 +19,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgaia_vbd.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["scene.cpp", "state_io.cpp", "vbd_engine.cu", "vbd_energy_noalloc.cu", "tet_cd.cu", "cloth_scene.cpp",
-           "cloth_cd.cu", "cloth_engine.cu"]
+SOURCES = ["scene.cpp", "state_io.cpp", "vbd_engine.cu", "vbd_energy_noalloc.cu", "tet_cd.cu", "coloring_gpu.cu",
+           "cloth_scene.cpp", "cloth_cd.cu", "cloth_engine.cu"]
 HEADERS = ["scene.hpp", "json_lite.hpp", "json_get.hpp", "vbd_kernels.cuh", "vbd_state.cuh", "cloth_scene.hpp",
            "cloth_cd.hpp", "cloth_dev.cuh", "lbvh.cuh", "state_io.hpp", "tet_cd.hpp"]
 PUBLIC_HEADERS = ["gaia_vbd.h", "gaia_cloth.h"]

@@ -259,6 +259,16 @@ def color_greedy(nv: int, tets: np.ndarray) -> np.ndarray:
     return out
 
 
+def color_gpu(nv: int, tets: np.ndarray, seed: int = 1) -> np.ndarray:
+    """Jones-Plassmann vertex coloring on the GPU (not the reference's coloring)."""
+    tets = np.ascontiguousarray(tets, dtype=np.int32)
+    out = np.empty(nv, dtype=np.int32)
+    n = lib().gaia_vbd_color_gpu(nv, len(tets), tets.ctypes.data, out.ctypes.data, seed)
+    if n < 0:
+        raise RuntimeError("GPU coloring failed")
+    return out
+
+
 def color_mcs(nv: int, tets: np.ndarray) -> np.ndarray:
     """GraphColoring tool, MCS (mcs.cpp:14-168), bit-exact."""
     tets = np.ascontiguousarray(tets, np.int32)

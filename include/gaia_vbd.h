@@ -210,6 +210,10 @@ int gaia_vbd_energy_noalloc(const double* x, const double* y, const double* mass
  * bit-exact with the reference. Return the number of colors, or -1 on error. */
 int32_t gaia_vbd_color_mcs(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
 int32_t gaia_vbd_color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
+/* Jones-Plassmann coloring on the GPU (hashed vertex priorities from `seed`, lowest free
+ * color): a faster alternative for meshes without a coloring file; not the reference's
+ * coloring. Same graph and return value as the two above. */
+int32_t gaia_vbd_color_gpu(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors, uint32_t seed);
 /* Write a coloring as the reference's JSON list of lists (ColoringAlgorithms.cpp:200-211). */
 int gaia_vbd_write_coloring(const char* path, int32_t nv, const int32_t* colors);
 /* Write a .t mesh ("Vertex id x y z" / "Tet id a b c d"). */
