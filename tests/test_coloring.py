@@ -98,3 +98,50 @@ def test_coloring_file_roundtrip(tmp_path, gaia_lib):
     p = tmp_path / "c.json"
     gaia_lib.write_coloring(str(p), colors)
     assert json.load(open(p)) == [[0, 4], [1, 5], [2], [3]]
+
+
+REF_GC = "/root/reference/Simulator/Modules/GraphColoring/mcs.cpp"
+
+
+def _vertex_graph(nv, tets):
+    """Sorted unique neighbours of every vertex (all vertex pairs sharing a tet)."""
+    t = np.asarray(tets, np.int64)
+    a = np.concatenate([t[:, i] for i in range(4) for j in range(4) if i != j])
+    b = np.concatenate([t[:, j] for i in range(4) for j in range(4) if i != j])
+    keep = a != b
+    key = np.unique(a[keep] * (nv + 1) + b[keep])
+    src, dst = key // (nv + 1), key % (nv + 1)
+    ofs = np.zeros(nv + 1, np.int64)
+    np.add.at(ofs, src + 1, 1)
+    return np.cumsum(ofs), dst.astype(np.int32)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_GC), reason="reference tree not present")
+def test_colorings_match_reference_build(oracle_lib, gaia_lib):
+    """The reference's own MCS and OrderedGreedy (GraphColoring/mcs.cpp, gready.cpp),
+    compiled into oracle/_ref/, against the library and the oracle on lattices and random
+    tet soups: identical colorings."""
+    import ctypes as C
+    import subprocess
+
+    from gaia_gb300 import scenes
+
+    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "..", "oracle"), "ref"], check=True)
+    ref = C.CDLL(os.path.join(HERE, "..", "oracle", "_ref", "libcolor_ref.so")).ref_color
+    ref.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]
+    ref.restype = C.c_int32
+    rng = np.random.default_rng(17)
+    cases = [scenes.lattice_cube(n, 0.01)[1] for n in ((3, 3, 3), (5, 4, 6), (9, 7, 8))]
+    for k in range(6):
+        nv = int(rng.integers(20, 400))
+        cases.append(np.stack([rng.choice(nv, 4, replace=False) for _ in range(int(rng.integers(10, 3 * nv)))])
+                     .astype(np.int32))
+    for tets in cases:
+        nv = int(tets.max()) + 1
+        ofs, adj = _vertex_graph(nv, tets)
+        for algo, lib_fn, orc_fn in ((0, gaia_lib.color_mcs, oracle_lib.color_mcs),
+                                     (1, gaia_lib.color_greedy, oracle_lib.color_greedy)):
+            out = np.empty(nv, np.int32)
+            assert ref(algo, nv, ofs.ctypes.data, adj.ctypes.data, out.ctypes.data) > 0
+            np.testing.assert_array_equal(lib_fn(nv, tets), out)
+            np.testing.assert_array_equal(orc_fn(nv, tets), out)
