@@ -103,6 +103,9 @@ _SIGNATURES = {
     "gaia_vbd_color_mcs": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "gaia_vbd_color_greedy": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "gaia_vbd_color_gpu": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint32]),
+    "gaia_vbd_color_tool": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_float,
+                                        C.c_void_p, C.c_void_p]),
+    "gaia_vbd_write_categories": (C.c_int, [C.c_char_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "gaia_vbd_write_coloring": (C.c_int, [C.c_char_p, C.c_int32, C.c_void_p]),
     "gaia_vbd_write_t": (C.c_int, [C.c_char_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
     # cloth (gaia_cloth.h)

@@ -155,6 +155,57 @@ int32_t color_greedy_graph(int32_t nv, const std::vector<int64_t>& ofs, const st
 }
 
 // ColoringAlgorithms.cpp:69-80 (convertToColoredCategories).
+void tet_vertex_graph(int32_t nv, int32_t ntet, const int32_t* tets, std::vector<int64_t>& ofs, std::vector<int32_t>& adj) {
+    vertex_graph(nv, ntet, tets, ofs, adj);
+}
+
+void balance_categories(int32_t nv, const std::vector<int64_t>& ofs, const std::vector<int32_t>& adj, int32_t* colors,
+                        std::vector<std::vector<int32_t>>& cats, float goal) {
+    auto movable = [&](int32_t node, int32_t dst) {
+        for (int64_t k = ofs[node]; k < ofs[node + 1]; ++k)
+            if (colors[adj[k]] == dst) return false;
+        return true;
+    };
+    auto first_movable = [&](int32_t src, int32_t dst) -> int64_t {
+        const auto& c = cats[size_t(src)];
+        for (size_t i = 0; i < c.size(); ++i)
+            if (movable(c[i], dst)) return int64_t(i);
+        return -1;
+    };
+    if (cats.empty()) return;
+    // the reference's loop has no bound and does not end on some graphs (moves can cycle
+    // between categories without reaching the goal); stop with an error instead
+    const int64_t max_moves = 64 * int64_t(nv) + 1024;
+    int64_t moves = 0;
+    float ratio;
+    do {
+        if (++moves > max_moves)
+            throw std::runtime_error("color balancing did not reach the goal ratio (the reference's loop would not end)");
+        // findLargestSmallestCategories: first largest, first smallest in color order
+        size_t big = 0, small = 0;
+        for (size_t c = 0; c < cats.size(); ++c) {
+            if (cats[big].size() < cats[c].size()) big = c;
+            if (cats[small].size() > cats[c].size()) small = c;
+        }
+        ratio = float(cats[big].size()) / float(cats[small].size());
+        int64_t id = first_movable(int32_t(big), int32_t(small));
+        if (id < 0)
+            for (size_t c = 0; c < cats.size(); ++c) {
+                if (c == big || c == small) continue;
+                id = first_movable(int32_t(c), int32_t(small));
+                if (id >= 0) {
+                    big = c;
+                    break;
+                }
+            }
+        if (id < 0) return;  // "not optimizable anymore"
+        const int32_t node = cats[big][size_t(id)];
+        colors[node] = int32_t(small);
+        cats[big].erase(cats[big].begin() + id);
+        cats[small].push_back(node);
+    } while (ratio > goal);
+}
+
 std::vector<std::vector<int32_t>> colors_to_categories(int32_t nv, const int32_t* colors) {
     int32_t n = 0;
     for (int32_t i = 0; i < nv; ++i) n = std::max(n, colors[i] + 1);

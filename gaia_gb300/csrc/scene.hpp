@@ -143,6 +143,17 @@ int32_t color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* col
 int32_t color_mcs_graph(int32_t nv, const std::vector<int64_t>& ofs, const std::vector<int32_t>& adj, int32_t* colors);
 int32_t color_greedy_graph(int32_t nv, const std::vector<int64_t>& ofs, const std::vector<int32_t>& adj, int32_t* colors);
 std::vector<std::vector<int32_t>> colors_to_categories(int32_t nv, const int32_t* colors);
+// GraphColor::balanceColoredCategories (GraphColoring/ColoringAlgorithms.cpp:142-196), the
+// GraphColoring tool's default post-pass (-b, ratio 1.05, GraphColoring.cpp:23-24, 182-189):
+// move a vertex from the largest category (or, if none of its vertices can move, from the
+// first other category that has one) to the smallest, until the largest/smallest size ratio
+// measured before a move is at most goal; categories keep the reference's order (a moved
+// vertex is erased from its list and appended to the destination's). Updates colors.
+// Throws where the reference's loop would not end (moves cycling short of the goal).
+void balance_categories(int32_t nv, const std::vector<int64_t>& ofs, const std::vector<int32_t>& adj, int32_t* colors,
+                        std::vector<std::vector<int32_t>>& cats, float goal);
+// The vertex graph of a tet mesh (all vertex pairs sharing a tet), CSR with sorted neighbours.
+void tet_vertex_graph(int32_t nv, int32_t ntet, const int32_t* tets, std::vector<int64_t>& ofs, std::vector<int32_t>& adj);
 
 void write_t(const std::string& path, int32_t nv, const double* X, int32_t ntet, const int32_t* tets);
 void write_coloring(const std::string& path, const std::vector<std::vector<int32_t>>& cats);

@@ -1487,6 +1487,43 @@ int32_t gaia_vbd_color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int
     return n;
 }
 
+int32_t gaia_vbd_color_tool(int32_t nv, int32_t ntet, const int32_t* tets, int32_t algorithm, int32_t balance,
+                            float goal_ratio, int32_t* colors, int32_t* order) {
+    if (nv <= 0 || ntet < 0 || (!tets && ntet) || !colors || (algorithm != 0 && algorithm != 1)) return -1;
+    int32_t n = -1;
+    if (guarded(nullptr, [&] {
+            n = algorithm == 0 ? gaia::color_mcs(nv, ntet, tets, colors) : gaia::color_greedy(nv, ntet, tets, colors);
+            auto cats = gaia::colors_to_categories(nv, colors);
+            if (balance) {
+                std::vector<int64_t> ofs;
+                std::vector<int32_t> adj;
+                gaia::tet_vertex_graph(nv, ntet, tets, ofs, adj);
+                gaia::balance_categories(nv, ofs, adj, colors, cats, goal_ratio);
+            }
+            if (order) {
+                size_t k = 0;
+                for (auto& c : cats)
+                    for (int32_t v : c) order[k++] = v;
+            }
+        }))
+        return -1;
+    return n;
+}
+
+int gaia_vbd_write_categories(const char* path, int32_t nv, const int32_t* colors, const int32_t* order) {
+    if (!path || nv <= 0 || !colors || !order) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(nullptr, [&] {
+        int32_t n = 0;
+        for (int32_t i = 0; i < nv; ++i) {
+            if (colors[i] < 0) throw std::invalid_argument("negative color");
+            n = std::max(n, colors[i] + 1);
+        }
+        std::vector<std::vector<int32_t>> cats(n);
+        for (int32_t i = 0; i < nv; ++i) cats[colors[order[i]]].push_back(order[i]);
+        gaia::write_coloring(path, cats);
+    });
+}
+
 int gaia_vbd_write_coloring(const char* path, int32_t nv, const int32_t* colors) {
     if (!path || nv <= 0 || !colors) return GAIA_VBD_E_INVALID_ARG;
     return guarded(nullptr, [&] {

@@ -259,6 +259,27 @@ def color_greedy(nv: int, tets: np.ndarray) -> np.ndarray:
     return out
 
 
+def color_tool(nv: int, tets: np.ndarray, algorithm: str = "mcs", balance: bool = True,
+               goal_ratio: float = 1.05) -> tuple[np.ndarray, np.ndarray]:
+    """The reference's GraphColoring tool (defaults: MCS, balanced to a 1.05 size ratio):
+    (colors, vertex order of the written categories)."""
+    tets = np.ascontiguousarray(tets, dtype=np.int32)
+    colors = np.empty(nv, dtype=np.int32)
+    order = np.empty(nv, dtype=np.int32)
+    n = lib().gaia_vbd_color_tool(nv, len(tets), tets.ctypes.data, 0 if algorithm == "mcs" else 1, int(balance),
+                                  goal_ratio, colors.ctypes.data, order.ctypes.data)
+    if n < 0:
+        raise RuntimeError("coloring failed")
+    return colors, order
+
+
+def write_categories(path: str, colors: np.ndarray, order: np.ndarray) -> None:
+    colors = np.ascontiguousarray(colors, np.int32)
+    order = np.ascontiguousarray(order, np.int32)
+    _check(lib().gaia_vbd_write_categories(os.fspath(path).encode(), len(colors), colors.ctypes.data,
+                                           order.ctypes.data))
+
+
 def color_gpu(nv: int, tets: np.ndarray, seed: int = 1) -> np.ndarray:
     """Jones-Plassmann vertex coloring on the GPU (not the reference's coloring)."""
     tets = np.ascontiguousarray(tets, dtype=np.int32)

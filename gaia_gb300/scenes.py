@@ -73,14 +73,21 @@ def lattice_cube(n: tuple[int, int, int], spacing: float = 0.01, origin=(0.0, 0.
     return X, tets.astype(np.int32)
 
 
-def _write_mesh(dirname: str, name: str, X: np.ndarray, tets: np.ndarray, coloring: str = "greedy") -> tuple[str, str]:
-    from .physics import color_greedy, color_mcs, write_coloring, write_t
+def _write_mesh(dirname: str, name: str, X: np.ndarray, tets: np.ndarray, coloring: str = "tool") -> tuple[str, str]:
+    """.t mesh plus its vertex coloring file. coloring = "tool": what the reference's
+    GraphColoring tool writes by default (MCS, categories balanced to a 1.05 size ratio);
+    "mcs" / "greedy": the plain algorithms."""
+    from .physics import color_greedy, color_mcs, color_tool, write_categories, write_coloring, write_t
     os.makedirs(dirname, exist_ok=True)
     tpath = os.path.join(dirname, name + ".t")
     cpath = tpath + ".vertexColoring.json"
     write_t(tpath, X, tets)
-    colors = color_greedy(len(X), tets) if coloring == "greedy" else color_mcs(len(X), tets)
-    write_coloring(cpath, colors)
+    if coloring == "tool":
+        colors, order = color_tool(len(X), tets)
+        write_categories(cpath, colors, order)
+    else:
+        colors = color_greedy(len(X), tets) if coloring == "greedy" else color_mcs(len(X), tets)
+        write_coloring(cpath, colors)
     return tpath, cpath
 
 
@@ -182,7 +189,7 @@ def stack_drop(dirname: str, n_lower: int = 6, n_upper: int = 5, spacing: float 
     top = spacing * (n_lower - 1)
     Xb, Tb = lattice_cube((n_upper,) * 3, spacing * 0.97, (offset[0], top + gap, offset[2]), jitter=1e-4,
                           seed=seed + 1)
-    ta, ca = _write_mesh(dirname, "lower", Xa, Ta)
+    ta, ca = _write_mesh(dirname, "lower", Xa, Ta, coloring="greedy")
     tb, cb = _write_mesh(dirname, "upper", Xb, Tb, coloring="mcs")
     models = [model_entry(ta, ca, frictionDynamic=0.2, frictionEpsV=0.01),
               model_entry(tb, cb, density=800.0, frictionDynamic=0.3, frictionEpsV=0.02,

@@ -214,6 +214,15 @@ int32_t gaia_vbd_color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int
  * color): a faster alternative for meshes without a coloring file; not the reference's
  * coloring. Same graph and return value as the two above. */
 int32_t gaia_vbd_color_gpu(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors, uint32_t seed);
+/* The GraphColoring tool as a whole (GraphColoring/GraphColoring.cpp:157-196): MCS
+ * (algorithm 0, the tool's default) or OrderedGreedy (1), then, with balance != 0 (the
+ * tool's default, goal ratio 1.05), balanceColoredCategories. colors receives each
+ * vertex's color; order (nv ints, optional) the vertices of every category in the order
+ * the tool writes them. Returns the number of colors, or -1 on error. */
+int32_t gaia_vbd_color_tool(int32_t nv, int32_t ntet, const int32_t* tets, int32_t algorithm, int32_t balance,
+                            float goal_ratio, int32_t* colors, int32_t* order);
+/* Write categories in a given vertex order (`order` from gaia_vbd_color_tool). */
+int gaia_vbd_write_categories(const char* path, int32_t nv, const int32_t* colors, const int32_t* order);
 /* Write a coloring as the reference's JSON list of lists (ColoringAlgorithms.cpp:200-211). */
 int gaia_vbd_write_coloring(const char* path, int32_t nv, const int32_t* colors);
 /* Write a .t mesh ("Vertex id x y z" / "Tet id a b c d"). */

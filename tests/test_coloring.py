@@ -145,3 +145,41 @@ def test_colorings_match_reference_build(oracle_lib, gaia_lib):
             assert ref(algo, nv, ofs.ctypes.data, adj.ctypes.data, out.ctypes.data) > 0
             np.testing.assert_array_equal(lib_fn(nv, tets), out)
             np.testing.assert_array_equal(orc_fn(nv, tets), out)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_GC), reason="reference tree not present")
+def test_coloring_tool_with_balance_matches_reference_build(gaia_lib):
+    """The tool's default pipeline (MCS, categories, balanceColoredCategories at 1.05) and
+    greedy + balance: colors and the written category order equal the reference's."""
+    import ctypes as C
+    import subprocess
+
+    from gaia_gb300 import physics, scenes
+
+    subprocess.run(["make", "-s", "-C", os.path.join(HERE, "..", "oracle"), "ref"], check=True)
+    ref = C.CDLL(os.path.join(HERE, "..", "oracle", "_ref", "libcolor_ref.so")).ref_color_tool
+    ref.argtypes = [C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    ref.restype = C.c_int32
+    rng = np.random.default_rng(23)
+    # the reference's balancing loop only ends when the goal ratio is reached or nothing can
+    # move: on random tet soups, and where the goal is out of reach (e.g. 64 vertices in 9
+    # colors at 1.05), it runs forever, so those cases run without it
+    both = ((1, 1.05), (1, 1.5), (0, 1.05))
+    runs = [(scenes.lattice_cube((6, 5, 7), 0.01)[1], both, both),
+            (scenes.lattice_ball(0.03, 0.008)[1], both, both),
+            (scenes.lattice_cube((4, 4, 4), 0.01)[1], both, ((1, 1.5), (0, 1.05)))]
+    for nv in rng.integers(30, 300, size=3):
+        soup = np.stack([rng.choice(nv, 4, replace=False) for _ in range(int(rng.integers(nv, 3 * nv)))])
+        runs.append((soup.astype(np.int32), ((0, 1.05),), ((0, 1.05),)))
+    for tets, mcs_settings, greedy_settings in runs:
+        nv = int(tets.max()) + 1
+        ofs, adj = _vertex_graph(nv, tets)
+        for algo, name, settings in ((0, "mcs", mcs_settings), (1, "greedy", greedy_settings)):
+            for balance, goal in settings:
+                col = np.empty(nv, np.int32)
+                order = np.empty(nv, np.int32)
+                assert ref(algo, balance, goal, nv, ofs.ctypes.data, adj.ctypes.data, col.ctypes.data,
+                           order.ctypes.data) > 0
+                c2, o2 = physics.color_tool(nv, tets, name, bool(balance), goal)
+                np.testing.assert_array_equal(c2, col)
+                np.testing.assert_array_equal(o2, order)
