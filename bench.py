@@ -36,8 +36,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "VBD vertex-solves/s & steps/s, FP32-mixed vs plain FP64 at <=1e-5 rel pos err"
 # dram__bytes_read.sum + dram__bytes_write.sum per solved incidence of k_solve, measured by
-# ncu on colors 0-2 of the 60^3 twist (2,354,128 incidences; see profiles/)
-TRAFFIC_BYTES_PER_INCIDENCE = {"fp32": 55.8, "mixed": 62.0}
+# ncu on colors 0-2 of the 60^3 twist (3 x ~1.01 M incidences; see profiles/)
+TRAFFIC_BYTES_PER_INCIDENCE = {"fp32": 54.8, "mixed": 59.9}
 
 
 def load_peaks() -> tuple[float, str]:
