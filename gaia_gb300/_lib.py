@@ -146,6 +146,8 @@ _SIGNATURES = {
     "gaia_cloth_get_group_lanes": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gaia_cloth_color_greedy": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
     "gaia_cloth_color_mcs": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]),
+    "gaia_cloth_color_tool": (C.c_int32, [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                          C.c_float, C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

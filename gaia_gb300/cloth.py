@@ -193,6 +193,20 @@ class VBDClothSimulationFramework:
         return s.as_dict()
 
 
+def color_trimesh_tool(nv: int, faces: np.ndarray, algorithm: str = "mcs", bending: bool = False, balance: bool = True,
+                       goal_ratio: float = 1.05) -> tuple[np.ndarray, np.ndarray]:
+    """The GraphColoring tool on a triangle mesh (defaults: MCS, balanced to 1.05):
+    (colors, vertex order of the written categories)."""
+    f = np.ascontiguousarray(faces, np.int32).reshape(-1)
+    colors = np.empty(nv, np.int32)
+    order = np.empty(nv, np.int32)
+    n = lib().gaia_cloth_color_tool(nv, len(f) // 3, _ptr(f), int(bending), 0 if algorithm == "mcs" else 1,
+                                    int(balance), goal_ratio, _ptr(colors), _ptr(order))
+    if n < 0:
+        raise GaiaError(1, lib().gaia_vbd_last_global_error().decode())
+    return colors, order
+
+
 def color_trimesh(nv: int, faces: np.ndarray, algorithm: str = "greedy", bending: bool = False) -> np.ndarray:
     """GraphColoring tool on a triangle mesh (vertex graph): per-vertex colors."""
     f = np.ascontiguousarray(faces, np.int32).reshape(-1)

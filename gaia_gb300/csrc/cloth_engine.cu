@@ -1659,4 +1659,33 @@ int32_t gaia_cloth_color_mcs(int32_t nv, int32_t nf, const int32_t* faces, int32
     return color_tri(nv, nf, faces, bending, colors, true);
 }
 
+int32_t gaia_cloth_color_tool(int32_t nv, int32_t nf, const int32_t* faces, int32_t bending, int32_t algorithm,
+                              int32_t balance, float goal_ratio, int32_t* colors, int32_t* order) {
+    if (nv <= 0 || nf < 0 || !faces || !colors || (algorithm != 0 && algorithm != 1)) return -1;
+    try {
+        gaia::cloth::TriMesh m;
+        m.X.assign(3 * size_t(nv), 0.f);
+        m.faces.assign(faces, faces + 3 * size_t(nf));
+        for (int32_t v : m.faces)
+            if (v < 0 || v >= nv) return -1;
+        gaia::cloth::build_topology(m);
+        std::vector<int64_t> ofs;
+        std::vector<int32_t> adj;
+        gaia::cloth::tri_vertex_graph(m, bending != 0, ofs, adj);
+        const int32_t n = algorithm == 0 ? gaia::color_mcs_graph(nv, ofs, adj, colors)
+                                         : gaia::color_greedy_graph(nv, ofs, adj, colors);
+        auto cats = gaia::colors_to_categories(nv, colors);
+        if (balance) gaia::balance_categories(nv, ofs, adj, colors, cats, goal_ratio);
+        if (order) {
+            size_t k = 0;
+            for (auto& c : cats)
+                for (int32_t v : c) order[k++] = v;
+        }
+        return n;
+    } catch (const std::exception& e) {
+        gaia::set_last_global_error(e.what());
+        return -1;
+    }
+}
+
 }  // extern "C"

@@ -419,10 +419,10 @@ def cloth_on_sphere(dirname: str, n: int = 512, side: float = 1.0, sphere_radius
     X, F = cloth_grid(n, side, sphere_radius + gap, noise, seed)
     cpath = os.path.join(dirname, f"cloth{n}.obj")
     write_obj(cpath, X, F)
-    from .cloth import color_trimesh
-    from .physics import write_coloring
+    from .cloth import color_trimesh_tool
+    from .physics import write_categories
     colpath = cpath + ".vertexColoring.json"
-    write_coloring(colpath, color_trimesh(len(X), F, "greedy"))
+    write_categories(colpath, *color_trimesh_tool(len(X), F))  # the coloring tool's default
     SX, SF = icosphere(sphere_level, sphere_radius)
     spath = os.path.join(dirname, f"sphere{sphere_level}.obj")
     write_obj(spath, SX, SF)

@@ -131,6 +131,11 @@ int gaia_cloth_get_stats(gaia_cloth* h, gaia_cloth_stats* out);
  * Returns the number of colors, or -1 on bad input. */
 int32_t gaia_cloth_color_greedy(int32_t nv, int32_t nf, const int32_t* faces, int32_t bending, int32_t* colors);
 int32_t gaia_cloth_color_mcs(int32_t nv, int32_t nf, const int32_t* faces, int32_t bending, int32_t* colors);
+/* The GraphColoring tool on a triangle mesh: MCS (0, default) or OrderedGreedy (1), then
+ * balanceColoredCategories when balance != 0 (the tool's default, goal 1.05); `order`
+ * (optional, nv ints) receives the categories' vertex order (see gaia_vbd_color_tool). */
+int32_t gaia_cloth_color_tool(int32_t nv, int32_t nf, const int32_t* faces, int32_t bending, int32_t algorithm,
+                              int32_t balance, float goal_ratio, int32_t* colors, int32_t* order);
 
 #ifdef __cplusplus
 }
