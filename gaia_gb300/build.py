@@ -1,8 +1,10 @@
 """Build libgaia_vbd.so in-tree with nvcc for sm_103a.
 
 Translation units compiled in parallel (host scene code, the tet and cloth
-engines, the cloth contact detector), one -gencode, no cmake. Output:
-gaia_gb300/libgaia_vbd.so.
+engines, the cloth contact detector), one -gencode, no cmake. Outputs:
+gaia_gb300/libgaia_vbd.so and the command-line runner gaia_gb300/vbd_dynamics
+(Models.json Parameters.json outFolder [-R repoRoot] [-r recoveryState]),
+linked against the library with an $ORIGIN rpath.
 """
 from __future__ import annotations
 
@@ -17,6 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgaia_vbd.so")
+CLI = os.path.join(HERE, "vbd_dynamics")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["scene.cpp", "state_io.cpp", "vbd_engine.cu", "vbd_energy_noalloc.cu", "tet_cd.cu", "coloring_gpu.cu",
@@ -76,6 +79,15 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    cli_src = os.path.join(CSRC, "vbd_dynamics.cpp")
+    cli_deps = [cli_src, LIB, os.path.join(INCLUDE, "gaia_vbd.h")] + [os.path.join(CSRC, h) for h in
+                                                                      ("json_lite.hpp", "json_get.hpp")]
+    if force or _stale(CLI, cli_deps):
+        cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-o", CLI, cli_src, "-I", INCLUDE, "-L", HERE,
+               "-lgaia_vbd", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"vbd_dynamics build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

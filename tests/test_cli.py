@@ -1,0 +1,122 @@
+"""The vbd_dynamics command-line runner (VBDDynamics/main.cpp + BasePhysicFramework::simulate
+and writeOutputs).
+
+CPU: argument handling and failures before any device work (usage, unknown option,
+unreadable parameter file, missing model file).
+GPU: a contact scene run for 6 frames writes the frame files and recovery states the
+reference's writeOutputs names; the last recovery state equals the positions the Python
+API reaches after the same 6 steps; a run recovered from frame 3 (-r) reaches the same
+frame 6, and "${REPO_ROOT}" paths with -R resolve.
+"""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+
+def _cli(gaia_lib):
+    from gaia_gb300 import build as gb
+
+    assert os.access(gb.CLI, os.X_OK)
+    return gb.CLI
+
+
+def _run(exe, *args):
+    return subprocess.run([exe, *args], capture_output=True, text=True, timeout=600)
+
+
+def test_usage_and_options(gaia_lib, tmp_path):
+    exe = _cli(gaia_lib)
+    r = _run(exe)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = _run(exe, "m.json", "p.json", str(tmp_path / "out"), "-x", "1")
+    assert r.returncode == 2 and "unknown option -x" in r.stderr
+
+
+def test_unreadable_inputs_fail_before_device_work(gaia_lib, tmp_path):
+    exe = _cli(gaia_lib)
+    r = _run(exe, "m.json", str(tmp_path / "missing.json"), str(tmp_path / "out"))
+    assert r.returncode == 1 and "cannot read" in r.stderr
+    pp = tmp_path / "p.json"
+    pp.write_text(json.dumps({"PhysicsParams": {"numFrames": 1}}))
+    r = _run(exe, str(tmp_path / "missing_models.json"), str(pp), str(tmp_path / "out"))
+    assert r.returncode == 1 and "create failed" in r.stderr
+    assert not (tmp_path / "out").exists()
+
+
+def _scene(tmp_path, **params):
+    from gaia_gb300 import scenes
+
+    mp, pp = scenes.stack_drop(str(tmp_path), spacing=0.03, gap=0.01, speed=1.0, precision="fp64")
+    P = json.load(open(pp))
+    P["PhysicsParams"].update(params)
+    json.dump(P, open(pp, "w"))
+    return mp, pp
+
+
+def _state_positions(path):
+    S = json.load(open(path))
+    return S["frameId"], [np.asarray(m["position"], np.float64).reshape(-1, 3) for m in S["meshesState"]]
+
+
+@pytest.mark.gpu
+def test_frames_and_states_match_api(gaia_lib, tmp_path):
+    from gaia_gb300 import VBDPhysics
+
+    exe = _cli(gaia_lib)
+    mp, pp = _scene(tmp_path, numFrames=6, outputExt="ply", saveAllModelsTogether=True, outputRecoveryState=True,
+                    outputRecoveryStateStep=3, outputRecoveryStateBinary=False)
+    out = tmp_path / "out"
+    r = _run(exe, mp, pp, str(out))
+    assert r.returncode == 0, r.stderr
+    assert "6 frames" in r.stdout
+    assert sorted(os.listdir(out / "RecoveryStates")) == ["A00000000.json", "A00000003.json", "A00000006.json"]
+    assert json.load(open(out / "RecoveryStates" / "A00000003.json"))["format"] == "text"
+    assert all((out / f"A{f:08d}.ply").exists() for f in range(7))
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, pp)
+    phys.initialize()
+    phys.runStep(6)
+    frame, X = _state_positions(out / "RecoveryStates" / "A00000006.json")
+    assert frame == 6
+    for m in range(2):  # the text state holds 9 significant digits
+        ref = phys.positions(m)
+        assert np.abs(X[m] - ref).max() <= 1e-8
+    phys.close()
+
+    # recovery from frame 3 reaches the same frame 6
+    out2 = tmp_path / "out2"
+    r = _run(exe, mp, pp, str(out2), "-r", str(out / "RecoveryStates" / "A00000003.json"))
+    assert r.returncode == 0, r.stderr
+    assert "3 frames" in r.stdout
+    assert not (out2 / "A00000001.ply").exists() and (out2 / "A00000006.ply").exists()
+    frame2, X2 = _state_positions(out2 / "RecoveryStates" / "A00000006.json")
+    assert frame2 == 6
+    for m in range(2):  # restarted from the rounded frame-3 state
+        assert np.abs(X2[m] - X[m]).max() <= 1e-6
+
+
+@pytest.mark.gpu
+def test_binary_output_and_repo_root(gaia_lib, tmp_path):
+    exe = _cli(gaia_lib)
+    mp, pp = _scene(tmp_path, numFrames=4, outputExt="bin", binaryModeVisualizationSteps=2, outputRecoveryState=True,
+                    outputRecoveryStateStep=4, outputRecoveryStateBinary=True)
+    out = "${REPO_ROOT}/outbin"
+    r = _run(exe, os.path.basename(mp).join(["${REPO_ROOT}/", ""]), os.path.basename(pp).join(["${REPO_ROOT}/", ""]),
+             out, "-R", str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    o = tmp_path / "outbin"
+    assert (o / "TemplateMesh" / "TemplateMesh.ply").exists()
+    assert all((o / f"A{f:08d}.bin").exists() for f in range(5))
+    assert sorted(p.name for p in o.glob("A*.ply")) == ["A00000000.ply", "A00000002.ply", "A00000004.ply"]
+    assert sorted(p.name for p in (o / "RecoveryStates").glob("*.json")) == ["A00000000.json", "A00000004.json"]
+    assert (o / "RecoveryStates" / "A00000004.pos").exists()
+    # the bin frame holds the surface vertices of both meshes as FP32 xyz
+    from gaia_gb300 import VBDPhysics
+
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, pp)
+    ns = sum(len(phys.surface(m)[1]) for m in range(2))
+    assert os.path.getsize(o / "A00000004.bin") == 12 * ns
