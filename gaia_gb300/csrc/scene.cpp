@@ -314,13 +314,20 @@ void extract_surface(TetMesh& m) {
     };
     std::sort(keys.begin(), keys.end(), [&](const Key& x, const Key& y) { return less3(x, y) || (!less3(y, x) && x.id < y.id); });
     std::vector<char> boundary(4 * size_t(m.ntet), 0);
+    // tetsNeighborTets (TetMesh/TetMeshFEM.cpp:40-70): the other tet of a face two tets share
+    m.tet_nbr.assign(4 * size_t(m.ntet), -1);
     for (size_t i = 0; i < keys.size();) {
         size_t j = i + 1;
         while (j < keys.size() && !less3(keys[i], keys[j])) ++j;
         if (j - i == 1) boundary[size_t(keys[i].id)] = 1;
+        if (j - i == 2) {
+            m.tet_nbr[size_t(keys[i].id)] = keys[i + 1].id / 4;
+            m.tet_nbr[size_t(keys[i + 1].id)] = keys[i].id / 4;
+        }
         i = j;
     }
     m.sfaces.clear();
+    m.sface_tet.clear();
     std::vector<char> on(size_t(m.nv), 0);
     for (int32_t t = 0; t < m.ntet; ++t) {
         const int32_t* tv = &m.tets[4 * size_t(t)];
@@ -333,6 +340,8 @@ void extract_surface(TetMesh& m) {
             if (!boundary[4 * size_t(t) + k]) continue;
             int32_t f[3] = {tv[kFace[k][0]], tv[kFace[k][1]], tv[kFace[k][2]]};
             if (vol < 0) std::swap(f[1], f[2]);
+            m.sface_tet.push_back(t);
+            m.sface_tet.push_back(k);
             for (int i = 0; i < 3; ++i) {
                 m.sfaces.push_back(f[i]);
                 on[size_t(f[i])] = 1;
@@ -546,6 +555,16 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         get(*cp, "handleSelfCollision", p.handleSelfCollision);
         get(*cp, "checkFeasibleRegion", p.checkFeasibleRegion);
         get(*cp, "feasibleRegionEpsilon", p.feasibleRegionEpsilon);
+        get(*cp, "checkTetTraverse", p.checkTetTraverse);
+        get(*cp, "tetrahedralTraverseForNonSelfIntersection", p.tetrahedralTraverseForNonSelfIntersection);
+        get(*cp, "stopTraversingAfterPassingQueryPoint", p.stopTraversingAfterPassingQueryPoint);
+        get(*cp, "shiftQueryPointToCenter", p.shiftQueryPointToCenter);
+        get(*cp, "useStaticTraverse", p.useStaticTraverse);
+        get(*cp, "loopLessTraverse", p.loopLessTraverse);
+        get(*cp, "centerShiftLevel", p.centerShiftLevel);
+        get(*cp, "rayTriIntersectionEPSILON", p.rayTriIntersectionEPSILON);
+        get(*cp, "maxSearchDistanceMultiplier", p.maxSearchDistanceMultiplier);
+        if (p.loopLessTraverse) throw std::runtime_error("CollisionParams loopLessTraverse is not supported");
     }
     if (p.numSubsteps <= 0 || p.timeStep <= 0) throw std::runtime_error("timeStep and numSubsteps must be positive");
     if (p.iterations < 0) throw std::runtime_error("iterations must be >= 0");

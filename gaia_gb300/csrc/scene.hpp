@@ -41,6 +41,16 @@ struct PhysicsParams {
     bool handleSelfCollision = true;
     bool checkFeasibleRegion = true;
     double feasibleRegionEpsilon = 1e-2;
+    // the DCD closest-point query's tetrahedral traversal check
+    bool checkTetTraverse = true;
+    bool tetrahedralTraverseForNonSelfIntersection = true;
+    bool stopTraversingAfterPassingQueryPoint = true;
+    bool shiftQueryPointToCenter = true;
+    bool useStaticTraverse = true;
+    bool loopLessTraverse = false;  // not supported (rejected)
+    double centerShiftLevel = 0.01;
+    double rayTriIntersectionEPSILON = 1e-10;
+    double maxSearchDistanceMultiplier = 1.8;
     int numThreadsVBDSolve = 16;
     bool useDouble3x3 = false;
     bool evaluateConvergence = false;
@@ -111,6 +121,8 @@ struct TetMesh {
     std::vector<int32_t> sverts;               // boundary vertices, ascending
     std::vector<int32_t> sface_nbr;            // 3 per face: face across edge AB, BC, CA (-1: none)
     std::vector<int32_t> sring_ofs, sring;     // per vertex: surface neighbours, ascending
+    std::vector<int32_t> sface_tet;            // 2 per face: the tet it bounds, the local vertex it omits
+    std::vector<int32_t> tet_nbr;              // 4 per tet: tet across the face omitting vertex k (-1: none)
 };
 
 struct Scene {

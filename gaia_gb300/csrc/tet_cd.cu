@@ -67,6 +67,8 @@ struct Dev {
     const int32_t* ring;
     const int4* tets;
     const int32_t* tet_mesh;
+    const int4* tet_nbr;   // per tet: tet across the face omitting vertex x/y/z/w (-1: none)
+    const int2* face_tet;  // per face: the tet it bounds, the local vertex it omits
     int32_t* hit;        // per surface vertex: global face or -1
     float* hit_tt;       // CCD time of impact, -1 for a DCD hit
     uint8_t* pen;        // per surface vertex: DCD found it inside a tet (substep start)
@@ -328,6 +330,170 @@ __device__ bool feasible(const Dev& D, const float4* P, float3 p, int32_t g, int
     return true;
 }
 
+// ---- tetrahedral traversal (TetMesh/TetMeshFEM.cpp:503-740 static, 908-1100 dynamic) ----
+// The walk from a surface face along a ray through the tets of its mesh that the DCD
+// closest-point query requires to reach the tet containing the query point
+// (CollisionDetector/DiscreteCollisionDetector.cpp:189-300). One thread walks; the
+// candidate exit faces form a stack of (tet << 2 | local face) entries.
+__constant__ int kTet4Faces[4][3] = {{1, 2, 3}, {2, 0, 3}, {0, 1, 3}, {1, 0, 2}};  // TetMeshFEM::tet4Faces
+__constant__ int kExit3[3][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}};                 // posibleExit3Faces
+constexpr int kStaticStack = 32;      // SIZE_CANDIDATE_FACE_STACK
+constexpr int kLoopRing = 32;         // SIZE_TRAVERSED_CIRCULAR_ARRAY
+constexpr int kPassThroughSteps = 5;  // TetMeshFEM::passThroughCheckSteps
+constexpr int kDynamicStack = 256;    // bound of the dynamic walk (a std::vector in the reference)
+constexpr int kMaxWalkSteps = 1 << 16;
+
+struct TraverseCfg {
+    int check, non_self, stop_after, shift_center, use_static;
+    float shift, eps, max_mult;
+};
+
+TraverseCfg traverse_cfg(const Params& p) {
+    return TraverseCfg{p.check_traverse, p.traverse_non_self, p.stop_after_passing, p.shift_to_center, p.static_traverse,
+                       p.center_shift, p.ray_eps, p.max_search_mult};
+}
+
+__device__ __forceinline__ int tv_of(int4 q, int k) { return k == 0 ? q.x : (k == 1 ? q.y : (k == 2 ? q.z : q.w)); }
+
+struct Walk {
+    const float4* P;
+    const int4* tets;
+    const int4* nbr;
+    float3 o, ax0, ax1;
+    float max_dis, eps;
+    int32_t target;
+
+    // projectTo2DCoordinates: the incoming face's vertices in tet4Faces order, then the apex
+    __device__ void project(int4 q, int inc, float2* p, float3* X) const {
+        for (int i = 0; i < 4; ++i) {
+            X[i] = ld3(P, tv_of(q, i < 3 ? kTet4Faces[inc][i] : inc));
+            const float3 d = sub(X[i], o);
+            p[i] = make_float2(dot(ax0, d), dot(ax1, d));
+        }
+    }
+    // exitFaceSelection (TetMesh/TetMeshFEM.h:423-483)
+    __device__ void exits(const float2* p, bool* out) const {
+        const float v1x = p[1].x - p[0].x, v1y = p[1].y - p[0].y, v2x = p[2].x - p[0].x, v2y = p[2].y - p[0].y;
+        const float area = v1x * v2y - v1y * v2x;
+        const float sg = copysignf(1.0f, area);
+        const float d0 = p[3].x * p[0].y - p[3].y * p[0].x;
+        const float d1 = p[3].x * p[1].y - p[3].y * p[1].x;
+        const float d2 = p[3].x * p[2].y - p[3].y * p[2].x;
+        out[0] = d1 * sg >= -eps && d2 * sg <= eps;
+        out[1] = d2 * sg >= -eps && d0 * sg <= eps;
+        out[2] = d0 * sg >= -eps && d1 * sg <= eps;
+    }
+    // the ray's crossing of exit face i lies beyond max_dis (originBarycentric2DTriangle)
+    __device__ bool passed(const float2* p, const float3* X, int i) const {
+        const float2 a = p[kExit3[i][0]], b = p[kExit3[i][1]], c = p[kExit3[i][2]];
+        const float v0x = b.x - a.x, v0y = b.y - a.y, v1x = c.x - a.x, v1y = c.y - a.y, v2x = -a.x, v2y = -a.y;
+        const float den = v0x * v1y - v1x * v0y;
+        const float w1 = (v2x * v1y - v1x * v2y) / den;
+        const float w2 = (v0x * v2y - v2x * v0y) / den;
+        const float w0 = 1.0f - w1 - w2;
+        const float3 A = X[kExit3[i][0]], B = X[kExit3[i][1]], C = X[kExit3[i][2]];
+        const float3 x = v3((w0 * A.x + w1 * B.x) + w2 * C.x, (w0 * A.y + w1 * B.y) + w2 * C.y,
+                            (w0 * A.z + w1 * B.z) + w2 * C.z);
+        const float3 d = sub(x, o);
+        return dot(d, d) > max_dis * max_dis;
+    }
+};
+
+// 1 reached, 0 not reached, -1 gave up on a bound
+__device__ __noinline__ int walk(const Walk& w, int32_t start, int start_face, bool dynamic, int32_t* stack) {
+    const int cap = dynamic ? kDynamicStack : kStaticStack;
+    int32_t ring[kLoopRing];
+    int nring = 0;
+    ring[nring++ % kLoopRing] = start;
+    float2 p[4];
+    float3 X[4];
+    bool ex[3];
+    int4 q = w.tets[start];
+    w.project(q, start_face, p, X);
+    w.exits(p, ex);
+    int sp = 0;
+    for (int i = 0; i < 3; ++i)
+        if (ex[i]) stack[sp++] = (start << 2) | kTet4Faces[start_face][i];
+    int n = 0;
+    for (int steps = 0; sp > 0; ++steps) {
+        if (steps >= kMaxWalkSteps) return -1;
+        const int32_t e = stack[--sp];
+        const int32_t prev = e >> 2;
+        const int f = e & 3;
+        const int4 qp = w.tets[prev];
+        const int32_t fv0 = tv_of(qp, kTet4Faces[f][0]), fv1 = tv_of(qp, kTet4Faces[f][1]), fv2 = tv_of(qp, kTet4Faces[f][2]);
+        const int32_t cur = tv_of(w.nbr[prev], f);
+        if (cur == w.target) return 1;
+        if (cur < 0) return 0;  // reached the boundary
+        bool seen = false;
+        const int m = nring < kLoopRing ? nring : kLoopRing;
+        for (int i = 0; i < m; ++i) seen |= ring[i] == cur;
+        if (seen) continue;
+        ring[nring++ % kLoopRing] = cur;
+        q = w.tets[cur];
+        const int32_t apex = q.x ^ q.y ^ q.z ^ q.w ^ fv0 ^ fv1 ^ fv2;
+        const int inc = apex == q.x ? 0 : (apex == q.y ? 1 : (apex == q.z ? 2 : 3));
+        w.project(q, inc, p, X);
+        w.exits(p, ex);
+        const int4 nb = w.nbr[cur];
+        for (int i = 0; i < 3; ++i) {
+            if (!ex[i]) continue;
+            const int ef = kTet4Faces[inc][i];
+            const int32_t next = tv_of(nb, ef);
+            if (!dynamic && next == w.target) return 1;
+            if (sp >= cap) return -1;
+            stack[sp++] = (cur << 2) | ef;
+            if (dynamic && next == w.target) return 1;
+            const bool check = dynamic ? (!(n % kPassThroughSteps) || n == 2) : !(n % kPassThroughSteps);
+            if (check && w.max_dis > 0.f && w.passed(p, X, i)) return 0;
+        }
+        ++n;
+    }
+    return 0;  // empty stack
+}
+
+// Orthonormal basis of the plane normal to unit n (CuMatrix::buildOrthonormalBasis, whose
+// source is not in the reference tree): Duff et al., "Building an Orthonormal Basis,
+// Revisited", JCGT 6(1), 2017.
+__device__ __forceinline__ void ortho_basis(float3 n, float3& b1, float3& b2) {
+    const float sign = copysignf(1.0f, n.z);
+    const float a = -1.0f / (sign + n.z);
+    const float b = n.x * n.y * a;
+    b1 = v3(1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x);
+    b2 = v3(b, sign + n.y * n.y * a, -n.y);
+}
+
+// The traversal check for surface face g with closest point cp (type 6 = interior) of
+// the query point moved toward the containing tet (target_pt).
+__device__ __noinline__ bool traverse_ok(const Dev& D, const float4* P, const TraverseCfg& c, int32_t g, int type,
+                                         float3 cp, float3 target_pt, int32_t target_tet) {
+    const int2 ft = D.face_tet[g];
+    if (ft.x == target_tet) return true;
+    const int4 fv = D.faces[g];
+    float3 o = cp;
+    if (type != 6) {
+        const float3 sum = add(add(ld3(P, fv.x), ld3(P, fv.y)), ld3(P, fv.z));
+        const float3 a = mul(1.f - c.shift, cp), b = mul(c.shift / 3.0f, sum);
+        o = add(a, b);
+    }
+    const float3 ray = sub(target_pt, o);
+    const float len = sqrtf(dot(ray, ray));
+    Walk w;
+    w.P = P;
+    w.tets = D.tets;
+    w.nbr = D.tet_nbr;
+    w.o = o;
+    ortho_basis(v3(ray.x / len, ray.y / len, ray.z / len), w.ax0, w.ax1);
+    w.max_dis = c.stop_after ? c.max_mult * len : -1.f;
+    w.eps = c.eps;
+    w.target = target_tet;
+    int32_t stack[kDynamicStack];
+    int r = c.use_static ? walk(w, ft.x, ft.y, false, stack) : -1;
+    if (r < 0) r = walk(w, ft.x, ft.y, true, stack);  // the static stack overflowed
+    if (r < 0) atomicAdd(&D.counters[cloth::CC_TRUNCATIONS], 1ull);
+    return r == 1;
+}
+
 __device__ __forceinline__ float box_dist2(float3 p, float4 lo, float4 hi) {
     const float dx = fmaxf(fmaxf(lo.x - p.x, 0.f), p.x - hi.x);
     const float dy = fmaxf(fmaxf(lo.y - p.y, 0.f), p.y - hi.y);
@@ -360,7 +526,7 @@ __global__ void k_clear_hits(Dev D) {
 // DCD of one surface vertex per thread.
 template <bool INTERMEDIATE>
 __global__ void k_dcd(Dev D, bvh::LbvhDev tb, bvh::LbvhDev fb, const float4* xf, const int* vol_flag, int ccd_on,
-                      int handle_self, int check_feasible, float eps, float off) {
+                      int handle_self, int check_feasible, float eps, float off, TraverseCfg tc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= D.nsv) return;
     const int2 q = D.sv[i];
@@ -390,7 +556,15 @@ __global__ void k_dcd(Dev D, bvh::LbvhDev tb, bvh::LbvhDev fb, const float4* xf,
     if (best_t == 0x7fffffff) return;
     if (!INTERMEDIATE) D.pen[i] = 1;
     const int im = D.tet_mesh[best_t];
-    // closestPointQuery: nearest feasible surface face of mesh im, ties to the lower face
+    // closestPointQuery: nearest feasible surface face of mesh im from which the
+    // tetrahedral traversal reaches best_t, ties to the lower face
+    const bool traverse = tc.check && (im == m || tc.non_self);
+    float3 target = p;
+    if (traverse && tc.shift_center) {
+        const int4 tv = D.tets[best_t];
+        const float3 cen = mul(0.25f, add(add(add(ld3(P, tv.x), ld3(P, tv.y)), ld3(P, tv.z)), ld3(P, tv.w)));
+        target = add(mul(1.f - tc.shift, p), mul(tc.shift, cen));
+    }
     float best = __int_as_float(0x7f800000);
     int32_t bestg = -1;
     int stack[kStack];
@@ -410,6 +584,7 @@ __global__ void k_dcd(Dev D, bvh::LbvhDev tb, bvh::LbvhDev fb, const float4* xf,
             const float d = sqrtf(dot(dd, dd));
             if (!(d < best || (d == best && g < bestg))) continue;
             if (check_feasible && !feasible(D, P, p, g, type, eps)) continue;
+            if (traverse && !traverse_ok(D, P, tc, g, type, cp, target, best_t)) continue;
             best = d;
             bestg = g;
         } else {
@@ -519,6 +694,8 @@ struct Detector::Impl {
     int2* sv = nullptr;
     int32_t *ring_ofs = nullptr, *ring = nullptr, *tet_mesh = nullptr;
     int4* tets = nullptr;
+    int4* tet_nbr = nullptr;
+    int2* face_tet = nullptr;
     int32_t* hit = nullptr;
     float* hit_tt = nullptr;
     uint8_t* pen = nullptr;
@@ -543,7 +720,7 @@ void Detector::release() {
     d_->face_bvh.release();
     d_->tet_bvh.release();
     for (void* p : {(void*)d_->faces, (void*)d_->face_nbr, (void*)d_->sv, (void*)d_->ring_ofs, (void*)d_->ring,
-                    (void*)d_->tet_mesh, (void*)d_->tets, (void*)d_->hit, (void*)d_->hit_tt, (void*)d_->pen,
+                    (void*)d_->tet_mesh, (void*)d_->tets, (void*)d_->tet_nbr, (void*)d_->face_tet, (void*)d_->hit, (void*)d_->hit_tt, (void*)d_->pen,
                     (void*)d_->info, (void*)d_->own, (void*)d_->rel, (void*)d_->list, (void*)d_->nlist,
                     (void*)d_->vol_flag, (void*)d_->keys, (void*)d_->keys_sorted, (void*)d_->counters, d_->sort_tmp,
                     d_->select_tmp})
@@ -576,6 +753,8 @@ void Detector::init(const Topo& t, const Params& prm, size_t& bytes) {
     I.ring = upload(t.ring, bytes);
     I.tets = upload(t.tets, bytes);
     I.tet_mesh = upload(t.tet_mesh, bytes);
+    I.tet_nbr = upload(t.tet_nbr, bytes);
+    I.face_tet = upload(t.face_tet, bytes);
     I.hit = dalloc<int32_t>(nsv_, bytes);
     I.hit_tt = dalloc<float>(nsv_, bytes);
     I.pen = dalloc<uint8_t>(nsv_, bytes);
@@ -611,6 +790,8 @@ void Detector::init(const Topo& t, const Params& prm, size_t& bytes) {
     D.ring = I.ring;
     D.tets = I.tets;
     D.tet_mesh = I.tet_mesh;
+    D.tet_nbr = I.tet_nbr;
+    D.face_tet = I.face_tet;
     D.hit = I.hit;
     D.hit_tt = I.hit_tt;
     D.pen = I.pen;
@@ -634,11 +815,11 @@ void Detector::enqueue(const float4* xf, bool intermediate, bool rebuild, cudaSt
         if (intermediate)
             k_dcd<true><<<blocks(nsv_, 128), 128, 0, st>>>(D, I.tet_bvh.dev(), I.face_bvh.dev(), xf, I.vol_flag, prm_.ccd,
                                                            prm_.handle_self, prm_.check_feasible, prm_.feasible_eps,
-                                                           prm_.off_height);
+                                                           prm_.off_height, traverse_cfg(prm_));
         else
             k_dcd<false><<<blocks(nsv_, 128), 128, 0, st>>>(D, I.tet_bvh.dev(), I.face_bvh.dev(), xf, I.vol_flag, prm_.ccd,
                                                             prm_.handle_self, prm_.check_feasible, prm_.feasible_eps,
-                                                            prm_.off_height);
+                                                            prm_.off_height, traverse_cfg(prm_));
     } else if (!intermediate) {
         k_clear_hits<<<blocks(nsv_, 256), 256, 0, st>>>(D);
     }

@@ -31,6 +31,8 @@ struct Topo {
     std::vector<int32_t> ring;      // ... as slots
     std::vector<int4> tets;         // per tet (meshes concatenated): slots
     std::vector<int32_t> tet_mesh;
+    std::vector<int4> tet_nbr;      // per tet: global tet across the face omitting vertex x/y/z/w (-1: none)
+    std::vector<int2> face_tet;     // per face: the global tet it bounds, the local vertex it omits
 };
 
 struct Params {
@@ -39,6 +41,15 @@ struct Params {
     bool check_feasible = true;    // checkFeasibleRegion
     float feasible_eps = 1e-2f;    // feasibleRegionEpsilon
     float off_height = 1e7f;       // collisionOffHeight (y)
+    // the DCD closest-point query's tetrahedral traversal check
+    bool check_traverse = true;     // checkTetTraverse
+    bool traverse_non_self = true;  // tetrahedralTraverseForNonSelfIntersection
+    bool stop_after_passing = true; // stopTraversingAfterPassingQueryPoint
+    bool shift_to_center = true;    // shiftQueryPointToCenter
+    bool static_traverse = true;    // useStaticTraverse
+    float center_shift = 0.01f;     // centerShiftLevel
+    float ray_eps = 1e-10f;         // rayTriIntersectionEPSILON
+    float max_search_mult = 1.8f;   // maxSearchDistanceMultiplier
 };
 
 // What the solve reads, per slot:

@@ -397,6 +397,14 @@ public:
         prm.check_feasible = p.checkFeasibleRegion;
         prm.feasible_eps = float(p.feasibleRegionEpsilon);
         prm.off_height = float(p.collisionOffHeight);
+        prm.check_traverse = p.checkTetTraverse;
+        prm.traverse_non_self = p.tetrahedralTraverseForNonSelfIntersection;
+        prm.stop_after_passing = p.stopTraversingAfterPassingQueryPoint;
+        prm.shift_to_center = p.shiftQueryPointToCenter;
+        prm.static_traverse = p.useStaticTraverse;
+        prm.center_shift = float(p.centerShiftLevel);
+        prm.ray_eps = float(p.rayTriIntersectionEPSILON);
+        prm.max_search_mult = float(p.maxSearchDistanceMultiplier);
         tetcd::Topo t;
         t.nslots = int32_t(nslots_);
         t.face_ofs.assign(nmesh_ + 1, 0);
@@ -416,10 +424,15 @@ public:
             for (int32_t v : M.sverts) t.verts.push_back(make_int2(slot(v), m));
             for (int32_t v = 0; v < M.nv; ++v)
                 for (int32_t r = M.sring_ofs[v]; r < M.sring_ofs[v + 1]; ++r) ring[slot(v)].push_back(slot(M.sring[r]));
+            const int32_t t0 = int32_t(t.tets.size());
+            for (size_t f = 0; f < nf; ++f) t.face_tet.push_back(make_int2(t0 + M.sface_tet[2 * f], M.sface_tet[2 * f + 1]));
             for (int32_t k = 0; k < M.ntet; ++k) {
                 const int32_t* tv = &M.tets[4 * size_t(k)];
                 t.tets.push_back(make_int4(slot(tv[0]), slot(tv[1]), slot(tv[2]), slot(tv[3])));
                 t.tet_mesh.push_back(m);
+                int32_t nb[4];
+                for (int j = 0; j < 4; ++j) nb[j] = M.tet_nbr[4 * size_t(k) + j] < 0 ? -1 : t0 + M.tet_nbr[4 * size_t(k) + j];
+                t.tet_nbr.push_back(make_int4(nb[0], nb[1], nb[2], nb[3]));
             }
         }
         t.ring_ofs.assign(size_t(nslots_) + 1, 0);

@@ -57,6 +57,10 @@ class OracleParams(C.Structure):
         ("intermediate_collision_iterations", C.c_int32),
         ("handle_self_collision", C.c_int32), ("check_feasible_region", C.c_int32),
         ("feasible_region_eps", C.c_double),
+        ("check_tet_traverse", C.c_int32), ("traverse_non_self", C.c_int32),
+        ("stop_traversing_after_passing", C.c_int32), ("shift_query_to_center", C.c_int32),
+        ("use_static_traverse", C.c_int32),
+        ("center_shift_level", C.c_double), ("ray_tri_eps", C.c_double), ("max_search_mult", C.c_double),
     ]
 
 
@@ -111,6 +115,9 @@ def lib():
         L.oracle_ccd_tri_point.restype = C.c_int32
         L.oracle_tet_surface.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_void_p]
+        L.oracle_tet_walk.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, fp, fp,
+                                      C.c_float, C.c_float, C.c_int32, C.POINTER(C.c_int32)]
+        L.oracle_tet_walk.restype = C.c_int32
     return _lib
 
 
@@ -143,6 +150,23 @@ def tet_surface(X: np.ndarray, tets: np.ndarray) -> tuple[np.ndarray, np.ndarray
     L.oracle_tet_surface(len(X) // 3, len(tets) // 4, tets.ctypes.data, X.ctypes.data, C.byref(nf), C.byref(nsv),
                          F.ctypes.data, V.ctypes.data)
     return F, V
+
+
+def tet_walk(X: np.ndarray, tets: np.ndarray, face: int, target: int, origin, direction, max_dis: float = -1.0,
+             ray_eps: float = 1e-10, use_static: bool = True) -> tuple[bool, int]:
+    """The DCD traversal walk from surface face `face` (tet_surface order) along the ray
+    origin + t * direction (FP32) -> (reached tet `target`, gave up on a size bound)."""
+    X = np.ascontiguousarray(X, np.float64).reshape(-1)
+    tets = np.ascontiguousarray(tets, np.int32).reshape(-1)
+    fp = C.POINTER(C.c_float)
+    o = np.ascontiguousarray(origin, np.float32).reshape(3)
+    d = np.ascontiguousarray(direction, np.float32).reshape(3)
+    st = C.c_int32()
+    r = lib().oracle_tet_walk(len(X) // 3, len(tets) // 4, tets.ctypes.data, X.ctypes.data, face, target,
+                              o.ctypes.data_as(fp), d.ctypes.data_as(fp), max_dis, ray_eps, int(use_static), C.byref(st))
+    if r < 0:
+        raise IndexError("face or target out of range")
+    return bool(r), bool(st.value)
 
 
 def ccd_tri_point(x0, x1, p0, p1):
@@ -241,6 +265,14 @@ class OracleScene:
         op.handle_self_collision = int(col.get("handleSelfCollision", True))
         op.check_feasible_region = int(col.get("checkFeasibleRegion", True))
         op.feasible_region_eps = col.get("feasibleRegionEpsilon", 1e-2)
+        op.check_tet_traverse = int(col.get("checkTetTraverse", True))
+        op.traverse_non_self = int(col.get("tetrahedralTraverseForNonSelfIntersection", True))
+        op.stop_traversing_after_passing = int(col.get("stopTraversingAfterPassingQueryPoint", True))
+        op.shift_query_to_center = int(col.get("shiftQueryPointToCenter", True))
+        op.use_static_traverse = int(col.get("useStaticTraverse", True))
+        op.center_shift_level = col.get("centerShiftLevel", 0.01)
+        op.ray_tri_eps = col.get("rayTriIntersectionEPSILON", 1e-10)
+        op.max_search_mult = col.get("maxSearchDistanceMultiplier", 1.8)
         defs = (OracleDeformer * max(1, len(scene["deformers"])))()
         for i, d in enumerate(scene["deformers"]):
             dd = defs[i]

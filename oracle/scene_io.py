@@ -27,7 +27,11 @@ PHYSICS_DEFAULTS = {
 }
 # CollisionDetector/CollisionDetertionParameters.h:41-78 (the keys the VBD step reads)
 COLLISION_DEFAULTS = {"allowCCD": True, "allowDCD": True, "handleSelfCollision": True, "checkFeasibleRegion": True,
-                      "feasibleRegionEpsilon": 1e-2}
+                      "feasibleRegionEpsilon": 1e-2, "checkTetTraverse": True,
+                      "tetrahedralTraverseForNonSelfIntersection": True, "stopTraversingAfterPassingQueryPoint": True,
+                      "shiftQueryPointToCenter": True, "useStaticTraverse": True, "loopLessTraverse": False,
+                      "centerShiftLevel": 0.01, "rayTriIntersectionEPSILON": 1e-10,
+                      "maxSearchDistanceMultiplier": 1.8}
 MATERIAL_DEFAULTS = {
     "density": 1.0, "frictionDynamic": 0.1, "frictionEpsV": 0.01, "exponentialVelDamping": 1.0,
     "constantVelDamping": 0.0, "initializationType": 0, "miu": 1e4, "lmbd": 1e4,
@@ -120,5 +124,7 @@ def load_scene(models_json: str, params_json: str, repo_root: str | None = None,
             meshes[mi]["fixed"][np.asarray(verts, np.int64)] = 1
     cp = dict(COLLISION_DEFAULTS)
     cp.update({k: v for k, v in params.get("CollisionParams", {}).items() if k in COLLISION_DEFAULTS})
+    if cp["loopLessTraverse"]:
+        raise ValueError("CollisionParams loopLessTraverse is not supported")
     pp["collision"] = cp
     return {"meshes": meshes, "params": pp, "deformers": deformers}

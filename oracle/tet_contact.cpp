@@ -20,15 +20,22 @@ void build_surface_topology(int nv, Surface& s);
 // ---------------------------------------------------------------------------
 Surface extract_surface(int nv, int ntet, const int32_t* tets, const double* X) {
     static const int kFace[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};
-    std::map<std::array<int32_t, 3>, int> count;
+    std::map<std::array<int32_t, 3>, std::vector<int32_t>> owners;  // sorted face -> 4 * tet + k
     for (int t = 0; t < ntet; ++t)
         for (int k = 0; k < 4; ++k) {
             std::array<int32_t, 3> key = {tets[4 * t + kFace[k][0]], tets[4 * t + kFace[k][1]],
                                           tets[4 * t + kFace[k][2]]};
             std::sort(key.begin(), key.end());
-            ++count[key];
+            owners[key].push_back(4 * t + k);
         }
     Surface s;
+    // neighbour across each face: the other tet of a face shared by exactly two
+    s.tet_nbr.assign(4 * size_t(ntet), -1);
+    for (const auto& kv : owners)
+        if (kv.second.size() == 2) {
+            s.tet_nbr[size_t(kv.second[0])] = kv.second[1] / 4;
+            s.tet_nbr[size_t(kv.second[1])] = kv.second[0] / 4;
+        }
     std::vector<char> on(size_t(nv), 0);
     for (int t = 0; t < ntet; ++t) {
         const int32_t* v = tets + 4 * t;
@@ -42,8 +49,10 @@ Surface extract_surface(int nv, int ntet, const int32_t* tets, const double* X) 
             std::array<int32_t, 3> f = {v[kFace[k][0]], v[kFace[k][1]], v[kFace[k][2]]};
             std::array<int32_t, 3> key = f;
             std::sort(key.begin(), key.end());
-            if (count[key] != 1) continue;
+            if (owners[key].size() != 1) continue;
             if (vol < 0) std::swap(f[1], f[2]);
+            s.face_tet.push_back(t);
+            s.face_tet.push_back(k);
             for (int i = 0; i < 3; ++i) {
                 s.faces.push_back(f[i]);
                 on[size_t(f[i])] = 1;
@@ -456,6 +465,173 @@ int closest_point(F3 p, F3 a, F3 b, F3 c, float bary[3], F3& cp) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// Tetrahedral traversal (TetMesh/TetMeshFEM.cpp:503-740 static, 908-1100 dynamic)
+// ---------------------------------------------------------------------------
+namespace {
+
+// TetMeshFEM::tet4Faces: the face omitting local vertex k, in the order the walk
+// projects it; posibleExit3Faces: the exit face across incoming-face vertex i, as
+// indices into (incoming face vertices 0..2, apex 3).
+const int kTet4Faces[4][3] = {{1, 2, 3}, {2, 0, 3}, {0, 1, 3}, {1, 0, 2}};
+const int kExit3[3][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}};
+constexpr int kStaticStack = 32;      // SIZE_CANDIDATE_FACE_STACK
+constexpr int kLoopRing = 32;         // SIZE_TRAVERSED_CIRCULAR_ARRAY
+constexpr int kPassThroughSteps = 5;  // TetMeshFEM::passThroughCheckSteps
+// Bounds of the dynamic walk (unbounded in the reference); shared with the GPU.
+constexpr int kDynamicStack = 1024;
+constexpr int kMaxWalkSteps = 1 << 16;
+
+// Orthonormal basis of the plane normal to unit n (CuMatrix::buildOrthonormalBasis;
+// its source is not in the reference tree): Duff et al., "Building an Orthonormal
+// Basis, Revisited", JCGT 6(1), 2017.
+void ortho_basis(F3 n, F3& b1, F3& b2) {
+    const float sign = std::copysign(1.0f, n.z);
+    const float a = -1.0f / (sign + n.z);
+    const float b = n.x * n.y * a;
+    b1 = F3{1.0f + sign * n.x * n.x * a, sign * b, -sign * n.x};
+    b2 = F3{b, sign + n.y * n.y * a, -n.y};
+}
+
+struct Walk {
+    const float* X;
+    const int32_t* tets;
+    const int32_t* nbr;
+    F3 o, ax0, ax1;
+    float max_dis, eps;
+    int32_t target;
+
+    int32_t tv(int32_t t, int k) const { return tets[4 * size_t(t) + size_t(k)]; }
+    F3 vert(int32_t t, int k) const { return ld(X, tv(t, k)); }
+    // projectTo2DCoordinates: incoming face's vertices in tet4Faces order, then the apex
+    void project(int32_t t, int inc, F2 p[4], F3 P[4]) const {
+        for (int i = 0; i < 4; ++i) {
+            P[i] = vert(t, i < 3 ? kTet4Faces[inc][i] : inc);
+            const F3 d = sub(P[i], o);
+            p[i] = F2{dot(ax0, d), dot(ax1, d)};
+        }
+    }
+    // exitFaceSelection (TetMesh/TetMeshFEM.h:423-483): the faces whose 2D wedge at the
+    // apex holds the ray (the origin), with the sign of the incoming triangle
+    static void exits(const F2 p[4], float eps, bool out[3]) {
+        const F2 v1{p[1].x - p[0].x, p[1].y - p[0].y}, v2{p[2].x - p[0].x, p[2].y - p[0].y};
+        const float area = v1.x * v2.y - v1.y * v2.x;
+        const float sg = std::copysign(1.0f, area);
+        const float d0 = p[3].x * p[0].y - p[3].y * p[0].x;
+        const float d1 = p[3].x * p[1].y - p[3].y * p[1].x;
+        const float d2 = p[3].x * p[2].y - p[3].y * p[2].x;
+        out[0] = d1 * sg >= -eps && d2 * sg <= eps;
+        out[1] = d2 * sg >= -eps && d0 * sg <= eps;
+        out[2] = d0 * sg >= -eps && d1 * sg <= eps;
+    }
+    // the ray's crossing of exit face i beyond max_dis from the origin
+    // (originBarycentric2DTriangle, TetMesh/TetMeshFEM.h:625-633)
+    bool passed(const F2 p[4], const F3 P[4], int i) const {
+        const F2 a = p[kExit3[i][0]], b = p[kExit3[i][1]], c = p[kExit3[i][2]];
+        const F2 v0{b.x - a.x, b.y - a.y}, v1{c.x - a.x, c.y - a.y}, v2{-a.x, -a.y};
+        const float den = v0.x * v1.y - v1.x * v0.y;
+        const float w1 = (v2.x * v1.y - v1.x * v2.y) / den;
+        const float w2 = (v0.x * v2.y - v2.x * v0.y) / den;
+        const float w0 = 1.0f - w1 - w2;
+        const F3 A = P[kExit3[i][0]], B = P[kExit3[i][1]], C = P[kExit3[i][2]];
+        const F3 x{(w0 * A.x + w1 * B.x) + w2 * C.x, (w0 * A.y + w1 * B.y) + w2 * C.y, (w0 * A.z + w1 * B.z) + w2 * C.z};
+        const F3 d = sub(x, o);
+        return dot(d, d) > max_dis * max_dis;
+    }
+};
+
+// Last kLoopRing tets entered (CircularArray::hasBackward of the traversed set).
+struct LoopRing {
+    int32_t v[kLoopRing];
+    int n = 0;
+    bool has(int32_t t) const {
+        const int m = n < kLoopRing ? n : kLoopRing;
+        for (int i = 0; i < m; ++i)
+            if (v[i] == t) return true;
+        return false;
+    }
+    void push(int32_t t) { v[n++ % kLoopRing] = t; }
+};
+
+// result: 1 reached, 0 not reached, -1 gave up on a bound
+int walk(const Walk& w, int32_t start, int start_face, bool dynamic) {
+    const int cap = dynamic ? kDynamicStack : kStaticStack;
+    std::vector<int32_t> sf(static_cast<size_t>(cap)), st(static_cast<size_t>(cap));
+    int sp = 0;
+    LoopRing ring;
+    ring.push(start);
+    F2 p[4];
+    F3 P[4];
+    bool ex[3];
+    w.project(start, start_face, p, P);
+    Walk::exits(p, w.eps, ex);
+    for (int i = 0; i < 3; ++i)
+        if (ex[i]) {
+            sf[size_t(sp)] = kTet4Faces[start_face][i];
+            st[size_t(sp++)] = start;
+        }
+    int n = 0;
+    for (int steps = 0; sp > 0; ++steps) {
+        if (steps >= kMaxWalkSteps) return -1;
+        --sp;
+        const int f = sf[size_t(sp)];
+        const int32_t prev = st[size_t(sp)];
+        const int32_t fv0 = w.tv(prev, kTet4Faces[f][0]), fv1 = w.tv(prev, kTet4Faces[f][1]),
+                      fv2 = w.tv(prev, kTet4Faces[f][2]);
+        const int32_t cur = w.nbr[4 * size_t(prev) + size_t(f)];
+        if (cur == w.target) return 1;
+        if (cur < 0) return 0;  // reached the boundary
+        if (ring.has(cur)) continue;
+        ring.push(cur);
+        const int32_t apex = w.tv(cur, 0) ^ w.tv(cur, 1) ^ w.tv(cur, 2) ^ w.tv(cur, 3) ^ fv0 ^ fv1 ^ fv2;
+        int inc = 3;
+        for (int k = 0; k < 3; ++k)
+            if (apex == w.tv(cur, k)) {
+                inc = k;
+                break;
+            }
+        w.project(cur, inc, p, P);
+        Walk::exits(p, w.eps, ex);
+        for (int i = 0; i < 3; ++i) {
+            if (!ex[i]) continue;
+            const int ef = kTet4Faces[inc][i];
+            const int32_t next = w.nbr[4 * size_t(cur) + size_t(ef)];
+            if (!dynamic && next == w.target) return 1;
+            if (sp >= cap) return -1;
+            sf[size_t(sp)] = ef;
+            st[size_t(sp++)] = cur;
+            if (dynamic && next == w.target) return 1;
+            const bool check = dynamic ? (!(n % kPassThroughSteps) || n == 2) : !(n % kPassThroughSteps);
+            if (check && w.max_dis > 0.f && w.passed(p, P, i)) return 0;
+        }
+        ++n;
+    }
+    return 0;  // empty stack
+}
+
+}  // namespace
+
+bool tet_traverse(const float* X, const int32_t* tets, const Surface& s, const float origin[3], const float dir[3],
+                  float max_dis, int32_t face, int32_t target, float ray_eps, bool use_static, int* status) {
+    *status = 0;
+    const int32_t start = s.face_tet[2 * size_t(face)];
+    const int start_face = s.face_tet[2 * size_t(face) + 1];
+    if (start == target) return true;
+    Walk w;
+    w.X = X;
+    w.tets = tets;
+    w.nbr = s.tet_nbr.data();
+    w.o = F3{origin[0], origin[1], origin[2]};
+    ortho_basis(F3{dir[0], dir[1], dir[2]}, w.ax0, w.ax1);
+    w.max_dis = max_dis;
+    w.eps = ray_eps;
+    w.target = target;
+    int r = use_static ? walk(w, start, start_face, false) : -1;
+    if (r < 0) r = walk(w, start, start_face, true);  // the static stack overflowed
+    if (r < 0) *status = 1;
+    return r == 1;
+}
+
+// ---------------------------------------------------------------------------
 // Surface topology for the feasible-region tests.
 // ---------------------------------------------------------------------------
 void build_surface_topology(int nv, Surface& s) {
@@ -636,6 +812,7 @@ bool Detector::dcd(int m, int i, const DcdParams& prm, CcdHit& hit) const {
     // vertexCollisionDetection (DiscreteCollisionDetector.cpp:517-536, callback 12-95):
     // the first tet (lowest mesh, tet) that strictly contains the vertex
     int im = -1;
+    int32_t it = -1;
     for (int32_t g : d_->tets.query(q)) {
         const auto [tm, t] = d_->tet_of(g);
         if (!prm.handle_self && tm == m) continue;
@@ -645,15 +822,25 @@ bool Detector::dcd(int m, int i, const DcdParams& prm, CcdHit& hit) const {
         const float* P = prev ? T.xprev : T.x;
         if (point_in_tet(p, ld(P, tv[0]), ld(P, tv[1]), ld(P, tv[2]), ld(P, tv[3]))) {
             im = tm;
+            it = t;
             break;
         }
     }
     if (im < 0) return false;
     // closestPointQuery (:538-660, callback 97-329): the nearest surface face of the
-    // intersected mesh whose closest point is not the vertex itself and lies in the
-    // face's feasible region; equal distances keep the lower face
+    // intersected mesh whose closest point is not the vertex itself, lies in the face's
+    // feasible region and from which the tetrahedral traversal reaches the containing
+    // tet (:189-300); equal distances keep the lower face
     const CcdMesh& S = d_->meshes[size_t(im)];
     const float* P = prev ? S.xprev : S.x;
+    const bool traverse = prm.check_traverse && (im == m || prm.traverse_non_self);
+    // the query point moved a little toward the containing tet's centroid (:215-224)
+    F3 target = p;
+    if (traverse && prm.shift_to_center) {
+        const int32_t* tv = &S.tets[4 * size_t(it)];
+        const F3 cen = scale(add(add(add(ld(P, tv[0]), ld(P, tv[1])), ld(P, tv[2])), ld(P, tv[3])), 0.25f);
+        target = add(scale(p, 1.f - prm.center_shift), scale(cen, prm.center_shift));
+    }
     float best = 3.4e38f;
     for (size_t f = 0; f < S.surf->faces.size() / 3; ++f) {
         const int32_t* fv = &S.surf->faces[3 * f];
@@ -665,6 +852,25 @@ bool Detector::dcd(int m, int i, const DcdParams& prm, CcdHit& hit) const {
         if (im == m && type <= 2 && fv[type] == v) continue;
         if (!(d < best)) continue;
         if (prm.check_feasible && !feasible(S, P, p, int32_t(f), type, prm.feasible_eps)) continue;
+        if (traverse) {
+            // from the closest point (moved a little toward the face's centroid unless it is
+            // interior) toward the query point (:206-247)
+            F3 o = cp;
+            if (type != 6) {
+                const F3 sum = add(add(ld(P, fv[0]), ld(P, fv[1])), ld(P, fv[2]));
+                o = add(scale(cp, 1.f - prm.center_shift), scale(sum, prm.center_shift / 3.0f));
+            }
+            const F3 ray = sub(target, o);
+            const float len = std::sqrt(dot(ray, ray));
+            const float dir[3] = {ray.x / len, ray.y / len, ray.z / len};
+            const float org[3] = {o.x, o.y, o.z};
+            const float max_dis = prm.stop_after_passing ? prm.max_search_mult * len : -1.f;
+            int status = 0;
+            const bool ok =
+                tet_traverse(P, S.tets, *S.surf, org, dir, max_dis, int32_t(f), it, prm.ray_eps, prm.static_traverse,
+                             &status);
+            if (!ok) continue;
+        }
         best = d;
         hit.fmesh = im;
         hit.face = int32_t(f);
@@ -682,6 +888,20 @@ extern "C" {
 int32_t oracle_ccd_tri_point(const float* x0, const float* x1, const float* p0, const float* p1, float* tt,
                              float* bary) {
     return oracle_tc::ccd_tri_point(x0, x1, p0, p1, tt, bary);
+}
+
+int32_t oracle_tet_walk(int32_t nv, int32_t ntet, const int32_t* tets, const double* X, int32_t face, int32_t target,
+                        const float* origin, const float* dir, float max_dis, float ray_eps, int32_t use_static,
+                        int32_t* status) {
+    const oracle_tc::Surface s = oracle_tc::extract_surface(nv, ntet, tets, X);
+    if (face < 0 || size_t(face) >= s.faces.size() / 3 || target < 0 || target >= ntet) return -1;
+    std::vector<float> xf(3 * size_t(nv));
+    for (size_t i = 0; i < xf.size(); ++i) xf[i] = float(X[i]);
+    int st = 0;
+    const bool ok = oracle_tc::tet_traverse(xf.data(), tets, s, origin, dir, max_dis, face, target, ray_eps, use_static != 0,
+                                            &st);
+    if (status) *status = st;
+    return ok ? 1 : 0;
 }
 
 void oracle_tet_surface(int32_t nv, int32_t ntet, const int32_t* tets, const double* X, int32_t* nfaces,

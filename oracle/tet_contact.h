@@ -33,6 +33,9 @@ struct Surface {
     std::vector<int32_t> verts;     // surface vertices, ascending
     std::vector<int32_t> face_nbr;  // 3 per face: the face across edge AB, BC, CA (-1: none)
     std::vector<int32_t> ring_ofs, ring;  // per mesh vertex: its surface neighbours, ascending
+    // tetrahedral traversal tables (TetMesh/TetMeshFEM.cpp:40-70, 173-214):
+    std::vector<int32_t> face_tet;  // 2 per face: the tet it bounds, the local vertex it omits
+    std::vector<int32_t> tet_nbr;   // 4 per tet: the tet across the face omitting local vertex k (-1: none)
 };
 
 // Boundary faces of a tet mesh in ascending (tet, local face) order; the face
@@ -65,7 +68,25 @@ struct DcdParams {
     bool handle_self = true;       // handleSelfCollision
     bool check_feasible = true;    // checkFeasibleRegion
     float feasible_eps = 1e-2f;    // feasibleRegionEpsilon
+    // the tetrahedral traversal check of the closest-point query
+    // (CollisionDetector/CollisionDetertionParameters.h:51-77)
+    bool check_traverse = true;     // checkTetTraverse
+    bool traverse_non_self = true;  // tetrahedralTraverseForNonSelfIntersection
+    bool stop_after_passing = true; // stopTraversingAfterPassingQueryPoint
+    bool shift_to_center = true;    // shiftQueryPointToCenter
+    bool static_traverse = true;    // useStaticTraverse
+    float center_shift = 0.01f;     // centerShiftLevel
+    float ray_eps = 1e-10f;         // rayTriIntersectionEPSILON
+    float max_search_mult = 1.8f;   // maxSearchDistanceMultiplier
 };
+
+// Walk from surface face `face` of a mesh, along the ray from `origin` in direction `dir`,
+// through the tets (tetrahedralTraverseTo / tetrahedralTraverseToDynamic,
+// TetMesh/TetMeshFEM.cpp:503-740, 908-1100): true when the walk reaches `target`.
+// max_dis <= 0 turns the pass-through test off. `status` gets 0, or 1 when the walk
+// gave up on its size bounds (candidate stack or step count).
+bool tet_traverse(const float* X, const int32_t* tets, const Surface& s, const float origin[3], const float dir[3],
+                  float max_dis, int32_t face, int32_t target, float ray_eps, bool use_static, int* status);
 
 // The two detectors of the tet-mesh contact path over all meshes:
 //   ccd(m, i): vertexContinuousCollisionDetection (ContinuousCollisionDetector.cpp:
@@ -76,8 +97,8 @@ struct DcdParams {
 //     12-95, 97-329, 517-660) at the positions given to build_tets: whether the vertex
 //     lies strictly inside a tet (the lowest (mesh, tet) of any mesh; own mesh only when
 //     handle_self and not incident), and then the nearest feasible surface face of that
-//     tet's mesh (hit.face = -1 when none). The tetrahedral traversal check of the
-//     closest-point query is not restated (it accepts every face of a convex mesh).
+//     tet's mesh (hit.face = -1 when none) from which the tetrahedral traversal
+//     (tet_traverse) reaches the containing tet.
 class Detector {
 public:
     explicit Detector(const std::vector<CcdMesh>& meshes);
@@ -104,6 +125,11 @@ extern "C" {
 /* Test entry points. */
 int32_t oracle_ccd_tri_point(const float* x0, const float* x1, const float* p0, const float* p1, float* tt,
                              float* bary);
+/* Tetrahedral walk of one tet mesh from surface face `face` toward tet `target` (1 reached,
+   0 not, -1 bad index); status = 1 when the walk gave up on a size bound. */
+int32_t oracle_tet_walk(int32_t nv, int32_t ntet, const int32_t* tets, const double* X, int32_t face, int32_t target,
+                        const float* origin, const float* dir, float max_dis, float ray_eps, int32_t use_static,
+                        int32_t* status);
 /* Surface of one tet mesh: call with faces == NULL to get the counts. */
 void oracle_tet_surface(int32_t nv, int32_t ntet, const int32_t* tets, const double* X, int32_t* nfaces,
                         int32_t* nverts, int32_t* faces, int32_t* verts);

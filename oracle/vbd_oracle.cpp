@@ -631,6 +631,14 @@ void detect_contacts(Scene<R>& s, bool intermediate) {
     dp.handle_self = s.p.handle_self_collision != 0;
     dp.check_feasible = s.p.check_feasible_region != 0;
     dp.feasible_eps = float(s.p.feasible_region_eps);
+    dp.check_traverse = s.p.check_tet_traverse != 0;
+    dp.traverse_non_self = s.p.traverse_non_self != 0;
+    dp.stop_after_passing = s.p.stop_traversing_after_passing != 0;
+    dp.shift_to_center = s.p.shift_query_to_center != 0;
+    dp.static_traverse = s.p.use_static_traverse != 0;
+    dp.center_shift = float(s.p.center_shift_level);
+    dp.ray_eps = float(s.p.ray_tri_eps);
+    dp.max_search_mult = float(s.p.max_search_mult);
     std::vector<std::vector<float>> xf(s.meshes.size()), pf(s.meshes.size());
     std::vector<oracle_tc::CcdMesh> cm(s.meshes.size());
     for (size_t im = 0; im < s.meshes.size(); ++im) {

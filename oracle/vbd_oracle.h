@@ -60,6 +60,13 @@ typedef struct {
     int32_t intermediate_collision_iterations;
     int32_t handle_self_collision, check_feasible_region;
     double feasible_region_eps;
+    /* the DCD closest-point query's tetrahedral traversal (CollisionParams
+       checkTetTraverse, tetrahedralTraverseForNonSelfIntersection,
+       stopTraversingAfterPassingQueryPoint, shiftQueryPointToCenter, useStaticTraverse,
+       centerShiftLevel, rayTriIntersectionEPSILON, maxSearchDistanceMultiplier) */
+    int32_t check_tet_traverse, traverse_non_self, stop_traversing_after_passing, shift_query_to_center,
+        use_static_traverse;
+    double center_shift_level, ray_tri_eps, max_search_mult;
 } OracleParams;
 
 typedef struct {

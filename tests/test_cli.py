@@ -51,7 +51,7 @@ def _scene(tmp_path, **params):
 
     mp, pp = scenes.stack_drop(str(tmp_path), spacing=0.03, gap=0.01, speed=1.0, precision="fp64")
     P = json.load(open(pp))
-    P["PhysicsParams"].update(params)
+    P["PhysicsParams"].update(saveOutputs=True, **params)
     json.dump(P, open(pp, "w"))
     return mp, pp
 

@@ -1,8 +1,9 @@
 """Tet-mesh vertex-face contact on the GPU against the oracle.
 
-- contact sets: the GPU detector (DCD point-in-tet + nearest feasible face, CCD of the
-  surface vertices' trajectories) returns exactly the oracle's rows on crafted states,
-  with FP32-representable positions so that both see identical inputs;
+- contact sets: the GPU detector (DCD point-in-tet + nearest feasible face reached by the
+  tetrahedral traversal, CCD of the surface vertices' trajectories) returns exactly the
+  oracle's rows on crafted states, with FP32-representable positions so that both see
+  identical inputs, under the traversal's parameter variants;
 - force and Hessian of vertices in contact (own contact and face-side relations) in
   the FP64 engine within 1e-9 of the oracle's;
 - trajectories of a cube dropped on another (contacts appear, persist and change) in
@@ -56,9 +57,25 @@ def _states(X0, X1, spacing, seed=0):
     return [tuple(tuple(_f32(a) for a in pair) for pair in st) for st in out]
 
 
-@pytest.mark.parametrize("spacing", [0.03, 0.01])
-def test_contact_sets_bit_exact(spacing, tmp_path, gaia_lib, oracle_lib):
+# CollisionParams variants of the DCD closest-point query's tetrahedral traversal: the
+# reference defaults (on convex bodies it rejects nothing), a pass-through limit that
+# makes walks give up (faces rejected), the dynamic walk alone, and the check off.
+TRAVERSAL = {
+    "default": {},
+    "short": {"maxSearchDistanceMultiplier": 0.05},
+    "dynamic": {"useStaticTraverse": False, "maxSearchDistanceMultiplier": 0.3},
+    "off": {"checkTetTraverse": False},
+}
+
+
+@pytest.mark.parametrize("spacing,traversal", [(0.03, "default"), (0.01, "default"), (0.03, "short"),
+                                               (0.03, "dynamic"), (0.03, "off")])
+def test_contact_sets_bit_exact(spacing, traversal, tmp_path, gaia_lib, oracle_lib):
     mp, pp = _scene(tmp_path, spacing)
+    if TRAVERSAL[traversal]:
+        P = json.load(open(pp))
+        P["CollisionParams"] = dict(TRAVERSAL[traversal])
+        json.dump(P, open(pp, "w"))
     phys, o = _pair(mp, pp)
     X0, X1 = phys.positions(0), phys.positions(1)
     total = 0

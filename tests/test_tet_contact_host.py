@@ -144,3 +144,124 @@ def test_oracle_stack_small_cells_ccd_only(tmp_path):
     stays below the surface after a substep)."""
     o, kinds = _run_stack(tmp_path, 0.01, 15)
     assert kinds and kinds <= {1}
+
+
+# ---- the DCD closest-point query's tetrahedral traversal (oracle) ------------------------
+
+def _walk_case(X, T, f, t, F, max_mult=1.8, shift=0.0):
+    """Ray from the centroid of surface face f toward the centroid of tet t, in FP32."""
+    from oracle import oracle as orc
+
+    o = X[F[f]].astype(np.float32).mean(0)
+    tgt = X[T[t]].astype(np.float32).mean(0)
+    d = (tgt - o).astype(np.float32)
+    L = np.float32(np.linalg.norm(d))
+    return orc.tet_walk(X, T, int(f), int(t), o, d / L, float(max_mult * L) if max_mult > 0 else -1.0)
+
+
+def test_walk_reaches_every_tet_of_a_convex_mesh(oracle_lib):
+    """Exact lattice (convex, with rays through edges and vertices): every walk from a
+    surface face's centroid to a tet's centroid arrives, static and dynamic. On a
+    jittered lattice, rays that leave through the start face itself (the target lies on
+    its outer side) find no exit face and fail."""
+    from gaia_gb300 import scenes
+    from oracle import oracle as orc
+
+    X, T = scenes.lattice_cube((5, 5, 5), 0.1)
+    F, _ = orc.tet_surface(X, T)
+    rng = np.random.default_rng(0)
+    for f in rng.choice(len(F), 30, replace=False):
+        for t in rng.choice(len(T), 8, replace=False):
+            assert _walk_case(X, T, f, t, F) == (True, False), (f, t)
+            o = X[F[f]].astype(np.float32).mean(0)
+            d = X[T[t]].astype(np.float32).mean(0) - o
+            ok, bound = orc.tet_walk(X, T, int(f), int(t), o, d / np.linalg.norm(d), -1.0, use_static=False)
+            assert ok and not bound, (f, t)
+    X, T = scenes.lattice_cube((5, 5, 5), 0.1, jitter=0.01, seed=4)
+    F, _ = orc.tet_surface(X, T)
+    outward = 0
+    for f in rng.choice(len(F), 60, replace=False):
+        a, b, c = X[F[f]]
+        n = np.cross(b - a, c - a)
+        for t in rng.choice(len(T), 8, replace=False):
+            ok, _ = _walk_case(X, T, f, t, F)
+            if np.dot(n, X[T[t]].mean(0) - (a + b + c) / 3) > 0:
+                outward += 1
+                assert not ok, (f, t)
+    assert outward > 0
+
+
+def test_walk_stops_at_the_boundary_of_a_nonconvex_mesh(oracle_lib):
+    """An L-shaped block: the ray from one arm to the other crosses the notch (outside the
+    mesh), so the walk reaches the boundary; within one arm it arrives."""
+    from gaia_gb300 import scenes
+    from oracle import oracle as orc
+
+    X, T = scenes.lattice_cube((6, 6, 3), 0.1)
+    cen = X[T].mean(1)
+    T = T[~((cen[:, 0] > 0.2) & (cen[:, 1] > 0.2))]
+    cen = X[T].mean(1)
+    F, _ = orc.tet_surface(X, T)
+    fc = X[F].mean(1)
+    # start: a face on the top of arm B (y = 0.2, x > 0.35); targets in arm A (x < 0.2, y > 0.4)
+    starts = np.where((np.abs(fc[:, 1] - 0.2) < 1e-9) & (fc[:, 0] > 0.35))[0]
+    far = np.where((cen[:, 0] < 0.15) & (cen[:, 1] > 0.4))[0]
+    near = np.where((cen[:, 0] > 0.3) & (cen[:, 1] < 0.1))[0]
+    assert len(starts) and len(far) and len(near)
+    for f in starts[:4]:
+        for t in far[:6]:
+            ok, bound = _walk_case(X, T, f, t, F, max_mult=-1)
+            assert not ok and not bound, (f, t)
+        for t in near[:6]:
+            ok, bound = _walk_case(X, T, f, t, F)
+            assert ok, (f, t)
+
+
+def test_walk_pass_through_limit(oracle_lib):
+    """maxSearchDistanceMultiplier: a walk that crosses an exit face farther than
+    max_dis from the origin (checked every fifth tet) gives up."""
+    from gaia_gb300 import scenes
+    from oracle import oracle as orc
+
+    X, T = scenes.lattice_cube((7, 7, 7), 0.1, jitter=0.005, seed=2)
+    F, _ = orc.tet_surface(X, T)
+    fc, cen = X[F].mean(1), X[T].mean(1)
+    f = int(np.argmin(np.linalg.norm(fc - np.array([0.3, 0.3, 0.0]), axis=1)))  # bottom face, middle
+    t = int(np.argmin(np.linalg.norm(cen - np.array([0.3, 0.3, 0.55]), axis=1)))  # near the top
+    assert _walk_case(X, T, f, t, F, max_mult=1.8)[0]
+    assert not _walk_case(X, T, f, t, F, max_mult=0.3)[0]
+
+
+def _deep_state_rows(tmp_path, collision):
+    """Contact rows of the oracle for the 3 cm stacked cubes with the upper cube's bottom
+    layers pushed into the lower one (every point-in-tet test live)."""
+    from gaia_gb300 import scenes
+    from oracle import oracle as orc
+    from oracle import scene_io
+
+    mp, pp = scenes.stack_drop(str(tmp_path), spacing=0.03, gap=0.01, speed=1.0)
+    P = json.load(open(pp))
+    P["CollisionParams"] = collision
+    json.dump(P, open(pp, "w"))
+    o = orc.OracleScene(scene_io.load_scene(mp, pp), 64, 0)
+    X0, X1 = o.positions(0), o.positions(1)
+    deep = np.float32(np.array([0.0, -0.05, 0.0]))
+    rng = np.random.default_rng(5)
+    X1d = (X1 + deep + rng.normal(0, 0.002, X1.shape)).astype(np.float32).astype(np.float64)
+    o.set_prev_positions(0, X0)
+    o.set_prev_positions(1, X1d)
+    o.set_positions(1, X1d)
+    o.collide()
+    return o.contacts()
+
+
+def test_traversal_accepts_the_nearest_face_of_convex_meshes(tmp_path, oracle_lib):
+    """For convex bodies the straight path from the nearest feasible face to an inner point
+    stays inside, so the check changes nothing; a pass-through limit far below the path
+    length rejects faces, which changes the rows."""
+    on = _deep_state_rows(tmp_path / "a", {})
+    off = _deep_state_rows(tmp_path / "b", {"checkTetTraverse": False})
+    short = _deep_state_rows(tmp_path / "c", {"maxSearchDistanceMultiplier": 0.05})
+    assert len(on) > 20 and (on[:, 7] == 2).sum() > 10
+    np.testing.assert_array_equal(on, off)
+    assert not np.array_equal(on, short)
