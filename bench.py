@@ -314,7 +314,8 @@ CLOTH_METRIC = "cloth VBD vertex-solves/s & steps/s (StVK + bending + VF/EE cont
 def cloth_scene(args, d: str, precision: str):
     from gaia_gb300 import scenes
 
-    return scenes.cloth_on_sphere(d, n=args.size, iterations=args.iterations, precision=precision)
+    extra = {"lanesPerVertex": args.lanes} if args.lanes else {}
+    return scenes.cloth_on_sphere(d, n=args.size, iterations=args.iterations, precision=precision, **extra)
 
 
 def cloth_algorithmic_bytes(c) -> tuple[float, dict]:
@@ -388,7 +389,8 @@ def run_cloth(args, world, rank, local):
     nv = c.numVertices(0)
     for _ in range(args.warmup):
         c.runStep(1)
-    c.autotune()  # lanes per vertex re-timed on a state with the drape's contacts
+    if not args.lanes:
+        c.autotune()  # lanes per vertex re-timed on a state with the drape's contacts
     c.runStep(1)
     c.synchronize()
     clk = ClockSampler(local)

@@ -464,7 +464,7 @@ __device__ void accumulate(const Args<R>& a, const Consts<R>& c, int v, R* f, R*
 // VBDStepWithExistingCollisions (VBDClothPhysics.cpp:1026-1154) with the conservative
 // bound truncation (applyConservativeBoundTruncation, :1223-1246). Writes x_next.
 template <int L, typename R>
-__global__ void __launch_bounds__(128) k_solve(Args<R> a, Consts<R> c, const int* verts, int n) {
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 1) k_solve(Args<R> a, Consts<R> c, const int* verts, int n) {
     using V = typename Vec<R>::T;
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = gid / L, lane = gid % L;
