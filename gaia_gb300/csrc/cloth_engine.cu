@@ -175,11 +175,13 @@ __device__ __forceinline__ void add_outer(R* H, R s, R nx, R ny, R nz) {
 // One vertex-face contact seen from vertex order `order` (3 = the vertex side, 0..2 =
 // a face vertex): accumulateVFContactForceAndHessian (VBDClothPhysics.cpp:1248-1321) with
 // the closest point recomputed from the current positions (updateVFContactPointInfo).
+// The face's vertex ids and positions come in already loaded (the face-side loop loads them
+// once per face).
 template <typename R>
-__device__ void vf_term(const Args<R>& a, const Consts<R>& c, int u, int face, int order, R* f, R* H) {
+__device__ void vf_term_at(const Args<R>& a, const Consts<R>& c, int u, int4 fv, typename Vec<R>::T A,
+                           typename Vec<R>::T B, typename Vec<R>::T C, int order, R* f, R* H) {
     using V = typename Vec<R>::T;
-    const int4 fv = a.faces[face];
-    const V xu = ld(a.x, u), A = ld(a.x, fv.x), B = ld(a.x, fv.y), C = ld(a.x, fv.z);
+    const V xu = ld(a.x, u);
     V bary, cp;
     closest_point_triangle<V, R>(xu, A, B, C, bary, cp);
     const V diff = sub(xu, cp);
@@ -207,13 +209,21 @@ __device__ void vf_term(const Args<R>& a, const Consts<R>& c, int u, int face, i
     friction<R>(mu, lambda, t0, t1, dot(e0, dx), dot(e1, dx), epsU, b, f, H);
 }
 
-// One edge-edge contact of edge e (this vertex has order 0/1 on it) with edge e2:
-// accumulateEEContactForceAndHessian (VBDClothPhysics.cpp:1323-1399).
 template <typename R>
-__device__ void ee_term(const Args<R>& a, const Consts<R>& c, int e, int e2, int order, R* f, R* H) {
+__device__ __forceinline__ void vf_term(const Args<R>& a, const Consts<R>& c, int u, int face, int order, R* f, R* H) {
+    const int4 fv = a.faces[face];
+    vf_term_at(a, c, u, fv, ld(a.x, fv.x), ld(a.x, fv.y), ld(a.x, fv.z), order, f, H);
+}
+
+// One edge-edge contact of edge e (this vertex has order 0/1 on it) with edge e2:
+// accumulateEEContactForceAndHessian (VBDClothPhysics.cpp:1323-1399). Edge e's vertex ids
+// and positions come in already loaded (the edge loop loads them once per edge).
+template <typename R>
+__device__ void ee_term_at(const Args<R>& a, const Consts<R>& c, int4 E, typename Vec<R>::T p1,
+                           typename Vec<R>::T p2, int e2, int order, R* f, R* H) {
     using V = typename Vec<R>::T;
-    const int4 E = a.edges[e], F = a.edges[e2];
-    const V p1 = ld(a.x, E.x), p2 = ld(a.x, E.y), q1 = ld(a.x, F.x), q2 = ld(a.x, F.y);
+    const int4 F = a.edges[e2];
+    const V q1 = ld(a.x, F.x), q2 = ld(a.x, F.y);
     V c1, c2;
     R s, t;
     closest_points_segments(p1, p2, q1, q2, c1, c2, s, t);
@@ -366,33 +376,38 @@ __device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, co
         else if (k < nF + nB) bending(a, c, mat, x, xp, a.vbList[ba + k - nF], f, H);
         else vf_term(a, c, v, a.cd.vfFace[size_t(v) * VF_CAP + (k - nF - nB)], 3, f, H);
     }
-    {   // face side: items (incident face i, link j) in face order
-        int i = 0, base = 0;
-        int cnt = nF > 0 ? min(a.cd.fvCount[a.vfList[fa].x], FV_CAP) : 0;
-        for (int t = lane;; t += L) {
-            while (i < nF && t >= base + cnt) {
-                base += cnt;
-                ++i;
-                cnt = i < nF ? min(a.cd.fvCount[a.vfList[fa + i].x], FV_CAP) : 0;
-            }
-            if (i >= nF) break;
+    // Face side: items (incident face i, link j) in face order; edges: items (incident edge
+    // i, contact j) in edge order. Lane `lane` takes the items whose flattened index is
+    // lane, lane + L, ...: per face (edge) the links j = j0, j0 + L, ... with
+    // (base + j0) % L == lane, base the items of the faces (edges) before it. The face's
+    // (edge's) own ids and positions are loaded once for all its items.
+    {
+        int base = 0;
+        for (int i = 0; i < nF; ++i) {
             const int2 fo = a.vfList[fa + i];
-            vf_term(a, c, a.cd.fvVert[size_t(fo.x) * FV_CAP + (t - base)], fo.x, fo.y, f, H);
+            const int cnt = min(a.cd.fvCount[fo.x], FV_CAP);
+            int j = (lane - base % L + L) % L;
+            base += cnt;
+            if (j >= cnt) continue;
+            const int4 fv = a.faces[fo.x];
+            const typename Vec<R>::T A = ld(a.x, fv.x), B = ld(a.x, fv.y), C = ld(a.x, fv.z);
+            for (; j < cnt; j += L)
+                vf_term_at(a, c, a.cd.fvVert[size_t(fo.x) * FV_CAP + j], fv, A, B, C, fo.y, f, H);
         }
     }
-    {   // edges: items (incident edge i, contact j) in edge order
+    {
         const int ea = a.veOfs[v], nE = a.veOfs[v + 1] - ea;
-        int i = 0, base = 0;
-        int cnt = nE > 0 ? min(a.cd.eeCount[a.veList[ea].x], EE_CAP) : 0;
-        for (int t = lane;; t += L) {
-            while (i < nE && t >= base + cnt) {
-                base += cnt;
-                ++i;
-                cnt = i < nE ? min(a.cd.eeCount[a.veList[ea + i].x], EE_CAP) : 0;
-            }
-            if (i >= nE) break;
+        int base = 0;
+        for (int i = 0; i < nE; ++i) {
             const int2 eo = a.veList[ea + i];
-            ee_term(a, c, eo.x, a.cd.eeOther[size_t(eo.x) * EE_CAP + (t - base)], eo.y, f, H);
+            const int cnt = min(a.cd.eeCount[eo.x], EE_CAP);
+            int j = (lane - base % L + L) % L;
+            base += cnt;
+            if (j >= cnt) continue;
+            const int4 E = a.edges[eo.x];
+            const typename Vec<R>::T p1 = ld(a.x, E.x), p2 = ld(a.x, E.y);
+            for (; j < cnt; j += L)
+                ee_term_at(a, c, E, p1, p2, a.cd.eeOther[size_t(eo.x) * EE_CAP + j], eo.y, f, H);
         }
     }
 }
