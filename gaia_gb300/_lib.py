@@ -35,6 +35,8 @@ class Stats(C.Structure):
         ("num_incidences", C.c_int64), ("kernel_launches_per_step", C.c_int64),
         ("fp64_fallback_solves", C.c_int64), ("failed_solves", C.c_int64), ("device_bytes", C.c_int64),
         ("autotune_ms_per_iteration", C.c_double), ("solve_variant", C.c_int32), ("reserved", C.c_int32),
+        ("contact_detections", C.c_int64), ("contact_stack_overflow", C.c_int64),
+        ("contact_traverse_bounds", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

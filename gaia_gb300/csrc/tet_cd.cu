@@ -490,7 +490,7 @@ __device__ __noinline__ bool traverse_ok(const Dev& D, const float4* P, const Tr
     int32_t stack[kDynamicStack];
     int r = c.use_static ? walk(w, ft.x, ft.y, false, stack) : -1;
     if (r < 0) r = walk(w, ft.x, ft.y, true, stack);  // the static stack overflowed
-    if (r < 0) atomicAdd(&D.counters[cloth::CC_TRUNCATIONS], 1ull);
+    if (r < 0) atomicAdd(&D.counters[cloth::CC_TRUNCATIONS], 1ull);  // the walk gave up on a bound
     return r == 1;
 }
 
@@ -652,6 +652,7 @@ __global__ void k_ccd(Dev D, bvh::LbvhDev fb, const float4* xf, float off) {
 // Own contacts and relation keys (face vertex slot, surface vertex, order).
 __global__ void k_own(Dev D, uint8_t* info, int4* own, unsigned long long* keys) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) atomicAdd(&D.counters[cloth::CC_DETECTIONS], 1ull);  // one per detection pass
     if (i >= D.nsv) return;
     const int g = D.hit[i];
     if (g < 0) {

@@ -1048,6 +1048,11 @@ public:
         s->device_bytes = int64_t(bytes_);
         s->autotune_ms_per_iteration = tuned_ms_;
         s->solve_variant = variant_;
+        unsigned long long cc[cloth::CC_N];
+        cd_.counters(cc, st_);
+        s->contact_detections = int64_t(cc[cloth::CC_DETECTIONS]);
+        s->contact_stack_overflow = int64_t(cc[cloth::CC_STACK_OVERFLOW]);
+        s->contact_traverse_bounds = int64_t(cc[cloth::CC_TRUNCATIONS]);
     }
 
 private:

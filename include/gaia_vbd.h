@@ -55,6 +55,10 @@ typedef struct {
     double autotune_ms_per_iteration; /* best measured sweep time per iteration (0 if not tuned) */
     int32_t solve_variant;        /* 0 = register-pipelined solve kernel, 1 = TMA-staged records */
     int32_t reserved;
+    /* tet-mesh contact detection (cumulative; 0 when contact is off) */
+    int64_t contact_detections;       /* detection passes run */
+    int64_t contact_stack_overflow;   /* hierarchy traversals that dropped a node (stack full) */
+    int64_t contact_traverse_bounds;  /* DCD tetrahedral walks that gave up on a size bound */
 } gaia_vbd_stats;
 
 /* ---- life cycle ------------------------------------------------------------

@@ -92,6 +92,9 @@ def test_contact_sets_bit_exact(spacing, traversal, tmp_path, gaia_lib, oracle_l
         np.testing.assert_array_equal(rg, ro)
         total += n
     assert total > 20
+    st = phys.stats()
+    assert st["contact_detections"] >= 3
+    assert st["contact_stack_overflow"] == 0 and st["contact_traverse_bounds"] == 0
     phys.close()
 
 
