@@ -140,7 +140,9 @@ def make_scene(workload: str, d: str, precision: str, size: int, iterations: int
     if workload == "twist":
         return scenes.twist_cube(d, n=size, iterations=iterations, precision=precision)
     if workload == "drop":
-        return scenes.drop_cube(d, n=size, iterations=iterations, precision=precision)
+        # the plain VBD drop: no contact detection, the reference's greedy coloring
+        return scenes.drop_cube(d, n=size, iterations=iterations, precision=precision, coloring="greedy",
+                                collision=scenes.NO_CONTACT)
     if workload == "batch":
         return scenes.batch_cubes(d, n_scenes=512, iterations=iterations, precision=precision)
     if workload == "collide":
@@ -206,6 +208,9 @@ def workload_name(args) -> str:
     if args.workload == "collide":
         return (f"collision_drop_32 (16 lattice cubes of 8..20 vertices per side, 16 tet balls r 0.05..0.15 m, "
                 f"1 m box, tet-surface CCD + DCD every substep), {args.iterations} iterations/step, dt=1/300")
+    if args.workload == "drop":
+        return (f"drop_cube_{args.size}^3 (ground plane, no contact detection, greedy coloring), "
+                f"{args.iterations} iterations/step, dt=1/300")
     return f"{args.workload}_cube_{args.size}^3, {args.iterations} iterations/step, dt=1/300"
 
 

@@ -164,16 +164,20 @@ def _write_json(dirname: str, models: list[dict], params: dict, deformers: list[
 
 
 def drop_cube(dirname: str, n: int = 10, precision: str = "mixed", iterations: int = 20, seed: int = 1,
-              spacing: float = 0.01, height: float = 0.2) -> tuple[str, str]:
+              spacing: float = 0.01, height: float = 0.2, coloring: str = "tool",
+              collision: dict | None = None) -> tuple[str, str]:
     """Plain VBD drop: an n^3 vertex lattice cube (spacing 1 cm, jitter 1e-4, seed 1),
     Neo-Hookean E=1e6, nu=0.4, rho=1000, bottom at `height` above a ground plane at
-    y=0 (stiffness 1e5, friction 0.2), dt=1/300, `iterations` per step."""
+    y=0 (stiffness 1e5, friction 0.2), dt=1/300, `iterations` per step. `coloring` as in
+    _write_mesh; `collision` = CollisionParams (None: the reference's defaults, tet-mesh
+    contact detection on)."""
     half = 0.5 * spacing * (n - 1)
     X, T = lattice_cube((n, n, n), spacing, (-half, height, -half), jitter=1e-4, seed=seed)
-    tp, cp = _write_mesh(dirname, f"cube{n}", X, T)
+    tp, cp = _write_mesh(dirname, f"cube{n}", X, T, coloring=coloring)
     models = [model_entry(tp, cp)]
     params = physics_params(1.0 / 300.0, iterations, ground_y=0.0, precision=precision)
-    return _write_json(dirname, models, params, meta={"workload": f"drop_cube_{n}", "seed": seed})
+    return _write_json(dirname, models, params, meta={"workload": f"drop_cube_{n}", "seed": seed},
+                       collision=collision)
 
 
 def stack_drop(dirname: str, n_lower: int = 6, n_upper: int = 5, spacing: float = 0.01, gap: float = 0.004,
