@@ -43,6 +43,20 @@ class Stats(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class OutputParams(C.Structure):
+    _fields_ = [
+        ("num_frames", C.c_int32), ("save_outputs", C.c_int32), ("save_all_models_together", C.c_int32),
+        ("binary_mode_visualization_steps", C.c_int32), ("output_recovery_state", C.c_int32),
+        ("output_recovery_state_step", C.c_int32), ("output_recovery_state_binary", C.c_int32),
+        ("reserved", C.c_int32), ("output_ext", C.c_char * 16),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+        d["output_ext"] = self.output_ext.decode()
+        return d
+
+
 class ClothStats(C.Structure):
     _fields_ = [
         ("precision", C.c_int32), ("num_groups", C.c_int32), ("num_vertices", C.c_int64),
@@ -97,6 +111,8 @@ _SIGNATURES = {
     "gaia_vbd_energy": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "gaia_vbd_vertex_force_hessian": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "gaia_vbd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "gaia_vbd_get_output_params": (C.c_int, [C.c_void_p, C.POINTER(OutputParams)]),
+    "gaia_vbd_frame": (C.c_int64, [C.c_void_p]),
     "gaia_vbd_get_color_config": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                             C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
     "gaia_vbd_energy_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,

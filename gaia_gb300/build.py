@@ -80,8 +80,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     cli_src = os.path.join(CSRC, "vbd_dynamics.cpp")
-    cli_deps = [cli_src, LIB, os.path.join(INCLUDE, "gaia_vbd.h")] + [os.path.join(CSRC, h) for h in
-                                                                      ("json_lite.hpp", "json_get.hpp")]
+    cli_deps = [cli_src, LIB, os.path.join(INCLUDE, "gaia_vbd.h"), os.path.join(INCLUDE, "gaia_vbd.hpp")]
     if force or _stale(CLI, cli_deps):
         cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-o", CLI, cli_src, "-I", INCLUDE, "-L", HERE,
                "-lgaia_vbd", "-Wl,-rpath,$ORIGIN"]

@@ -541,6 +541,14 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         get(*pp, "numThreadsVBDSolve", p.numThreadsVBDSolve);
         get(*pp, "useDouble3x3", p.useDouble3x3);
         get(*pp, "evaluateConvergence", p.evaluateConvergence);
+        get(*pp, "numFrames", p.numFrames);
+        get(*pp, "saveOutputs", p.saveOutputs);
+        get(*pp, "saveAllModelsTogether", p.saveAllModelsTogether);
+        get(*pp, "outputExt", p.outputExt);
+        get(*pp, "binaryModeVisualizationSteps", p.binaryModeVisualizationSteps);
+        get(*pp, "outputRecoveryState", p.outputRecoveryState);
+        get(*pp, "outputRecoveryStateStep", p.outputRecoveryStateStep);
+        get(*pp, "outputRecoveryStateBinary", p.outputRecoveryStateBinary);
         get(*pp, "gpuPrecision", p.gpuPrecision);
         get(*pp, "lanesPerVertex", p.lanesPerVertex);
         get(*pp, "blockSize", p.blockSize);

@@ -54,6 +54,15 @@ struct PhysicsParams {
     int numThreadsVBDSolve = 16;
     bool useDouble3x3 = false;
     bool evaluateConvergence = false;
+    // output of the frame loop (Parameters/PhysicsParameters.h:30, 87-99)
+    int numFrames = 5000;
+    bool saveOutputs = true;
+    bool saveAllModelsTogether = true;
+    std::string outputExt = "ply";
+    int binaryModeVisualizationSteps = 100;
+    bool outputRecoveryState = true;
+    int outputRecoveryStateStep = 10;
+    bool outputRecoveryStateBinary = true;
     // derived (BasePhysicsFramework.cpp:245-249)
     double dt = -1.0, dtSqrReciprocal = -1.0;
     // GB300 engine keys (extensions; absent in reference files -> defaults)

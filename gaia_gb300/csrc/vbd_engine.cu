@@ -1491,6 +1491,24 @@ int gaia_vbd_get_stats(gaia_vbd* h, gaia_vbd_stats* out) {
     return guarded(h, [&] { h->eng->stats(out); });
 }
 
+int gaia_vbd_get_output_params(const gaia_vbd* h, gaia_vbd_output_params* out) {
+    if (!h) return GAIA_VBD_E_INVALID_ARG;
+    if (!out) return GAIA_VBD_E_INVALID_ARG;
+    std::memset(out, 0, sizeof(*out));
+    const gaia::PhysicsParams& p = h->scene.p;
+    out->num_frames = p.numFrames;
+    out->save_outputs = p.saveOutputs;
+    out->save_all_models_together = p.saveAllModelsTogether;
+    out->binary_mode_visualization_steps = p.binaryModeVisualizationSteps;
+    out->output_recovery_state = p.outputRecoveryState;
+    out->output_recovery_state_step = p.outputRecoveryStateStep;
+    out->output_recovery_state_binary = p.outputRecoveryStateBinary;
+    std::snprintf(out->output_ext, sizeof(out->output_ext), "%s", p.outputExt.c_str());
+    return GAIA_VBD_OK;
+}
+
+int64_t gaia_vbd_frame(const gaia_vbd* h) { return h ? h->frame : -1; }
+
 int32_t gaia_vbd_color_mcs(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors) {
     if (nv <= 0 || ntet < 0 || (!tets && ntet) || !colors) return -1;
     int32_t n = -1;

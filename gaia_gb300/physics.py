@@ -13,7 +13,7 @@ import os
 
 import numpy as np
 
-from ._lib import GaiaError, Stats, lib
+from ._lib import GaiaError, OutputParams, Stats, lib
 
 
 def _check(rc: int, handle=None) -> None:
@@ -242,6 +242,14 @@ class VBDPhysics:
                    self.handle)
             out.append({"lanes": L.value, "block": B.value, "variant": V.value, "ms": ms.value})
         return out
+
+    def outputParams(self) -> dict:
+        """The frame loop's output settings from Parameters.json (host data)."""
+        if not self._h:
+            raise RuntimeError("call loadRunningparameters first")
+        o = OutputParams()
+        _check(lib().gaia_vbd_get_output_params(self._h, C.byref(o)), self._h)
+        return o.as_dict()
 
     def stats(self) -> dict:
         s = Stats()

@@ -177,6 +177,24 @@ int gaia_vbd_energy(gaia_vbd* h, double* out);
 int gaia_vbd_vertex_force_hessian(gaia_vbd* h, int32_t mesh, int32_t vertex, int32_t apply_friction,
                                   double* f3, double* h9);
 int gaia_vbd_get_stats(gaia_vbd* h, gaia_vbd_stats* out);
+
+/* Output settings of the frame loop as Parameters.json gives them (PhysicsParams keys,
+ * defaults of Parameters/PhysicsParameters.h:30, 87-99), read by simulate / writeOutputs
+ * (Framework/BasePhysicsFramework.cpp:284-393, 442-506); frame = runStep calls since
+ * initialize, or the frameId of the last loaded recovery state. Host data (no GPU). */
+typedef struct {
+    int32_t num_frames;                        /* numFrames */
+    int32_t save_outputs;                      /* saveOutputs */
+    int32_t save_all_models_together;          /* saveAllModelsTogether */
+    int32_t binary_mode_visualization_steps;   /* binaryModeVisualizationSteps */
+    int32_t output_recovery_state;             /* outputRecoveryState */
+    int32_t output_recovery_state_step;        /* outputRecoveryStateStep */
+    int32_t output_recovery_state_binary;      /* outputRecoveryStateBinary */
+    int32_t reserved;
+    char output_ext[16];                       /* outputExt, NUL-terminated ("ply", "bin", ...) */
+} gaia_vbd_output_params;
+int gaia_vbd_get_output_params(const gaia_vbd* h, gaia_vbd_output_params* out);
+int64_t gaia_vbd_frame(const gaia_vbd* h);
 /* Launch configuration the autotuner chose for merged color g (parallel group g):
  * lanes per vertex, block size, kernel variant (0 registers, 1 TMA-staged), and the
  * measured time of one launch in ms (0 when not tuned). Any pointer may be NULL.

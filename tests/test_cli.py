@@ -38,12 +38,64 @@ def test_usage_and_options(gaia_lib, tmp_path):
 def test_unreadable_inputs_fail_before_device_work(gaia_lib, tmp_path):
     exe = _cli(gaia_lib)
     r = _run(exe, "m.json", str(tmp_path / "missing.json"), str(tmp_path / "out"))
-    assert r.returncode == 1 and "cannot read" in r.stderr
+    assert r.returncode == 1 and "loadRunningparameters" in r.stderr
     pp = tmp_path / "p.json"
     pp.write_text(json.dumps({"PhysicsParams": {"numFrames": 1}}))
     r = _run(exe, str(tmp_path / "missing_models.json"), str(pp), str(tmp_path / "out"))
-    assert r.returncode == 1 and "create failed" in r.stderr
+    assert r.returncode == 1 and "loadRunningparameters" in r.stderr
     assert not (tmp_path / "out").exists()
+    r = _run(exe, "m.json", "p.json", str(tmp_path / "out"), "-R")
+    assert r.returncode == 2 and "needs a value" in r.stderr
+
+
+FACADE_PROBE = r"""
+#include <cstdio>
+#include "gaia_vbd.hpp"
+int main(int argc, char** argv) {
+    gaia::VBDPhysics p;
+    try {
+        p.initialize();
+    } catch (const gaia::VBDError& e) {
+        std::printf("before load: %s\n", e.what());
+    }
+    p.loadRunningparameters(argv[1], argv[2], "${REPO_ROOT}/out", argv[3]);
+    const gaia_vbd_output_params o = p.outputParams();
+    std::printf("%d %d %d %s %d %d %d %d %d %s\n", p.numMeshes(), o.num_frames, o.save_outputs, o.output_ext,
+                o.binary_mode_visualization_steps, o.output_recovery_state, o.output_recovery_state_step,
+                o.output_recovery_state_binary, o.save_all_models_together, p.outputFolder.c_str());
+    return 0;
+}
+"""
+
+
+def test_cpp_facade_loads_and_reads_output_params(gaia_lib, tmp_path):
+    """The header-only gaia::VBDPhysics facade, host side: errors before loading, the
+    output settings of Parameters.json (reference defaults where absent), ${REPO_ROOT}."""
+    import shutil
+
+    from gaia_gb300 import build as gb
+    from gaia_gb300 import scenes
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "probe.cpp"
+    src.write_text(FACADE_PROBE)
+    exe = tmp_path / "probe"
+    inc = os.path.join(os.path.dirname(gb.HERE), "include")
+    r = subprocess.run([cxx, "-std=c++17", "-O1", str(src), "-o", str(exe), "-I", inc, "-L", gb.HERE, "-lgaia_vbd",
+                        "-Wl,-rpath," + gb.HERE], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    mp, pp = scenes.stack_drop(str(tmp_path / "s"), spacing=0.03)
+    P = json.load(open(pp))
+    P["PhysicsParams"].pop("saveOutputs", None)
+    P["PhysicsParams"].update(numFrames=7, outputExt="bin", outputRecoveryStateStep=3)
+    json.dump(P, open(pp, "w"))
+    r = subprocess.run([str(exe), mp, pp, str(tmp_path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    assert lines[0].startswith("before load: ") and "loadRunningparameters" in lines[0]
+    assert lines[1].split() == ["2", "7", "1", "bin", "100", "1", "3", "1", "1", str(tmp_path) + "/out"]
 
 
 def _scene(tmp_path, **params):
@@ -122,3 +174,14 @@ def test_binary_output_and_repo_root(gaia_lib, tmp_path):
     phys.loadRunningparameters(mp, pp)
     ns = sum(len(phys.surface(m)[1]) for m in range(2))
     assert os.path.getsize(o / "A00000004.bin") == 12 * ns
+
+
+def test_python_output_params(gaia_lib, tmp_path):
+    from gaia_gb300 import VBDPhysics, scenes
+
+    mp, pp = scenes.stack_drop(str(tmp_path), spacing=0.03)
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, pp)
+    o = phys.outputParams()
+    assert o["num_frames"] == 5000 and o["output_ext"] == "ply" and o["save_outputs"] == 0
+    assert o["output_recovery_state_step"] == 10 and o["binary_mode_visualization_steps"] == 100
