@@ -8,7 +8,6 @@ library; this class only marshals arguments and raises on error codes.
 from __future__ import annotations
 
 import ctypes as C
-import json
 import os
 
 import numpy as np
@@ -32,7 +31,6 @@ class VBDPhysics:
         self.params_json = None
         self.out_folder = None
         self.repo_root = None
-        self.frameId = 0
 
     # -- VBDPhysics::loadRunningparameters (VBDPhysics.cpp:90-97): host only, no GPU needed
     def loadRunningparameters(self, models_json: str, params_json: str, out_folder: str | None = None,
@@ -81,12 +79,54 @@ class VBDPhysics:
     def runStep(self, n: int = 1) -> None:
         _check(lib().gaia_vbd_run_step(self.handle, n), self.handle)
 
-    # -- BasePhysicFramework::simulate (BasePhysicsFramework.cpp:284-393), without file output
-    def simulate(self, num_frames: int) -> None:
-        for _ in range(num_frames):
+    @property
+    def frameId(self) -> int:
+        """runStep calls since initialize, or the frameId of the last recovered state."""
+        return int(lib().gaia_vbd_frame(self._h)) if self._h else 0
+
+    # -- BasePhysicFramework::writeOutputs (BasePhysicsFramework.cpp:442-506)
+    def writeOutputs(self, out_folder: str, frame: int) -> None:
+        o = self.outputParams()
+        base = os.path.join(out_folder, f"A{frame:08d}")
+        together = bool(o["save_all_models_together"])
+        ext = o["output_ext"]
+        if ext == "bin":
+            if frame == 0:
+                os.makedirs(os.path.join(out_folder, "TemplateMesh"), exist_ok=True)
+                self.writePLY(os.path.join(out_folder, "TemplateMesh", "TemplateMesh.ply"), False, True)
+            self.writeBinary(base + ".bin")
+            if frame % max(1, o["binary_mode_visualization_steps"]) == 0:
+                self.writePLY(base + ".ply", together, together)
+        elif ext == "ply":
+            self.writePLY(base + ".ply", together, together)
+        elif ext != "obj":
+            print(f"[Error] Unsupported output EXT name: {ext}")
+            return
+        if o["output_recovery_state"] and frame % max(1, o["output_recovery_state_step"]) == 0:
+            self.saveState(os.path.join(out_folder, "RecoveryStates", f"A{frame:08d}.json"),
+                           binary=bool(o["output_recovery_state_binary"]))
+
+    # -- BasePhysicFramework::simulate (BasePhysicsFramework.cpp:284-393): frame frameId, then
+    # runStep and the outputs of every frame up to numFrames (num_frames overrides it). Files
+    # go to the out_folder given to loadRunningparameters; without one nothing is written.
+    def simulate(self, num_frames: int | None = None, save_outputs: bool | None = None) -> int:
+        o = self.outputParams()
+        last = o["num_frames"] if num_frames is None else num_frames
+        save = bool(o["save_outputs"]) if save_outputs is None else save_outputs
+        out = self.out_folder
+        if out:
+            os.makedirs(out, exist_ok=True)
+            if o["output_recovery_state"]:
+                os.makedirs(os.path.join(out, "RecoveryStates"), exist_ok=True)
+            self.writeOutputs(out, self.frameId)
+        steps = 0
+        while self.frameId < last:
             self.runStep(1)
-            self.frameId += 1
+            steps += 1
+            if out and save:
+                self.writeOutputs(out, self.frameId)
         self.synchronize()
+        return steps
 
     def synchronize(self) -> None:
         _check(lib().gaia_vbd_synchronize(self.handle), self.handle)
@@ -99,7 +139,6 @@ class VBDPhysics:
     def reset(self) -> None:
         """Back to the initial state (rest positions, initial velocities, t = 0)."""
         _check(lib().gaia_vbd_reset(self.handle), self.handle)
-        self.frameId = 0
 
     # -- tet-mesh contact (VBDPhysics::dcd / ccd / prepareCollisionDataGPU)
     def surface(self, mesh: int = 0) -> tuple[np.ndarray, np.ndarray]:
@@ -140,8 +179,6 @@ class VBDPhysics:
 
     def recoverFromState(self, path: str) -> None:
         _check(lib().gaia_vbd_load_state(self.handle, path.encode()), self.handle)
-        with open(path) as f:
-            self.frameId = int(json.load(f).get("frameId", -1))
 
     # -- output frames (BasePhysicsFramework.cpp:442-489, IO/FileIO.cpp)
     def writePLY(self, path: str, saveAllModelsTogether: bool = False, addModelName: bool = False) -> None:

@@ -185,3 +185,23 @@ def test_python_output_params(gaia_lib, tmp_path):
     o = phys.outputParams()
     assert o["num_frames"] == 5000 and o["output_ext"] == "ply" and o["save_outputs"] == 0
     assert o["output_recovery_state_step"] == 10 and o["binary_mode_visualization_steps"] == 100
+
+
+@pytest.mark.gpu
+def test_python_simulate_writes_frames(gaia_lib, tmp_path):
+    from gaia_gb300 import VBDPhysics
+
+    mp, pp = _scene(tmp_path, numFrames=4, outputExt="ply", outputRecoveryStateStep=2,
+                    outputRecoveryStateBinary=False)
+    out = tmp_path / "pyout"
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, pp, str(out))
+    phys.initialize()
+    assert phys.simulate() == 4 and phys.frameId == 4
+    assert all((out / f"A{f:08d}.ply").exists() for f in range(5))
+    assert sorted(p.name for p in (out / "RecoveryStates").glob("*.json")) == [
+        "A00000000.json", "A00000002.json", "A00000004.json"]
+    frame, X = _state_positions(out / "RecoveryStates" / "A00000004.json")
+    assert frame == 4
+    assert np.abs(X[1] - phys.positions(1)).max() <= 6e-8
+    phys.close()
