@@ -202,11 +202,16 @@ __global__ void k_fv_sort(CDTopo t, CDOut o, const int* req) {
 // Edge-edge query of one simulated edge: triMeshEdgeContactQueryFunc
 // (ClothContactDetector.cpp:731-813) with the query sphere of contactQueryEE
 // (:1106-1135): centre at the edge midpoint, radius maxQueryDis + half the edge length.
+// Thread i takes the edge of leaf i of the edge hierarchy (Morton order of the last build),
+// so the queries of a warp are neighbours in space and walk much the same nodes; leaves of
+// collider edges have no query.
 __global__ void __launch_bounds__(128) k_ee_query(CDTopo t, bvh::LbvhDev eb, const float4* xf, float r, CDOut o,
                                                   const int* req) {
     if (*req == 0) return;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= t.nSimE) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= eb.n) return;
+    const int e = int(eb.keys[i] & 0xffffffffull);
+    if (e < 0 || e >= t.nSimE) return;
     const int4 E = t.edges[e];
     const int m1 = t.edgeInfo[e].z;
     const float3 p1 = ld3(xf, E.x), p2 = ld3(xf, E.y);
@@ -273,6 +278,7 @@ ContactDetector::~ContactDetector() {
         edgeBvh_->release();
         delete edgeBvh_;
     }
+
     for (void* p : {(void*)out_.vfFace, (void*)out_.vfCount, (void*)out_.vfMinDis, (void*)out_.fMinDisBits,
                     (void*)out_.fvVert, (void*)out_.fvCount, (void*)out_.eeOther, (void*)out_.eeCount,
                     (void*)out_.eeMinDis})
@@ -312,7 +318,7 @@ void ContactDetector::enqueue_detect(const float4* xf, float maxQueryDis, const 
     k_cd_reset<<<blocks(nr, 256), 256, 0, st>>>(t_, out_, maxQueryDis, d_req);
     if (t_.nV > 0) k_vf_query<<<blocks(t_.nV, 128), 128, 0, st>>>(t_, faceBvh_->dev(), xf, maxQueryDis, out_, d_req);
     if (t_.nSimF > 0) k_fv_sort<<<blocks(t_.nSimF, 128), 128, 0, st>>>(t_, out_, d_req);
-    if (t_.nSimE > 0) k_ee_query<<<blocks(t_.nSimE, 128), 128, 0, st>>>(t_, edgeBvh_->dev(), xf, maxQueryDis, out_, d_req);
+    if (t_.nSimE > 0) k_ee_query<<<blocks(t_.nE, 128), 128, 0, st>>>(t_, edgeBvh_->dev(), xf, maxQueryDis, out_, d_req);
     CD_CUDA(cudaGetLastError());
 }
 

@@ -723,8 +723,9 @@ public:
 
     void run_steps(int n) override {
         for (int i = 0; i < n; ++i) {
-            if (sc_.p.handleCollision && sc_.p.contactBVHReconstructionSteps > 0 &&
-                frame_ % sc_.p.contactBVHReconstructionSteps == 0)
+            if (sc_.p.handleCollision &&
+                (!bvh_built_ || (sc_.p.contactBVHReconstructionSteps > 0 &&
+                                 frame_ % sc_.p.contactBVHReconstructionSteps == 0)))
                 rebuild_bvh();
             for (int s = 0; s < sc_.p.numSubsteps; ++s) CL_CUDA(cudaGraphLaunch(graph_, st_));
             ++frame_;
@@ -1219,6 +1220,7 @@ private:
     void rebuild_bvh() {
         if (cdt_.nSimV > 0) kern::k_snapshot<R><<<nblk(cdt_.nSimV, 256), 256, 0, st_>>>(a_, cdt_.nSimV, nullptr);
         cd_.rebuild(xf_.p, st_);
+        bvh_built_ = true;
     }
 
     // snapshot -> refit + queries -> bounds, each gated on the device flag
@@ -1298,6 +1300,7 @@ private:
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
     cudaGraphExec_t graph_ = nullptr;
     int64_t frame_ = 0;
+    bool bvh_built_ = false;  // the contact hierarchies exist (built at least once)
     int launches_per_substep_ = 0;
     size_t bytes_ = 0;
     std::vector<int> vbase_, fbase_, ebase_, vmesh_, vlocal_, fmesh_, emesh_;
