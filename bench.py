@@ -666,6 +666,10 @@ def main():
             "gpu_launches": st["kernel_launches_per_step"] * args.steps,
             "fp64_fallback_solves": st["fp64_fallback_solves"], "failed_solves": st["failed_solves"],
         }
+        if st.get("contact_detections"):
+            # tet-mesh contact detection of the timed engine (cumulative over its life)
+            line["contact"] = {k: st[k] for k in ("contact_detections", "contact_stack_overflow",
+                                                   "contact_traverse_bounds")}
         print(json.dumps(line), flush=True)
 
 
