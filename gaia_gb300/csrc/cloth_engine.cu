@@ -364,18 +364,17 @@ __device__ __forceinline__ void bending(const Args<R>& a, const Consts<R>& c, co
 // Lane `lane` of an L-lane group's share of vertex v's incident terms: membrane (into Hm,
 // for the Rayleigh term), bending, vertex-side VF contacts, face-side VF contacts (the
 // vertices linked to each incident face, flattened over faces) and EE contacts (flattened
-// over the incident edges). Lane k takes items k, k + L, ...
+// over the incident edges). Within each kind, lane k takes items k, k + L, ...
 template <int L, typename R>
 __device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, const ClothMat<R>& mat, int v, int lane,
                                         typename Vec<R>::T x, typename Vec<R>::T xp, R* f, R* H, R* Hm) {
     const int fa = a.vfOfs[v], nF = a.vfOfs[v + 1] - fa;
     const int ba = a.vbOfs[v], nB = mat.kBend != R(0) ? a.vbOfs[v + 1] - ba : 0;
     const int nVF = min(a.cd.vfCount[v], VF_CAP);
-    for (int k = lane; k < nF + nB + nVF; k += L) {
-        if (k < nF) membrane(a, mat, a.vfList[fa + k], f, Hm);
-        else if (k < nF + nB) bending(a, c, mat, x, xp, a.vbList[ba + k - nF], f, H);
-        else vf_term(a, c, v, a.cd.vfFace[size_t(v) * VF_CAP + (k - nF - nB)], 3, f, H);
-    }
+    // one loop per kind of item, so that the lanes of a warp run the same code together
+    for (int k = lane; k < nF; k += L) membrane(a, mat, a.vfList[fa + k], f, Hm);
+    for (int k = lane; k < nB; k += L) bending(a, c, mat, x, xp, a.vbList[ba + k], f, H);
+    for (int k = lane; k < nVF; k += L) vf_term(a, c, v, a.cd.vfFace[size_t(v) * VF_CAP + k], 3, f, H);
     // Face side: items (incident face i, link j) in face order; edges: items (incident edge
     // i, contact j) in edge order. Lane `lane` takes the items whose flattened index is
     // lane, lane + L, ...: per face (edge) the links j = j0, j0 + L, ... with
