@@ -36,8 +36,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "VBD vertex-solves/s & steps/s, FP32-mixed vs plain FP64 at <=1e-5 rel pos err"
 # dram__bytes_read.sum + dram__bytes_write.sum per solved incidence of k_solve, measured by
-# ncu on colors 0-2 of the 60^3 twist (3 x ~1.01 M incidences; see profiles/)
-TRAFFIC_BYTES_PER_INCIDENCE = {"fp32": 54.8, "mixed": 59.9}
+# ncu: FP32 on 8 color launches of the 100^3 twist (4.8 M incidences each), double-float on
+# colors 0-2 of the 60^3 twist (3 x ~1.01 M incidences); see profiles/
+TRAFFIC_BYTES_PER_INCIDENCE = {"fp32": 54.4, "mixed": 59.9}
 
 
 def load_peaks() -> tuple[float, str]:
@@ -637,7 +638,8 @@ def main():
         per_inc = TRAFFIC_BYTES_PER_INCIDENCE.get(head["precision"])
         traffic = per_inc * ninc / st["num_groups"] if per_inc else None
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                    "traffic": traffic, "traffic_source": "60^3 ncu capture, scaled per incidence",
+                    "traffic": traffic, "traffic_source": "ncu DRAM bytes per incidence (FP32: 100^3 twist launches; double-float: "
+                                      "60^3 twist), times this launch's incidences",
                     "peak_kind": peak_kind, "kernel": "k_solve",
                     "algorithmic_bytes_per_launch": alg_bytes_iter / st["num_groups"],
                     "avg_launch_us": 1e3 * head["sweep_ms"] / launches_solve}
