@@ -633,13 +633,14 @@ def main():
         launches_solve = st["num_groups"] * args.iterations * args.steps
         alg_bytes_iter = 64.0 * nact + 61.0 * ninc
         achieved = alg_bytes_iter * args.iterations * args.steps / (head["sweep_ms"] / 1e3) / 1e9
-        # DRAM bytes per solved incidence (records + per-vertex data) from the ncu capture of the
-        # 60^3 twist (profiles/k_solve_twist60_*_full.md), scaled to one average launch here
+        # DRAM bytes per solved incidence (records + per-vertex data) from the ncu captures
+        # (TRAFFIC_BYTES_PER_INCIDENCE), scaled to one average launch here
         per_inc = TRAFFIC_BYTES_PER_INCIDENCE.get(head["precision"])
         traffic = per_inc * ninc / st["num_groups"] if per_inc else None
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                    "traffic": traffic, "traffic_source": "ncu DRAM bytes per incidence (FP32: 100^3 twist launches; double-float: "
-                                      "60^3 twist), times this launch's incidences",
+                    "traffic": traffic,
+                    "traffic_source": "ncu DRAM bytes per incidence (FP32: 100^3 twist launches; double-float: 60^3 "
+                                      "twist), times this launch's incidences",
                     "peak_kind": peak_kind, "kernel": "k_solve",
                     "algorithmic_bytes_per_launch": alg_bytes_iter / st["num_groups"],
                     "avg_launch_us": 1e3 * head["sweep_ms"] / launches_solve}
