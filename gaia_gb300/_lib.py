@@ -21,10 +21,12 @@ E_CUDA = 5
 E_NONFINITE = 6
 E_NO_DEVICE = 7
 E_UNSUPPORTED = 8
+E_DEVICE_TIMEOUT = 9
 
 STATUS_NAMES = {
     OK: "OK", E_INVALID_ARG: "INVALID_ARG", E_INPUT: "INPUT", E_COLORING: "COLORING", E_MESH: "MESH",
     E_CUDA: "CUDA", E_NONFINITE: "NONFINITE", E_NO_DEVICE: "NO_DEVICE", E_UNSUPPORTED: "UNSUPPORTED",
+    E_DEVICE_TIMEOUT: "DEVICE_TIMEOUT",
 }
 
 
@@ -36,7 +38,7 @@ class Stats(C.Structure):
         ("fp64_fallback_solves", C.c_int64), ("failed_solves", C.c_int64), ("device_bytes", C.c_int64),
         ("autotune_ms_per_iteration", C.c_double), ("solve_variant", C.c_int32), ("reserved", C.c_int32),
         ("contact_detections", C.c_int64), ("contact_stack_overflow", C.c_int64),
-        ("contact_traverse_bounds", C.c_int64),
+        ("contact_traverse_bounds", C.c_int64), ("device_timeouts", C.c_int64), ("nonfinite_solves", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

@@ -260,19 +260,19 @@ __device__ __forceinline__ bool solve_block(const R* H, const R* b, R* x, unsign
 template <>
 __device__ __forceinline__ bool solve_block<float>(const float* H, const float* b, float* x,
                                                    unsigned long long* counters) {
-    if (gaia::dev::ldlt3<float>(H, b, x, 1e-5f)) return true;
+    if (gaia::dev::ldlt3<float>(H, b, x, gaia::dev::kFp32Pivot)) return true;
     double Hd[6], bd[3], xd[3];
     for (int i = 0; i < 6; ++i) Hd[i] = H[i];
     for (int i = 0; i < 3; ++i) bd[i] = b[i];
     atomicAdd(&counters[CC_FP64_SOLVES], 1ull);
-    if (!gaia::dev::ldlt3<double>(Hd, bd, xd, 1e-12)) return false;
+    if (!gaia::dev::ldlt3<double>(Hd, bd, xd, gaia::dev::kRetryPivot)) return false;
     for (int i = 0; i < 3; ++i) x[i] = float(xd[i]);
     return true;
 }
 template <>
 __device__ __forceinline__ bool solve_block<double>(const double* H, const double* b, double* x,
                                                     unsigned long long*) {
-    return gaia::dev::ldlt3<double>(H, b, x, 1e-12);
+    return gaia::dev::ldlt3<double>(H, b, x, gaia::dev::kFp64Pivot);
 }
 
 // StVK membrane of one incident face: with F = [f0 f1] = Ds DmInv, G = (F^T F - I) / 2,

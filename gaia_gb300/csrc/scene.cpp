@@ -556,6 +556,7 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         get(*pp, "usePDL", p.usePDL);
         get(*pp, "smallColorVertices", p.smallColorVertices);
         get(*pp, "solveVariant", p.solveVariant);
+        get(*pp, "waitPollLimit", p.waitPollLimit);
     }
     if (const json::Value* cp = params.find("CollisionParams")) {
         get(*cp, "allowCCD", p.allowCCD);

@@ -14,6 +14,25 @@
 //   then the records: every hit becomes its vertex's own contact and a relation of each
 //   face vertex that has fewer than four, in (mesh, surface vertex) order.
 // Results of vertices a pass does not revisit are kept, as in the reference.
+//
+// The cubic root finder below (cubic_roots, find_closed, quadratic_roots) follows, branch
+// for branch, the one in Cem Yuksel's cyCodeBase (cyPolynomial.h, the method of "High-
+// Performance Polynomial Root Finding for Graphics", HPG 2022), specialised to float and
+// degree 3; the CCD result must equal the reference's bit for bit, so the structure is
+// kept. cyCodeBase is distributed under the MIT license:
+//   Copyright (c) 2022, Cem Yuksel <cem@cemyuksel.com>. All rights reserved.
+//   Permission is hereby granted, free of charge, to any person obtaining a copy of this
+//   software and associated documentation files (the "Software"), to deal in the Software
+//   without restriction, including without limitation the rights to use, copy, modify,
+//   merge, publish, distribute, sublicense, and/or sell copies of the Software, and to
+//   permit persons to whom the Software is furnished to do so, subject to the following
+//   conditions: The above copyright notice and this permission notice shall be included in
+//   all copies or substantial portions of the Software. THE SOFTWARE IS PROVIDED "AS IS",
+//   WITHOUT WARRANTY OF ANY KIND, EXPRESS OR IMPLIED, INCLUDING BUT NOT LIMITED TO THE
+//   WARRANTIES OF MERCHANTABILITY, FITNESS FOR A PARTICULAR PURPOSE AND NONINFRINGEMENT. IN
+//   NO EVENT SHALL THE AUTHORS OR COPYRIGHT HOLDERS BE LIABLE FOR ANY CLAIM, DAMAGES OR
+//   OTHER LIABILITY, WHETHER IN AN ACTION OF CONTRACT, TORT OR OTHERWISE, ARISING FROM, OUT
+//   OF OR IN CONNECTION WITH THE SOFTWARE OR THE USE OR OTHER DEALINGS IN THE SOFTWARE.
 #include "tet_cd.hpp"
 
 #include <cub/cub.cuh>

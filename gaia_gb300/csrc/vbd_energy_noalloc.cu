@@ -106,7 +106,10 @@ __global__ void __launch_bounds__(kThreads) k_energy_finish(const double* partia
     if (threadIdx.x == 0) *out = e;
 }
 
-// Device address of the scratch array on the current device, looked up once per device.
+// Device address of the scratch array on the current device, looked up once per device and
+// kept for the life of the process. A cudaDeviceReset of that device unloads the module and
+// makes the kept address stale, so the entry point must not be called on a device after it
+// was reset (the library would have to be loaded again).
 cudaError_t scratch_for_current_device(double** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

@@ -33,6 +33,11 @@ struct CudaError : std::runtime_error {
     using std::runtime_error::runtime_error;
 };
 
+// A bounded device-side wait ran out (GAIA_VBD_E_DEVICE_TIMEOUT).
+struct DeviceTimeout : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
 #define GAIA_CUDA(call)                                                                                  \
     do {                                                                                                 \
         cudaError_t e__ = (call);                                                                        \
@@ -311,6 +316,7 @@ public:
         c_.step_gd = R(p.stepSizeGD);
         c_.plane = p.usePlaneGround ? 1 : 0;
         c_.assoc_grav = p.associateGravityWithInertia ? 1 : 0;
+        c_.spin_limit = p.waitPollLimit >= 0 ? p.waitPollLimit : dev::kMbarSpinLimit;
     }
 
     void set_record(int32_t r, const int* nb, double mv[3][3]) {
@@ -832,7 +838,8 @@ public:
         GAIA_CUDA(cudaMemcpyAsync(d_y_.p, h_pos_.data(), nslots_ * sizeof(S4), cudaMemcpyHostToDevice, st_));
         GAIA_CUDA(cudaMemcpyAsync(d_xprev_.p, h_pos_.data(), nslots_ * sizeof(S4), cudaMemcpyHostToDevice, st_));
         GAIA_CUDA(cudaMemsetAsync(d_time_.p, 0, sizeof(double), st_));
-        GAIA_CUDA(cudaMemsetAsync(d_counters_.p + dev::CNT_NONFINITE, 0, sizeof(unsigned long long), st_));
+        // the status counters (non-finite solves, device timeouts) start again from zero
+        GAIA_CUDA(cudaMemsetAsync(d_counters_.p + dev::CNT_NONFINITE, 0, 3 * sizeof(unsigned long long), st_));
         cd_.reset(st_);
         GAIA_CUDA(cudaStreamSynchronize(st_));
     }
@@ -847,11 +854,27 @@ public:
     }
 
     // ---- state access -------------------------------------------------------------
+    // Status of the device work so far: a bounded wait that ran out, then non-finite solves.
+    // Each is reported once: the call that throws moves the device counts into the handle's
+    // totals (stats) and clears them, so the calls after it see the state as it was left.
     void check_nonfinite() {
         unsigned long long h[dev::CNT_N];
         GAIA_CUDA(cudaMemcpyAsync(h, d_counters_.p, sizeof(h), cudaMemcpyDeviceToHost, st_));
         GAIA_CUDA(cudaStreamSynchronize(st_));
-        if (h[dev::CNT_NONFINITE]) throw std::domain_error("a vertex solve produced a non-finite position");
+        if (!h[dev::CNT_TIMEOUT] && !h[dev::CNT_NONFINITE]) return;
+        reported_timeouts_ += int64_t(h[dev::CNT_TIMEOUT]);
+        reported_nonfinite_ += int64_t(h[dev::CNT_NONFINITE]);
+        GAIA_CUDA(cudaMemsetAsync(d_counters_.p + dev::CNT_NONFINITE, 0, 3 * sizeof(unsigned long long), st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        if (h[dev::CNT_TIMEOUT])
+            throw DeviceTimeout(std::to_string(h[dev::CNT_TIMEOUT]) +
+                                " solve block(s) gave up on a bounded device wait and skipped their vertices" +
+                                (h[dev::CNT_DRAIN] ? " (" + std::to_string(h[dev::CNT_DRAIN]) +
+                                                         " still had copies in flight)"
+                                                   : std::string()));
+        if (h[dev::CNT_NONFINITE])
+            throw std::domain_error(std::to_string(h[dev::CNT_NONFINITE]) +
+                                    " vertex solve(s) met a non-finite force or step (not written)");
     }
 
     void sync() override {
@@ -1053,6 +1076,8 @@ public:
         s->contact_detections = int64_t(cc[cloth::CC_DETECTIONS]);
         s->contact_stack_overflow = int64_t(cc[cloth::CC_STACK_OVERFLOW]);
         s->contact_traverse_bounds = int64_t(cc[cloth::CC_TRUNCATIONS]);
+        s->device_timeouts = reported_timeouts_ + int64_t(h[dev::CNT_TIMEOUT]);
+        s->nonfinite_solves = reported_nonfinite_ + int64_t(h[dev::CNT_NONFINITE]);
     }
 
 private:
@@ -1079,6 +1104,7 @@ private:
     static constexpr int kContactBlocks = 64;
     double tuned_ms_ = 0.0;
     int64_t launches_per_substep_ = 0, launches_per_step_ = 0;
+    int64_t reported_timeouts_ = 0, reported_nonfinite_ = 0;  // status counts already reported
     size_t bytes_ = 0;
     dev::Consts<R> c_{};
     std::vector<int64_t> mesh_off_;
@@ -1154,6 +1180,9 @@ int guarded(gaia_vbd* h, Fn&& fn) {
     } catch (const std::domain_error& e) {
         (h ? h->err : gaia::g_last_error) = e.what();
         return GAIA_VBD_E_NONFINITE;
+    } catch (const gaia::DeviceTimeout& e) {
+        (h ? h->err : gaia::g_last_error) = e.what();
+        return GAIA_VBD_E_DEVICE_TIMEOUT;
     } catch (const std::exception& e) {
         (h ? h->err : gaia::g_last_error) = e.what();
         std::string m = e.what();

@@ -70,6 +70,7 @@ struct Consts {
     double lo[3], hi[3];
     float dt_f, g_f[3], lo_f[3], hi_f[3];  // the same constants for FP32 state arithmetic
     int32_t plane, assoc_grav;
+    int32_t spin_limit;  // polls of a bounded wait before it gives up (kMbarSpinLimit unless a test lowers it)
 };
 
 // The FP64 or FP32 copy of a constant, matching the state scalar type.
@@ -86,8 +87,10 @@ __device__ __forceinline__ double pick<double>(double d, float) { return d; }
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
-// Counter slots in device memory.
-enum { CNT_FP64_SOLVES = 0, CNT_FAILED_SOLVES = 1, CNT_NONFINITE = 2, CNT_N = 4 };
+// Counter slots in device memory. CNT_TIMEOUT: blocks whose bounded wait on staged
+// records (or on a grid barrier) ran out and that skipped their vertices; CNT_DRAIN: of
+// those, blocks whose final drain wait ran out too.
+enum { CNT_FP64_SOLVES = 0, CNT_FAILED_SOLVES = 1, CNT_NONFINITE = 2, CNT_TIMEOUT = 3, CNT_DRAIN = 4, CNT_N = 8 };
 
 template <typename ST, typename R>
 struct Ptrs {
@@ -160,26 +163,35 @@ __device__ __forceinline__ bool ldlt3(const R* H, const R* b, R* x, R rel_tol) {
     return isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]);
 }
 
+// Relative pivot thresholds of the 3x3 LDL^T: an FP32 factorisation, the FP64 retry of an
+// FP32-accumulated block, and an FP64 block. The retry's entries carry the rounding of
+// their FP32 accumulation (a few 1e-7 of the largest diagonal after 10-30 incidences), so
+// a pivot below kRetryPivot of it is rounding noise, not information: such a block is
+// treated as singular (the gradient step) instead of being solved into a wild step.
+constexpr float kFp32Pivot = 1e-5f;
+constexpr double kRetryPivot = 2e-6;
+constexpr double kFp64Pivot = 1e-12;
+
 // FP32 solve with FP64 retry for ill-conditioned blocks; FP64 solve directly.
 template <typename R>
 __device__ __forceinline__ bool solve3(const R* H, const R* b, R* x, unsigned long long* counters);
 template <>
 __device__ __forceinline__ bool solve3<float>(const float* H, const float* b, float* x, unsigned long long* counters) {
-    if (ldlt3<float>(H, b, x, 1e-5f)) return true;
+    if (ldlt3<float>(H, b, x, kFp32Pivot)) return true;
     double Hd[6], bd[3], xd[3];
 #pragma unroll
     for (int i = 0; i < 6; ++i) Hd[i] = H[i];
 #pragma unroll
     for (int i = 0; i < 3; ++i) bd[i] = b[i];
     atomicAdd(&counters[CNT_FP64_SOLVES], 1ull);
-    if (!ldlt3<double>(Hd, bd, xd, 1e-12)) return false;
+    if (!ldlt3<double>(Hd, bd, xd, kRetryPivot)) return false;
 #pragma unroll
     for (int i = 0; i < 3; ++i) x[i] = float(xd[i]);
     return true;
 }
 template <>
 __device__ __forceinline__ bool solve3<double>(const double* H, const double* b, double* x, unsigned long long*) {
-    return ldlt3<double>(H, b, x, 1e-12);
+    return ldlt3<double>(H, b, x, kFp64Pivot);
 }
 
 // One incidence record as loaded from HBM (streaming loads: each record is
@@ -584,8 +596,14 @@ __device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R
         probe_out[9] = H[2]; probe_out[10] = H[4]; probe_out[11] = H[5];
         return;
     }
-    // CMP_EPSILON2 gate (Types/Types.h:20-21; VBDPhysics.cpp:2432)
-    if (!(f[0] * f[0] + f[1] * f[1] + f[2] * f[2] > R(1e-5f * 1e-5f))) return;
+    // CMP_EPSILON2 gate (Types/Types.h:20-21; VBDPhysics.cpp:2432); a non-finite force (a
+    // NaN or Inf position among the vertex's neighbours) is counted, as the reference's
+    // CPU path stops on a NaN descent direction (VBDPhysics.cpp:2460-2464)
+    const R fn2 = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
+    if (!(fn2 > R(1e-5f * 1e-5f))) {
+        if (!(fn2 <= R(1e-5f * 1e-5f))) atomicAdd(&P.counters[CNT_NONFINITE], 1ull);
+        return;
+    }
     R d3[3];
     R step = c.step;
     if (!solve3<R>(H, f, d3, P.counters)) {
@@ -613,25 +631,42 @@ __device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R
 // as in k_solve. max_rec bounds the records of any block of this launch (the
 // host sizes the dynamic shared memory from it).
 // ---------------------------------------------------------------------------
-enum { CNT_TIMEOUT = 3 };
 constexpr int kMbarSpinLimit = 1 << 20;
+// Polls of the final drain wait of a block whose first wait ran out, each after a 1 us
+// sleep: about two seconds in all, far beyond the time any issued copy takes to land.
+constexpr int kDrainPolls = 1 << 21;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-// Bounded wait on an mbarrier phase; false if the phase did not complete within the limit.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (int i = 0; i < kMbarSpinLimit; ++i) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(bar), "r"(parity)
-            : "memory");
-        if (done) return true;
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Bounded wait on an mbarrier phase: at most `limit` polls; false if the phase did not
+// complete within them.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit) {
+    for (int i = 0; i < limit; ++i)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+
+// The wait of a block that gave up: the phase completes when every byte its copies
+// declared (expect_tx = exactly the bytes issued) has landed, so this waits, bounded and
+// with sleeps, until no copy of the block is left writing into its shared memory.
+__device__ __forceinline__ bool mbar_drain(uint32_t bar, uint32_t parity) {
+    for (int i = 0; i < kDrainPolls; ++i) {
+        if (mbar_test(bar, parity)) return true;
+        __nanosleep(1000);
     }
     return false;
 }
@@ -690,7 +725,8 @@ __global__ void __launch_bounds__(256, 4)
     pdl_wait();
     U uo{};
     if (valid) uo = P.u[v];
-    const bool ok = mbar_wait(bar, 0);
+    // the block goes on only if every thread saw the records land within the limit
+    const bool ok = __syncthreads_and(mbar_wait(bar, 0, c.spin_limit)) != 0;
     Acc<float> acc = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (valid && ok) {
         for (int r = rb; r < re; r += L) {
@@ -705,14 +741,19 @@ __global__ void __launch_bounds__(256, 4)
             incidence<float>(e0, e1, e2, m0, m1, m2, mat.mu, mat.lmbd, acc);
         }
     }
-    if (!ok && threadIdx.x == 0) {
-        // the copies did not land within the limit: record it, give them one more bounded
-        // wait so no copy is left writing into this block's shared memory, and skip the update
-        atomicAdd(&P.counters[CNT_TIMEOUT], 1ull);
-        mbar_wait(bar, 0);
+    if (!ok) {
+        // the records did not land within the limit: the block skips its vertices (none
+        // moves) and records it, which the host reports as a device-timeout status; thread
+        // 0 then drains the copies so that none is left writing into this block's shared
+        // memory after it exits
+        if (threadIdx.x == 0) {
+            atomicAdd(&P.counters[CNT_TIMEOUT], 1ull);
+            if (!mbar_drain(bar, 0)) atomicAdd(&P.counters[CNT_DRAIN], 1ull);
+        }
+        return;
     }
     reduce_group<L, float>(acc);
-    if (!valid || lane != 0 || !ok) return;
+    if (!valid || lane != 0) return;
     vertex_tail<ST, float, false>(P, c, v, uo, mat, acc, friction, nullptr, beg, end);
 }
 

@@ -320,6 +320,45 @@ def collision_drop(dirname: str, n_objects: int = 32, precision: str = "mixed", 
                        meta={"workload": f"collision_drop_{n_objects}", "seed": seed, "vertices": nv})
 
 
+def contact_cluster(dirname: str, precision: str = "mixed", iterations: int = 30, seed: int = 11,
+                    spacing: float = 0.025, gap: float = 0.004, speed: float = 0.8,
+                    sizes=(4, 0.045, 3, 0.04)) -> tuple[str, str]:
+    """The collision-heavy drop at test size: two lattice cubes (`sizes` vertices per side)
+    and two tetrahedralised balls (`sizes` radii) stacked in a column with `gap` between
+    neighbours, seeded random orientations, the upper three moving down at `speed` m/s
+    onto the lowest cube, which rests on the floor of a 0.5 m world box. Same material and
+    contact settings as collision_drop (CCD and DCD, contact stiffness 1e5); cells of
+    2.5 cm keep |6V| of every tet above the 1e-5 below which the reference's discrete test
+    rejects a tet, so both kinds of contact occur."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    os.makedirs(dirname, exist_ok=True)
+    shapes = []
+    for k, (kind, size) in enumerate(zip(("cube", "ball", "cube", "ball"), sizes)):
+        if kind == "cube":
+            X, T = lattice_cube((size,) * 3, spacing, (0.0, 0.0, 0.0), jitter=1e-4, seed=seed + k)
+        else:
+            X, T = lattice_ball(size, spacing, jitter=1e-4 * spacing / 0.01, seed=seed + k)
+        X = X - X.mean(axis=0)
+        shapes.append((f"{kind}{k}", X, T))
+    models = []
+    y = 0.0
+    for k, (name, X, T) in enumerate(shapes):
+        tp, cp = _write_mesh(dirname, name, X, T)
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        angle = float(rng.uniform(0, np.pi)) if k else 0.0
+        R = float(np.linalg.norm(X, axis=1).max()) if k else float(-X[:, 1].min())
+        y += R if k else R + 1e-4
+        shift = rng.uniform(-0.3, 0.3, size=2) * spacing
+        models.append(model_entry(tp, cp, rotation=(axis * angle).tolist(),
+                                  translation=[0.25 + shift[0], y, 0.25 + shift[1]],
+                                  initialVelocity=[0.0, -speed if k else 0.0, 0.0]))
+        y += R + gap
+    params = physics_params(1.0 / 300.0, iterations, precision=precision,
+                            worldBounds=[[0.0, 0.0, 0.0], [0.5, 0.5, 0.5]], collisionStiffness=1e5)
+    return _write_json(dirname, models, params, meta={"workload": "contact_cluster_4", "seed": seed})
+
+
 def set_precision(params_json: str, precision: str, out_path: str | None = None, **overrides) -> str:
     """Copy of a Parameters.json with gpuPrecision (and other PhysicsParams) replaced."""
     with open(params_json) as f:

@@ -34,8 +34,13 @@ enum {
     GAIA_VBD_E_CUDA = 5,         /* a CUDA runtime call failed (message in last_error) */
     GAIA_VBD_E_NONFINITE = 6,    /* a solve produced NaN/Inf; positions are left as they were written */
     GAIA_VBD_E_NO_DEVICE = 7,    /* no CUDA device is visible */
-    GAIA_VBD_E_UNSUPPORTED = 8   /* input asks for a feature outside the VBD tet step */
+    GAIA_VBD_E_UNSUPPORTED = 8,  /* input asks for a feature outside the VBD tet step */
+    GAIA_VBD_E_DEVICE_TIMEOUT = 9 /* a bounded device-side wait ran out: the blocks that gave up
+                                     skipped their vertices (none of them moved) */
 };
+/* NONFINITE and DEVICE_TIMEOUT come from device work and are returned by the next
+ * synchronizing call (synchronize, get_positions, ...). Each is returned once: that call
+ * clears it, and gaia_vbd_get_stats keeps the running totals. */
 
 typedef struct gaia_vbd gaia_vbd;
 
@@ -59,6 +64,9 @@ typedef struct {
     int64_t contact_detections;       /* detection passes run */
     int64_t contact_stack_overflow;   /* hierarchy traversals that dropped a node (stack full) */
     int64_t contact_traverse_bounds;  /* DCD tetrahedral walks that gave up on a size bound */
+    int64_t device_timeouts;          /* blocks whose bounded wait (staged records, grid barrier) ran
+                                         out; the call that reports it returns GAIA_VBD_E_DEVICE_TIMEOUT */
+    int64_t nonfinite_solves;         /* vertex solves with a non-finite force or step (not written) */
 } gaia_vbd_stats;
 
 /* ---- life cycle ------------------------------------------------------------
@@ -219,7 +227,8 @@ int gaia_vbd_get_color_config(gaia_vbd* h, int32_t g, int32_t* lanes, int32_t* b
  * Limits: nv and ntet each at most 2^24; larger calls fail with GAIA_VBD_E_INVALID_ARG
  * and a message in gaia_vbd_last_global_error. The first call on a device looks up
  * the scratch array's device address for that device; make that first call before
- * any stream capture. The call is asynchronous on `stream`. All calls share the one
+ * any stream capture. The address is kept for the life of the process: do not call this
+ * on a device after a cudaDeviceReset of it. The call is asynchronous on `stream`. All calls share the one
  * scratch array: calls whose kernels overlap on the GPU (different streams or
  * threads) race and must be serialized by the caller. */
 int gaia_vbd_energy_noalloc(const double* x, const double* y, const double* mass, int32_t nv,

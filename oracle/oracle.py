@@ -18,6 +18,22 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(_HERE, "liboracle.so")
 
 
+def reference_root() -> str | None:
+    """Root of the reference project's source tree, for the checker builds and the tests
+    that read its files: the GAIA_REFERENCE_ROOT environment variable, else the REF_ROOT
+    default of this directory's Makefile recipe. None where that tree is absent (the tests
+    that need it skip)."""
+    root = os.environ.get("GAIA_REFERENCE_ROOT")
+    if not root:
+        try:
+            r = subprocess.run(["make", "-s", "-C", _HERE, "print-ref-root"], capture_output=True, text=True,
+                               timeout=60)
+            root = r.stdout.strip() if r.returncode == 0 else None
+        except Exception:
+            root = None
+    return root if root and os.path.isdir(os.path.join(root, "Simulator")) else None
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (g++, no GPU needed)."""
     srcs = [os.path.join(_HERE, f) for f in ("vbd_oracle.cpp", "vbd_oracle.h", "cloth_oracle.cpp", "cloth_oracle.h",
@@ -103,6 +119,8 @@ def lib():
         L.oracle_energy.argtypes = [C.c_void_p]
         L.oracle_energy.restype = C.c_double
         L.oracle_solve_failures.argtypes = [C.c_void_p]
+        L.oracle_nh_element.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
+                                        C.c_int32, C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_void_p]
         L.oracle_set_prev_positions.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
         L.oracle_collide.argtypes = [C.c_void_p]
         L.oracle_collide.restype = C.c_int32
@@ -177,6 +195,20 @@ def ccd_tri_point(x0, x1, p0, p1):
     b = np.zeros(3, np.float32)
     hit = lib().oracle_ccd_tri_point(*[v.ctypes.data_as(fp) for v in a], tt.ctypes.data_as(fp), b.ctypes.data_as(fp))
     return int(hit), float(tt[0]), b
+
+
+def nh_element(x, xprev, dminv, mu: float, lmbd: float, A: float, order: int, kh: float = 0.0, kd: float = 0.0,
+               dt: float = 1.0 / 300.0):
+    """One tet's Neo-Hookean force (3) and 3x3 Hessian on its vertex `order` (FP64; x and
+    xprev are the tet's 4 vertex positions, dminv 9 values column-major)."""
+    x = np.ascontiguousarray(x, np.float64).reshape(-1)
+    xp = np.ascontiguousarray(xprev, np.float64).reshape(-1)
+    dm = np.ascontiguousarray(dminv, np.float64).reshape(-1)
+    f = np.zeros(3, np.float64)
+    h = np.zeros(9, np.float64)
+    lib().oracle_nh_element(x.ctypes.data, xp.ctypes.data, dm.ctypes.data, mu, lmbd, A, int(order), kh, kd, dt,
+                            f.ctypes.data, h.ctypes.data)
+    return f, h.reshape(3, 3)
 
 
 def color_mcs(nv: int, tets: np.ndarray) -> np.ndarray:

@@ -3,6 +3,12 @@
 // Paths are relative to the reference project's Simulator/Modules directory unless
 // they start with Simulator/. Compiled with -ffp-contract=off: every FP32 operation
 // of the CCD test rounds on its own, as in the reference's SSE build.
+//
+// The cubic root finder of the CCD test restates the one in Cem Yuksel's cyCodeBase
+// (cyPolynomial.h; "High-Performance Polynomial Root Finding for Graphics", HPG 2022),
+// which is MIT-licensed: Copyright (c) 2022, Cem Yuksel <cem@cemyuksel.com>; the
+// permission notice and warranty disclaimer are reproduced in the header of the GPU
+// detector, gaia_gb300/csrc/tet_cd.cu.
 #include "tet_contact.h"
 
 #include <algorithm>

@@ -144,7 +144,9 @@ bool solve3x3_ldlt(const R* H, const R* b, R* x, R rel_tol) {
 }
 
 // The solve policy of the mixed-precision path: FP32 attempt, FP64 retry
-// when the FP32 pivots are too small, failure only when FP64 fails too.
+// when the FP32 pivots are too small, failure only when FP64 fails too. The retry
+// solves an FP32-accumulated block, whose pivots below 2e-6 of the largest diagonal
+// are rounding noise: it treats them as singular (the same thresholds as the GPU).
 template <typename R>
 bool solve3x3(const R* H, const R* b, R* x, int* fp64_used);
 template <>
@@ -158,7 +160,7 @@ bool solve3x3<float>(const float* H, const float* b, float* x, int* fp64_used) {
     for (int i = 0; i < 9; ++i) Hd[i] = H[i];
     for (int i = 0; i < 3; ++i) bd[i] = b[i];
     if (fp64_used) ++*fp64_used;
-    if (!solve3x3_ldlt<double>(Hd, bd, xd, 1e-12)) return false;
+    if (!solve3x3_ldlt<double>(Hd, bd, xd, 2e-6)) return false;
     for (int i = 0; i < 3; ++i) x[i] = float(xd[i]);
     return true;
 }
@@ -277,99 +279,107 @@ void build_adjacency(Mesh<R>& m) {
         }
 }
 
-// Neo-Hookean per-vertex force and Hessian, restating
+// Neo-Hookean force and Hessian of one tet on one of its vertices, restating
 // VBD_NeoHookean.cpp:379-581 (accumlateMaterialForceAndHessian2): the 9x9
 // d2E/dF2 = A*lambda*(g g^T + (detF - a) * d2det/dF2) contracted with the
 // vertex's row of dF/dx, mu*A*|m|^2 added on the 3x3 diagonal, and the
 // Rayleigh-like damping Hessian (k_h * H_lambda + k_d * mu*A*|m|^2 I)/dt.
+// xt: the tet's 4 vertex positions (3 each); disp = x_v - x_prev,v of the vertex;
+// force (3) and H (9, row-major) are accumulated.
+template <typename R>
+void tet_force_hessian(const R* xt, const R* Dinv, R A, int ord, R miu, R lmbd, R kh, R kd, R dt, const R* disp,
+                       R* force, R* H) {
+    const R a = R(1) + miu / lmbd;
+    R Ds[9];
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) Ds[3 * c + r] = xt[3 * (c + 1) + r] - xt[r];
+    R F[9];  // column-major F = Ds * DmInv
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) {
+            R s = 0;
+            for (int q = 0; q < 3; ++q) s += Ds[3 * q + r] * Dinv[3 * c + q];
+            F[3 * c + r] = s;
+        }
+    auto f = [&](int r, int c) { return F[3 * c + r]; };
+    // d(det F)/dF, column-major (VBD_NeoHookean.cpp:424-433)
+    R g[9];
+    g[0] = f(1, 1) * f(2, 2) - f(1, 2) * f(2, 1);
+    g[1] = f(0, 2) * f(2, 1) - f(0, 1) * f(2, 2);
+    g[2] = f(0, 1) * f(1, 2) - f(0, 2) * f(1, 1);
+    g[3] = f(1, 2) * f(2, 0) - f(1, 0) * f(2, 2);
+    g[4] = f(0, 0) * f(2, 2) - f(0, 2) * f(2, 0);
+    g[5] = f(0, 2) * f(1, 0) - f(0, 0) * f(1, 2);
+    g[6] = f(1, 0) * f(2, 1) - f(1, 1) * f(2, 0);
+    g[7] = f(0, 1) * f(2, 0) - f(0, 0) * f(2, 1);
+    g[8] = f(0, 0) * f(1, 1) - f(0, 1) * f(1, 0);
+    R detF = f(0, 0) * g[0] + f(1, 0) * g[1] + f(2, 0) * g[2];
+    R kk = detF - a;
+    // d2E/dF2 without the mu term (VBD_NeoHookean.cpp:436-494), times A.
+    // The second derivative of det F: d2J/dF_pj dF_ql = sum_rs eps_pqr eps_jls F_rs,
+    // which has a single non-zero term (r = 3-p-q, s = 3-j-l) when p != q and j != l.
+    auto eps = [](int a, int b, int c) { return (a - b) * (b - c) * (c - a) / 2; };
+    R d2[9][9];
+    for (int j = 0; j < 3; ++j)
+        for (int p = 0; p < 3; ++p)
+            for (int l = 0; l < 3; ++l)
+                for (int q = 0; q < 3; ++q) {
+                    int I = p + 3 * j, J = q + 3 * l;
+                    R hd = 0;
+                    if (p != q && j != l) {
+                        int r = 3 - p - q, s = 3 - j - l;
+                        hd = R(eps(p, q, r) * eps(j, l, s)) * f(r, s);
+                    }
+                    d2[I][J] = (g[I] * g[J] + kk * hd) * lmbd * A;
+                }
+    R dEdF[9];
+    for (int i = 0; i < 9; ++i) dEdF[i] = A * (miu * F[i] + lmbd * kk * g[i]);
+    // rows of dF/dx: VBD_NeoHookean.cpp:526-553
+    R mv[3];
+    if (ord == 0) {
+        for (int c = 0; c < 3; ++c) mv[c] = -Dinv[3 * c + 0] - Dinv[3 * c + 1] - Dinv[3 * c + 2];
+    } else {
+        for (int c = 0; c < 3; ++c) mv[c] = Dinv[3 * c + (ord - 1)];
+    }
+    R dEdx[3], Hl[9];
+    for (int i = 0; i < 3; ++i) {
+        R s = 0;
+        for (int j = 0; j < 3; ++j) s += dEdF[i + 3 * j] * mv[j];
+        dEdx[i] = s;
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int q = 0; q < 3; ++q) {
+            R s = 0;
+            for (int j = 0; j < 3; ++j)
+                for (int l = 0; l < 3; ++l) s += mv[j] * mv[l] * d2[i + 3 * j][q + 3 * l];
+            Hl[3 * i + q] = s;
+        }
+    R dampH[9];
+    for (int i = 0; i < 9; ++i) dampH[i] = Hl[i] * kh;
+    R tmp = (mv[0] * mv[0] + mv[1] * mv[1] + mv[2] * mv[2]) * miu * A;
+    Hl[0] += tmp; Hl[4] += tmp; Hl[8] += tmp;
+    tmp *= kd;
+    dampH[0] += tmp; dampH[4] += tmp; dampH[8] += tmp;
+    for (int i = 0; i < 9; ++i) dampH[i] /= dt;
+    for (int i = 0; i < 3; ++i) {
+        R df = dampH[3 * i + 0] * disp[0] + dampH[3 * i + 1] * disp[1] + dampH[3 * i + 2] * disp[2];
+        force[i] -= dEdx[i] + df;
+    }
+    for (int i = 0; i < 9; ++i) H[i] += Hl[i] + dampH[i];
+}
+
+// Neo-Hookean per-vertex force and Hessian: the incident tets in ascending id.
 template <typename R>
 void material_force_hessian(const Mesh<R>& m, int iv, R dt, R* force, R* H) {
-    const R miu = m.miu, lmbd = m.lmbd;
-    const R a = R(1) + miu / lmbd;
     R disp[3];
     for (int d = 0; d < 3; ++d) disp[d] = m.x[3 * size_t(iv) + d] - m.xprev[3 * size_t(iv) + d];
     for (int k = m.nbr_ofs[iv]; k < m.nbr_ofs[iv + 1]; ++k) {
         int t = m.nbr_tet[k];
-        int ord = m.nbr_order[k];
         const int32_t* tv = &m.tets[4 * size_t(t)];
-        const R* Dinv = &m.dminv[9 * size_t(t)];
-        const R A = m.vol[t];
-        R Ds[9];
-        for (int c = 0; c < 3; ++c)
-            for (int r = 0; r < 3; ++r)
-                Ds[3 * c + r] = m.x[3 * size_t(tv[c + 1]) + r] - m.x[3 * size_t(tv[0]) + r];
-        R F[9];  // column-major F = Ds * DmInv
-        for (int c = 0; c < 3; ++c)
-            for (int r = 0; r < 3; ++r) {
-                R s = 0;
-                for (int q = 0; q < 3; ++q) s += Ds[3 * q + r] * Dinv[3 * c + q];
-                F[3 * c + r] = s;
-            }
-        auto f = [&](int r, int c) { return F[3 * c + r]; };
-        // d(det F)/dF, column-major (VBD_NeoHookean.cpp:424-433)
-        R g[9];
-        g[0] = f(1, 1) * f(2, 2) - f(1, 2) * f(2, 1);
-        g[1] = f(0, 2) * f(2, 1) - f(0, 1) * f(2, 2);
-        g[2] = f(0, 1) * f(1, 2) - f(0, 2) * f(1, 1);
-        g[3] = f(1, 2) * f(2, 0) - f(1, 0) * f(2, 2);
-        g[4] = f(0, 0) * f(2, 2) - f(0, 2) * f(2, 0);
-        g[5] = f(0, 2) * f(1, 0) - f(0, 0) * f(1, 2);
-        g[6] = f(1, 0) * f(2, 1) - f(1, 1) * f(2, 0);
-        g[7] = f(0, 1) * f(2, 0) - f(0, 0) * f(2, 1);
-        g[8] = f(0, 0) * f(1, 1) - f(0, 1) * f(1, 0);
-        R detF = f(0, 0) * g[0] + f(1, 0) * g[1] + f(2, 0) * g[2];
-        R kk = detF - a;
-        // d2E/dF2 without the mu term (VBD_NeoHookean.cpp:436-494), times A.
-        // The second derivative of det F: d2J/dF_pj dF_ql = sum_rs eps_pqr eps_jls F_rs,
-        // which has a single non-zero term (r = 3-p-q, s = 3-j-l) when p != q and j != l.
-        auto eps = [](int a, int b, int c) { return (a - b) * (b - c) * (c - a) / 2; };
-        R d2[9][9];
-        for (int j = 0; j < 3; ++j)
-            for (int p = 0; p < 3; ++p)
-                for (int l = 0; l < 3; ++l)
-                    for (int q = 0; q < 3; ++q) {
-                        int I = p + 3 * j, J = q + 3 * l;
-                        R hd = 0;
-                        if (p != q && j != l) {
-                            int r = 3 - p - q, s = 3 - j - l;
-                            hd = R(eps(p, q, r) * eps(j, l, s)) * f(r, s);
-                        }
-                        d2[I][J] = (g[I] * g[J] + kk * hd) * lmbd * A;
-                    }
-        R dEdF[9];
-        for (int i = 0; i < 9; ++i) dEdF[i] = A * (miu * F[i] + lmbd * kk * g[i]);
-        // rows of dF/dx: VBD_NeoHookean.cpp:526-553
-        R mv[3];
-        if (ord == 0) {
-            for (int c = 0; c < 3; ++c) mv[c] = -Dinv[3 * c + 0] - Dinv[3 * c + 1] - Dinv[3 * c + 2];
-        } else {
-            for (int c = 0; c < 3; ++c) mv[c] = Dinv[3 * c + (ord - 1)];
-        }
-        R dEdx[3], Hl[9];
-        for (int i = 0; i < 3; ++i) {
-            R s = 0;
-            for (int j = 0; j < 3; ++j) s += dEdF[i + 3 * j] * mv[j];
-            dEdx[i] = s;
-        }
-        for (int i = 0; i < 3; ++i)
-            for (int q = 0; q < 3; ++q) {
-                R s = 0;
-                for (int j = 0; j < 3; ++j)
-                    for (int l = 0; l < 3; ++l) s += mv[j] * mv[l] * d2[i + 3 * j][q + 3 * l];
-                Hl[3 * i + q] = s;
-            }
-        R dampH[9];
-        for (int i = 0; i < 9; ++i) dampH[i] = Hl[i] * m.kh;
-        R tmp = (mv[0] * mv[0] + mv[1] * mv[1] + mv[2] * mv[2]) * miu * A;
-        Hl[0] += tmp; Hl[4] += tmp; Hl[8] += tmp;
-        tmp *= m.kd;
-        dampH[0] += tmp; dampH[4] += tmp; dampH[8] += tmp;
-        for (int i = 0; i < 9; ++i) dampH[i] /= dt;
-        for (int i = 0; i < 3; ++i) {
-            R df = dampH[3 * i + 0] * disp[0] + dampH[3 * i + 1] * disp[1] + dampH[3 * i + 2] * disp[2];
-            force[i] -= dEdx[i] + df;
-        }
-        for (int i = 0; i < 9; ++i) H[i] += Hl[i] + dampH[i];
+        R xt[12];
+        for (int j = 0; j < 4; ++j)
+            for (int r = 0; r < 3; ++r) xt[3 * j + r] = m.x[3 * size_t(tv[j]) + r];
+        tet_force_hessian<R>(xt, &m.dminv[9 * size_t(t)], m.vol[t], m.nbr_order[k], m.miu, m.lmbd, m.kh, m.kd, dt,
+                             disp, force, H);
     }
 }
 
@@ -1150,6 +1160,15 @@ int32_t oracle_color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int32
             if (deg[nb] != -1) deg[nb]--;
     }
     return maxColor + 1;
+}
+
+// One tet's Neo-Hookean force (3) and Hessian (9, row-major) on its vertex `order`, in FP64
+// (the per-tet term of the vertex block; accumulated into f and h).
+void oracle_nh_element(const double* x12, const double* xprev12, const double* dminv9, double mu, double lmbd,
+                       double A, int32_t order, double kh, double kd, double dt, double* f, double* h) {
+    double disp[3];
+    for (int d = 0; d < 3; ++d) disp[d] = x12[3 * order + d] - xprev12[3 * order + d];
+    tet_force_hessian<double>(x12, dminv9, A, order, mu, lmbd, kh, kd, dt, disp, f, h);
 }
 
 void* oracle_create(int32_t precision, int32_t nmesh, const OracleMesh* meshes, const OracleParams* params,

@@ -108,6 +108,10 @@ void oracle_vertex_force_hessian(void* h, int32_t mesh, int32_t v, int32_t apply
 /* Total elastic (Neo-Hookean, rest energy removed) + inertia energy, in double. */
 double oracle_energy(void* h);
 int32_t oracle_solve_failures(void* h);
+/* One tet's Neo-Hookean force (3) and Hessian (9, row-major) on its vertex `order` in
+ * FP64, the per-tet term of oracle_vertex_force_hessian; accumulated into f and h. */
+void oracle_nh_element(const double* x12, const double* xprev12, const double* dminv9, double mu, double lmbd,
+                       double A, int32_t order, double kh, double kd, double dt, double* f, double* h);
 
 /* Tet-mesh contact. oracle_collide runs the substep-start detection on the current
  * positions (trajectories from the previous positions) and builds the contact

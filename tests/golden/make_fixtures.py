@@ -58,4 +58,13 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/Data/mesh_models")
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    else:
+        sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+        from oracle.oracle import reference_root
+
+        root = reference_root()
+        if not root:
+            sys.exit("the reference tree is not present (set GAIA_REFERENCE_ROOT or pass the mesh_models folder)")
+        main(os.path.join(root, "Data", "mesh_models"))

@@ -10,7 +10,17 @@ import numpy as np
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_MODELS = "/root/reference/Data/mesh_models"
+
+
+def _ref_path(*parts):
+    """A path in the reference's source tree, or a path that does not exist without it."""
+    from oracle.oracle import reference_root
+
+    root = reference_root()
+    return os.path.join(root, *parts) if root else os.path.join(HERE, "no-reference-tree", *parts)
+
+
+REF_MODELS = _ref_path("Data", "mesh_models")
 
 
 def _fixtures():
@@ -100,7 +110,7 @@ def test_coloring_file_roundtrip(tmp_path, gaia_lib):
     assert json.load(open(p)) == [[0, 4], [1, 5], [2], [3]]
 
 
-REF_GC = "/root/reference/Simulator/Modules/GraphColoring/mcs.cpp"
+REF_GC = _ref_path("Simulator", "Modules", "GraphColoring", "mcs.cpp")
 
 
 def _vertex_graph(nv, tets):

@@ -185,3 +185,63 @@ def test_collision_off_matches_oracle(tmp_path, gaia_lib, oracle_lib):
     x, xo = phys.positions(1), o.positions(1)
     assert np.abs(x - xo).max() <= 1e-9
     phys.close()
+
+
+@pytest.fixture(scope="module")
+def cluster(tmp_path_factory, gaia_lib, oracle_lib):
+    """The collision-heavy drop at test size (two cubes and two balls colliding in a
+    column, CCD and DCD every substep), with the FP64 oracle's trajectory and its contact
+    rows after every step."""
+    from gaia_gb300 import scenes
+    from oracle import scene_io
+
+    d = tmp_path_factory.mktemp("cluster")
+    mp, pp = scenes.contact_cluster(str(d), precision="fp64", iterations=20)
+    o = oracle_lib.OracleScene(scene_io.load_scene(mp, pp), 64, 0)
+    nm = len(json.load(open(mp))["Models"])
+    x0 = np.concatenate([o.positions(m) for m in range(nm)])
+    rows, xs = [], []
+    for _ in range(20):
+        o.step(1)
+        rows.append(o.contacts())
+        xs.append(np.concatenate([o.positions(m) for m in range(nm)]))
+    return mp, pp, nm, x0, rows, xs
+
+
+def test_cluster_contact_rows_every_step_fp64(cluster):
+    """FP64 engine: the contact rows of every substep's detection equal the oracle's, and the
+    positions stay within 1e-8."""
+    mp, pp, nm, x0, rows, xs = cluster
+    phys, _ = _pair(mp, pp)
+    kinds, total = set(), 0
+    for k in range(20):
+        phys.runStep(1)
+        rg = phys.contacts()
+        np.testing.assert_array_equal(rg, rows[k], err_msg=f"step {k}")
+        total += len(rg)
+        kinds |= set(rg[:, 7].tolist()) if len(rg) else set()
+        x = np.concatenate([phys.positions(m) for m in range(nm)])
+        rel = np.linalg.norm(x - xs[k]) / max(np.linalg.norm(xs[k] - x0), 1e-30)
+        assert rel <= 1e-8, (k, rel)
+    st = phys.stats()
+    print(f"contact rows over 20 steps: {total}, kinds {sorted(kinds)}")
+    assert total > 50 and {1, 2} <= kinds
+    assert st["contact_stack_overflow"] == 0 and st["contact_traverse_bounds"] == 0
+    phys.close()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp32"])
+def test_cluster_trajectory_fp32_compute(cluster, precision):
+    """FP32-compute engines on the colliding cluster after 20 steps against the FP64 oracle."""
+    from gaia_gb300 import VBDPhysics, scenes
+
+    mp, pp, nm, x0, rows, xs = cluster
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, scenes.set_precision(pp, precision))
+    phys.initialize()
+    phys.runStep(20)
+    x = np.concatenate([phys.positions(m) for m in range(nm)])
+    rel = float(np.linalg.norm(x - xs[-1]) / np.linalg.norm(xs[-1] - x0))
+    print(f"cluster {precision}: rel err {rel:.3e}")
+    assert rel <= (1e-5 if precision == "mixed" else 1e-4), rel
+    phys.close()

@@ -1,0 +1,176 @@
+"""Failure detection and the solve's fallback paths on the GPU, in safe forms only.
+
+- a bounded device wait that runs out: the TMA-staged solve's wait on its staged records
+  is given a limit of zero polls (the test-only PhysicsParams key waitPollLimit), so every
+  block gives up after its copies were issued; each block drains its copies before it
+  exits, skips its vertices, and the next synchronizing call returns
+  GAIA_VBD_E_DEVICE_TIMEOUT (once). No vertex was moved by the solve: the positions equal
+  those of a run with no iterations at all. Nothing hangs or faults: the drain completes
+  because every issued byte lands.
+- a non-finite position injected on the host (set_positions with a NaN) makes the
+  neighbours' forces non-finite; the solve counts them and writes nothing, and the next
+  synchronizing call returns GAIA_VBD_E_NONFINITE (the reference's CPU path stops on a NaN
+  descent direction, VBD/VBDPhysics.cpp:2460-2464).
+- an ill-conditioned 3x3 block (one free vertex of a single tet, nu = 0.4999995, almost no
+  mass; LDL^T pivots 5.9e-6 and 4.4e-6 of the largest diagonal): the FP32 factorisation
+  rejects a pivot (below 1e-5) and the FP64 retry solves it (above its 2e-6 noise floor):
+  fp64_fallback_solves > 0, no failed solve, compared with the FP64 oracle.
+- a singular block (mu = 0, almost no mass: rank one): every precision fails the solve
+  and takes the reference's gradient step along the force with stepSizeGD
+  (VBD/VBDPhysics.cpp:2452-2458), as the oracle does; in the FP32-compute modes the FP64
+  retry sees only FP32 rounding noise in the soft pivots and rejects it too.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from gaia_gb300._lib import E_DEVICE_TIMEOUT, E_NONFINITE, GaiaError
+
+pytestmark = pytest.mark.gpu
+
+
+def _handle(mp, pp):
+    from gaia_gb300 import VBDPhysics
+
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, pp)
+    phys.initialize()
+    return phys
+
+
+@pytest.fixture(scope="module")
+def drop6(tmp_path_factory, gaia_lib):
+    from gaia_gb300 import scenes
+
+    d = tmp_path_factory.mktemp("drop6")
+    return scenes.drop_cube(str(d), n=6, iterations=10, height=0.02, collision=scenes.NO_CONTACT)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_staged_wait_timeout_is_reported(drop6, precision):
+    from gaia_gb300 import scenes
+
+    mp, pp = drop6
+    common = dict(lanesPerVertex=4, blockSize=128, autotune=False, smallColorVertices=0, solveVariant=1)
+    phys = _handle(mp, scenes.set_precision(pp, precision, waitPollLimit=0, **common))
+    ref = _handle(mp, scenes.set_precision(pp, precision, out_path=pp + ".noiter.json", iterations=0, **common))
+    ok = _handle(mp, scenes.set_precision(pp, precision, out_path=pp + ".ok.json", **common))
+    # a deformed start, so that the solve has something to move
+    rng = np.random.default_rng(4)
+    x0 = phys.positions(0)
+    x0 = x0 + rng.uniform(-2e-4, 2e-4, size=x0.shape)
+    for h in (phys, ref, ok):
+        h.setPositions(0, x0)
+    phys.runStep(1)
+    with pytest.raises(GaiaError) as ei:
+        phys.synchronize()
+    assert ei.value.code == E_DEVICE_TIMEOUT, str(ei.value)
+    st = phys.stats()
+    assert st["device_timeouts"] > 0 and st["solve_variant"] == 1
+    # reported once: the state is readable afterwards, and no vertex was moved by a solve
+    phys.synchronize()
+    ref.runStep(1)
+    x, xr = phys.positions(0), ref.positions(0)
+    np.testing.assert_array_equal(x, xr)
+    assert np.isfinite(x).all()
+    # with the built-in limit the same step moves them
+    ok.runStep(1)
+    ok.synchronize()
+    assert ok.stats()["device_timeouts"] == 0
+    assert np.abs(ok.positions(0) - xr).max() > 0
+    for h in (phys, ref, ok):
+        h.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32"])
+def test_nonfinite_position_is_reported(drop6, precision):
+    from gaia_gb300 import scenes
+
+    mp, pp = drop6
+    phys = _handle(mp, scenes.set_precision(pp, precision))
+    x = phys.positions(0)
+    bad = 100  # an interior vertex of the 6^3 lattice
+    x[bad] = np.nan
+    phys.setPositions(0, x)
+    phys.runStep(1)
+    with pytest.raises(GaiaError) as ei:
+        phys.synchronize()
+    assert ei.value.code == E_NONFINITE, str(ei.value)
+    assert phys.stats()["nonfinite_solves"] > 0
+    xs = phys.positions(0)  # reported once; the finite vertices stayed finite
+    assert np.isnan(xs[bad]).all()
+    others = np.delete(xs, bad, axis=0)
+    assert np.isfinite(others).all()
+    phys.close()
+
+
+def _single_cell(d, miu=None, lmbd=None, nu=0.4, density=1000.0, iterations=10):
+    """One 2x2x2 lattice cell (5 tets); every vertex but vertex 0 fixed. Vertex 0 (a corner
+    of the cell) lies in one tet, so its 3x3 block is lambda A g g^T + (mu A |m|^2 +
+    m / dt^2) I: a rank-one stiff part and an isotropic soft part. No gravity."""
+    from gaia_gb300 import scenes
+
+    os.makedirs(d, exist_ok=True)
+    X, T = scenes.lattice_cube((2, 2, 2), 0.01, (0.0, 0.0, 0.0), jitter=1e-4, seed=3)
+    tp, cp = scenes._write_mesh(d, "cell", X, T, coloring="greedy")
+    m = scenes.model_entry(tp, cp, E=1e6, nu=nu, density=density, fixedPoints=list(range(1, 8)))
+    if miu is not None:
+        m["miu"] = miu
+    if lmbd is not None:
+        m["lmbd"] = lmbd
+    params = scenes.physics_params(1.0 / 300.0, iterations, gravity=(0.0, 0.0, 0.0), precision="fp64")
+    return scenes._write_json(d, [m], params, collision=scenes.NO_CONTACT)
+
+
+def _displaced_pair(mp, pp, precision, oracle_lib):
+    from gaia_gb300 import scenes
+    from oracle import scene_io
+
+    phys = _handle(mp, scenes.set_precision(pp, precision))
+    o = oracle_lib.OracleScene(scene_io.load_scene(mp, pp), precision=64, nthreads=1)
+    x = o.positions(0)
+    x[0] += np.array([1.0e-3, -2.0e-3, 0.5e-3])
+    x = x.astype(np.float32).astype(np.float64)
+    phys.setPositions(0, x)
+    o.set_positions(0, x)
+    return phys, o, x
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32"])
+def test_fp64_retry_of_ill_conditioned_block(tmp_path, precision, oracle_lib, gaia_lib):
+    mp, pp = _single_cell(str(tmp_path), nu=0.4999995, density=1e-3)
+    phys, o, x0 = _displaced_pair(mp, pp, precision, oracle_lib)
+    phys.runStep(3)
+    o.step(3)
+    x, xo = phys.positions(0), o.positions(0)
+    st = phys.stats()
+    rel = float(np.linalg.norm(x - xo) / np.linalg.norm(xo - x0))
+    print(f"{precision}: rel {rel:.3e} fp64 retries {st['fp64_fallback_solves']} failed {st['failed_solves']}")
+    assert st["failed_solves"] == 0 and o.solve_failures() == 0
+    if precision == "fp64":
+        assert rel <= 1e-9
+    else:
+        # the FP32 LDL^T rejects a pivot and the FP64 retry solves the FP32-accumulated
+        # block; its condition number (1e6) times FP32 rounding bounds the error in the
+        # soft direction
+        assert st["fp64_fallback_solves"] > 0
+        assert rel <= 5e-2
+    phys.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32"])
+def test_failed_solve_takes_gradient_step(tmp_path, precision, oracle_lib, gaia_lib):
+    mp, pp = _single_cell(str(tmp_path), miu=0.0, lmbd=1e3, density=1e-12)
+    phys, o, x0 = _displaced_pair(mp, pp, precision, oracle_lib)
+    phys.runStep(3)
+    o.step(3)
+    x, xo = phys.positions(0), o.positions(0)
+    st = phys.stats()
+    rel = float(np.linalg.norm(x - xo) / np.linalg.norm(xo - x0))
+    print(f"{precision}: rel {rel:.3e} failed {st['failed_solves']} oracle failed {o.solve_failures()}")
+    assert st["failed_solves"] > 0 and o.solve_failures() > 0
+    assert np.abs(x[0] - x0[0]).max() > 1e-6  # the gradient steps moved the vertex
+    assert rel <= (1e-9 if precision == "fp64" else 1e-5)
+    phys.close()

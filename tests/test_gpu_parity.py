@@ -4,7 +4,11 @@ Tolerances (relative position error rel = |x - x_ref|_2 / |x_ref - x_ref,0|_2
 over all vertices, the metric named for this path):
   * fp64 engine  vs FP64 oracle: 1e-9 (same algorithm, different summation order)
   * mixed engine vs FP64 oracle: 1e-5 (the stated bound)
-  * fp32 engine  vs FP64 oracle: 5e-3 (FP32 state; reported, not the target)
+  * fp32 engine  vs FP64 oracle: 1e-5 (the stated bound) wherever the benchmark reports the
+    FP32 mode as within it (the twist, contact-free scenes); on the drop configuration with
+    ground contact the FP32 state's rounding is amplified by the landing and the test states
+    the measured bound instead (FP32_DROP_BOUND), and the benchmark reports the double-float
+    mode there.
 """
 import os
 
@@ -13,7 +17,10 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-9, "mixed": 1e-5, "fp32": 5e-3}
+TOL = {"fp64": 1e-9, "mixed": 1e-5, "fp32": 1e-5}
+# fp32 on the 10^3 drop of the plain-drop configuration after 100 steps (measured 1.6e-5 vs
+# the FP64 engine): the landing amplifies FP32 state rounding
+FP32_DROP_BOUND = 5e-5
 
 
 def _rel(x, xr, x0):
@@ -101,11 +108,33 @@ def test_twist(tmp_path, gaia_lib, oracle_lib):
 
     mp, pp = scenes.twist_cube(str(tmp_path), n=10, iterations=20)
     ref = _run_oracle(mp, pp, 20, oracle_lib)
-    for precision in ("fp64", "mixed"):
+    for precision in ("fp64", "mixed", "fp32"):
         x0, xs, st = _run_gpu(mp, pp, precision, 20)
         rel = _rel(xs[0], ref[0], x0[0])
         print(f"twist {precision}: rel {rel:.3e}")
         assert rel <= TOL[precision]
+
+
+@pytest.fixture(scope="module")
+def plain_drop(tmp_path_factory, gaia_lib, oracle_lib):
+    from gaia_gb300 import scenes
+
+    d = tmp_path_factory.mktemp("plain_drop")
+    mp, pp = scenes.drop_cube(str(d), n=10, iterations=20, coloring="greedy", collision=scenes.NO_CONTACT)
+    return mp, pp, _run_oracle(mp, pp, 100, oracle_lib)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32"])
+def test_plain_drop_configuration(precision, plain_drop):
+    """The plain VBD drop exactly as configured for the CPU-runnable case: a 10^3-vertex
+    lattice (3645 tets) 0.2 m above the ground plane, OrderedGreedy coloring, no contact
+    detection, 20 iterations per step, 100 steps (it lands near step 60 and slides)."""
+    mp, pp, ref = plain_drop
+    x0, xs, st = _run_gpu(mp, pp, precision, 100)
+    rel = _rel(xs[0], ref[0], x0[0])
+    print(f"plain drop {precision}: rel err {rel:.3e} max {np.abs(xs[0] - ref[0]).max():.3e}")
+    assert ref[0][:, 1].min() < 0.01  # it landed (the bottom started 0.2 m up)
+    assert rel <= (FP32_DROP_BOUND if precision == "fp32" else TOL[precision])
 
 
 def test_batch_scenes(tmp_path, gaia_lib, oracle_lib):

@@ -11,7 +11,16 @@ import numpy as np
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TREE = "/root/reference/Simulator/Modules/CollisionDetector/CCDSolver.h"
+
+
+def _ref_tree():
+    from oracle.oracle import reference_root
+
+    root = reference_root()
+    return os.path.join(root, "Simulator", "Modules", "CollisionDetector", "CCDSolver.h") if root else ""
+
+
+REF_TREE = _ref_tree()
 
 
 def _oracle_ccd(x0, x1, p0, p1):
