@@ -151,14 +151,15 @@ def make_scene(workload: str, d: str, precision: str, size: int, iterations: int
     raise ValueError(workload)
 
 
-def cpu_sample(mp: str, pp: str, iters: int, reps: int, nthreads: int = 0) -> dict:
-    """Oracle (CPU restatement of the reference VBD step, FP64, all host threads):
-    `reps` samples of one substep with `iters` iterations each."""
+def cpu_sample(mp: str, pp: str, iters: int, reps: int, precision: int = 32, nthreads: int = 0) -> dict:
+    """Oracle (CPU restatement of the reference VBD step, all host threads; precision 32 =
+    the reference's FloatingType, float): `reps` samples of one substep with `iters`
+    iterations each."""
     from oracle import oracle as orc
     from oracle import scene_io
 
     sc = scene_io.load_scene(mp, pp)
-    o = orc.OracleScene(sc, precision=64, nthreads=nthreads)
+    o = orc.OracleScene(sc, precision=precision, nthreads=nthreads)
     nact = sum(int(len(m["fixed"]) - m["fixed"].sum()) for m in sc["meshes"])
     t0 = time.perf_counter()
     for _ in range(reps):
@@ -170,34 +171,50 @@ def cpu_sample(mp: str, pp: str, iters: int, reps: int, nthreads: int = 0) -> di
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the oracle (CPU restatement of the reference's VBD step in float,
+    the reference's FloatingType) on all host threads, on the same scene files as the GPU
+    arm, written without the product library (scene writer "oracle": plain-Python .t and
+    coloring files, the oracle's or stored colorings). Each step is one substep of the
+    configuration with as many of its iterations as fit the time budget (all of them when
+    they fit); warm-up steps run one iteration each."""
     if rank != 0:
         return
-    with tempfile.TemporaryDirectory() as d:
-        mp, pp = make_scene(args.workload, d, "fp64", args.size, args.iterations)
-        from oracle import oracle as orc
-        from oracle import scene_io
+    from gaia_gb300 import scenes
+    from oracle import oracle as orc
+    from oracle import scene_io
 
+    scenes.set_writer("oracle")
+    with tempfile.TemporaryDirectory() as d:
+        mp, pp = make_scene(args.workload, d, "fp32", args.size, args.iterations)
         sc = scene_io.load_scene(mp, pp)
-        o = orc.OracleScene(sc, precision=64, nthreads=0)
+        o = orc.OracleScene(sc, precision=32, nthreads=0)
         nact = sum(int(len(m["fixed"]) - m["fixed"].sum()) for m in sc["meshes"])
-        for _ in range(args.warmup):
-            o.substep_sample(args.ref_iters)
+        t_it = None
+        for _ in range(max(args.warmup, 1)):
+            t0 = time.perf_counter()
+            o.substep_sample(1)
+            t_it = time.perf_counter() - t0
+        iters = args.iterations
+        if args.ref_iters > 0:
+            iters = min(iters, args.ref_iters)
+        else:
+            iters = max(1, min(iters, int(args.ref_budget / max(args.steps, 1) / max(t_it, 1e-9))))
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            o.substep_sample(args.ref_iters)
+            o.substep_sample(iters)
         dt = time.perf_counter() - t0
-    v = nact * args.ref_iters * args.steps / dt
+    v = nact * iters * args.steps / dt
     cores = os.cpu_count() or 1
+    sample = (f"each step = one substep with {iters} of the configuration's {args.iterations} iterations over "
+              f"{nact} active vertices (float oracle, {cores} threads); warm-up steps 1 iteration each")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "vertex-solves/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "steps_per_s_extrapolated": v / (nact * args.iterations),
-        "config": {"workload": workload_name(args), "vertices_active": nact,
-                   "sample": f"each step = one substep with {args.ref_iters} iterations"},
-        "cpu_baseline": {"value": v, "unit": "vertex-solves/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} samples of one substep x {args.ref_iters} iterations, "
-                                   f"{nact} active vertices"},
+        "config": {"workload": workload_name(args), "vertices_active": nact, "iterations_per_sample": iters,
+                   "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "vertex-solves/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "vertex-solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -457,9 +474,9 @@ def run_cloth(args, world, rank, local):
     c.close()
     cpu = None
     if rank == 0 and not args.no_cpu:
-        s = cloth_cpu_sample(mp, pp, args.ref_iters, args.cpu_reps)
+        s = cloth_cpu_sample(mp, pp, args.cpu_iters, args.cpu_reps)
         cpu = {"value": s["value"], "unit": "vertex-solves/s", "cores": s["cores"], "kind": "port",
-               "sample": f"{args.cpu_reps} x one substep with {args.ref_iters} iterations (contact detection "
+               "sample": f"{args.cpu_reps} x one substep with {args.cpu_iters} iterations (contact detection "
                          f"included) over {s['vertices']} vertices ({s['seconds']:.1f} s), CPU restatement of the "
                          "reference cloth step"}
     tmp.cleanup()
@@ -496,11 +513,22 @@ def run_cloth(args, world, rank, local):
 
 
 def run_cloth_reference(args, world, rank):
+    """The cloth reference arm: the cloth oracle (FP64 solve, FP32 detection) on all host
+    threads, on scene files written without the product library; each step is one substep
+    with as many of the configuration's iterations as fit the time budget."""
     if rank != 0:
         return
+    from gaia_gb300 import scenes
+
+    scenes.set_writer("oracle")
     with tempfile.TemporaryDirectory() as d:
         mp, pp = cloth_scene(args, d, "fp64")
-        s = cloth_cpu_sample(mp, pp, args.ref_iters, args.steps)
+        w = cloth_cpu_sample(mp, pp, 1, max(args.warmup, 1))
+        t_it = w["seconds"] / max(args.warmup, 1)
+        iters = args.ref_iters if args.ref_iters > 0 else max(1, min(args.iterations, int(
+            args.ref_budget / max(args.steps, 1) / max(t_it, 1e-9))))
+        s = cloth_cpu_sample(mp, pp, iters, args.steps)
+    args.ref_iters = iters
     v = s["value"]
     line = {
         "impl": "reference", "metric": CLOTH_METRIC, "value": v, "unit": "vertex-solves/s", "n_gpus": args.gpus,
@@ -530,8 +558,12 @@ def main():
                     help="batch workload: steps of the one-handle-per-scene loop it is compared with")
     ap.add_argument("--error-steps", type=int, default=100)
     ap.add_argument("--fp64-steps", type=int, default=10)
-    ap.add_argument("--ref-iters", type=int, default=2)
+    ap.add_argument("--ref-iters", type=int, default=0,
+                    help="iterations per CPU sample (0 = as many of the configuration's as fit the budget)")
+    ap.add_argument("--ref-budget", type=float, default=120.0,
+                    help="seconds of timed CPU work the reference arm aims at")
     ap.add_argument("--cpu-reps", type=int, default=2)
+    ap.add_argument("--cpu-iters", type=int, default=2, help="iterations per cpu_baseline sample of the GPU arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="auto", choices=["auto", "mixed", "fp32", "fp64"],
@@ -620,10 +652,13 @@ def main():
     # ---- CPU baseline: the oracle on a bounded sample of the same workload ------------------
     cpu = None
     if rank == 0 and not args.no_cpu:
-        s = cpu_sample(mp, pp, iters=args.ref_iters, reps=args.cpu_reps)
+        s = cpu_sample(mp, pp, iters=args.cpu_iters, reps=args.cpu_reps, precision=32)
+        s64 = cpu_sample(mp, pp, iters=args.cpu_iters, reps=1, precision=64)
         cpu = {"value": s["vertex_solves_per_s"], "unit": "vertex-solves/s", "cores": s["cores"], "kind": "port",
                "sample": f"{s['reps']} x one substep with {s['iterations']} iterations over {s['active_vertices']} "
-                         f"active vertices ({s['seconds']:.1f} s), FP64 CPU restatement of the reference step"}
+                         f"active vertices ({s['seconds']:.1f} s), float CPU restatement of the reference step "
+                         "(the reference's FloatingType)",
+               "fp64_value": s64["vertex_solves_per_s"]}
     tmp.cleanup()
 
     if rank == 0:

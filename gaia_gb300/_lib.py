@@ -39,6 +39,8 @@ class Stats(C.Structure):
         ("autotune_ms_per_iteration", C.c_double), ("solve_variant", C.c_int32), ("reserved", C.c_int32),
         ("contact_detections", C.c_int64), ("contact_stack_overflow", C.c_int64),
         ("contact_traverse_bounds", C.c_int64), ("device_timeouts", C.c_int64), ("nonfinite_solves", C.c_int64),
+        ("sweep_mode", C.c_int32), ("reserved2", C.c_int32), ("sweep_ms_merged", C.c_double),
+        ("sweep_ms_scenes", C.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -111,6 +113,8 @@ _SIGNATURES = {
     "gaia_vbd_get_coloring": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "gaia_vbd_get_rest_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gaia_vbd_energy": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "gaia_vbd_convergence": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gaia_vbd_get_convergence_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "gaia_vbd_vertex_force_hessian": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "gaia_vbd_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
     "gaia_vbd_get_output_params": (C.c_int, [C.c_void_p, C.POINTER(OutputParams)]),

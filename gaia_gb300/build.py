@@ -24,7 +24,8 @@ CLI = os.path.join(HERE, "vbd_dynamics")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["scene.cpp", "state_io.cpp", "vbd_engine.cu", "vbd_energy_noalloc.cu", "tet_cd.cu", "coloring_gpu.cu",
            "cloth_scene.cpp", "cloth_cd.cu", "cloth_engine.cu"]
-HEADERS = ["scene.hpp", "json_lite.hpp", "json_get.hpp", "vbd_kernels.cuh", "vbd_state.cuh", "cloth_scene.hpp",
+HEADERS = ["scene.hpp", "json_lite.hpp", "json_get.hpp", "vbd_kernels.cuh", "vbd_convergence.cuh", "vbd_state.cuh",
+           "cloth_scene.hpp",
            "cloth_cd.hpp", "cloth_dev.cuh", "lbvh.cuh", "state_io.hpp", "tet_cd.hpp"]
 PUBLIC_HEADERS = ["gaia_vbd.h", "gaia_cloth.h"]
 # The contact detector's predicates must round like the CPU restatement: no FMA contraction.

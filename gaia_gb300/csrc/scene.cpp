@@ -541,6 +541,7 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         get(*pp, "numThreadsVBDSolve", p.numThreadsVBDSolve);
         get(*pp, "useDouble3x3", p.useDouble3x3);
         get(*pp, "evaluateConvergence", p.evaluateConvergence);
+        get(*pp, "evaluationSteps", p.evaluationSteps);
         get(*pp, "numFrames", p.numFrames);
         get(*pp, "saveOutputs", p.saveOutputs);
         get(*pp, "saveAllModelsTogether", p.saveAllModelsTogether);
@@ -557,6 +558,7 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         get(*pp, "smallColorVertices", p.smallColorVertices);
         get(*pp, "solveVariant", p.solveVariant);
         get(*pp, "waitPollLimit", p.waitPollLimit);
+        get(*pp, "sweepMode", p.sweepMode);
     }
     if (const json::Value* cp = params.find("CollisionParams")) {
         get(*cp, "allowCCD", p.allowCCD);
@@ -577,6 +579,9 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
     }
     if (p.numSubsteps <= 0 || p.timeStep <= 0) throw std::runtime_error("timeStep and numSubsteps must be positive");
     if (p.iterations < 0) throw std::runtime_error("iterations must be >= 0");
+    if (p.evaluationSteps < 1) throw std::runtime_error("evaluationSteps must be >= 1");
+    if (p.sweepMode != "auto" && p.sweepMode != "merged" && p.sweepMode != "scenes")
+        throw std::runtime_error("sweepMode must be \"auto\", \"merged\" or \"scenes\"");
     if (p.gpuPrecision != "fp32" && p.gpuPrecision != "mixed" && p.gpuPrecision != "fp64")
         throw std::runtime_error("gpuPrecision must be \"mixed\", \"fp32\" or \"fp64\"");
     p.dt = p.timeStep / p.numSubsteps;

@@ -54,6 +54,7 @@ struct PhysicsParams {
     int numThreadsVBDSolve = 16;
     bool useDouble3x3 = false;
     bool evaluateConvergence = false;
+    int evaluationSteps = 10;  // with evaluateConvergence: evaluate after iterations 0, n, 2n, ...
     // output of the frame loop (Parameters/PhysicsParameters.h:30, 87-99)
     int numFrames = 5000;
     bool saveOutputs = true;
@@ -73,6 +74,7 @@ struct PhysicsParams {
     bool usePDL = true;                  // programmatic dependent launch between color kernels
     int smallColorVertices = 16384;      // colors up to this size use one warp per vertex
     int solveVariant = -1;               // -1 autotune, 0 register-pipelined, 1 TMA-staged records
+    std::string sweepMode = "auto";      // color scheduling: "auto", "merged", "scenes"
     int waitPollLimit = -1;              // polls of a bounded device wait (-1: the built-in limit); tests
                                          // lower it to make the wait run out
 };

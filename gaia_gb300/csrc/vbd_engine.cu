@@ -21,6 +21,7 @@
 #include "scene.hpp"
 #include "state_io.hpp"
 #include "tet_cd.hpp"
+#include "vbd_convergence.cuh"
 #include "vbd_kernels.cuh"
 
 namespace gaia {
@@ -82,9 +83,14 @@ void set_last_global_error(const std::string& msg) { g_last_error = msg; }
 template <typename R>
 void make_record(int4& n, dev::R4<R>& a, dev::R4<R>& b, R* c, const int* nb, double mv[3][3]);
 
+enum { kSweepMerged = 0, kSweepScenes = 1 };
+
 class EngineBase {
 public:
     virtual ~EngineBase() {}
+    virtual int mode() const = 0;
+    virtual double tuned_ms() const = 0;
+    virtual double measure_sweep_ms() = 0;
     virtual void run_steps(int n) = 0;
     virtual void run_steps_timed(int n, float* total_ms, float* sweep_ms) = 0;
     virtual void autotune() = 0;
@@ -97,6 +103,8 @@ public:
     virtual void get_positions_f32(float* x) = 0;
     virtual void get_velocities_f32(float* v) = 0;
     virtual double energy() = 0;
+    virtual void convergence(double* out4) = 0;
+    virtual void convergence_log(std::vector<double>& rows) = 0;
     virtual void vertex_force_hessian(int mesh, int v, int friction, double* f3, double* h9) = 0;
     virtual void stats(gaia_vbd_stats* s) = 0;
     virtual void sync() = 0;
@@ -117,7 +125,9 @@ class Engine : public EngineBase {
     using R4 = dev::R4<R>;
 
 public:
-    explicit Engine(const Scene& s) : sc_(s) {
+    // mode: kSweepMerged (one launch per merged color and iteration) or kSweepScenes (one
+    // persistent launch per substep running every scene's iterations, scene-major slots)
+    Engine(const Scene& s, int mode) : sc_(s), mode_(mode) {
         GAIA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         GAIA_CUDA(cudaEventCreate(&ev_a_));
         GAIA_CUDA(cudaEventCreate(&ev_b_));
@@ -139,10 +149,19 @@ public:
             throw std::runtime_error("solveVariant must be -1 (autotune), 0 (registers) or 1 (TMA-staged)");
         if (variant_fixed_ == 1 && sizeof(R) != 4) variant_fixed_ = 0;  // the FP64 engine has no TMA variant
         if (variant_fixed_ >= 0) variant_ = variant_fixed_;
-        if ((lanes_ == 0 || block_ == 0 || variant_fixed_ < 0) && sc_.p.autotune) autotune_impl();
-        finalize_cfg();
+        if (mode_ == kSweepScenes) {
+            setup_scenes();
+            if ((lanes_ == 0 || block_ == 0) && sc_.p.autotune) autotune_scenes();
+            finalize_scenes();
+        } else {
+            if ((lanes_ == 0 || block_ == 0 || variant_fixed_ < 0) && sc_.p.autotune) autotune_impl();
+            finalize_cfg();
+        }
+        if (sc_.p.evaluateConvergence) setup_conv();
         capture();
     }
+
+    int mode() const override { return mode_; }
 
     void color_config(int g, int32_t* L, int32_t* B, int32_t* variant, float* ms) const override {
         if (g < 0 || size_t(g) >= ccfg_.size()) throw std::invalid_argument("color index out of range");
@@ -172,13 +191,37 @@ public:
         int32_t slot = 0;
         group_beg_.clear();
         group_end_.clear();
-        for (auto& g : sc_.groups) {
-            group_beg_.push_back(slot);
-            for (size_t i = 0; i + 1 < g.size(); i += 2) {
-                int m = g[i], v = g[i + 1];
-                if (!meshes[m].fixed[v]) slot_of_[mesh_off_[m] + v] = slot++;
+        scene_colors_.clear();
+        scene_ofs_.assign(1, 0);
+        if (mode_ == kSweepScenes) {
+            // scene-major: mesh by mesh, within a mesh its vertices of merged color 0, 1, ...
+            std::vector<std::vector<std::vector<int32_t>>> per(size_t(nmesh_),
+                                                               std::vector<std::vector<int32_t>>(sc_.groups.size()));
+            for (size_t gi = 0; gi < sc_.groups.size(); ++gi) {
+                const auto& g = sc_.groups[gi];
+                for (size_t i = 0; i + 1 < g.size(); i += 2) {
+                    const int m = g[i], v = g[i + 1];
+                    if (!meshes[m].fixed[v]) per[size_t(m)][gi].push_back(v);
+                }
             }
-            group_end_.push_back(slot);
+            for (int m = 0; m < nmesh_; ++m) {
+                for (auto& verts : per[size_t(m)]) {
+                    if (verts.empty()) continue;
+                    const int32_t beg = slot;
+                    for (int32_t v : verts) slot_of_[mesh_off_[m] + v] = slot++;
+                    scene_colors_.push_back(make_int2(beg, slot));
+                }
+                scene_ofs_.push_back(int32_t(scene_colors_.size()));
+            }
+        } else {
+            for (auto& g : sc_.groups) {
+                group_beg_.push_back(slot);
+                for (size_t i = 0; i + 1 < g.size(); i += 2) {
+                    int m = g[i], v = g[i + 1];
+                    if (!meshes[m].fixed[v]) slot_of_[mesh_off_[m] + v] = slot++;
+                }
+                group_end_.push_back(slot);
+            }
         }
         nactive_ = slot;
         for (int64_t gi = 0; gi < nslots_; ++gi)
@@ -355,7 +398,6 @@ public:
         d_stage_f32_.alloc(6 * size_t(nslots_), &bytes_);
         d_stage_f64_.alloc(3 * size_t(nslots_), &bytes_);
         d_probe_.alloc(12, &bytes_);
-        d_energy_.alloc(1, &bytes_);
         GAIA_CUDA(cudaStreamSynchronize(st_));
         // keep host copies small: records are device-only from here on
         std::vector<int4>().swap(h_rec_n_);
@@ -650,6 +692,8 @@ public:
                                                                           *omega, cd_.records().info);
             GAIA_CUDA(cudaGetLastError());
         }
+        // evaluateConvergence (VBDPhysics.cpp:948-951): a record after iterations 0, n, 2n, ...
+        if (sc_.p.evaluateConvergence && it % sc_.p.evaluationSteps == 0) enqueue_conv(true);
     }
 
     void enqueue_velocity() {
@@ -706,6 +750,12 @@ public:
         g_init_rb_ = cd_.enabled() ? capture_one([&] { enqueue_init(true); }, &k_init_rb) : nullptr;
         g_sweep_ = capture_one(
             [&] {
+                if (mode_ == kSweepScenes) {
+                    enqueue_scenes_sweep(scene_L_, scene_B_);
+                    return;
+                }
+                // evaluateConvergence at iteration -1, on the initial guess (VBDPhysics.cpp:866-870)
+                if (sc_.p.evaluateConvergence) enqueue_conv(true);
                 double omega = 1.0;
                 for (int it = 0; it < sc_.p.iterations; ++it) enqueue_iteration(it, &omega, sc_.p.useAccelerator);
             },
@@ -720,9 +770,15 @@ public:
     // step and refitted in the others.
     cudaGraphExec_t init_graph(int sub) const { return sub == 0 && g_init_rb_ ? g_init_rb_ : g_init_; }
 
+    // The convergence log holds the records of the last step.
+    void start_step_log() {
+        if (sc_.p.evaluateConvergence) GAIA_CUDA(cudaMemsetAsync(d_conv_count_.p, 0, sizeof(int32_t), st_));
+    }
+
     void run_steps(int n) override {
         for (int k = 0; k < n; ++k)
             for (int sub = 0; sub < sc_.p.numSubsteps; ++sub) {
+                if (sub == 0) start_step_log();
                 GAIA_CUDA(cudaGraphLaunch(init_graph(sub), st_));
                 GAIA_CUDA(cudaGraphLaunch(g_sweep_, st_));
                 GAIA_CUDA(cudaGraphLaunch(g_vel_, st_));
@@ -738,6 +794,7 @@ public:
         int q = 0;
         for (int k = 0; k < n; ++k)
             for (int sub = 0; sub < sc_.p.numSubsteps; ++sub, ++q) {
+                if (sub == 0) start_step_log();
                 GAIA_CUDA(cudaGraphLaunch(init_graph(sub), st_));
                 GAIA_CUDA(cudaEventRecord(ev[2 * q], st_));
                 GAIA_CUDA(cudaGraphLaunch(g_sweep_, st_));
@@ -821,6 +878,100 @@ public:
         }
     }
 
+    // ---- persistent scene-major sweep (k_sweep_scenes) ------------------------------
+    void setup_scenes() {
+        std::vector<int64_t> work(size_t(nmesh_), 0);
+        for (int m = 0; m < nmesh_; ++m)
+            for (int32_t ci = scene_ofs_[m]; ci < scene_ofs_[m + 1]; ++ci)
+                work[size_t(m)] += inc_ofs_[scene_colors_[ci].y] - inc_ofs_[scene_colors_[ci].x];
+        std::vector<int32_t> order;
+        for (int m = 0; m < nmesh_; ++m)
+            if (scene_ofs_[m + 1] > scene_ofs_[m]) order.push_back(m);
+        // largest scene first: the work counter hands them out in this order
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work[size_t(a)] > work[size_t(b)]; });
+        nscenes_ = int32_t(order.size());
+        d_scene_colors_.upload(scene_colors_, &bytes_, st_);
+        d_scene_ofs_.upload(scene_ofs_, &bytes_, st_);
+        d_scene_order_.upload(order, &bytes_, st_);
+        d_scene_work_.alloc(1, &bytes_);
+        GAIA_CUDA(cudaMemsetAsync(d_scene_work_.p, 0, sizeof(int32_t), st_));
+        int dev = 0;
+        GAIA_CUDA(cudaGetDevice(&dev));
+        GAIA_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    template <int L>
+    void launch_scenes_l(int B) {
+        auto kern = dev::k_sweep_scenes<L, ST, R>;
+        int per_sm = 0;
+        GAIA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, B, 0));
+        const int grid = std::max(1, std::min(nscenes_, std::max(per_sm, 1) * num_sms_));
+        kern<<<grid, B, 0, st_>>>(ptrs(), c_, d_scene_colors_.p, d_scene_ofs_.p, d_scene_order_.p, nscenes_,
+                                  sc_.p.iterations, sc_.p.frictionStartIter, d_scene_work_.p);
+        GAIA_CUDA(cudaGetLastError());
+    }
+
+    // One substep's iterations: reset the work counter, one persistent launch.
+    void enqueue_scenes_sweep(int L, int B) {
+        if (nscenes_ == 0 || sc_.p.iterations == 0) return;
+        GAIA_CUDA(cudaMemsetAsync(d_scene_work_.p, 0, sizeof(int32_t), st_));
+        switch (L) {
+            case 2: launch_scenes_l<2>(B); break;
+            case 4: launch_scenes_l<4>(B); break;
+            case 8: launch_scenes_l<8>(B); break;
+            case 16: launch_scenes_l<16>(B); break;
+            default: launch_scenes_l<32>(B); break;
+        }
+    }
+
+    // Lanes per vertex and block size of the persistent sweep: every pair timed on a full
+    // sweep of the current state (restored afterwards); ms per iteration of the fastest.
+    void autotune_scenes() {
+        if (nactive_ == 0 || nscenes_ == 0 || sc_.p.iterations == 0) return;
+        DevBuf<S4> save;
+        save.alloc(nslots_, nullptr);
+        GAIA_CUDA(cudaMemcpyAsync(save.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+        const int Ls[] = {4, 8, 16, 32};
+        const int Bs[] = {256, 512, 1024};
+        float best = 1e30f;
+        for (int L : Ls) {
+            if (lanes_ && L != lanes_) continue;
+            for (int B : Bs) {
+                if (block_ && B != block_) continue;
+                enqueue_scenes_sweep(L, B);  // warm-up
+                GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+                GAIA_CUDA(cudaEventRecord(ev_a_, st_));
+                enqueue_scenes_sweep(L, B);
+                GAIA_CUDA(cudaEventRecord(ev_b_, st_));
+                GAIA_CUDA(cudaEventSynchronize(ev_b_));
+                float ms = 0.f;
+                GAIA_CUDA(cudaEventElapsedTime(&ms, ev_a_, ev_b_));
+                GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+                if (ms < best) {
+                    best = ms;
+                    scene_L_ = L;
+                    scene_B_ = B;
+                }
+            }
+        }
+        GAIA_CUDA(cudaMemsetAsync(d_counters_.p, 0, dev::CNT_N * sizeof(unsigned long long), st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        tuned_ms_ = double(best) / sc_.p.iterations;
+        tuned_ = true;
+    }
+
+    void finalize_scenes() {
+        if (!tuned_) {
+            scene_L_ = lanes_ ? lanes_ : 8;
+            scene_B_ = block_ ? block_ : 512;
+        }
+        lanes_ = scene_L_;
+        block_ = scene_B_;
+        variant_ = 2;
+        ccfg_.assign(sc_.groups.size(), ColorCfg{scene_L_, scene_B_, 2, float(tuned_ms_)});
+    }
+
     double get_time() override {
         double t = 0.0;
         GAIA_CUDA(cudaMemcpyAsync(&t, d_time_.p, sizeof(double), cudaMemcpyDeviceToHost, st_));
@@ -848,9 +999,41 @@ public:
         lanes_ = sc_.p.lanesPerVertex;
         block_ = sc_.p.blockSize;
         tuned_ = false;
-        autotune_impl();
-        finalize_cfg();
+        if (mode_ == kSweepScenes) {
+            autotune_scenes();
+            finalize_scenes();
+        } else {
+            autotune_impl();
+            finalize_cfg();
+        }
         capture();
+    }
+
+    double tuned_ms() const override { return tuned_ms_; }
+
+    // Device time of the captured sweep graph (all iterations of one substep) on the
+    // current state, per iteration; the state is restored afterwards.
+    double measure_sweep_ms() override {
+        DevBuf<S4> save;
+        save.alloc(nslots_, nullptr);
+        GAIA_CUDA(cudaMemcpyAsync(save.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+        GAIA_CUDA(cudaGraphLaunch(g_sweep_, st_));  // warm-up
+        const int reps = 3;
+        float total = 0.f;
+        for (int r = 0; r < reps; ++r) {
+            GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+            GAIA_CUDA(cudaEventRecord(ev_a_, st_));
+            GAIA_CUDA(cudaGraphLaunch(g_sweep_, st_));
+            GAIA_CUDA(cudaEventRecord(ev_b_, st_));
+            GAIA_CUDA(cudaEventSynchronize(ev_b_));
+            float ms = 0.f;
+            GAIA_CUDA(cudaEventElapsedTime(&ms, ev_a_, ev_b_));
+            total += ms;
+        }
+        GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+        GAIA_CUDA(cudaMemsetAsync(d_counters_.p, 0, dev::CNT_N * sizeof(unsigned long long), st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        return double(total) / reps / std::max(sc_.p.iterations, 1);
     }
 
     // ---- state access -------------------------------------------------------------
@@ -999,44 +1182,138 @@ public:
         GAIA_CUDA(cudaStreamSynchronize(st_));
     }
 
-    double energy() override {
-        if (!d_tet_slots_.p) {
-            // per-tet data for the energy reduction, built on first use
-            std::vector<int4> ts;
-            std::vector<double> dm, vol;
-            std::vector<int32_t> tm;
-            for (int m = 0; m < nmesh_; ++m) {
-                const TetMesh& M = sc_.meshes[m];
-                for (int t = 0; t < M.ntet; ++t) {
-                    const int32_t* tv = &M.tets[4 * size_t(t)];
-                    ts.push_back(make_int4(slot_of_[mesh_off_[m] + tv[0]], slot_of_[mesh_off_[m] + tv[1]],
-                                           slot_of_[mesh_off_[m] + tv[2]], slot_of_[mesh_off_[m] + tv[3]]));
-                    dm.insert(dm.end(), M.dminv.begin() + 9 * size_t(t), M.dminv.begin() + 9 * size_t(t) + 9);
-                    vol.push_back(M.vol[t]);
-                    tm.push_back(m);
-                }
+    // ---- FP64 convergence reduction (vbd_convergence.cuh) -----------------------------
+    // Per-tet FP64 data (global tet order: meshes in order, tets in order), each active
+    // slot's incidences as (tet, order) in the solve's CSR, partial-sum buffers and the
+    // record log; built on first use, or at construction when the step logs records.
+    void setup_conv() {
+        if (conv_ready_) return;
+        std::vector<int4> ts;
+        std::vector<double> dm, vol;
+        std::vector<int32_t> tm, tet_off(nmesh_ + 1, 0);
+        for (int m = 0; m < nmesh_; ++m) {
+            const TetMesh& M = sc_.meshes[m];
+            tet_off[m + 1] = tet_off[m] + M.ntet;
+            for (int t = 0; t < M.ntet; ++t) {
+                const int32_t* tv = &M.tets[4 * size_t(t)];
+                ts.push_back(make_int4(slot_of_[mesh_off_[m] + tv[0]], slot_of_[mesh_off_[m] + tv[1]],
+                                       slot_of_[mesh_off_[m] + tv[2]], slot_of_[mesh_off_[m] + tv[3]]));
+                dm.insert(dm.end(), M.dminv.begin() + 9 * size_t(t), M.dminv.begin() + 9 * size_t(t) + 9);
+                vol.push_back(M.vol[t]);
+                tm.push_back(m);
             }
-            d_tet_slots_.upload(ts, &bytes_, st_);
-            d_tet_dminv_.upload(dm, &bytes_, st_);
-            d_tet_vol_.upload(vol, &bytes_, st_);
-            d_tet_mesh_.upload(tm, &bytes_, st_);
-            std::vector<double2> ml;
-            for (int m = 0; m < nmesh_; ++m) ml.push_back(make_double2(sc_.objs[m].miu, sc_.objs[m].lmbd));
-            d_mu_lmbd_.upload(ml, &bytes_, st_);
         }
-        GAIA_CUDA(cudaMemsetAsync(d_energy_.p, 0, sizeof(double), st_));
-        int32_t nt = int32_t(d_tet_slots_.n);
-        if (nt)
-            dev::k_energy_tets<ST><<<div_up(nt, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, d_tet_slots_.p,
-                                                                     d_tet_dminv_.p, d_tet_vol_.p, d_tet_mesh_.p,
-                                                                     d_mu_lmbd_.p, nt, d_energy_.p);
-        dev::k_energy_inertia<ST><<<div_up(nactive_, 256), 256, 0, st_>>>(d_pos_.p, d_y_.p, nactive_,
-                                                                         0.5 * sc_.p.dtSqrReciprocal, d_energy_.p);
-        GAIA_CUDA(cudaGetLastError());
-        double e = 0;
-        GAIA_CUDA(cudaMemcpyAsync(&e, d_energy_.p, sizeof(double), cudaMemcpyDeviceToHost, st_));
+        // incidences in slot order, as the solve's records are stored
+        std::vector<int32_t> inc_tet;
+        std::vector<int8_t> inc_ord;
+        inc_tet.reserve(size_t(ninc_));
+        inc_ord.reserve(size_t(ninc_));
+        for (int32_t sl = 0; sl < nactive_; ++sl) {
+            const int m = slot_mesh_[sl];
+            const TetMesh& M = sc_.meshes[m];
+            const int v = orig_of_[sl] - int32_t(mesh_off_[m]);
+            const int32_t base = tet_off[m];
+            for (int k = M.nbr_ofs[v]; k < M.nbr_ofs[v + 1]; ++k) {
+                inc_tet.push_back(base + M.nbr_tet[k]);
+                inc_ord.push_back(static_cast<int8_t>(M.nbr_order[k]));
+            }
+        }
+        std::vector<double4> mat(nmesh_);
+        for (int m = 0; m < nmesh_; ++m) {
+            const ObjectParams& o = sc_.objs[m];
+            mat[m] = make_double4(o.miu, o.lmbd, o.dampingHydrostatic, o.dampingDeviatoric);
+        }
+        d_tet_slots_.upload(ts, &bytes_, st_);
+        d_tet_dminv_.upload(dm, &bytes_, st_);
+        d_tet_vol_.upload(vol, &bytes_, st_);
+        d_tet_mesh_.upload(tm, &bytes_, st_);
+        d_conv_inc_tet_.upload(inc_tet, &bytes_, st_);
+        d_conv_inc_ord_.upload(inc_ord, &bytes_, st_);
+        d_conv_mat_.upload(mat, &bytes_, st_);
+        conv_nb_t_ = std::max(1, div_up(int64_t(ts.size()), dev::kConvThreads));
+        conv_nb_v_ = std::max(1, div_up(nslots_, dev::kConvThreads));
+        d_conv_part_.alloc(size_t(conv_nb_t_) + 2 * size_t(conv_nb_v_), &bytes_);
+        d_conv_out_.alloc(4, &bytes_);
+        conv_per_substep_ = 1 + (sc_.p.iterations + sc_.p.evaluationSteps - 1) / sc_.p.evaluationSteps;
+        if (sc_.p.iterations == 0) conv_per_substep_ = 1;
+        conv_cap_ = sc_.p.evaluateConvergence ? conv_per_substep_ * sc_.p.numSubsteps : 0;
+        d_conv_log_.alloc(4 * size_t(std::max(conv_cap_, 1)), &bytes_);
+        d_conv_count_.alloc(1, &bytes_);
+        GAIA_CUDA(cudaMemsetAsync(d_conv_count_.p, 0, sizeof(int32_t), st_));
         GAIA_CUDA(cudaStreamSynchronize(st_));
-        return e;
+        conv_ready_ = true;
+    }
+
+    dev::ConvData conv_data() const {
+        dev::ConvData D;
+        D.tet_slots = d_tet_slots_.p;
+        D.tet_dminv = d_tet_dminv_.p;
+        D.tet_vol = d_tet_vol_.p;
+        D.tet_mesh = d_tet_mesh_.p;
+        D.mesh_mat = d_conv_mat_.p;
+        D.slot_mesh = d_slot_mesh_.p;
+        D.inc_ofs = d_inc_ofs_.p;
+        D.inc_tet = d_conv_inc_tet_.p;
+        D.inc_ord = d_conv_inc_ord_.p;
+        D.ntet = int32_t(d_tet_slots_.n);
+        D.nactive = nactive_;
+        D.nslots = int32_t(nslots_);
+        D.dt2inv = sc_.p.dtSqrReciprocal;
+        D.inv_dt = 1.0 / sc_.p.dt;
+        return D;
+    }
+
+    // Three kernels: elastic partials, inertia / force-norm partials, the fixed-order finish
+    // into the log (to_log) or into the single-record output.
+    void enqueue_conv(bool to_log) {
+        const dev::ConvData D = conv_data();
+        double* pe = d_conv_part_.p;
+        double* pi = pe + conv_nb_t_;
+        double* pf = pi + conv_nb_v_;
+        if (D.ntet) dev::k_conv_tets<ST><<<conv_nb_t_, dev::kConvThreads, 0, st_>>>(d_pos_.p, d_rest_.p, D, pe);
+        else GAIA_CUDA(cudaMemsetAsync(pe, 0, sizeof(double), st_));
+        dev::k_conv_verts<ST><<<conv_nb_v_, dev::kConvThreads, 0, st_>>>(d_pos_.p, d_y_.p, d_xprev_.p, d_rest_.p, D, pi,
+                                                                         pf);
+        dev::k_conv_finish<<<1, dev::kConvThreads, 0, st_>>>(pe, D.ntet ? conv_nb_t_ : 1, pi, pf, conv_nb_v_,
+                                                             1.0 / double(std::max<int64_t>(nslots_, 1)),
+                                                             to_log ? d_conv_log_.p : d_conv_out_.p,
+                                                             to_log ? d_conv_count_.p : nullptr,
+                                                             to_log ? conv_cap_ : 1);
+        GAIA_CUDA(cudaGetLastError());
+    }
+
+    // evaluateConvergenceGPU on the current state: energy, inertia, elastic, average force norm.
+    void convergence(double* out4) override {
+        setup_conv();
+        enqueue_conv(false);
+        GAIA_CUDA(cudaMemcpyAsync(out4, d_conv_out_.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    double energy() override {
+        double out[4];
+        convergence(out);
+        return out[0];
+    }
+
+    // Records of the last step: (substep, iteration, energy, inertia, elastic, average force norm).
+    void convergence_log(std::vector<double>& rows) override {
+        rows.clear();
+        if (!sc_.p.evaluateConvergence) return;
+        int32_t n = 0;
+        GAIA_CUDA(cudaMemcpyAsync(&n, d_conv_count_.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        n = std::min(n, conv_cap_);
+        std::vector<double> log(4 * size_t(std::max(n, 1)));
+        if (n) GAIA_CUDA(cudaMemcpyAsync(log.data(), d_conv_log_.p, 4 * size_t(n) * sizeof(double),
+                                         cudaMemcpyDeviceToHost, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        for (int k = 0; k < n; ++k) {
+            const int sub = k / conv_per_substep_, e = k % conv_per_substep_;
+            rows.push_back(double(sub));
+            rows.push_back(e == 0 ? -1.0 : double((e - 1) * sc_.p.evaluationSteps));
+            rows.insert(rows.end(), log.begin() + 4 * size_t(k), log.begin() + 4 * size_t(k) + 4);
+        }
     }
 
     void vertex_force_hessian(int mesh, int v, int friction, double* f3, double* h9) override {
@@ -1061,7 +1338,8 @@ public:
         s->precision = sizeof(R) == 8 ? 64 : (sizeof(S4) == 32 ? 48 : 32);
         s->lanes_per_vertex = lanes_;
         s->block_size = block_;
-        s->num_groups = int32_t(group_beg_.size());
+        s->num_groups = int32_t(sc_.groups.size());
+        s->sweep_mode = mode_;
         s->num_vertices = nslots_;
         s->num_active_vertices = nactive_;
         s->num_incidences = ninc_;
@@ -1097,7 +1375,15 @@ private:
     bool tuned_ = false;
     bool use_pdl_ = true;
     int small_color_ = 16384;
-    int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma
+    int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma, 2 = k_sweep_scenes
+    int mode_ = 0;             // kSweepMerged or kSweepScenes
+    // scene-major mode: per mesh its color slot ranges, in sweep order
+    std::vector<int2> scene_colors_;
+    std::vector<int32_t> scene_ofs_;
+    int32_t nscenes_ = 0;
+    int scene_L_ = 8, scene_B_ = 512, num_sms_ = 1;
+    DevBuf<int2> d_scene_colors_;
+    DevBuf<int32_t> d_scene_ofs_, d_scene_order_, d_scene_work_;
     int variant_fixed_ = -1;   // from PhysicsParams solveVariant (-1 = autotune)
     std::map<std::pair<int, int>, int> maxrec_cache_;
     static constexpr size_t kTmaSmemMax = 200 * 1024;
@@ -1121,14 +1407,20 @@ private:
     std::vector<double> h_def_a_, h_def_b_;
     DevBuf<S4> d_pos_, d_y_, d_xprev_, d_acc_pp_, d_acc_prev_;
     DevBuf<V4> d_vel_, d_vprev_;
-    DevBuf<double2> d_mu_lmbd_;
     DevBuf<int32_t> d_inc_ofs_, d_slot_mesh_, d_slot_of_, d_def_slot_, d_def_idx_, d_tet_mesh_;
     DevBuf<int4> d_rec_n_, d_tet_slots_;
     DevBuf<R4> d_rec_a_, d_rec_b_;
     DevBuf<R> d_rec_c_;
     DevBuf<dev::MeshMat<R>> d_mats_;
     DevBuf<unsigned long long> d_counters_;
-    DevBuf<double> d_time_, d_def_a_, d_def_b_, d_stage_f64_, d_probe_, d_energy_, d_tet_dminv_, d_tet_vol_;
+    DevBuf<double> d_time_, d_def_a_, d_def_b_, d_stage_f64_, d_probe_, d_tet_dminv_, d_tet_vol_;
+    // convergence reduction
+    bool conv_ready_ = false;
+    int conv_nb_t_ = 1, conv_nb_v_ = 1, conv_per_substep_ = 1, conv_cap_ = 0;
+    DevBuf<int32_t> d_conv_inc_tet_, d_conv_count_;
+    DevBuf<int8_t> d_conv_inc_ord_;
+    DevBuf<double4> d_conv_mat_;
+    DevBuf<double> d_conv_part_, d_conv_out_, d_conv_log_;
     DevBuf<dev::DeformerDev> d_defs_;
     DevBuf<float4> d_rest_;
     DevBuf<float> d_stage_f32_;
@@ -1161,6 +1453,7 @@ struct gaia_vbd {
     std::unique_ptr<gaia::EngineBase> eng;
     std::string err;
     int64_t frame = 0;  // runStep calls since initialize / the last loaded state
+    double sweep_ms[2] = {0.0, 0.0};  // autotuned schedule choice: measured ms per iteration, merged / scenes
 };
 
 namespace {
@@ -1225,10 +1518,34 @@ int gaia_vbd_initialize(gaia_vbd* h) {
         return GAIA_VBD_E_NO_DEVICE;
     }
     return guarded(h, [&] {
-        const std::string& pr = h->scene.p.gpuPrecision;
-        if (pr == "fp64") h->eng.reset(new gaia::Engine<gaia::dev::StF64, double>(h->scene));
-        else if (pr == "fp32") h->eng.reset(new gaia::Engine<gaia::dev::StF32, float>(h->scene));
-        else h->eng.reset(new gaia::Engine<gaia::dev::StDF, float>(h->scene));
+        const gaia::PhysicsParams& p = h->scene.p;
+        auto make = [&](int mode) -> gaia::EngineBase* {
+            if (p.gpuPrecision == "fp64") return new gaia::Engine<gaia::dev::StF64, double>(h->scene, mode);
+            if (p.gpuPrecision == "fp32") return new gaia::Engine<gaia::dev::StF32, float>(h->scene, mode);
+            return new gaia::Engine<gaia::dev::StDF, float>(h->scene, mode);
+        };
+        // color scheduling: merged colors (one launch per merged color and iteration) or
+        // scene-major (one persistent launch per substep). The scene-major sweep needs meshes
+        // that do not interact within a sweep and no per-iteration work outside the solve.
+        const bool scenes_ok = !(p.allowCCD || p.allowDCD) && !p.useAccelerator && !p.evaluateConvergence &&
+                               p.iterations > 0;
+        if (p.sweepMode == "scenes" && !scenes_ok)
+            throw std::runtime_error("sweepMode \"scenes\" is not supported with contact detection, the accelerator "
+                                     "or evaluateConvergence");
+        if (p.sweepMode == "merged" || !scenes_ok || (p.sweepMode == "auto" && !p.autotune)) {
+            h->eng.reset(make(gaia::kSweepMerged));
+        } else if (p.sweepMode == "scenes") {
+            h->eng.reset(make(gaia::kSweepScenes));
+        } else {
+            // autotuned: both schedules built and their sweep graphs timed; the faster is kept
+            std::unique_ptr<gaia::EngineBase> a(make(gaia::kSweepMerged));
+            const double ta = a->measure_sweep_ms();
+            std::unique_ptr<gaia::EngineBase> b(make(gaia::kSweepScenes));
+            const double tb = b->measure_sweep_ms();
+            h->sweep_ms[0] = ta;
+            h->sweep_ms[1] = tb;
+            h->eng = tb < ta ? std::move(b) : std::move(a);
+        }
     });
 }
 
@@ -1500,6 +1817,23 @@ int gaia_vbd_energy(gaia_vbd* h, double* out) {
     return guarded(h, [&] { *out = h->eng->energy(); });
 }
 
+int gaia_vbd_convergence(gaia_vbd* h, double* out4) {
+    GAIA_NEED(h);
+    if (!out4) return GAIA_VBD_E_INVALID_ARG;
+    return guarded(h, [&] { h->eng->convergence(out4); });
+}
+
+int gaia_vbd_get_convergence_log(gaia_vbd* h, double* rows, int32_t cap, int32_t* n_rows) {
+    GAIA_NEED(h);
+    return guarded(h, [&] {
+        std::vector<double> r;
+        h->eng->convergence_log(r);
+        const int32_t n = int32_t(r.size() / 6);
+        if (n_rows) *n_rows = n;
+        if (rows) std::copy(r.begin(), r.begin() + 6 * std::min(n, std::max(cap, 0)), rows);
+    });
+}
+
 int gaia_vbd_vertex_force_hessian(gaia_vbd* h, int32_t mesh, int32_t vertex, int32_t apply_friction, double* f3,
                                   double* h9) {
     GAIA_NEED(h);
@@ -1517,7 +1851,11 @@ int gaia_vbd_get_stats(gaia_vbd* h, gaia_vbd_stats* out) {
     GAIA_NEED(h);
     if (!out) return GAIA_VBD_E_INVALID_ARG;
     std::memset(out, 0, sizeof(*out));
-    return guarded(h, [&] { h->eng->stats(out); });
+    return guarded(h, [&] {
+        h->eng->stats(out);
+        out->sweep_ms_merged = h->sweep_ms[0];
+        out->sweep_ms_scenes = h->sweep_ms[1];
+    });
 }
 
 int gaia_vbd_get_output_params(const gaia_vbd* h, gaia_vbd_output_params* out) {

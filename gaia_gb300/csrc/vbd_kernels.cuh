@@ -468,6 +468,40 @@ __global__ void __launch_bounds__(128) k_contact_color(Ptrs<ST, R> P, Consts<R> 
     }
 }
 
+// The incidence loop of one lane: records r, r + L, ... below e, the first (`cur`) already
+// loaded; two-stage pipeline (the next record is in flight during this incidence).
+// COHERENT: neighbour states with plain loads, for a kernel that itself wrote them
+// earlier (the persistent sweep); otherwise through the read-only cache.
+template <int L, typename ST, typename R, bool COHERENT>
+__device__ __forceinline__ void accumulate_records(const Ptrs<ST, R>& P, int r, int e, RecRaw<R> cur,
+                                                   const typename ST::U& uo, R mu, R lmbd, Acc<R>& acc) {
+    using U = typename ST::U;
+    while (r < e) {
+        const int rn = r + L;
+        RecRaw<R> nxt;
+        if (rn < e) nxt.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, rn);
+        U q0, q1, q2;
+        if constexpr (COHERENT) {
+            q0 = ST::ld(P.u, cur.n.x);
+            q1 = ST::ld(P.u, cur.n.y);
+            q2 = ST::ld(P.u, cur.n.z);
+        } else {
+            q0 = ST::ldg(P.u, cur.n.x);
+            q1 = ST::ldg(P.u, cur.n.y);
+            q2 = ST::ldg(P.u, cur.n.z);
+        }
+        R m0[3], m1[3], m2[3];
+        cur.rows(m0, m1, m2);
+        R e0[3], e1[3], e2[3];
+        ST::diff(q0, uo, e0);
+        ST::diff(q1, uo, e1);
+        ST::diff(q2, uo, e2);
+        incidence<R>(e0, e1, e2, m0, m1, m2, mu, lmbd, acc);
+        cur = nxt;
+        r = rn;
+    }
+}
+
 // Minimum resident blocks of 256 threads: caps FP32-compute kernels at 64
 // registers (32 warps per SM, no spills); the FP64 kernel keeps its registers.
 template <typename R>
@@ -501,22 +535,7 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
     pdl_wait();
     if (valid) {
         uo = P.u[v];
-        while (r < e) {
-            // two-stage pipeline: the next record is in flight during this incidence
-            const int rn = r + L;
-            RecRaw<R> nxt;
-            if (rn < e) nxt.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, rn);
-            const U q0 = ST::ldg(P.u, cur.n.x), q1 = ST::ldg(P.u, cur.n.y), q2 = ST::ldg(P.u, cur.n.z);
-            R m0[3], m1[3], m2[3];
-            cur.rows(m0, m1, m2);
-            R e0[3], e1[3], e2[3];
-            ST::diff(q0, uo, e0);
-            ST::diff(q1, uo, e1);
-            ST::diff(q2, uo, e2);
-            incidence<R>(e0, e1, e2, m0, m1, m2, mat.mu, mat.lmbd, acc);
-            cur = nxt;
-            r = rn;
-        }
+        accumulate_records<L, ST, R, false>(P, r, e, cur, uo, mat.mu, mat.lmbd, acc);
     }
     reduce_group<L, R>(acc);
     if (!valid || lane != 0) return;
@@ -757,6 +776,63 @@ __global__ void __launch_bounds__(256, 4)
     vertex_tail<ST, float, false>(P, c, v, uo, mat, acc, friction, nullptr, beg, end);
 }
 
+// ---------------------------------------------------------------------------
+// Persistent scene-major sweep: every iteration of a substep in one launch. Each block
+// takes whole scenes (meshes) from a work counter, in the order `scene_order` (largest
+// first), and runs all `iterations` of that scene: per iteration its colors in sequence,
+// each color's vertices over the block's vertex groups, a block barrier between colors.
+// Meshes do not interact (no contact records in this mode), so per mesh the sequence
+// of color updates, and every vertex's arithmetic, equal the merged color-major sweep's;
+// a scene's records and states stay in the block's L1 / the L2 across its iterations,
+// and no launch or device-wide barrier separates colors. Layout: the slots of a mesh
+// are contiguous and color-major within it; colors[scene_ofs[m] .. scene_ofs[m + 1])
+// are mesh m's color slot ranges in sweep order.
+// ---------------------------------------------------------------------------
+template <int L, typename ST, typename R>
+__global__ void __launch_bounds__(1024) k_sweep_scenes(Ptrs<ST, R> P, Consts<R> c, const int2* colors,
+                                                       const int32_t* scene_ofs, const int32_t* scene_order,
+                                                       int32_t nscenes, int32_t iterations, int32_t friction_start,
+                                                       int32_t* work) {
+    using U = typename ST::U;
+    __shared__ int s_scene;
+    const int groups = int(blockDim.x) / L;
+    const int g = int(threadIdx.x) / L;
+    const int lane = int(threadIdx.x) & (L - 1);
+    for (;;) {
+        if (threadIdx.x == 0) s_scene = atomicAdd(work, 1);
+        __syncthreads();
+        const int k = s_scene;
+        __syncthreads();  // every thread has read s_scene before it is written again
+        if (k >= nscenes) return;
+        const int sc = scene_order[k];
+        const int c0 = scene_ofs[sc], c1 = scene_ofs[sc + 1];
+        for (int it = 0; it < iterations; ++it) {
+            const int friction = it >= friction_start ? 1 : 0;
+            for (int ci = c0; ci < c1; ++ci) {
+                const int2 rg = colors[ci];
+                for (int base = rg.x; base < rg.y; base += groups) {
+                    const int v = base + g;
+                    const bool valid = v < rg.y;
+                    Acc<R> acc = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+                    U uo{};
+                    MeshMat<R> mat;
+                    if (valid) {
+                        mat = P.mats[P.slot_mesh[v]];
+                        const int r = P.inc_ofs[v] + lane, e = P.inc_ofs[v + 1];
+                        RecRaw<R> cur;
+                        if (r < e) cur.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r);
+                        uo = ST::ld(P.u, v);
+                        accumulate_records<L, ST, R, true>(P, r, e, cur, uo, mat.mu, mat.lmbd, acc);
+                    }
+                    reduce_group<L, R>(acc);
+                    if (valid && lane == 0) vertex_tail<ST, R, false>(P, c, v, uo, mat, acc, friction, nullptr, rg.x, rg.y);
+                }
+                __syncthreads();  // this color's updates before the next color reads them
+            }
+        }
+    }
+}
+
 // Initial step of a substep over all slots: VBD_BaseMaterial.h:201-259 and
 // VBD_BaseMaterial.cpp:7-31 (initialization types 0..4). Displacements: every
 // update is linear in x, so it reads as in positions.
@@ -981,78 +1057,6 @@ __global__ void k_scatter_velocities_f64(typename ST::V* vel, const double* in, 
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     vel[slot_of[i]] = typename ST::V{Sc(in[3 * size_t(i)]), Sc(in[3 * size_t(i) + 1]), Sc(in[3 * size_t(i) + 2]), Sc(0)};
-}
-
-// ---------------------------------------------------------------------------
-// Energy: per-tet Neo-Hookean energy with the rest energy removed
-// (VBDPhysicsCompute.cu:1775-1810) and inertia energy 1/(2dt^2) m |x-y|^2
-// (VBD_BaseMaterial.h:223-241), evaluated and reduced in FP64.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void block_add(double val, double* out) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) val += __shfl_xor_sync(0xffffffffu, val, off);
-    __shared__ double part[32];
-    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) part[w] = val;
-    __syncthreads();
-    if (w == 0) {
-        val = l < (blockDim.x >> 5) ? part[l] : 0.0;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) val += __shfl_xor_sync(0xffffffffu, val, off);
-        if (l == 0) atomicAdd(out, val);
-    }
-}
-
-// mu_lmbd: per mesh (mu, lambda) in FP64.
-template <typename ST>
-__global__ void k_energy_tets(const typename ST::U* u, const float4* rest, const int4* tet_slots,
-                              const double* tet_dminv, const double* tet_vol, const int32_t* tet_mesh,
-                              const double2* mu_lmbd, int32_t ntet, double* out) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    double e = 0.0;
-    if (t < ntet) {
-        int4 sv = tet_slots[t];
-        const int ids[4] = {sv.x, sv.y, sv.z, sv.w};
-        double p[4][3];
-        for (int k = 0; k < 4; ++k) {
-            ST::to_d(u[ids[k]], p[k]);
-            const float4 X = rest[ids[k]];
-            p[k][0] += double(X.x);
-            p[k][1] += double(X.y);
-            p[k][2] += double(X.z);
-        }
-        double Ds[9] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2],
-                        p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2],
-                        p[3][0] - p[0][0], p[3][1] - p[0][1], p[3][2] - p[0][2]};
-        const double* Di = tet_dminv + 9 * size_t(t);
-        double F[9];
-        for (int cc = 0; cc < 3; ++cc)
-            for (int r = 0; r < 3; ++r)
-                F[3 * cc + r] = Ds[r] * Di[3 * cc] + Ds[3 + r] * Di[3 * cc + 1] + Ds[6 + r] * Di[3 * cc + 2];
-        double det = F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
-                     F[6] * (F[1] * F[5] - F[4] * F[2]);
-        double n2 = 0;
-        for (int i = 0; i < 9; ++i) n2 += F[i] * F[i];
-        const double2 ml = mu_lmbd[tet_mesh[t]];
-        double mu = ml.x, lm = ml.y, a = 1.0 + mu / lm, A = tet_vol[t];
-        e = A * (mu * 0.5 * (n2 - 3.0) + lm * 0.5 * (det - a) * (det - a)) - 0.5 * A * lm * (1.0 - a) * (1.0 - a);
-    }
-    block_add(e, out);
-}
-
-template <typename ST>
-__global__ void k_energy_inertia(const typename ST::U* u, const typename ST::U* y, int32_t n, double half_dt2inv,
-                                 double* out) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    double e = 0.0;
-    if (s < n) {
-        double p[3], q[3];
-        ST::to_d(u[s], p);
-        ST::to_d(y[s], q);
-        double dx = p[0] - q[0], dy = p[1] - q[1], dz = p[2] - q[2];
-        e = half_dt2inv * ST::mass(u[s]) * (dx * dx + dy * dy + dz * dz);
-    }
-    block_add(e, out);
 }
 
 }  // namespace dev

@@ -8,7 +8,7 @@
 //           GB300 executes FP64 at a small fraction of its FP32 rate.
 //   StF64 : displacement as FP64                          (32 B per vertex, w = mass)
 //
-// Each trait provides load / read-only load / store, a - b rounded to the
+// Each trait provides read-only (ldg) and coherent (ld) loads, a - b rounded to the
 // compute type R, a + d for a delta d in the velocity type, conversions from
 // and to double, and (c - X - u) for the world-box tests.
 #pragma once
@@ -56,6 +56,11 @@ struct StF32 {
         float4 v = __ldg(reinterpret_cast<const float4*>(p) + i);
         return U{v.x, v.y, v.z, v.w};
     }
+    // coherent load: for state written earlier in the same kernel (ordered by a barrier)
+    __device__ static U ld(const U* p, int i) {
+        float4 v = reinterpret_cast<const float4*>(p)[i];
+        return U{v.x, v.y, v.z, v.w};
+    }
     template <typename R>
     __device__ static void diff(const U& a, const U& b, R* o) {
         o[0] = R(a.x - b.x); o[1] = R(a.y - b.y); o[2] = R(a.z - b.z);
@@ -81,6 +86,11 @@ struct StF64 {
     __device__ static U ldg(const U* p, int i) {
         const double2* q = reinterpret_cast<const double2*>(p + i);
         double2 a = __ldg(q), b = __ldg(q + 1);
+        return U{a.x, a.y, b.x, b.y};
+    }
+    __device__ static U ld(const U* p, int i) {
+        const double2* q = reinterpret_cast<const double2*>(p + i);
+        double2 a = q[0], b = q[1];
         return U{a.x, a.y, b.x, b.y};
     }
     template <typename R>
@@ -120,6 +130,11 @@ struct StDF {
     __device__ static U ldg(const U* p, int i) {
         const float4* q = reinterpret_cast<const float4*>(p + i);
         float4 a = __ldg(q), b = __ldg(q + 1);
+        return U{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    }
+    __device__ static U ld(const U* p, int i) {
+        const float4* q = reinterpret_cast<const float4*>(p + i);
+        float4 a = q[0], b = q[1];
         return U{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     }
     // (a.hi - b.hi) + (a.lo - b.lo): relative error ~2^-23 of the result

@@ -263,6 +263,24 @@ class VBDPhysics:
         _check(lib().gaia_vbd_energy(self.handle, C.byref(e)), self.handle)
         return e.value
 
+    def evaluateConvergence(self) -> dict:
+        """evaluateConvergenceGPU on the current state, reduced in FP64 in a fixed order:
+        energy, inertia and elastic energy, average force norm."""
+        out = np.empty(4, np.float64)
+        _check(lib().gaia_vbd_convergence(self.handle, out.ctypes.data), self.handle)
+        return {"energy": out[0], "inertia": out[1], "elastic": out[2], "avg_force_norm": out[3]}
+
+    def convergenceLog(self) -> np.ndarray:
+        """The last step's in-graph records (PhysicsParams evaluateConvergence): rows of
+        substep, iteration (-1 = initial guess), energy, inertia, elastic, avg force norm."""
+        n = C.c_int32()
+        _check(lib().gaia_vbd_get_convergence_log(self.handle, None, 0, C.byref(n)), self.handle)
+        rows = np.zeros((n.value, 6), np.float64)
+        if n.value:
+            _check(lib().gaia_vbd_get_convergence_log(self.handle, rows.ctypes.data, n.value, C.byref(n)),
+                   self.handle)
+        return rows
+
     def vertexForceHessian(self, mesh: int, v: int, apply_friction: bool = True):
         f = np.empty(3, np.float64)
         H = np.empty(9, np.float64)

@@ -73,14 +73,49 @@ def lattice_cube(n: tuple[int, int, int], spacing: float = 0.01, origin=(0.0, 0.
     return X, tets.astype(np.int32)
 
 
+# Who writes mesh and coloring files: "library" (the product's writers and colorings) or
+# "oracle" (plain-Python writers and the oracle's colorings, for the CPU reference arm of
+# the benchmark, which must not load the product library).
+_WRITER = "library"
+
+
+def set_writer(name: str) -> None:
+    global _WRITER
+    if name not in ("library", "oracle"):
+        raise ValueError(name)
+    _WRITER = name
+
+
+def _py_write_t(path: str, X: np.ndarray, tets: np.ndarray) -> None:
+    """The .t format the library writes ("Vertex id x y z" with %.9g, "Tet id a b c d")."""
+    X = np.asarray(X, np.float64)
+    with open(path, "w") as f:
+        f.writelines("Vertex %d %.9g %.9g %.9g\n" % (i, x[0], x[1], x[2]) for i, x in enumerate(X))
+        f.writelines("Tet %d %d %d %d %d\n" % (i, t[0], t[1], t[2], t[3]) for i, t in enumerate(np.asarray(tets)))
+
+
+def _py_write_categories(path: str, colors: np.ndarray, order: np.ndarray) -> None:
+    cats = [[] for _ in range(int(np.max(colors)) + 1)]
+    for v in np.asarray(order).tolist():
+        cats[int(colors[v])].append(v)
+    with open(path, "w") as f:
+        f.write("[" + ",".join("[" + ",".join(map(str, c)) + "]" for c in cats) + "]")
+
+
 def _write_mesh(dirname: str, name: str, X: np.ndarray, tets: np.ndarray, coloring: str = "tool") -> tuple[str, str]:
     """.t mesh plus its vertex coloring file. coloring = "tool": what the reference's
     GraphColoring tool writes by default (MCS, categories balanced to a 1.05 size ratio);
     "mcs" / "greedy": the plain algorithms."""
-    from .physics import color_greedy, color_mcs, color_tool, write_categories, write_coloring, write_t
     os.makedirs(dirname, exist_ok=True)
     tpath = os.path.join(dirname, name + ".t")
     cpath = tpath + ".vertexColoring.json"
+    if _WRITER == "oracle":
+        from oracle.scene_colorings import tet_coloring
+
+        _py_write_t(tpath, X, tets)
+        _py_write_categories(cpath, *tet_coloring(len(X), np.asarray(tets, np.int32), coloring))
+        return tpath, cpath
+    from .physics import color_greedy, color_mcs, color_tool, write_categories, write_coloring, write_t
     write_t(tpath, X, tets)
     if coloring == "tool":
         colors, order = color_tool(len(X), tets)
@@ -462,10 +497,16 @@ def cloth_on_sphere(dirname: str, n: int = 512, side: float = 1.0, sphere_radius
     X, F = cloth_grid(n, side, sphere_radius + gap, noise, seed)
     cpath = os.path.join(dirname, f"cloth{n}.obj")
     write_obj(cpath, X, F)
-    from .cloth import color_trimesh_tool
-    from .physics import write_categories
     colpath = cpath + ".vertexColoring.json"
-    write_categories(colpath, *color_trimesh_tool(len(X), F))  # the coloring tool's default
+    if _WRITER == "oracle":
+        from oracle.scene_colorings import trimesh_coloring
+
+        _py_write_categories(colpath, *trimesh_coloring(len(X), np.asarray(F, np.int32)))
+    else:
+        from .cloth import color_trimesh_tool
+        from .physics import write_categories
+
+        write_categories(colpath, *color_trimesh_tool(len(X), F))  # the coloring tool's default
     SX, SF = icosphere(sphere_level, sphere_radius)
     spath = os.path.join(dirname, f"sphere{sphere_level}.obj")
     write_obj(spath, SX, SF)

@@ -67,6 +67,11 @@ typedef struct {
     int64_t device_timeouts;          /* blocks whose bounded wait (staged records, grid barrier) ran
                                          out; the call that reports it returns GAIA_VBD_E_DEVICE_TIMEOUT */
     int64_t nonfinite_solves;         /* vertex solves with a non-finite force or step (not written) */
+    int32_t sweep_mode;               /* color scheduling: 0 = merged colors (a launch per merged color
+                                         and iteration), 1 = scene-major persistent sweep (solve_variant 2) */
+    int32_t reserved2;
+    double sweep_ms_merged;           /* sweep time per iteration the autotuner measured for each */
+    double sweep_ms_scenes;           /* schedule (0 when it did not compare them) */
 } gaia_vbd_stats;
 
 /* ---- life cycle ------------------------------------------------------------
@@ -78,8 +83,11 @@ typedef struct {
  * (computing the reference's OrderedGreedy coloring when a model gives no
  * coloring file), precomputes the rest shape in FP64, merges colors into
  * parallel groups and uploads everything. repo_root may be NULL.
- * Extra PhysicsParams keys: "gpuPrecision" ("fp32" | "fp64"),
- * "lanesPerVertex", "blockSize" (0 = autotune), "autotune" (bool).
+ * Extra PhysicsParams keys: "gpuPrecision" ("fp32" | "mixed" | "fp64"),
+ * "lanesPerVertex", "blockSize" (0 = autotune), "autotune" (bool), "sweepMode"
+ * ("auto" | "merged" | "scenes": color scheduling, see gaia_vbd_stats.sweep_mode; auto
+ * times both and keeps the faster when the scene allows the scene-major sweep, which needs
+ * contact detection, the accelerator and evaluateConvergence off).
  */
 int gaia_vbd_create(const char* models_json, const char* params_json, const char* repo_root, gaia_vbd** out);
 /* The two halves of gaia_vbd_create. gaia_vbd_load is host-only (no GPU needed):
@@ -178,8 +186,20 @@ int gaia_vbd_get_coloring(const gaia_vbd* h, int32_t mesh, int32_t* colors);
 int gaia_vbd_get_rest_shape(const gaia_vbd* h, int32_t mesh, double* dminv, double* vol, double* mass);
 /* Total Neo-Hookean elastic energy (rest energy removed) plus inertia energy
  * (VBDPhysicsCompute.cu:1223-1237, 1775-1810; VBD_BaseMaterial.h:223-241), evaluated on
- * the device and reduced in FP64. */
+ * the device and reduced in FP64 in a fixed order (gaia_vbd_convergence). */
 int gaia_vbd_energy(gaia_vbd* h, double* out);
+/* evaluateConvergenceGPU (VBD/VBDPhysics.cpp:3508-3556, with evaluateMeritEnergyGPU :3851-3871)
+ * on the current state, reduced in FP64 in a fixed order (repeated calls on one state
+ * return bit-identical values): out4 = total energy, inertia energy (all vertices),
+ * elastic energy, and the average over all vertices of the norm of the material (with
+ * damping) plus inertia force, zero for fixed vertices. gaia_vbd_energy returns out4[0]. */
+int gaia_vbd_convergence(gaia_vbd* h, double* out4);
+/* With PhysicsParams evaluateConvergence, every step records the same four values on the
+ * device, inside its CUDA graphs, at iteration -1 (the initial guess) and after iterations
+ * 0, evaluationSteps, 2 * evaluationSteps, ... of every substep (VBDPhysics.cpp:866-870,
+ * 948-951). This returns the last step's records, 6 doubles each: substep, iteration,
+ * energy, inertia, elastic, average force norm (n_rows = count; at most cap written). */
+int gaia_vbd_get_convergence_log(gaia_vbd* h, double* rows, int32_t cap, int32_t* n_rows);
 /* Per-vertex force and 3x3 Hessian (material + inertia + ground) at the current state,
  * computed by the solve kernel without moving the vertex: f3 = 3 values, h9 = 9 (row-major). */
 int gaia_vbd_vertex_force_hessian(gaia_vbd* h, int32_t mesh, int32_t vertex, int32_t apply_friction,

@@ -119,6 +119,7 @@ def lib():
         L.oracle_energy.argtypes = [C.c_void_p]
         L.oracle_energy.restype = C.c_double
         L.oracle_solve_failures.argtypes = [C.c_void_p]
+        L.oracle_convergence.argtypes = [C.c_void_p, C.c_void_p]
         L.oracle_nh_element.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double,
                                         C.c_int32, C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_void_p]
         L.oracle_set_prev_positions.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
@@ -227,6 +228,24 @@ def color_greedy(nv: int, tets: np.ndarray) -> np.ndarray:
     if n < 0:
         raise RuntimeError("oracle greedy coloring failed")
     return out
+
+
+def color_tool(nv: int, tets: np.ndarray, algorithm: str = "mcs", balance: bool = True,
+               goal_ratio: float = 1.05) -> tuple[np.ndarray, np.ndarray]:
+    """The reference's GraphColoring tool (MCS or OrderedGreedy, then balancing), O(V^2) as
+    the reference writes it: (colors, vertex order of the written categories)."""
+    tets = np.ascontiguousarray(tets, np.int32)
+    colors = np.empty(nv, np.int32)
+    order = np.empty(nv, np.int32)
+    L = lib()
+    L.oracle_color_tool.restype = C.c_int32
+    L.oracle_color_tool.argtypes = [C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_void_p,
+                                    C.c_void_p]
+    n = L.oracle_color_tool(nv, len(tets), tets.ctypes.data, 0 if algorithm == "mcs" else 1, int(balance),
+                            goal_ratio, colors.ctypes.data, order.ctypes.data)
+    if n < 0:
+        raise RuntimeError("coloring failed")
+    return colors, order
 
 
 def colors_to_categories(colors: np.ndarray) -> list[list[int]]:
@@ -401,6 +420,12 @@ class OracleScene:
         if n:
             lib().oracle_get_contacts(self.h, rows.ctypes.data, n)
         return rows
+
+    def convergence(self) -> dict:
+        """evaluateConvergence in FP64: energy, inertia, elastic, average force norm."""
+        out = np.empty(4, np.float64)
+        lib().oracle_convergence(self.h, out.ctypes.data)
+        return {"energy": out[0], "inertia": out[1], "elastic": out[2], "avg_force_norm": out[3]}
 
     def solve_failures(self) -> int:
         return int(lib().oracle_solve_failures(self.h))

@@ -1053,6 +1053,45 @@ double energy(Scene<R>& s) {
     return E;
 }
 
+// evaluateConvergence (VBDPhysics.cpp:3459-3506) in FP64: energy, inertia, elastic, and
+// the average over all vertices of |material force (with damping) + inertia force|,
+// zero for fixed vertices.
+template <typename R>
+void convergence(Scene<R>& s, double* out) {
+    double total = energy(s), inertia = 0.0, fsum = 0.0;
+    int64_t nall = 0;
+    for (auto& m : s.meshes) {
+        for (int i = 0; i < m.nv; ++i) {
+            double d2 = 0;
+            for (int d = 0; d < 3; ++d) {
+                const double q = double(m.x[3 * size_t(i) + d]) - double(m.y[3 * size_t(i) + d]);
+                d2 += q * q;
+            }
+            inertia += 0.5 * s.dt2inv * double(m.mass[i]) * d2;
+        }
+        nall += m.nv;
+        if (!m.active) continue;
+        std::vector<double> fn(size_t(m.nv), 0.0);
+        s.pool->run(m.nv, [&](int64_t b, int64_t e) {
+            for (int64_t i = b; i < e; ++i) {
+                if (m.fixed[i]) continue;
+                R f[3] = {0, 0, 0}, H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                material_force_hessian<R>(m, int(i), R(s.dt), f, H);
+                const double w = double(m.mass[i]) * s.dt2inv;
+                double g[3];
+                for (int d = 0; d < 3; ++d)
+                    g[d] = double(f[d]) + w * (double(m.y[3 * size_t(i) + d]) - double(m.x[3 * size_t(i) + d]));
+                fn[size_t(i)] = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+            }
+        });
+        for (double v : fn) fsum += v;
+    }
+    out[0] = total;
+    out[1] = inertia;
+    out[2] = total - inertia;
+    out[3] = nall ? fsum / double(nall) : 0.0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1171,6 +1210,65 @@ void oracle_nh_element(const double* x12, const double* xprev12, const double* d
     tet_force_hessian<double>(x12, dminv9, A, order, mu, lmbd, kh, kd, dt, disp, f, h);
 }
 
+// The GraphColoring tool's pipeline (GraphColoring/GraphColoring.cpp:170-189): MCS
+// (algorithm 0) or OrderedGreedy (1), categories in color order with vertices ascending,
+// then, with balance, balanceColoredCategories (ColoringAlgorithms.cpp:142-196): move the
+// first vertex of the largest category (or of the first other category that has one) that
+// no neighbour of the smallest category blocks to the end of the smallest, the loop body
+// running once before the max/min size ratio is compared with the goal. colors: each
+// vertex's color; order: the vertices of every category in the order the tool writes them.
+int32_t oracle_color_tool(int32_t nv, int32_t ntet, const int32_t* tets, int32_t algorithm, int32_t balance,
+                          float goal, int32_t* colors, int32_t* order) {
+    const int32_t n = algorithm == 0 ? oracle_color_mcs(nv, ntet, tets, colors)
+                                     : oracle_color_greedy(nv, ntet, tets, colors);
+    if (n <= 0) return n;
+    std::vector<std::vector<int>> cats(static_cast<size_t>(n));
+    for (int v = 0; v < nv; ++v) cats[size_t(colors[v])].push_back(v);
+    if (balance) {
+        auto g = vertex_graph(nv, ntet, tets);
+        auto free_in = [&](int src, int dst) {
+            const auto& c = cats[size_t(src)];
+            for (size_t i = 0; i < c.size(); ++i) {
+                bool ok = true;
+                for (int nb : g[size_t(c[i])])
+                    if (colors[nb] == dst) { ok = false; break; }
+                if (ok) return int(i);
+            }
+            return -1;
+        };
+        const int64_t cap = 64 * int64_t(nv) + 1024;
+        int64_t moves = 0;
+        float ratio;
+        do {
+            if (++moves > cap) return -1;
+            int big = 0, small = 0;
+            for (int c = 0; c < n; ++c) {
+                if (cats[size_t(big)].size() < cats[size_t(c)].size()) big = c;
+                if (cats[size_t(small)].size() > cats[size_t(c)].size()) small = c;
+            }
+            ratio = float(cats[size_t(big)].size()) / float(cats[size_t(small)].size());
+            int id = free_in(big, small);
+            if (id < 0)
+                for (int c = 0; c < n && id < 0; ++c) {
+                    if (c == big || c == small) continue;
+                    id = free_in(c, small);
+                    if (id >= 0) big = c;
+                }
+            if (id < 0) break;
+            const int node = cats[size_t(big)][size_t(id)];
+            colors[node] = small;
+            cats[size_t(big)].erase(cats[size_t(big)].begin() + id);
+            cats[size_t(small)].push_back(node);
+        } while (ratio > goal);
+    }
+    if (order) {
+        size_t k = 0;
+        for (auto& c : cats)
+            for (int v : c) order[k++] = v;
+    }
+    return n;
+}
+
 void* oracle_create(int32_t precision, int32_t nmesh, const OracleMesh* meshes, const OracleParams* params,
                     int32_t ndef, const OracleDeformer* defs, int32_t nthreads) {
     Handle* h = new Handle();
@@ -1266,6 +1364,10 @@ void oracle_vertex_force_hessian(void* h, int32_t mesh, int32_t v, int32_t apply
 double oracle_energy(void* h) {
     return dispatch(h, [&](auto& s) { return energy(s); });
 }
+void oracle_convergence(void* h, double* out4) {
+    dispatch(h, [&](auto& s) { convergence(s, out4); });
+}
+
 int32_t oracle_solve_failures(void* h) {
     return dispatch(h, [&](auto& s) { return int32_t(s.failures.load()); });
 }

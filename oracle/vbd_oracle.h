@@ -85,6 +85,10 @@ int32_t oracle_read_t(const char* path, int32_t* nv, int32_t* ntet, double* X, i
 /* Graph coloring restatements (return number of colors, -1 on error). */
 int32_t oracle_color_mcs(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
 int32_t oracle_color_greedy(int32_t nv, int32_t ntet, const int32_t* tets, int32_t* colors);
+/* The GraphColoring tool: MCS (0) or OrderedGreedy (1), then balanceColoredCategories when
+ * balance != 0; colors per vertex and the written categories' vertex order. */
+int32_t oracle_color_tool(int32_t nv, int32_t ntet, const int32_t* tets, int32_t algorithm, int32_t balance,
+                          float goal, int32_t* colors, int32_t* order);
 
 /* Simulation. precision = 64 (double) or 32 (float). nthreads <= 0: all cores. */
 void* oracle_create(int32_t precision, int32_t nmesh, const OracleMesh* meshes,
@@ -108,6 +112,9 @@ void oracle_vertex_force_hessian(void* h, int32_t mesh, int32_t v, int32_t apply
 /* Total elastic (Neo-Hookean, rest energy removed) + inertia energy, in double. */
 double oracle_energy(void* h);
 int32_t oracle_solve_failures(void* h);
+/* evaluateConvergence in FP64: energy, inertia energy, elastic energy, average force norm
+ * (material with damping plus inertia; zero for fixed vertices; over all vertices). */
+void oracle_convergence(void* h, double* out4);
 /* One tet's Neo-Hookean force (3) and Hessian (9, row-major) on its vertex `order` in
  * FP64, the per-tet term of oracle_vertex_force_hessian; accumulated into f and h. */
 void oracle_nh_element(const double* x12, const double* xprev12, const double* dminv9, double mu, double lmbd,

@@ -153,10 +153,10 @@ def test_fp64_retry_of_ill_conditioned_block(tmp_path, precision, oracle_lib, ga
         assert rel <= 1e-9
     else:
         # the FP32 LDL^T rejects a pivot and the FP64 retry solves the FP32-accumulated
-        # block; its condition number (1e6) times FP32 rounding bounds the error in the
-        # soft direction
+        # block (measured 1e-7; its condition number, 1e6, amplifies FP32 rounding in the
+        # soft direction)
         assert st["fp64_fallback_solves"] > 0
-        assert rel <= 5e-2
+        assert rel <= 1e-5
     phys.close()
 
 

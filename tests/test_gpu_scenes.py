@@ -1,0 +1,138 @@
+"""The scene-major persistent sweep (sweepMode "scenes", k_sweep_scenes) and the autotuned
+choice of color scheduling.
+
+In this mode one launch per substep runs every scene's iterations: each block takes whole
+meshes, their colors in the merged groups' order, a block barrier between colors. Meshes
+do not interact there, so per mesh the update sequence equals the merged sweep's:
+- against the FP64 oracle at the parity tolerances (the plain-drop configuration, a batch
+  of uneven cubes with different materials, the twist with its rotating face);
+- bit-identical to the merged sweep when both use the same lanes per vertex;
+- the autotuner times both schedules and keeps the faster (stats report both times);
+- the mode is refused where it cannot hold: contact detection on.
+"""
+import numpy as np
+import pytest
+
+from gaia_gb300._lib import E_UNSUPPORTED, GaiaError
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-9, "mixed": 1e-5, "fp32": 1e-5}
+
+
+def _run(mp, pp, precision, steps, **over):
+    from gaia_gb300 import VBDPhysics, scenes
+
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, scenes.set_precision(pp, precision, out_path=pp + f".{precision}.s.json", **over))
+    phys.initialize()
+    x0 = [phys.positions(m) for m in range(phys.numMeshes())]
+    phys.runStep(steps)
+    phys.synchronize()
+    xs = [phys.positions(m) for m in range(phys.numMeshes())]
+    st = phys.stats()
+    phys.close()
+    return np.concatenate(x0), np.concatenate(xs), st
+
+
+def _oracle(mp, pp, steps, oracle_lib):
+    from oracle import scene_io
+
+    sc = scene_io.load_scene(mp, pp)
+    o = oracle_lib.OracleScene(sc, precision=64, nthreads=0)
+    o.step(steps)
+    return np.concatenate([o.positions(m) for m in range(len(sc["meshes"]))])
+
+
+def _rel(x, xr, x0):
+    return float(np.linalg.norm(x - xr) / np.linalg.norm(xr - x0))
+
+
+@pytest.fixture(scope="module")
+def plain_drop(tmp_path_factory, gaia_lib, oracle_lib):
+    from gaia_gb300 import scenes
+
+    d = tmp_path_factory.mktemp("plain_drop_s")
+    mp, pp = scenes.drop_cube(str(d), n=10, iterations=20, coloring="greedy", collision=scenes.NO_CONTACT)
+    return mp, pp, _oracle(mp, pp, 100, oracle_lib)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32"])
+def test_plain_drop_scenes_mode(plain_drop, precision):
+    from tests.test_gpu_parity import FP32_DROP_BOUND
+
+    mp, pp, ref = plain_drop
+    x0, x, st = _run(mp, pp, precision, 100, sweepMode="scenes")
+    assert st["sweep_mode"] == 1 and st["solve_variant"] == 2
+    rel = _rel(x, ref, x0)
+    print(f"plain drop, scenes mode, {precision}: rel {rel:.3e}, lanes {st['lanes_per_vertex']} block "
+          f"{st['block_size']}, {st['kernel_launches_per_step']} launches per step")
+    assert rel <= (FP32_DROP_BOUND if precision == "fp32" else TOL[precision])
+    assert st["kernel_launches_per_step"] <= 4
+
+
+@pytest.fixture(scope="module")
+def batch(tmp_path_factory, gaia_lib, oracle_lib):
+    from gaia_gb300 import scenes
+
+    d = tmp_path_factory.mktemp("batch_s")
+    mp, pp = scenes.batch_cubes(str(d), n_scenes=24, side_range=(3, 9), iterations=8)
+    return mp, pp, _oracle(mp, pp, 30, oracle_lib)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32"])
+def test_batch_scenes_mode(batch, precision):
+    mp, pp, ref = batch
+    x0, x, st = _run(mp, pp, precision, 30, sweepMode="scenes")
+    rel = _rel(x, ref, x0)
+    print(f"batch of 24, scenes mode, {precision}: rel {rel:.3e}")
+    assert st["sweep_mode"] == 1
+    assert rel <= TOL[precision] * (3 if precision == "fp32" else 1)
+
+
+def test_twist_scenes_mode(tmp_path, gaia_lib, oracle_lib):
+    """Fixed faces and the rotator (deformed fixed vertices are neighbours of solved ones)."""
+    from gaia_gb300 import scenes
+
+    mp, pp = scenes.twist_cube(str(tmp_path), n=10, iterations=20)
+    ref = _oracle(mp, pp, 20, oracle_lib)
+    for precision in ("fp64", "mixed", "fp32"):
+        x0, x, st = _run(mp, pp, precision, 20, sweepMode="scenes")
+        assert _rel(x, ref, x0) <= TOL[precision], precision
+
+
+@pytest.mark.parametrize("lanes", [4, 16])
+def test_scenes_mode_equals_merged(batch, lanes):
+    """Same lanes per vertex: the two schedules give bit-identical positions."""
+    mp, pp, _ = batch
+    common = dict(lanesPerVertex=lanes, blockSize=256, autotune=False, smallColorVertices=0, solveVariant=0)
+    _, xa, sa = _run(mp, pp, "mixed", 10, sweepMode="merged", **common)
+    _, xb, sb = _run(mp, pp, "mixed", 10, sweepMode="scenes", **common)
+    assert sa["sweep_mode"] == 0 and sb["sweep_mode"] == 1
+    np.testing.assert_array_equal(xa, xb)
+
+
+def test_autotuner_picks_schedule(plain_drop, batch):
+    for mp, pp, _ in (plain_drop, batch):
+        _, _, st = _run(mp, pp, "mixed", 1)
+        print(f"merged {st['sweep_ms_merged']:.4f} ms/iteration, scenes {st['sweep_ms_scenes']:.4f}: "
+              f"mode {st['sweep_mode']}")
+        assert st["sweep_ms_merged"] > 0 and st["sweep_ms_scenes"] > 0
+        assert st["sweep_mode"] == (1 if st["sweep_ms_scenes"] < st["sweep_ms_merged"] else 0)
+
+
+def test_scenes_mode_refused_with_contact(tmp_path, gaia_lib):
+    from gaia_gb300 import VBDPhysics, scenes
+
+    mp, pp = scenes.drop_cube(str(tmp_path), n=5, iterations=5)  # contact detection on (defaults)
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, scenes.set_precision(pp, "mixed", sweepMode="scenes"))
+    with pytest.raises(GaiaError) as ei:
+        phys.initialize()
+    assert ei.value.code == E_UNSUPPORTED and "sweepMode" in str(ei.value)
+    # auto falls back to the merged schedule there
+    phys2 = VBDPhysics()
+    phys2.loadRunningparameters(mp, scenes.set_precision(pp, "mixed", out_path=pp + ".auto.json"))
+    phys2.initialize()
+    assert phys2.stats()["sweep_mode"] == 0
+    phys2.close()

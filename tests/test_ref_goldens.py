@@ -192,3 +192,32 @@ def test_live_reference_element(live_ref, oracle_lib):
                                        int(T["order"][i]))
         _close(fo, f, TOL64, f"force of tet {i}")
         _close(ho, h.reshape(3, 3).T, TOL64, f"Hessian of tet {i}")
+
+
+def test_oracle_convergence_terms(tmp_path, oracle_lib, gaia_lib):
+    """The oracle's FP64 convergence evaluation (VBDPhysics.cpp:3459-3506): its energy is the
+    reference's per-tet energies summed plus inertia, and its average force norm is the mean
+    over all vertices of |sum of the per-tet material terms (pinned above) + inertia force|."""
+    from oracle import scene_io
+
+    mp, pp = _drop6(tmp_path)
+    sc = scene_io.load_scene(mp, pp)
+    o = oracle_lib.OracleScene(sc, precision=64, nthreads=1)
+    X = o.positions(0)
+    dminv, vol, mass = o.rest(0)
+    o.set_positions(0, G["blk_x"])
+    c = o.convergence()
+    dt = sc["params"]["timeStep"] / sc["params"]["numSubsteps"]
+    inertia = 0.5 / dt ** 2 * float((mass * ((G["blk_x"] - X) ** 2).sum(axis=1)).sum())
+    assert abs(c["elastic"] - float(G["blk_elastic_energy64"])) <= 1e-10 * abs(c["elastic"])
+    assert abs(c["inertia"] - inertia) <= 1e-12 * inertia
+    assert c["energy"] == o.energy()
+    mat = sc["meshes"][0]["material"]
+    T = np.asarray(sc["meshes"][0]["tets"])
+    f = mass[:, None] / dt ** 2 * (X - G["blk_x"])
+    for t in range(len(T)):
+        for k in range(4):
+            ft, _ = oracle_lib.nh_element(G["blk_x"][T[t]], X[T[t]], dminv[t], mat["miu"], mat["lmbd"], vol[t], k)
+            f[T[t, k]] += ft
+    avg = float(np.linalg.norm(f, axis=1).mean())
+    assert abs(c["avg_force_norm"] - avg) <= 1e-10 * avg
