@@ -389,11 +389,12 @@ def cloth_algorithmic_bytes(c) -> tuple[float, dict]:
     return b, {"vertices": nv, "faces": nf, "edges": ne, "interior_edges": interior}
 
 
-def cloth_engine(mp, pp, precision):
+def cloth_engine(mp, pp, precision, **overrides):
     from gaia_gb300 import VBDClothSimulationFramework, scenes
 
     c = VBDClothSimulationFramework()
-    c.loadRunningparameters(mp, scenes.set_precision(pp, precision))
+    c.loadRunningparameters(mp, scenes.set_precision(pp, precision, out_path=pp + f".{precision}.{len(overrides)}.json",
+                                                     **overrides))
     c.initialize()
     return c
 
@@ -439,8 +440,27 @@ def run_cloth(args, world, rank, local):
         ce.runStep(args.error_steps)
         x = ce.positions(0)
         ce.close()
+        # the divergence floor of the drape: two FP64 runs that differ only in summation order
+        # (one and two lanes per vertex, all else equal); a precision mode cannot get closer
+        # to an FP64 run than two FP64 runs get to each other
+        floor = []
+        for lanes in (1, 2):
+            cf = cloth_engine(mp, pp, "fp64", lanesPerVertex=lanes)
+            cf.runStep(args.error_steps)
+            floor.append(cf.positions(0))
+            cf.close()
         err = {"steps": args.error_steps, "rel": float(np.linalg.norm(x - xref) / np.linalg.norm(xref - x0)),
-               "max_abs_m": float(np.abs(x - xref).max()), "reference": "fp64 engine, same kernels"}
+               "max_abs_m": float(np.abs(x - xref).max()), "reference": "fp64 engine, same kernels",
+               "fp64_vs_fp64_summation_order": float(np.linalg.norm(floor[0] - floor[1]) /
+                                                     np.linalg.norm(xref - x0))}
+        steps_short = max(1, args.error_steps // 10)
+        for prec in ("fp32", "fp64"):
+            cs = cloth_engine(mp, pp, prec)
+            cs.runStep(steps_short)
+            err[f"{prec}_after_{steps_short}_steps"] = cs.positions(0)
+            cs.close()
+        a, b = err.pop(f"fp32_after_{steps_short}_steps"), err.pop(f"fp64_after_{steps_short}_steps")
+        err["short_horizon"] = {"steps": steps_short, "rel": float(np.linalg.norm(a - b) / np.linalg.norm(b - x0))}
     c = cloth_engine(mp, pp, "fp32")
     nv = c.numVertices(0)
     for _ in range(args.warmup):
@@ -566,8 +586,8 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=2, help="iterations per cpu_baseline sample of the GPU arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
-    ap.add_argument("--precision", default="auto", choices=["auto", "mixed", "fp32", "fp64"],
-                    help="auto: measure fp32 and mixed, report the fastest within the 1e-5 error bound")
+    ap.add_argument("--precision", default="auto", choices=["auto", "mixed", "dfhi", "fp32", "fp64"],
+                    help="auto: measure fp32, dfhi and mixed, report the fastest within the 1e-5 error bound")
     ap.add_argument("--tolerance", type=float, default=1e-5)
     ap.add_argument("--lanes", type=int, default=0, help="lanes per vertex (0 = autotune)")
     ap.add_argument("--block", type=int, default=0, help="solve block size (0 = autotune)")
@@ -634,7 +654,7 @@ def main():
                 "unit": "vertex-solves/s", "ms_per_step": t64 / args.fp64_steps}
 
     # ---- FP32-compute engines ------------------------------------------------------------
-    modes = ["fp32", "mixed"] if args.precision == "auto" else [args.precision]
+    modes = ["fp32", "dfhi", "mixed"] if args.precision == "auto" else [args.precision]
     runs = [measure_mode(args, mp, pp, m, overrides, world, local, xref) for m in modes]
     ok = [r for r in runs if r["error"] is None or r["error"]["rel"] <= args.tolerance]
     head = max(ok, key=lambda r: r["value"]) if ok else min(runs, key=lambda r: r["error"]["rel"])
@@ -685,8 +705,8 @@ def main():
             "metric": METRIC, "value": head["value"], "unit": "vertex-solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
             "steps_per_s": head["steps_per_s"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32" if head["precision"] == "fp32" else ("f32 (double-float state)"
-                                                               if head["precision"] == "mixed" else "f64"),
+            "dtype": {"fp32": "f32", "mixed": "f32 (double-float state)",
+                      "dfhi": "f32 (double-float state, FP32 neighbour reads)"}.get(head["precision"], "f64"),
             "data": "synthetic (seeded PCG64 lattice)",
             "config": {"workload": workload_name(args), "vertices": n, "solved_incidences": ninc,
                        "precision": head["precision"], "colors": st["num_groups"],

@@ -582,8 +582,8 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
     if (p.evaluationSteps < 1) throw std::runtime_error("evaluationSteps must be >= 1");
     if (p.sweepMode != "auto" && p.sweepMode != "merged" && p.sweepMode != "scenes")
         throw std::runtime_error("sweepMode must be \"auto\", \"merged\" or \"scenes\"");
-    if (p.gpuPrecision != "fp32" && p.gpuPrecision != "mixed" && p.gpuPrecision != "fp64")
-        throw std::runtime_error("gpuPrecision must be \"mixed\", \"fp32\" or \"fp64\"");
+    if (p.gpuPrecision != "fp32" && p.gpuPrecision != "mixed" && p.gpuPrecision != "dfhi" && p.gpuPrecision != "fp64")
+        throw std::runtime_error("gpuPrecision must be \"mixed\", \"dfhi\", \"fp32\" or \"fp64\"");
     p.dt = p.timeStep / p.numSubsteps;
     p.dtSqrReciprocal = 1.0 / (p.dt * p.dt);
 

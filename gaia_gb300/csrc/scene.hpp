@@ -67,7 +67,8 @@ struct PhysicsParams {
     // derived (BasePhysicsFramework.cpp:245-249)
     double dt = -1.0, dtSqrReciprocal = -1.0;
     // GB300 engine keys (extensions; absent in reference files -> defaults)
-    std::string gpuPrecision = "mixed";  // "mixed" (FP64 state, FP32 element math), "fp32" or "fp64"
+    std::string gpuPrecision = "mixed";  // "mixed" (double-float state, FP32 element math), "dfhi" (double-float
+                                         // state read as FP32 by neighbours), "fp32" or "fp64"
     int lanesPerVertex = 0;              // 0 = autotune
     int blockSize = 0;                   // 0 = autotune
     bool autotune = true;

@@ -27,6 +27,7 @@ struct ConvData {
     const int32_t* tet_mesh;   // mesh of each tet
     const double4* mesh_mat;   // per mesh: mu, lambda, dampingHydrostatic, dampingDeviatoric
     const int32_t* slot_mesh;  // mesh of each slot
+    const double* slot_mass;   // FP64 lumped mass of each slot (the states hold it in their own precision)
     const int32_t* inc_ofs;    // per active slot: its incidences [inc_ofs[s], inc_ofs[s + 1])
     const int32_t* inc_tet;    // tet of each incidence
     const int8_t* inc_ord;     // the slot's vertex order in that tet
@@ -118,7 +119,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv_verts(const typename ST::
         double x[3], yy[3];
         ST::to_d(u[s], x);
         ST::to_d(y[s], yy);
-        const double mass = double(ST::mass(u[s]));
+        const double mass = D.slot_mass[s];
         const double w = mass * D.dt2inv;
         const double d0 = yy[0] - x[0], d1 = yy[1] - x[1], d2 = yy[2] - x[2];
         ei = 0.5 * w * (d0 * d0 + d1 * d1 + d2 * d2);
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(kConvThreads) k_conv_verts(const typename ST::
 // Pass 2: one block adds each quantity's partials in index order and writes one record
 // (energy, inertia, elastic, average force norm) to out[4 * k], k = *counter (then
 // incremented) when a counter is given, else k = 0; records beyond cap are dropped.
-__global__ void __launch_bounds__(kConvThreads) k_conv_finish(const double* part_elastic, int nb_t,
+static __global__ void __launch_bounds__(kConvThreads) k_conv_finish(const double* part_elastic, int nb_t,
                                                               const double* part_inertia, const double* part_fnorm,
                                                               int nb_v, double inv_nslots, double* out,
                                                               int32_t* counter, int32_t cap) {

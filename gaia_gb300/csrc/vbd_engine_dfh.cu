@@ -1,0 +1,7 @@
+// The StDFH engine (vbd_engine.cuh), compiled on its own so that the precision modes build in
+// parallel.
+#include "vbd_engine.cuh"
+
+namespace gaia {
+EngineBase* make_engine_dfh(const Scene& s, int mode) { return new Engine<dev::StDFH, float>(s, mode); }
+}  // namespace gaia

@@ -1,0 +1,7 @@
+// The StF32 engine (vbd_engine.cuh), compiled on its own so that the precision modes build in
+// parallel.
+#include "vbd_engine.cuh"
+
+namespace gaia {
+EngineBase* make_engine_f32(const Scene& s, int mode) { return new Engine<dev::StF32, float>(s, mode); }
+}  // namespace gaia

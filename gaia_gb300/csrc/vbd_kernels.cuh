@@ -786,10 +786,11 @@ __global__ void __launch_bounds__(256, 4)
 // a scene's records and states stay in the block's L1 / the L2 across its iterations,
 // and no launch or device-wide barrier separates colors. Layout: the slots of a mesh
 // are contiguous and color-major within it; colors[scene_ofs[m] .. scene_ofs[m + 1])
-// are mesh m's color slot ranges in sweep order.
+// are mesh m's color slot ranges in sweep order. MAXB bounds the block size (and so the
+// registers a thread may use: 256 leaves the compiler all it needs, 1024 caps it at 64).
 // ---------------------------------------------------------------------------
-template <int L, typename ST, typename R>
-__global__ void __launch_bounds__(1024) k_sweep_scenes(Ptrs<ST, R> P, Consts<R> c, const int2* colors,
+template <int L, typename ST, typename R, int MAXB>
+__global__ void __launch_bounds__(MAXB) k_sweep_scenes(Ptrs<ST, R> P, Consts<R> c, const int2* colors,
                                                        const int32_t* scene_ofs, const int32_t* scene_order,
                                                        int32_t nscenes, int32_t iterations, int32_t friction_start,
                                                        int32_t* work) {

@@ -6,6 +6,7 @@
 //           operations only (error-free two-sum), so the state carries ~48
 //           significant bits while no FP64 instruction runs per incidence:
 //           GB300 executes FP64 at a small fraction of its FP32 rate.
+//   StDFH : StDF state whose neighbour reads load the FP32 high part only (see below)
 //   StF64 : displacement as FP64                          (32 B per vertex, w = mass)
 //
 // Each trait provides read-only (ldg) and coherent (ld) loads, a - b rounded to the
@@ -47,6 +48,7 @@ struct StF32 {
     using U = R4<float>;
     using V = R4<float>;
     using Sc = float;
+    static constexpr int kCode = 32;  // gaia_vbd_stats.precision
     __host__ __device__ static U from_d(const double* x, double w) {
         return U{float(x[0]), float(x[1]), float(x[2]), float(w)};
     }
@@ -80,6 +82,7 @@ struct StF64 {
     using U = R4<double>;
     using V = R4<double>;
     using Sc = double;
+    static constexpr int kCode = 64;
     __host__ __device__ static U from_d(const double* x, double w) { return U{x[0], x[1], x[2], w}; }
     __device__ static void to_d(const U& u, double* x) { x[0] = u.x; x[1] = u.y; x[2] = u.z; }
     __device__ static Sc mass(const U& u) { return u.w; }
@@ -112,6 +115,7 @@ struct StDF {
     using U = DF4;
     using V = R4<float>;
     using Sc = float;
+    static constexpr int kCode = 48;
     __host__ __device__ static U from_d(const double* x, double w) {
         U u;
         u.hx = float(x[0]); u.lx = float(x[0] - double(u.hx));
@@ -155,6 +159,25 @@ struct StDF {
         float h = d == 0 ? u.hx : (d == 1 ? u.hy : u.hz);
         float l = d == 0 ? u.lx : (d == 1 ? u.ly : u.lz);
         return R(__fsub_rn(__fsub_rn(__fsub_rn(c, X), h), l));
+    }
+};
+
+// Double-float state read as FP32 by its neighbours: a vertex's own state (its update, its
+// inertia, damping, friction and ground terms) keeps both parts, so positions do not drift
+// by FP32 rounding from update to update, while the neighbour reads of the incidence loop
+// load only the high half (16 B instead of 32 B per gather; the low half counts as zero).
+// A neighbour's relative position then carries one FP32 rounding of its position, the
+// rounding of the FP32 mode's force, without the FP32 mode's accumulation of rounded
+// updates.
+struct StDFH : StDF {
+    static constexpr int kCode = 40;
+    __device__ static U ldg(const U* p, int i) {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(p + i));
+        return U{a.x, a.y, a.z, a.w, 0.f, 0.f, 0.f, 0.f};
+    }
+    __device__ static U ld(const U* p, int i) {
+        const float4 a = reinterpret_cast<const float4*>(p + i)[0];
+        return U{a.x, a.y, a.z, a.w, 0.f, 0.f, 0.f, 0.f};
     }
 };
 

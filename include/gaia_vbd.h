@@ -46,7 +46,9 @@ typedef struct gaia_vbd gaia_vbd;
 
 /* Run-time counters of one handle. */
 typedef struct {
-    int32_t precision;            /* 32 = FP32-mixed engine, 64 = plain FP64 engine */
+    int32_t precision;            /* state / arithmetic of the engine (gpuPrecision): 32 = "fp32",
+                                     48 = "mixed" (double-float state), 40 = "dfhi" (double-float state,
+                                     neighbours read in FP32), 64 = "fp64" (the plain FP64 engine) */
     int32_t lanes_per_vertex;     /* threads cooperating on one vertex solve */
     int32_t block_size;           /* threads per block of the solve kernel */
     int32_t num_groups;           /* merged colors ("parallel groups") */
@@ -83,7 +85,7 @@ typedef struct {
  * (computing the reference's OrderedGreedy coloring when a model gives no
  * coloring file), precomputes the rest shape in FP64, merges colors into
  * parallel groups and uploads everything. repo_root may be NULL.
- * Extra PhysicsParams keys: "gpuPrecision" ("fp32" | "mixed" | "fp64"),
+ * Extra PhysicsParams keys: "gpuPrecision" ("fp32" | "mixed" | "dfhi" | "fp64"),
  * "lanesPerVertex", "blockSize" (0 = autotune), "autotune" (bool), "sweepMode"
  * ("auto" | "merged" | "scenes": color scheduling, see gaia_vbd_stats.sweep_mode; auto
  * times both and keeps the faster when the scene allows the scene-major sweep, which needs

