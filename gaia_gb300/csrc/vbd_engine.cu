@@ -20,7 +20,8 @@ struct gaia_vbd {
     std::unique_ptr<gaia::EngineBase> eng;
     std::string err;
     int64_t frame = 0;  // runStep calls since initialize / the last loaded state
-    double sweep_ms[2] = {0.0, 0.0};  // autotuned schedule choice: measured ms per iteration, merged / scenes
+    double sweep_ms[3] = {0.0, 0.0, 0.0};  // autotuned schedule choice: measured ms per iteration, merged /
+                                           // scenes / cluster (0 where not timed)
 };
 
 namespace {
@@ -97,22 +98,41 @@ int gaia_vbd_initialize(gaia_vbd* h) {
         // that do not interact within a sweep and no per-iteration work outside the solve.
         const bool scenes_ok = !(p.allowCCD || p.allowDCD) && !p.useAccelerator && !p.evaluateConvergence &&
                                p.iterations > 0;
-        if (p.sweepMode == "scenes" && !scenes_ok)
-            throw std::runtime_error("sweepMode \"scenes\" is not supported with contact detection, the accelerator "
-                                     "or evaluateConvergence");
+        if ((p.sweepMode == "scenes" || p.sweepMode == "cluster") && !scenes_ok)
+            throw std::runtime_error("sweepMode \"" + p.sweepMode + "\" is not supported with contact detection, "
+                                     "the accelerator or evaluateConvergence");
         if (p.sweepMode == "merged" || !scenes_ok || (p.sweepMode == "auto" && !p.autotune)) {
             h->eng.reset(make(gaia::kSweepMerged));
         } else if (p.sweepMode == "scenes") {
             h->eng.reset(make(gaia::kSweepScenes));
+        } else if (p.sweepMode == "cluster") {
+            h->eng.reset(make(gaia::kSweepCluster));
         } else {
-            // autotuned: both schedules built and their sweep graphs timed; the faster is kept
-            std::unique_ptr<gaia::EngineBase> a(make(gaia::kSweepMerged));
-            const double ta = a->measure_sweep_ms();
-            std::unique_ptr<gaia::EngineBase> b(make(gaia::kSweepScenes));
-            const double tb = b->measure_sweep_ms();
-            h->sweep_ms[0] = ta;
-            h->sweep_ms[1] = tb;
-            h->eng = tb < ta ? std::move(b) : std::move(a);
+            // autotuned: every schedule the scene allows is built and its sweep graph timed;
+            // the fastest is kept (the cluster sweep only where every scene fits on-chip)
+            std::unique_ptr<gaia::EngineBase> best(make(gaia::kSweepMerged));
+            h->sweep_ms[0] = best->measure_sweep_ms();
+            double tbest = h->sweep_ms[0];
+            for (int mode : {gaia::kSweepScenes, gaia::kSweepCluster}) {
+                std::unique_ptr<gaia::EngineBase> e;
+                if (mode == gaia::kSweepCluster) {
+                    try {
+                        e.reset(make(mode));
+                    } catch (const std::runtime_error& ex) {
+                        if (std::string(ex.what()).find("does not fit") == std::string::npos) throw;
+                        continue;  // a scene too large for a cluster's shared memory
+                    }
+                } else {
+                    e.reset(make(mode));
+                }
+                const double t = e->measure_sweep_ms();
+                h->sweep_ms[mode] = t;
+                if (t < tbest) {
+                    tbest = t;
+                    best = std::move(e);
+                }
+            }
+            h->eng = std::move(best);
         }
     });
 }
@@ -423,6 +443,7 @@ int gaia_vbd_get_stats(gaia_vbd* h, gaia_vbd_stats* out) {
         h->eng->stats(out);
         out->sweep_ms_merged = h->sweep_ms[0];
         out->sweep_ms_scenes = h->sweep_ms[1];
+        out->sweep_ms_cluster = h->sweep_ms[2];
     });
 }
 

@@ -26,6 +26,7 @@
 #include "scene.hpp"
 #include "state_io.hpp"
 #include "tet_cd.hpp"
+#include "vbd_cluster.cuh"
 #include "vbd_convergence.cuh"
 #include "vbd_kernels.cuh"
 
@@ -101,7 +102,7 @@ inline void make_record<double>(int4& n, dev::R4<double>& a, dev::R4<double>& b,
     *c = mv[2][2];
 }
 
-enum { kSweepMerged = 0, kSweepScenes = 1 };
+enum { kSweepMerged = 0, kSweepScenes = 1, kSweepCluster = 2 };
 
 class EngineBase {
 public:
@@ -143,8 +144,16 @@ class Engine : public EngineBase {
     using R4 = dev::R4<R>;
 
 public:
-    // mode: kSweepMerged (one launch per merged color and iteration) or kSweepScenes (one
-    // persistent launch per substep running every scene's iterations, scene-major slots)
+    // cluster mode: a cluster size whose blocks hold every scene (states and owned records)
+    struct ClusterFit {
+        int C;
+        int32_t pos_cap, rec_cap;
+        size_t bytes;
+    };
+
+    // mode: kSweepMerged (one launch per merged color and iteration), kSweepScenes (one
+    // persistent launch per substep running every scene's iterations, scene-major slots) or
+    // kSweepCluster (the same on thread-block clusters with the scene in shared memory)
     Engine(const Scene& s, int mode) : sc_(s), mode_(mode) {
         GAIA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         GAIA_CUDA(cudaEventCreate(&ev_a_));
@@ -171,6 +180,11 @@ public:
             setup_scenes();
             if ((lanes_ == 0 || block_ == 0) && sc_.p.autotune) autotune_scenes();
             finalize_scenes();
+        } else if (mode_ == kSweepCluster) {
+            setup_scenes();
+            setup_cluster();
+            if ((lanes_ == 0 || block_ == 0 || sc_.p.clusterSize == 0) && sc_.p.autotune) autotune_cluster();
+            finalize_cluster();
         } else {
             if ((lanes_ == 0 || block_ == 0 || variant_fixed_ < 0) && sc_.p.autotune) autotune_impl();
             finalize_cfg();
@@ -211,7 +225,7 @@ public:
         group_end_.clear();
         scene_colors_.clear();
         scene_ofs_.assign(1, 0);
-        if (mode_ == kSweepScenes) {
+        if (mode_ != kSweepMerged) {
             // scene-major: mesh by mesh, within a mesh its vertices of merged color 0, 1, ...
             std::vector<std::vector<std::vector<int32_t>>> per(size_t(nmesh_),
                                                                std::vector<std::vector<int32_t>>(sc_.groups.size()));
@@ -772,6 +786,10 @@ public:
                     enqueue_scenes_sweep(scene_L_, scene_B_);
                     return;
                 }
+                if (mode_ == kSweepCluster) {
+                    enqueue_cluster_sweep(scene_C_, scene_L_, scene_B_);
+                    return;
+                }
                 // evaluateConvergence at iteration -1, on the initial guess (VBDPhysics.cpp:866-870)
                 if (sc_.p.evaluateConvergence) enqueue_conv(true);
                 double omega = 1.0;
@@ -985,6 +1003,162 @@ public:
         tuned_ = true;
     }
 
+    // ---- cluster sweep (vbd_cluster.cuh) ---------------------------------------------
+    // Per scene: its active and fixed slot ranges, and how many states and records one
+    // block of a C-block cluster holds; the cluster sizes whose largest block fits.
+    void setup_cluster() {
+        std::vector<int4> slots(size_t(nmesh_), make_int4(0, 0, 0, 0));
+        int64_t f0 = nactive_;
+        for (int m = 0; m < nmesh_; ++m) {
+            int32_t a0 = 0, a1 = 0;
+            if (scene_ofs_[m + 1] > scene_ofs_[m]) {
+                a0 = scene_colors_[scene_ofs_[m]].x;
+                a1 = scene_colors_[scene_ofs_[m + 1] - 1].y;
+            }
+            int64_t nf = 0;
+            for (int v = 0; v < sc_.meshes[m].nv; ++v) nf += sc_.meshes[m].fixed[v] ? 1 : 0;
+            slots[size_t(m)] = make_int4(a0, a1, int32_t(f0), int32_t(f0 + nf));
+            f0 += nf;
+        }
+        int dev = 0;
+        GAIA_CUDA(cudaGetDevice(&dev));
+        int smem_optin = 0;
+        GAIA_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        const size_t budget = size_t(std::max(0, smem_optin - 4096));  // static shared memory and slack
+        cluster_fits_.clear();
+        for (int C : {2, 4, 8, 16}) {
+            int64_t pos_cap = 0, rec_cap = 0;
+            bool ok = true;
+            for (int m = 0; m < nmesh_ && ok; ++m) {
+                const int4 sl = slots[size_t(m)];
+                pos_cap = std::max<int64_t>(pos_cap, int64_t(sl.y - sl.x) + (sl.w - sl.z));
+                if (scene_ofs_[m + 1] - scene_ofs_[m] > dev::kClusterMaxColors) ok = false;
+                std::vector<int64_t> per_rank(size_t(C), 0);
+                for (int32_t ci = scene_ofs_[m]; ci < scene_ofs_[m + 1]; ++ci) {
+                    const int2 rg = scene_colors_[ci];
+                    const int per = (rg.y - rg.x + C - 1) / C;
+                    for (int r = 0; r < C; ++r) {
+                        const int beg = std::min(rg.y, rg.x + r * per), end = std::min(rg.y, beg + per);
+                        per_rank[size_t(r)] += inc_ofs_[end] - inc_ofs_[beg];
+                    }
+                }
+                for (int64_t x : per_rank) rec_cap = std::max(rec_cap, x);
+            }
+            const size_t bytes = sizeof(S4) * size_t(pos_cap) + sizeof(dev::RecS<R>) * size_t(rec_cap);
+            if (ok && bytes <= budget) cluster_fits_.push_back({C, int32_t(pos_cap), int32_t(rec_cap), bytes});
+        }
+        if (cluster_fits_.empty())
+            throw std::runtime_error("sweepMode \"cluster\" is not supported: a scene does not fit in the shared "
+                                     "memory of a 16-block cluster");
+        d_scene_slots_.upload(slots, &bytes_, st_);
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    const ClusterFit* cluster_fit(int C) const {
+        for (auto& f : cluster_fits_)
+            if (f.C == C) return &f;
+        return nullptr;
+    }
+
+    template <int L>
+    void launch_cluster_l(const ClusterFit& f, int B) {
+        auto kern = dev::k_sweep_cluster<L, ST, R>;
+        GAIA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(f.bytes)));
+        if (f.C > 8) GAIA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = unsigned(f.C);
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cfg.blockDim = dim3(unsigned(B));
+        cfg.dynamicSmemBytes = f.bytes;
+        cfg.stream = st_;
+        cfg.gridDim = dim3(unsigned(f.C));
+        int nclusters = 0;
+        GAIA_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg));
+        if (nclusters < 1) throw std::runtime_error("no cluster of this size fits on the device");
+        cfg.gridDim = dim3(unsigned(f.C * std::min(nscenes_, nclusters)));
+        dev::ClusterScenes S;
+        S.colors = d_scene_colors_.p;
+        S.scene_ofs = d_scene_ofs_.p;
+        S.scene_order = d_scene_order_.p;
+        S.scene_slots = d_scene_slots_.p;
+        S.nscenes = nscenes_;
+        S.iterations = sc_.p.iterations;
+        S.friction_start = sc_.p.frictionStartIter;
+        S.pos_cap = f.pos_cap;
+        S.rec_cap = f.rec_cap;
+        GAIA_CUDA(cudaLaunchKernelEx(&cfg, kern, ptrs(), c_, S, d_scene_work_.p));
+    }
+
+    void enqueue_cluster_sweep(int C, int L, int B) {
+        if (nscenes_ == 0 || sc_.p.iterations == 0) return;
+        const ClusterFit* f = cluster_fit(C);
+        if (!f) throw std::runtime_error("clusterSize: scenes do not fit a cluster of " + std::to_string(C) + " blocks");
+        GAIA_CUDA(cudaMemsetAsync(d_scene_work_.p, 0, sizeof(int32_t), st_));
+        switch (L) {
+            case 4: launch_cluster_l<4>(*f, B); break;
+            case 8: launch_cluster_l<8>(*f, B); break;
+            case 16: launch_cluster_l<16>(*f, B); break;
+            default: launch_cluster_l<32>(*f, B); break;
+        }
+    }
+
+    // Cluster size, lanes per vertex and block size of the cluster sweep, each combination
+    // timed on a full sweep of the current state (restored afterwards).
+    void autotune_cluster() {
+        if (nactive_ == 0 || nscenes_ == 0 || sc_.p.iterations == 0) return;
+        DevBuf<S4> save;
+        save.alloc(nslots_, nullptr);
+        GAIA_CUDA(cudaMemcpyAsync(save.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+        float best = 1e30f;
+        for (const ClusterFit& f : cluster_fits_) {
+            if (sc_.p.clusterSize && f.C != sc_.p.clusterSize) continue;
+            for (int L : {4, 8, 16, 32}) {
+                if (lanes_ && L != lanes_) continue;
+                for (int B : {128, 256}) {
+                    if (block_ && B != block_) continue;
+                    enqueue_cluster_sweep(f.C, L, B);  // warm-up
+                    GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+                    GAIA_CUDA(cudaEventRecord(ev_a_, st_));
+                    enqueue_cluster_sweep(f.C, L, B);
+                    GAIA_CUDA(cudaEventRecord(ev_b_, st_));
+                    GAIA_CUDA(cudaEventSynchronize(ev_b_));
+                    float ms = 0.f;
+                    GAIA_CUDA(cudaEventElapsedTime(&ms, ev_a_, ev_b_));
+                    GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+                    if (ms < best) {
+                        best = ms;
+                        scene_C_ = f.C;
+                        scene_L_ = L;
+                        scene_B_ = B;
+                    }
+                }
+            }
+        }
+        GAIA_CUDA(cudaMemsetAsync(d_counters_.p, 0, dev::CNT_N * sizeof(unsigned long long), st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        tuned_ms_ = double(best) / sc_.p.iterations;
+        tuned_ = true;
+    }
+
+    void finalize_cluster() {
+        if (!tuned_) {
+            scene_C_ = sc_.p.clusterSize ? sc_.p.clusterSize : cluster_fits_.back().C;
+            scene_L_ = lanes_ ? lanes_ : 8;
+            scene_B_ = block_ ? block_ : 128;
+        }
+        if (!cluster_fit(scene_C_))
+            throw std::runtime_error("clusterSize: scenes do not fit a cluster of " + std::to_string(scene_C_) + " blocks");
+        lanes_ = scene_L_;
+        block_ = scene_B_;
+        variant_ = 3;
+        ccfg_.assign(sc_.groups.size(), ColorCfg{scene_L_, scene_B_, 3, float(tuned_ms_)});
+    }
+
     void finalize_scenes() {
         if (!tuned_) {
             scene_L_ = lanes_ ? lanes_ : 8;
@@ -1026,6 +1200,9 @@ public:
         if (mode_ == kSweepScenes) {
             autotune_scenes();
             finalize_scenes();
+        } else if (mode_ == kSweepCluster) {
+            autotune_cluster();
+            finalize_cluster();
         } else {
             autotune_impl();
             finalize_cfg();
@@ -1369,6 +1546,7 @@ public:
         s->block_size = block_;
         s->num_groups = int32_t(sc_.groups.size());
         s->sweep_mode = mode_;
+        s->cluster_size = mode_ == kSweepCluster ? scene_C_ : 0;
         s->num_vertices = nslots_;
         s->num_active_vertices = nactive_;
         s->num_incidences = ninc_;
@@ -1404,15 +1582,18 @@ private:
     bool tuned_ = false;
     bool use_pdl_ = true;
     int small_color_ = 16384;
-    int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma, 2 = k_sweep_scenes
+    int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma, 2 = k_sweep_scenes,
+                               // 3 = k_sweep_cluster
     int mode_ = 0;             // kSweepMerged or kSweepScenes
     // scene-major mode: per mesh its color slot ranges, in sweep order
     std::vector<int2> scene_colors_;
     std::vector<int32_t> scene_ofs_;
     int32_t nscenes_ = 0;
-    int scene_L_ = 8, scene_B_ = 512, num_sms_ = 1;
+    int scene_L_ = 8, scene_B_ = 512, scene_C_ = 8, num_sms_ = 1;
     DevBuf<int2> d_scene_colors_;
     DevBuf<int32_t> d_scene_ofs_, d_scene_order_, d_scene_work_;
+    std::vector<ClusterFit> cluster_fits_;
+    DevBuf<int4> d_scene_slots_;
     int variant_fixed_ = -1;   // from PhysicsParams solveVariant (-1 = autotune)
     std::map<std::pair<int, int>, int> maxrec_cache_;
     static constexpr size_t kTmaSmemMax = 200 * 1024;

@@ -334,9 +334,9 @@ __device__ __forceinline__ void axis_friction(int d, const R* dx, R mu, R lambda
 // probe_out instead of moving it.
 // ---------------------------------------------------------------------------
 template <typename ST, typename R, bool PROBE>
-__device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R>& c, int v, const typename ST::U& uo,
+__device__ __forceinline__ bool vertex_tail(const Ptrs<ST, R>& P, const Consts<R>& c, int v, const typename ST::U& uo,
                                             const MeshMat<R>& mat, const Acc<R>& acc, int friction,
-                                            double* probe_out, int beg, int end);
+                                            double* probe_out, int beg, int end, typename ST::U* unew = nullptr);
 
 // ---------------------------------------------------------------------------
 // Tet-mesh vertex-face contact (VBDPhysicsCompute.cu:1731-1773, 1812-1930)
@@ -544,10 +544,11 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
 
 // ---- per-vertex tail (lane 0 of a vertex group): damping, inertia, ground and
 // friction, 3x3 solve, update ------------------------------------------------------
+// The new state goes to P.u[v], or to *unew when given; returns whether the vertex moved.
 template <typename ST, typename R, bool PROBE>
-__device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R>& c, int v, const typename ST::U& uo,
+__device__ __forceinline__ bool vertex_tail(const Ptrs<ST, R>& P, const Consts<R>& c, int v, const typename ST::U& uo,
                                             const MeshMat<R>& mat, const Acc<R>& acc, int friction,
-                                            double* probe_out, int beg, int end) {
+                                            double* probe_out, int beg, int end, typename ST::U* unew) {
     using U = typename ST::U;
     using Sc = typename ST::Sc;
     R f[3] = {acc.f0, acc.f1, acc.f2};
@@ -613,7 +614,7 @@ __device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R
         probe_out[3] = H[0]; probe_out[4] = H[1]; probe_out[5] = H[2];
         probe_out[6] = H[1]; probe_out[7] = H[3]; probe_out[8] = H[4];
         probe_out[9] = H[2]; probe_out[10] = H[4]; probe_out[11] = H[5];
-        return;
+        return false;
     }
     // CMP_EPSILON2 gate (Types/Types.h:20-21; VBDPhysics.cpp:2432); a non-finite force (a
     // NaN or Inf position among the vertex's neighbours) is counted, as the reference's
@@ -621,7 +622,7 @@ __device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R
     const R fn2 = f[0] * f[0] + f[1] * f[1] + f[2] * f[2];
     if (!(fn2 > R(1e-5f * 1e-5f))) {
         if (!(fn2 <= R(1e-5f * 1e-5f))) atomicAdd(&P.counters[CNT_NONFINITE], 1ull);
-        return;
+        return false;
     }
     R d3[3];
     R step = c.step;
@@ -634,9 +635,11 @@ __device__ __forceinline__ void vertex_tail(const Ptrs<ST, R>& P, const Consts<R
     const Sc s0 = Sc(step * d3[0]), s1 = Sc(step * d3[1]), s2 = Sc(step * d3[2]);
     if (!(isfinite(s0) && isfinite(s1) && isfinite(s2))) {
         atomicAdd(&P.counters[CNT_NONFINITE], 1ull);
-        return;
+        return false;
     }
-    P.u[v] = ST::add(uo, s0, s1, s2);
+    if (unew) *unew = ST::add(uo, s0, s1, s2);
+    else P.u[v] = ST::add(uo, s0, s1, s2);
+    return true;
 }
 
 // ---------------------------------------------------------------------------

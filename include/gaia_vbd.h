@@ -70,10 +70,13 @@ typedef struct {
                                          out; the call that reports it returns GAIA_VBD_E_DEVICE_TIMEOUT */
     int64_t nonfinite_solves;         /* vertex solves with a non-finite force or step (not written) */
     int32_t sweep_mode;               /* color scheduling: 0 = merged colors (a launch per merged color
-                                         and iteration), 1 = scene-major persistent sweep (solve_variant 2) */
-    int32_t reserved2;
+                                         and iteration), 1 = scene-major persistent sweep, one block per
+                                         scene (solve_variant 2), 2 = scene-major sweep on thread-block
+                                         clusters with the scene in shared memory (solve_variant 3) */
+    int32_t cluster_size;             /* blocks per cluster of the cluster sweep (0 otherwise) */
     double sweep_ms_merged;           /* sweep time per iteration the autotuner measured for each */
-    double sweep_ms_scenes;           /* schedule (0 when it did not compare them) */
+    double sweep_ms_scenes;           /* schedule (0 where it did not time it) */
+    double sweep_ms_cluster;
 } gaia_vbd_stats;
 
 /* ---- life cycle ------------------------------------------------------------
@@ -87,9 +90,10 @@ typedef struct {
  * parallel groups and uploads everything. repo_root may be NULL.
  * Extra PhysicsParams keys: "gpuPrecision" ("fp32" | "mixed" | "dfhi" | "fp64"),
  * "lanesPerVertex", "blockSize" (0 = autotune), "autotune" (bool), "sweepMode"
- * ("auto" | "merged" | "scenes": color scheduling, see gaia_vbd_stats.sweep_mode; auto
- * times both and keeps the faster when the scene allows the scene-major sweep, which needs
- * contact detection, the accelerator and evaluateConvergence off).
+ * ("auto" | "merged" | "scenes" | "cluster": color scheduling, see gaia_vbd_stats.sweep_mode;
+ * auto times every schedule the scene allows and keeps the fastest; the scene-major sweeps
+ * need contact detection, the accelerator and evaluateConvergence off, and the cluster sweep
+ * scenes that fit in the shared memory of a cluster), "clusterSize" (0 = autotune, 2-16).
  */
 int gaia_vbd_create(const char* models_json, const char* params_json, const char* repo_root, gaia_vbd** out);
 /* The two halves of gaia_vbd_create. gaia_vbd_load is host-only (no GPU needed):

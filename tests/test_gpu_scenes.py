@@ -1,5 +1,5 @@
-"""The scene-major persistent sweep (sweepMode "scenes", k_sweep_scenes) and the autotuned
-choice of color scheduling.
+"""The scene-major persistent sweeps (sweepMode "scenes", k_sweep_scenes; sweepMode
+"cluster", k_sweep_cluster) and the autotuned choice of color scheduling.
 
 In this mode one launch per substep runs every scene's iterations: each block takes whole
 meshes, their colors in the merged groups' order, a block barrier between colors. Meshes
@@ -115,10 +115,11 @@ def test_scenes_mode_equals_merged(batch, lanes):
 def test_autotuner_picks_schedule(plain_drop, batch):
     for mp, pp, _ in (plain_drop, batch):
         _, _, st = _run(mp, pp, "mixed", 1)
-        print(f"merged {st['sweep_ms_merged']:.4f} ms/iteration, scenes {st['sweep_ms_scenes']:.4f}: "
+        times = [st["sweep_ms_merged"], st["sweep_ms_scenes"], st["sweep_ms_cluster"]]
+        print(f"ms/iteration: merged {times[0]:.4f}, scenes {times[1]:.4f}, cluster {times[2]:.4f}: "
               f"mode {st['sweep_mode']}")
-        assert st["sweep_ms_merged"] > 0 and st["sweep_ms_scenes"] > 0
-        assert st["sweep_mode"] == (1 if st["sweep_ms_scenes"] < st["sweep_ms_merged"] else 0)
+        assert all(t > 0 for t in times)
+        assert st["sweep_mode"] == int(np.argmin(times))
 
 
 def test_scenes_mode_refused_with_contact(tmp_path, gaia_lib):
@@ -135,4 +136,70 @@ def test_scenes_mode_refused_with_contact(tmp_path, gaia_lib):
     phys2.loadRunningparameters(mp, scenes.set_precision(pp, "mixed", out_path=pp + ".auto.json"))
     phys2.initialize()
     assert phys2.stats()["sweep_mode"] == 0
+    phys2.close()
+
+
+# ---------------------------------------------------------------- the cluster sweep
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "dfhi", "fp32"])
+def test_plain_drop_cluster_mode(plain_drop, precision):
+    """The plain-drop configuration on a thread-block cluster with the scene in distributed
+    shared memory (every copy of the states updated through DSMEM, a cluster barrier per
+    color), against the FP64 oracle."""
+    from tests.test_gpu_parity import FP32_DROP_BOUND
+
+    mp, pp, ref = plain_drop
+    x0, x, st = _run(mp, pp, precision, 100, sweepMode="cluster")
+    assert st["sweep_mode"] == 2 and st["solve_variant"] == 3 and st["cluster_size"] in (2, 4, 8, 16)
+    rel = _rel(x, ref, x0)
+    print(f"plain drop, cluster mode, {precision}: rel {rel:.3e}, cluster {st['cluster_size']} lanes "
+          f"{st['lanes_per_vertex']} block {st['block_size']}")
+    assert rel <= (FP32_DROP_BOUND if precision == "fp32" else TOL[precision])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("cluster", [2, 16])
+def test_batch_cluster_mode(batch, precision, cluster):
+    mp, pp, ref = batch
+    x0, x, st = _run(mp, pp, precision, 30, sweepMode="cluster", clusterSize=cluster)
+    assert st["sweep_mode"] == 2 and st["cluster_size"] == cluster
+    assert _rel(x, ref, x0) <= TOL[precision]
+
+
+def test_twist_cluster_mode(tmp_path, gaia_lib, oracle_lib):
+    """Fixed faces driven by the rotator: fixed states are staged into every copy each substep."""
+    from gaia_gb300 import scenes
+
+    mp, pp = scenes.twist_cube(str(tmp_path), n=10, iterations=20)
+    ref = _oracle(mp, pp, 20, oracle_lib)
+    for precision in ("fp64", "mixed"):
+        x0, x, st = _run(mp, pp, precision, 20, sweepMode="cluster")
+        assert _rel(x, ref, x0) <= TOL[precision], precision
+
+
+@pytest.mark.parametrize("cluster", [4, 16])
+def test_cluster_mode_equals_merged(batch, cluster):
+    mp, pp, _ = batch
+    common = dict(lanesPerVertex=8, blockSize=128, autotune=False, smallColorVertices=0, solveVariant=0)
+    _, xa, _ = _run(mp, pp, "mixed", 10, sweepMode="merged", **common)
+    _, xc, sc = _run(mp, pp, "mixed", 10, sweepMode="cluster", clusterSize=cluster, **common)
+    assert sc["sweep_mode"] == 2
+    np.testing.assert_array_equal(xa, xc)
+
+
+def test_cluster_mode_refused_when_too_large(tmp_path, gaia_lib):
+    """A 40^3 lattice (64k vertices) does not fit in a 16-block cluster's shared memory:
+    the explicit mode is refused, and the autotuner leaves it out."""
+    from gaia_gb300 import VBDPhysics, scenes
+
+    mp, pp = scenes.twist_cube(str(tmp_path), n=40, iterations=4)
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, scenes.set_precision(pp, "mixed", sweepMode="cluster"))
+    with pytest.raises(GaiaError) as ei:
+        phys.initialize()
+    assert ei.value.code == E_UNSUPPORTED and "does not fit" in str(ei.value)
+    phys2 = VBDPhysics()
+    phys2.loadRunningparameters(mp, scenes.set_precision(pp, "mixed", out_path=pp + ".auto.json"))
+    phys2.initialize()
+    st = phys2.stats()
+    assert st["sweep_mode"] in (0, 1) and st["sweep_ms_cluster"] == 0
     phys2.close()
