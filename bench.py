@@ -249,8 +249,12 @@ def timed_steps(phys, steps: int, local: int) -> tuple[float, float, str]:
 
     l2 = l2_bytes(local)
     data = phys.stats()["device_bytes"]
+    # an NVTX range around the timed steps, so that a profiler can select their launches
+    # (ncu --nvtx --nvtx-include "timed_steps/")
+    torch.cuda.nvtx.range_push("timed_steps")
     if data >= 4 * l2:
         tot, sw = phys.run_steps_timed(steps)
+        torch.cuda.nvtx.range_pop()
         return tot, sw, f"inputs larger than L2 ({data / 1e6:.0f} MB of device data, L2 {l2 / 1e6:.0f} MB)"
     buf = torch.empty(2 * l2 // 4, dtype=torch.float32, device=f"cuda:{local}")
     tot = sw = 0.0
@@ -260,6 +264,7 @@ def timed_steps(phys, steps: int, local: int) -> tuple[float, float, str]:
         t, s = phys.run_steps_timed(1)
         tot += t
         sw += s
+    torch.cuda.nvtx.range_pop()
     del buf
     return tot, sw, (f"L2 flushed before every timed step ({2 * l2 / 1e6:.0f} MB write; {data / 1e6:.0f} MB of "
                      f"device data), steps timed one at a time")

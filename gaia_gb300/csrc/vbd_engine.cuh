@@ -103,6 +103,7 @@ inline void make_record<double>(int4& n, dev::R4<double>& a, dev::R4<double>& b,
 }
 
 enum { kSweepMerged = 0, kSweepScenes = 1, kSweepCluster = 2 };
+constexpr int kVariantDeep = 4;  // solve variant: k_solve_deep
 
 class EngineBase {
 public:
@@ -172,8 +173,9 @@ public:
         small_color_ = sc_.p.smallColorVertices;
         set_tma_smem_limits();
         variant_fixed_ = sc_.p.solveVariant;
-        if (variant_fixed_ != -1 && variant_fixed_ != 0 && variant_fixed_ != 1)
-            throw std::runtime_error("solveVariant must be -1 (autotune), 0 (registers) or 1 (TMA-staged)");
+        if (variant_fixed_ != -1 && variant_fixed_ != 0 && variant_fixed_ != 1 && variant_fixed_ != kVariantDeep)
+            throw std::runtime_error("solveVariant must be -1 (autotune), 0 (registers), 1 (TMA-staged) or 4 (registers, "
+                                     "deeper record pipeline)");
         if (variant_fixed_ == 1 && sizeof(R) != 4) variant_fixed_ = 0;  // the FP64 engine has no TMA variant
         if (variant_fixed_ >= 0) variant_ = variant_fixed_;
         if (mode_ == kSweepScenes) {
@@ -634,11 +636,36 @@ public:
         }
     }
 
+    template <int L>
+    void launch_solve_deep_l(int grid, int B, int beg, int end, int friction, bool pdl) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(B);
+        cfg.stream = st_;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = pdl ? attr : nullptr;
+        cfg.numAttrs = pdl ? 1 : 0;
+        GAIA_CUDA(cudaLaunchKernelEx(&cfg, dev::k_solve_deep<L, ST, R>, ptrs(), c_, beg, end, friction));
+    }
+
     template <bool PROBE>
     void launch_solve(int L, int B, int beg, int end, int friction, double* probe, bool pdl = false,
                       int variant = 0) {
         if (end <= beg) return;
         if (!PROBE && variant == 1 && launch_solve_tma(L, B, beg, end, friction, pdl)) return;
+        if (!PROBE && variant == kVariantDeep) {
+            const int grid = div_up(int64_t(end - beg) * L, B);
+            switch (L) {
+                case 2: launch_solve_deep_l<2>(grid, B, beg, end, friction, pdl); break;
+                case 4: launch_solve_deep_l<4>(grid, B, beg, end, friction, pdl); break;
+                case 8: launch_solve_deep_l<8>(grid, B, beg, end, friction, pdl); break;
+                case 16: launch_solve_deep_l<16>(grid, B, beg, end, friction, pdl); break;
+                default: launch_solve_deep_l<32>(grid, B, beg, end, friction, pdl); break;
+            }
+            return;
+        }
         int grid = div_up(int64_t(end - beg) * L, B);
         switch (L) {
             case 2: launch_solve_l<PROBE, 2>(grid, B, beg, end, friction, probe, pdl); break;
@@ -863,7 +890,10 @@ public:
         GAIA_CUDA(cudaMemcpyAsync(save.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
         const int Ls[] = {2, 4, 8, 16, 32};
         const int Bs[] = {128, 256};
-        const int nvar = sizeof(R) == 4 ? 2 : 1;
+        // kernel variants: 0 register-pipelined, 1 TMA-staged (FP32 compute only), 4 deeper
+        // register pipeline
+        std::vector<int> variants = {0, kVariantDeep};
+        if (sizeof(R) == 4) variants.push_back(1);
         const int reps = 4;
         ccfg_.assign(group_beg_.size(), ColorCfg{});
         double total = 0.0;
@@ -872,7 +902,7 @@ public:
             if (end <= beg) continue;
             ColorCfg best;
             best.ms = 1e30f;
-            for (int var = 0; var < nvar; ++var) {
+            for (int var : variants) {
                 if (variant_fixed_ >= 0 && var != variant_fixed_) continue;
                 for (int L : Ls) {
                     if (lanes_ && L != lanes_) continue;
@@ -1583,7 +1613,7 @@ private:
     bool use_pdl_ = true;
     int small_color_ = 16384;
     int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma, 2 = k_sweep_scenes,
-                               // 3 = k_sweep_cluster
+                               // 3 = k_sweep_cluster, 4 = k_solve_deep
     int mode_ = 0;             // kSweepMerged or kSweepScenes
     // scene-major mode: per mesh its color slot ranges, in sweep order
     std::vector<int2> scene_colors_;

@@ -542,6 +542,66 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
     vertex_tail<ST, R, PROBE>(P, c, v, uo, mat, acc, friction, probe_out, beg, end);
 }
 
+// The same incidence loop with two records in flight beyond the one being computed
+// (`cur` and `nx1` already loaded): more loads outstanding per lane, for colors whose
+// record stream is long enough to need the memory-level parallelism (HBM-bound sweeps).
+template <int L, typename ST, typename R>
+__device__ __forceinline__ void accumulate_records3(const Ptrs<ST, R>& P, int r, int e, RecRaw<R> cur,
+                                                    RecRaw<R> nx1, const typename ST::U& uo, R mu, R lmbd,
+                                                    Acc<R>& acc) {
+    using U = typename ST::U;
+    while (r < e) {
+        const int r2 = r + 2 * L;
+        RecRaw<R> nx2;
+        if (r2 < e) nx2.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r2);
+        const U q0 = ST::ldg(P.u, cur.n.x), q1 = ST::ldg(P.u, cur.n.y), q2 = ST::ldg(P.u, cur.n.z);
+        R m0[3], m1[3], m2[3];
+        cur.rows(m0, m1, m2);
+        R e0[3], e1[3], e2[3];
+        ST::diff(q0, uo, e0);
+        ST::diff(q1, uo, e1);
+        ST::diff(q2, uo, e2);
+        incidence<R>(e0, e1, e2, m0, m1, m2, mu, lmbd, acc);
+        cur = nx1;
+        nx1 = nx2;
+        r += L;
+    }
+}
+
+// k_solve with the deeper record pipeline (variant 4): the prologue loads the first two
+// records of each lane before the programmatic-dependency wait. Three resident blocks of
+// 256 threads leave it the registers the second record in flight needs (no spills).
+template <int L, typename ST, typename R>
+__global__ void __launch_bounds__(256, sizeof(R) == 8 ? 2 : 3)
+    k_solve_deep(Ptrs<ST, R> P, Consts<R> c, int beg, int end, int friction) {
+    using U = typename ST::U;
+    pdl_launch_dependents();
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = tid & (L - 1);
+    const int v = beg + tid / L;
+    const bool valid = v < end;
+    Acc<R> acc = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    U uo{};
+    MeshMat<R> mat;
+    int r = 0, e = 0;
+    RecRaw<R> cur, nx1;
+    if (valid) {
+        mat = P.mats[P.slot_mesh[v]];
+        r = P.inc_ofs[v] + lane;
+        e = P.inc_ofs[v + 1];
+        if (r < e) cur.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r);
+        if (r + L < e) nx1.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r + L);
+    }
+    pdl_wait();
+    if (valid) {
+        uo = P.u[v];
+        accumulate_records3<L, ST, R>(P, r, e, cur, nx1, uo, mat.mu, mat.lmbd, acc);
+    }
+    reduce_group<L, R>(acc);
+    if (!valid || lane != 0) return;
+    vertex_tail<ST, R, false>(P, c, v, uo, mat, acc, friction, nullptr, beg, end);
+}
+
 // ---- per-vertex tail (lane 0 of a vertex group): damping, inertia, ground and
 // friction, 3x3 solve, update ------------------------------------------------------
 // The new state goes to P.u[v], or to *unew when given; returns whether the vertex moved.

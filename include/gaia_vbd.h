@@ -60,7 +60,9 @@ typedef struct {
     int64_t failed_solves;        /* solves that fell back to the gradient step (cumulative) */
     int64_t device_bytes;         /* device memory owned by the handle */
     double autotune_ms_per_iteration; /* best measured sweep time per iteration (0 if not tuned) */
-    int32_t solve_variant;        /* 0 = register-pipelined solve kernel, 1 = TMA-staged records */
+    int32_t solve_variant;        /* 0 = register-pipelined solve kernel, 1 = TMA-staged records,
+                                     2 = scene-major persistent sweep, 3 = cluster sweep, 4 = register
+                                     pipeline two records deep (of the largest color) */
     int32_t reserved;
     /* tet-mesh contact detection (cumulative; 0 when contact is off) */
     int64_t contact_detections;       /* detection passes run */

@@ -88,16 +88,16 @@ def test_lanes_per_vertex_agree(drop_scene, drop_ref, lanes):
     assert _rel(xs[0], drop_ref[0], x0[0]) <= TOL["fp64"]
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 4])
 @pytest.mark.parametrize("lanes", [4, 32])
 @pytest.mark.parametrize("precision", ["mixed", "dfhi", "fp32"])
 def test_solve_variants_agree(drop_scene, drop_ref, variant, lanes, precision):
-    """Register-pipelined (0) and TMA-staged (1) solve kernels, with and without
-    programmatic dependent launch, give the oracle's result."""
+    """Register-pipelined (0), TMA-staged (1) and two-deep register-pipelined (4) solve
+    kernels, with and without programmatic dependent launch, give the oracle's result."""
     mp, pp = drop_scene
     for pdl in (True, False):
         x0, xs, st = _run_gpu(mp, pp, precision, 40, lanesPerVertex=lanes, blockSize=128, autotune=False,
-                              solveVariant=variant, usePDL=pdl, smallColorVertices=0)
+                              solveVariant=variant, usePDL=pdl, smallColorVertices=0, sweepMode="merged")
         assert st["solve_variant"] == variant
         assert _rel(xs[0], drop_ref[0], x0[0]) <= TOL[precision], (variant, lanes, precision, pdl)
 
