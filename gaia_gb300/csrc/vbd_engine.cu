@@ -113,7 +113,18 @@ int gaia_vbd_initialize(gaia_vbd* h) {
             std::unique_ptr<gaia::EngineBase> best(make(gaia::kSweepMerged));
             h->sweep_ms[0] = best->measure_sweep_ms();
             double tbest = h->sweep_ms[0];
+            // a scene-major sweep runs each scene on one block (or one cluster): a scene much
+            // larger than a block can hold on-chip only serialises its work, so the autotuner
+            // does not time those schedules when a mesh has more than kSceneMajorMaxVertices
+            int64_t largest = 0;
+            for (const auto& m : h->scene.meshes) {
+                int64_t n = 0;
+                for (uint8_t f : m.fixed) n += f ? 0 : 1;
+                largest = std::max(largest, n);
+            }
+            constexpr int64_t kSceneMajorMaxVertices = 65536;
             for (int mode : {gaia::kSweepScenes, gaia::kSweepCluster}) {
+                if (largest > kSceneMajorMaxVertices) break;
                 std::unique_ptr<gaia::EngineBase> e;
                 if (mode == gaia::kSweepCluster) {
                     try {
