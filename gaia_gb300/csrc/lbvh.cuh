@@ -209,26 +209,39 @@ __device__ __forceinline__ bool sphere_box(float3 p, float r2, float4 lo, float4
     return dx * dx + dy * dy + dz * dz <= r2;
 }
 
-// Visits every primitive whose box is within sqrt(r2) of p (stack traversal).
+// Visits every primitive whose box is within sqrt(r2) of p, that is every leaf whose box
+// and whose ancestors' boxes all pass the test (stack traversal). Both children of a node
+// are tested together when the node is popped (two independent box loads in flight), a
+// leaf that passes is visited at once, and only passing internal nodes are pushed; the
+// set of visited leaves is that of a one-node-at-a-time traversal, the order differs.
 template <typename F>
 __device__ __forceinline__ void traverse(const LbvhDev& b, float3 p, float r2, unsigned long long* counters, F&& leaf) {
     if (b.n <= 0) return;
+    if (!sphere_box(p, r2, b.bmin[0], b.bmax[0])) return;
+    if (b.n == 1) {
+        leaf(int(b.keys[0] & 0xffffffffull));
+        return;
+    }
     int stack[64];
     int sp = 0;
     stack[sp++] = 0;
     while (sp > 0) {
         const int node = stack[--sp];
-        if (!sphere_box(p, r2, b.bmin[node], b.bmax[node])) continue;
-        if (node >= b.n - 1) {
-            leaf(int(b.keys[node - (b.n - 1)] & 0xffffffffull));
-        } else {
-            if (sp + 2 > 64) {
+        const int2 c = b.child[node];
+        const float4 lo0 = b.bmin[c.x], hi0 = b.bmax[c.x], lo1 = b.bmin[c.y], hi1 = b.bmax[c.y];
+        const bool h0 = sphere_box(p, r2, lo0, hi0), h1 = sphere_box(p, r2, lo1, hi1);
+        const int ch[2] = {c.x, c.y};
+        const bool hit[2] = {h0, h1};
+#pragma unroll
+        for (int k = 1; k >= 0; --k) {  // c.x ends on top of the stack, as before
+            if (!hit[k]) continue;
+            if (ch[k] >= b.n - 1) {
+                leaf(int(b.keys[ch[k] - (b.n - 1)] & 0xffffffffull));
+            } else if (sp + 1 > 64) {
                 atomicAdd(&counters[CC_STACK_OVERFLOW], 1ull);
-                continue;
+            } else {
+                stack[sp++] = ch[k];
             }
-            const int2 c = b.child[node];
-            stack[sp++] = c.y;
-            stack[sp++] = c.x;
         }
     }
 }
