@@ -361,6 +361,42 @@ __device__ __forceinline__ void bending(const Args<R>& a, const Consts<R>& c, co
     H[5] += hb;
 }
 
+// The flattened face-side (faces = 1: items of the incident faces' FV links) or edge
+// (faces = 0: items of the incident edges' EE contacts) contact terms of one lane: items
+// lane, lane + L, ... of the concatenation, in order.
+template <int L, typename R, int CAP>
+__device__ __forceinline__ void flat_items(const Args<R>& a, const Consts<R>& c, int lane, const int2* list, int n,
+                                           const int* counts, int faces, R* f, R* H) {
+    using V = typename Vec<R>::T;
+    int i = -1, first = 0, cnt = 0;  // current primitive, its first flattened item, its item count
+    int4 ids = make_int4(0, 0, 0, 0);
+    V A{}, B{}, C{};
+    int2 o = make_int2(0, 0);
+    for (int k = lane;; k += L) {
+        while (k >= first + cnt) {  // advance to the primitive holding item k
+            first += cnt;
+            if (++i >= n) return;
+            o = list[i];
+            cnt = min(counts[o.x], CAP);
+            if (k < first + cnt) {
+                if (faces) {
+                    ids = a.faces[o.x];
+                    A = ld(a.x, ids.x);
+                    B = ld(a.x, ids.y);
+                    C = ld(a.x, ids.z);
+                } else {
+                    ids = a.edges[o.x];
+                    A = ld(a.x, ids.x);
+                    B = ld(a.x, ids.y);
+                }
+            }
+        }
+        const int j = k - first;
+        if (faces) vf_term_at(a, c, a.cd.fvVert[size_t(o.x) * CAP + j], ids, A, B, C, o.y, f, H);
+        else ee_term_at(a, c, ids, A, B, a.cd.eeOther[size_t(o.x) * CAP + j], o.y, f, H);
+    }
+}
+
 // Lane `lane` of an L-lane group's share of vertex v's incident terms: membrane (into Hm,
 // for the Rayleigh term), bending, vertex-side VF contacts, face-side VF contacts (the
 // vertices linked to each incident face, flattened over faces) and EE contacts (flattened
@@ -377,38 +413,14 @@ __device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, co
     for (int k = lane; k < nVF; k += L) vf_term(a, c, v, a.cd.vfFace[size_t(v) * VF_CAP + k], 3, f, H);
     // Face side: items (incident face i, link j) in face order; edges: items (incident edge
     // i, contact j) in edge order. Lane `lane` takes the items whose flattened index is
-    // lane, lane + L, ...: per face (edge) the links j = j0, j0 + L, ... with
-    // (base + j0) % L == lane, base the items of the faces (edges) before it. The face's
-    // (edge's) own ids and positions are loaded once for all its items.
-    {
-        int base = 0;
-        for (int i = 0; i < nF; ++i) {
-            const int2 fo = a.vfList[fa + i];
-            const int cnt = min(a.cd.fvCount[fo.x], FV_CAP);
-            int j = (lane - base % L + L) % L;
-            base += cnt;
-            if (j >= cnt) continue;
-            const int4 fv = a.faces[fo.x];
-            const typename Vec<R>::T A = ld(a.x, fv.x), B = ld(a.x, fv.y), C = ld(a.x, fv.z);
-            for (; j < cnt; j += L)
-                vf_term_at(a, c, a.cd.fvVert[size_t(fo.x) * FV_CAP + j], fv, A, B, C, fo.y, f, H);
-        }
-    }
-    {
-        const int ea = a.veOfs[v], nE = a.veOfs[v + 1] - ea;
-        int base = 0;
-        for (int i = 0; i < nE; ++i) {
-            const int2 eo = a.veList[ea + i];
-            const int cnt = min(a.cd.eeCount[eo.x], EE_CAP);
-            int j = (lane - base % L + L) % L;
-            base += cnt;
-            if (j >= cnt) continue;
-            const int4 E = a.edges[eo.x];
-            const typename Vec<R>::T p1 = ld(a.x, E.x), p2 = ld(a.x, E.y);
-            for (; j < cnt; j += L)
-                ee_term_at(a, c, E, p1, p2, a.cd.eeOther[size_t(eo.x) * EE_CAP + j], eo.y, f, H);
-        }
-    }
+    // lane, lane + L, ..., so every lane of the group has work until the last L items
+    // (a face or an edge holds fewer items than a wide group has lanes, and a loop over the
+    // faces would leave the other lanes idle). The face (edge) of each item follows from the
+    // prefix of the item counts, which a lane walks forward as its index grows; the face's
+    // (edge's) ids and positions are loaded again only when the lane's face (edge) changes.
+    flat_items<L, R, FV_CAP>(a, c, lane, a.vfList + fa, nF, a.cd.fvCount, 1, f, H);
+    flat_items<L, R, EE_CAP>(a, c, lane, a.veList + a.veOfs[v], a.veOfs[v + 1] - a.veOfs[v], a.cd.eeCount, 0, f,
+                             H);
 }
 
 // Per-vertex terms: the membrane's Rayleigh damping on its own Hessian, inertia
