@@ -210,6 +210,13 @@ struct RecRaw<float> {
         a = __ldcs(reinterpret_cast<const float4*>(rec_a) + r);
         b = __ldcs(reinterpret_cast<const float4*>(rec_b) + r);
     }
+    // cached (not streaming): for a kernel that reads the same records every iteration
+    __device__ __forceinline__ void load_kept(const int4* rec_n, const R4<float>* rec_a, const R4<float>* rec_b,
+                                              const float*, int r) {
+        n = __ldg(rec_n + r);
+        a = __ldg(reinterpret_cast<const float4*>(rec_a) + r);
+        b = __ldg(reinterpret_cast<const float4*>(rec_b) + r);
+    }
     __device__ __forceinline__ void rows(float* m0, float* m1, float* m2) const {
         m0[0] = a.x; m0[1] = a.y; m0[2] = a.z;
         m1[0] = a.w; m1[1] = b.x; m1[2] = b.y;
@@ -228,6 +235,14 @@ struct RecRaw<double> {
         const double2* pb = reinterpret_cast<const double2*>(rec_b + r);
         a0 = __ldcs(pa); a1 = __ldcs(pa + 1); b0 = __ldcs(pb); b1 = __ldcs(pb + 1);
         c = __ldcs(rec_c + r);
+    }
+    __device__ __forceinline__ void load_kept(const int4* rec_n, const R4<double>* rec_a, const R4<double>* rec_b,
+                                              const double* rec_c, int r) {
+        n = __ldg(rec_n + r);
+        const double2* pa = reinterpret_cast<const double2*>(rec_a + r);
+        const double2* pb = reinterpret_cast<const double2*>(rec_b + r);
+        a0 = __ldg(pa); a1 = __ldg(pa + 1); b0 = __ldg(pb); b1 = __ldg(pb + 1);
+        c = __ldg(rec_c + r);
     }
     __device__ __forceinline__ void rows(double* m0, double* m1, double* m2) const {
         m0[0] = a0.x; m0[1] = a0.y; m0[2] = a1.x;
@@ -471,7 +486,8 @@ __global__ void __launch_bounds__(128) k_contact_color(Ptrs<ST, R> P, Consts<R> 
 // The incidence loop of one lane: records r, r + L, ... below e, the first (`cur`) already
 // loaded; two-stage pipeline (the next record is in flight during this incidence).
 // COHERENT: neighbour states with plain loads, for a kernel that itself wrote them
-// earlier (the persistent sweep); otherwise through the read-only cache.
+// earlier (the persistent sweep), and records kept in the caches (that kernel reads them
+// every iteration); otherwise states through the read-only cache and records streamed.
 template <int L, typename ST, typename R, bool COHERENT>
 __device__ __forceinline__ void accumulate_records(const Ptrs<ST, R>& P, int r, int e, RecRaw<R> cur,
                                                    const typename ST::U& uo, R mu, R lmbd, Acc<R>& acc) {
@@ -479,7 +495,10 @@ __device__ __forceinline__ void accumulate_records(const Ptrs<ST, R>& P, int r, 
     while (r < e) {
         const int rn = r + L;
         RecRaw<R> nxt;
-        if (rn < e) nxt.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, rn);
+        if (rn < e) {
+            if constexpr (COHERENT) nxt.load_kept(P.rec_n, P.rec_a, P.rec_b, P.rec_c, rn);
+            else nxt.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, rn);
+        }
         U q0, q1, q2;
         if constexpr (COHERENT) {
             q0 = ST::ld(P.u, cur.n.x);
@@ -884,7 +903,7 @@ __global__ void __launch_bounds__(MAXB) k_sweep_scenes(Ptrs<ST, R> P, Consts<R> 
                         mat = P.mats[P.slot_mesh[v]];
                         const int r = P.inc_ofs[v] + lane, e = P.inc_ofs[v + 1];
                         RecRaw<R> cur;
-                        if (r < e) cur.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r);
+                        if (r < e) cur.load_kept(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r);
                         uo = ST::ld(P.u, v);
                         accumulate_records<L, ST, R, true>(P, r, e, cur, uo, mat.mu, mat.lmbd, acc);
                     }
