@@ -72,6 +72,19 @@ struct ClusterScenes {
     int32_t rec_cap;           // records each block holds
 };
 
+// A state broadcast from lane src of the warp (every field of the trait's state type).
+template <typename ST>
+__device__ __forceinline__ typename ST::U shfl_state(typename ST::U u, int src) {
+    constexpr int kWords = int(sizeof(typename ST::U) / 4);
+    static_assert(sizeof(typename ST::U) % 4 == 0, "state of whole 32-bit words");
+    uint32_t w[kWords];
+    memcpy(w, &u, sizeof(u));
+#pragma unroll
+    for (int k = 0; k < kWords; ++k) w[k] = __shfl_sync(0xffffffffu, w[k], src);
+    memcpy(&u, w, sizeof(u));
+    return u;
+}
+
 template <int L, typename ST, typename R>
 __global__ void __launch_bounds__(256) k_sweep_cluster(Ptrs<ST, R> P, Consts<R> c, ClusterScenes S, int32_t* work) {
     using U = typename ST::U;
@@ -142,28 +155,37 @@ __global__ void __launch_bounds__(256) k_sweep_cluster(Ptrs<ST, R> P, Consts<R> 
                     U uo{};
                     MeshMat<R> mat;
                     if (valid) {
+                        if (lane == 0) prefetch_tail(P, v);
                         mat = P.mats[P.slot_mesh[v]];
                         uo = spos[v - sl.x];
+                        const U uon = ST::nb(uo);
                         const int e = rb + P.inc_ofs[v + 1] - r0;
                         for (int r = rb + P.inc_ofs[v] - r0 + lane; r < e; r += L) {
                             const RecRaw<R>& rec = srec[r].r;
-                            const U q0 = spos[loc(rec.n.x)], q1 = spos[loc(rec.n.y)], q2 = spos[loc(rec.n.z)];
+                            const U q0 = ST::nb(spos[loc(rec.n.x)]), q1 = ST::nb(spos[loc(rec.n.y)]),
+                                    q2 = ST::nb(spos[loc(rec.n.z)]);
                             R m0[3], m1[3], m2[3];
                             rec.rows(m0, m1, m2);
                             R e0[3], e1[3], e2[3];
-                            ST::diff(q0, uo, e0);
-                            ST::diff(q1, uo, e1);
-                            ST::diff(q2, uo, e2);
+                            ST::diff(q0, uon, e0);
+                            ST::diff(q1, uon, e1);
+                            ST::diff(q2, uon, e2);
                             incidence<R>(e0, e1, e2, m0, m1, m2, mat.mu, mat.lmbd, acc);
                         }
                     }
                     reduce_group<L, R>(acc);
-                    if (valid && lane == 0) {
-                        U un;
-                        if (vertex_tail<ST, R, false>(P, c, v, uo, mat, acc, friction, nullptr, beg, end, &un)) {
-                            const int lv = v - sl.x;
-                            for (int r = 0; r < C; ++r) *cluster.map_shared_rank(&spos[lv], r) = un;
-                        }
+                    // lane 0 solves; the group's lanes then write the new state into the C
+                    // copies, one remote store each, instead of lane 0 writing all of them
+                    U un{};
+                    int moved = 0;
+                    if (valid && lane == 0)
+                        moved = vertex_tail<ST, R, false>(P, c, v, uo, mat, acc, friction, nullptr, beg, end, &un) ? 1 : 0;
+                    const int src = int(threadIdx.x) & ~(L - 1) & 31;
+                    moved = __shfl_sync(0xffffffffu, moved, src);
+                    un = shfl_state<ST>(un, src);
+                    if (valid && moved) {
+                        const int lv = v - sl.x;
+                        for (int r = lane; r < C; r += L) *cluster.map_shared_rank(&spos[lv], r) = un;
                     }
                 }
                 cluster.sync();  // this color's states in every copy before the next color

@@ -483,6 +483,16 @@ __global__ void __launch_bounds__(128) k_contact_color(Ptrs<ST, R> P, Consts<R> 
     }
 }
 
+// The vertex tail's own inputs (inertia target, start-of-substep state, rest position) into
+// L1 while the incidence loop runs: they do not change during a sweep, and loaded only in
+// the tail their latency would follow the lane reduction on the critical path.
+template <typename ST, typename R>
+__device__ __forceinline__ void prefetch_tail(const Ptrs<ST, R>& P, int v) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(P.y + v));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(P.xprev + v));
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(P.rest + v));
+}
+
 // The incidence loop of one lane: records r, r + L, ... below e, the first (`cur`) already
 // loaded; two-stage pipeline (the next record is in flight during this incidence).
 // COHERENT: neighbour states with plain loads, for a kernel that itself wrote them
@@ -490,8 +500,9 @@ __global__ void __launch_bounds__(128) k_contact_color(Ptrs<ST, R> P, Consts<R> 
 // every iteration); otherwise states through the read-only cache and records streamed.
 template <int L, typename ST, typename R, bool COHERENT>
 __device__ __forceinline__ void accumulate_records(const Ptrs<ST, R>& P, int r, int e, RecRaw<R> cur,
-                                                   const typename ST::U& uo, R mu, R lmbd, Acc<R>& acc) {
+                                                   const typename ST::U& uo_full, R mu, R lmbd, Acc<R>& acc) {
     using U = typename ST::U;
+    const U uo = ST::nb(uo_full);
     while (r < e) {
         const int rn = r + L;
         RecRaw<R> nxt;
@@ -550,6 +561,7 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
         r = P.inc_ofs[v] + lane;
         e = P.inc_ofs[v + 1];
         if (r < e) cur.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r);
+        if (lane == 0 && !PROBE) prefetch_tail(P, v);
     }
     pdl_wait();
     if (valid) {
@@ -566,9 +578,10 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
 // record stream is long enough to need the memory-level parallelism (HBM-bound sweeps).
 template <int L, typename ST, typename R>
 __device__ __forceinline__ void accumulate_records3(const Ptrs<ST, R>& P, int r, int e, RecRaw<R> cur,
-                                                    RecRaw<R> nx1, const typename ST::U& uo, R mu, R lmbd,
+                                                    RecRaw<R> nx1, const typename ST::U& uo_full, R mu, R lmbd,
                                                     Acc<R>& acc) {
     using U = typename ST::U;
+    const U uo = ST::nb(uo_full);
     while (r < e) {
         const int r2 = r + 2 * L;
         RecRaw<R> nx2;
@@ -610,6 +623,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 8 ? 2 : 3)
         e = P.inc_ofs[v + 1];
         if (r < e) cur.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r);
         if (r + L < e) nx1.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r + L);
+        if (lane == 0) prefetch_tail(P, v);
     }
     pdl_wait();
     if (valid) {
@@ -830,15 +844,16 @@ __global__ void __launch_bounds__(256, 4)
     const bool ok = __syncthreads_and(mbar_wait(bar, 0, c.spin_limit)) != 0;
     Acc<float> acc = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (valid && ok) {
+        const U uon = ST::nb(uo);
         for (int r = rb; r < re; r += L) {
             const int4 n = s_n[r];
             const float4 a = s_a[r], b = s_b[r];
             const U q0 = ST::ldg(P.u, n.x), q1 = ST::ldg(P.u, n.y), q2 = ST::ldg(P.u, n.z);
             const float m0[3] = {a.x, a.y, a.z}, m1[3] = {a.w, b.x, b.y}, m2[3] = {b.z, b.w, f_bits(n.w)};
             float e0[3], e1[3], e2[3];
-            ST::diff(q0, uo, e0);
-            ST::diff(q1, uo, e1);
-            ST::diff(q2, uo, e2);
+            ST::diff(q0, uon, e0);
+            ST::diff(q1, uon, e1);
+            ST::diff(q2, uon, e2);
             incidence<float>(e0, e1, e2, m0, m1, m2, mat.mu, mat.lmbd, acc);
         }
     }
@@ -904,6 +919,7 @@ __global__ void __launch_bounds__(MAXB) k_sweep_scenes(Ptrs<ST, R> P, Consts<R> 
                         const int r = P.inc_ofs[v] + lane, e = P.inc_ofs[v + 1];
                         RecRaw<R> cur;
                         if (r < e) cur.load_kept(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r);
+                        if (lane == 0) prefetch_tail(P, v);
                         uo = ST::ld(P.u, v);
                         accumulate_records<L, ST, R, true>(P, r, e, cur, uo, mat.mu, mat.lmbd, acc);
                     }

@@ -63,6 +63,8 @@ struct StF32 {
         float4 v = reinterpret_cast<const float4*>(p)[i];
         return U{v.x, v.y, v.z, v.w};
     }
+    // the state as the incidence loop uses it (the vertex's own, like its neighbours')
+    __device__ static U nb(const U& u) { return u; }
     template <typename R>
     __device__ static void diff(const U& a, const U& b, R* o) {
         o[0] = R(a.x - b.x); o[1] = R(a.y - b.y); o[2] = R(a.z - b.z);
@@ -96,6 +98,7 @@ struct StF64 {
         double2 a = q[0], b = q[1];
         return U{a.x, a.y, b.x, b.y};
     }
+    __device__ static U nb(const U& u) { return u; }
     template <typename R>
     __device__ static void diff(const U& a, const U& b, R* o) {
         o[0] = R(a.x - b.x); o[1] = R(a.y - b.y); o[2] = R(a.z - b.z);
@@ -141,6 +144,7 @@ struct StDF {
         float4 a = q[0], b = q[1];
         return U{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     }
+    __device__ static U nb(const U& u) { return u; }
     // (a.hi - b.hi) + (a.lo - b.lo): relative error ~2^-23 of the result
     template <typename R>
     __device__ static void diff(const U& a, const U& b, R* o) {
@@ -162,13 +166,14 @@ struct StDF {
     }
 };
 
-// Double-float state read as FP32 by its neighbours: a vertex's own state (its update, its
-// inertia, damping, friction and ground terms) keeps both parts, so positions do not drift
-// by FP32 rounding from update to update, while the neighbour reads of the incidence loop
-// load only the high half (16 B instead of 32 B per gather; the low half counts as zero).
-// A neighbour's relative position then carries one FP32 rounding of its position, the
-// rounding of the FP32 mode's force, without the FP32 mode's accumulation of rounded
-// updates.
+// Double-float state read as FP32 in the incidence loop: a vertex's own state (its update,
+// its inertia, damping, friction and ground terms) keeps both parts, so positions do not
+// drift by FP32 rounding from update to update, while the incidence loop works on the high
+// halves only, the neighbours' (whose gathers load 16 B instead of 32 B) and the vertex's
+// own alike (nb): the element forces are those of the FP32 mode on the rounded positions,
+// consistent between the vertices of a tet (with the own low half but not the neighbours',
+// the forces of a tet's vertices would not balance and a body would drift), without the
+// FP32 mode's accumulation of rounded updates.
 struct StDFH : StDF {
     static constexpr int kCode = 40;
     __device__ static U ldg(const U* p, int i) {
@@ -179,6 +184,7 @@ struct StDFH : StDF {
         const float4 a = reinterpret_cast<const float4*>(p + i)[0];
         return U{a.x, a.y, a.z, a.w, 0.f, 0.f, 0.f, 0.f};
     }
+    __device__ static U nb(const U& u) { return U{u.hx, u.hy, u.hz, u.w, 0.f, 0.f, 0.f, 0.f}; }
 };
 
 }  // namespace dev

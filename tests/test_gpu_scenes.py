@@ -157,7 +157,7 @@ def test_plain_drop_cluster_mode(plain_drop, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("cluster", [2, 16])
+@pytest.mark.parametrize("cluster", [4, 16])
 def test_batch_cluster_mode(batch, precision, cluster):
     mp, pp, ref = batch
     x0, x, st = _run(mp, pp, precision, 30, sweepMode="cluster", clusterSize=cluster)
