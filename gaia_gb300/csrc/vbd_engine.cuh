@@ -1080,6 +1080,10 @@ public:
         if (cluster_fits_.empty())
             throw std::runtime_error("sweepMode \"cluster\" is not supported: a scene does not fit in the shared "
                                      "memory of a 16-block cluster");
+        if (sc_.p.clusterSize && !cluster_fit(sc_.p.clusterSize))
+            throw std::runtime_error("sweepMode \"cluster\" is not supported with clusterSize " +
+                                     std::to_string(sc_.p.clusterSize) + ": a scene does not fit in the shared "
+                                     "memory of a cluster of that many blocks");
         d_scene_slots_.upload(slots, &bytes_, st_);
         GAIA_CUDA(cudaStreamSynchronize(st_));
     }
@@ -1171,6 +1175,7 @@ public:
         }
         GAIA_CUDA(cudaMemsetAsync(d_counters_.p, 0, dev::CNT_N * sizeof(unsigned long long), st_));
         GAIA_CUDA(cudaStreamSynchronize(st_));
+        if (!(best < 1e30f)) throw std::runtime_error("cluster sweep: no configuration was timed");
         tuned_ms_ = double(best) / sc_.p.iterations;
         tuned_ = true;
     }

@@ -156,13 +156,27 @@ def test_plain_drop_cluster_mode(plain_drop, precision):
     assert rel <= (FP32_DROP_BOUND if precision == "fp32" else TOL[precision])
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("cluster", [4, 16])
+@pytest.mark.parametrize("precision,cluster", [("fp64", 8), ("fp64", 16), ("mixed", 4), ("mixed", 16)])
 def test_batch_cluster_mode(batch, precision, cluster):
     mp, pp, ref = batch
     x0, x, st = _run(mp, pp, precision, 30, sweepMode="cluster", clusterSize=cluster)
     assert st["sweep_mode"] == 2 and st["cluster_size"] == cluster
     assert _rel(x, ref, x0) <= TOL[precision]
+
+
+def test_cluster_size_that_does_not_fit_is_refused(batch):
+    """The 9^3 cube's FP64 records (96 B each) split over 4 blocks need ~350 KB of shared
+    memory per block: an explicit clusterSize 4 is refused, not launched."""
+    from gaia_gb300 import VBDPhysics, scenes
+
+    mp, pp, _ = batch
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, scenes.set_precision(pp, "fp64", out_path=pp + ".c4.json", sweepMode="cluster",
+                                                        clusterSize=4))
+    with pytest.raises(GaiaError) as ei:
+        phys.initialize()
+    assert ei.value.code == E_UNSUPPORTED and "clusterSize 4" in str(ei.value)
+    phys.close()
 
 
 def test_twist_cluster_mode(tmp_path, gaia_lib, oracle_lib):
