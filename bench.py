@@ -689,20 +689,28 @@ def main():
     if rank == 0:
         st = head["stats"]
         nact, ninc, n = head["nact"], head["ninc"], head["n"]
-        # roofline of the solve kernel: algorithmic bytes per iteration 64 B/vertex + 61 B/incidence
-        launches_solve = st["num_groups"] * args.iterations * args.steps
+        # roofline of the solve kernel: algorithmic bytes per iteration 64 B/vertex + 61 B/incidence;
+        # the persistent schedules run a substep's iterations in one launch
         alg_bytes_iter = 64.0 * nact + 61.0 * ninc
+        sweep_mode = st.get("sweep_mode", 0)
+        if sweep_mode == 0:
+            launches_solve, kernel, per_launch = st["num_groups"] * args.iterations * args.steps, "k_solve", \
+                alg_bytes_iter / st["num_groups"]
+        else:
+            launches_solve = args.steps * head.get("substeps", 1)
+            kernel = {1: "k_sweep_scenes", 2: "k_sweep_cluster", 3: "k_sweep_grid"}[sweep_mode]
+            per_launch = alg_bytes_iter * args.iterations
         achieved = alg_bytes_iter * args.iterations * args.steps / (head["sweep_ms"] / 1e3) / 1e9
         # DRAM bytes per solved incidence (records + per-vertex data) from the ncu captures
         # (TRAFFIC_BYTES_PER_INCIDENCE), scaled to one average launch here
         per_inc = TRAFFIC_BYTES_PER_INCIDENCE.get(head["precision"])
-        traffic = per_inc * ninc / st["num_groups"] if per_inc else None
+        traffic = per_inc * ninc / st["num_groups"] if per_inc and sweep_mode == 0 else None
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                     "traffic": traffic,
                     "traffic_source": "ncu DRAM bytes per incidence (FP32: 100^3 twist launches; double-float: 60^3 "
                                       "twist), times this launch's incidences",
-                    "peak_kind": peak_kind, "kernel": "k_solve",
-                    "algorithmic_bytes_per_launch": alg_bytes_iter / st["num_groups"],
+                    "peak_kind": peak_kind, "kernel": kernel,
+                    "algorithmic_bytes_per_launch": per_launch,
                     "avg_launch_us": 1e3 * head["sweep_ms"] / launches_solve}
         if fp64:
             fp64["speedup_over_fp64"] = head["value"] / fp64["value"]
@@ -718,6 +726,10 @@ def main():
                        "lanes_per_vertex": st["lanes_per_vertex"], "block": st["block_size"],
                        "solve_variant": st.get("solve_variant"), "overrides": overrides,
                        "color_configs": [[c["lanes"], c["block"], c["variant"]] for c in head["ccfg"]],
+                       "schedule": {"sweep_mode": ["merged", "scenes", "cluster", "grid"][sweep_mode],
+                                    "cluster_size": st.get("cluster_size", 0),
+                                    "autotuned_ms_per_iteration": {k: st.get(f"sweep_ms_{k}", 0.0) for k in
+                                                                   ("merged", "scenes", "cluster", "grid")}},
                        "l2": head["l2"]},
             "e2e": {"value": head["e2e_value"], "unit": "vertex-solves/s", "h2d_bytes_per_step": 24 * n,
                     "d2h_bytes_per_step": 24 * n, "steps": head["e2e_steps"]},

@@ -40,7 +40,7 @@ class Stats(C.Structure):
         ("contact_detections", C.c_int64), ("contact_stack_overflow", C.c_int64),
         ("contact_traverse_bounds", C.c_int64), ("device_timeouts", C.c_int64), ("nonfinite_solves", C.c_int64),
         ("sweep_mode", C.c_int32), ("cluster_size", C.c_int32), ("sweep_ms_merged", C.c_double),
-        ("sweep_ms_scenes", C.c_double), ("sweep_ms_cluster", C.c_double),
+        ("sweep_ms_scenes", C.c_double), ("sweep_ms_cluster", C.c_double), ("sweep_ms_grid", C.c_double),
     ]
 
     def as_dict(self) -> dict:

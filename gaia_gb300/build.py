@@ -25,10 +25,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["scene.cpp", "state_io.cpp", "vbd_engine.cu", "vbd_engine_f32.cu", "vbd_engine_df.cu", "vbd_engine_dfh.cu",
            "vbd_engine_f64.cu", "vbd_energy_noalloc.cu", "tet_cd.cu", "coloring_gpu.cu", "cloth_scene.cpp", "cloth_cd.cu",
            "cloth_engine.cu"]
-HEADERS = ["scene.hpp", "json_lite.hpp", "json_get.hpp", "vbd_engine.cuh", "vbd_kernels.cuh", "vbd_convergence.cuh",
-           "vbd_state.cuh",
-           "cloth_scene.hpp",
-           "cloth_cd.hpp", "cloth_dev.cuh", "lbvh.cuh", "state_io.hpp", "tet_cd.hpp"]
+# every header of csrc/ is a dependency of every translation unit
+HEADERS = sorted(f for f in os.listdir(CSRC) if f.endswith((".cuh", ".hpp", ".h")))
 PUBLIC_HEADERS = ["gaia_vbd.h", "gaia_cloth.h"]
 # The contact detector's predicates must round like the CPU restatement: no FMA contraction.
 EXTRA_FLAGS = {"cloth_cd.cu": ["--fmad=false"], "tet_cd.cu": ["--fmad=false"]}

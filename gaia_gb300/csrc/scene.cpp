@@ -581,8 +581,9 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
     if (p.numSubsteps <= 0 || p.timeStep <= 0) throw std::runtime_error("timeStep and numSubsteps must be positive");
     if (p.iterations < 0) throw std::runtime_error("iterations must be >= 0");
     if (p.evaluationSteps < 1) throw std::runtime_error("evaluationSteps must be >= 1");
-    if (p.sweepMode != "auto" && p.sweepMode != "merged" && p.sweepMode != "scenes" && p.sweepMode != "cluster")
-        throw std::runtime_error("sweepMode must be \"auto\", \"merged\", \"scenes\" or \"cluster\"");
+    if (p.sweepMode != "auto" && p.sweepMode != "merged" && p.sweepMode != "scenes" && p.sweepMode != "cluster" &&
+        p.sweepMode != "grid")
+        throw std::runtime_error("sweepMode must be \"auto\", \"merged\", \"scenes\", \"cluster\" or \"grid\"");
     if (p.clusterSize != 0 && p.clusterSize != 2 && p.clusterSize != 4 && p.clusterSize != 8 && p.clusterSize != 16)
         throw std::runtime_error("clusterSize must be 0 (autotune), 2, 4, 8 or 16");
     if (p.gpuPrecision != "fp32" && p.gpuPrecision != "mixed" && p.gpuPrecision != "dfhi" && p.gpuPrecision != "fp64")

@@ -20,8 +20,8 @@ struct gaia_vbd {
     std::unique_ptr<gaia::EngineBase> eng;
     std::string err;
     int64_t frame = 0;  // runStep calls since initialize / the last loaded state
-    double sweep_ms[3] = {0.0, 0.0, 0.0};  // autotuned schedule choice: measured ms per iteration, merged /
-                                           // scenes / cluster (0 where not timed)
+    double sweep_ms[4] = {0.0, 0.0, 0.0, 0.0};  // autotuned schedule choice: measured ms per iteration,
+                                                // merged / scenes / cluster / grid (0 where not timed)
 };
 
 namespace {
@@ -93,12 +93,13 @@ int gaia_vbd_initialize(gaia_vbd* h) {
             if (p.gpuPrecision == "dfhi") return gaia::make_engine_dfh(h->scene, mode);
             return gaia::make_engine_df(h->scene, mode);
         };
-        // color scheduling: merged colors (one launch per merged color and iteration) or
-        // scene-major (one persistent launch per substep). The scene-major sweep needs meshes
-        // that do not interact within a sweep and no per-iteration work outside the solve.
+        // color scheduling: merged colors (one launch per merged color and iteration), scene-major
+        // (one persistent launch per substep) or the grid sweep (one cooperative launch per
+        // substep over the merged colors). The persistent sweeps need no per-iteration work
+        // outside the solve; the scene-major ones also meshes that do not interact.
         const bool scenes_ok = !(p.allowCCD || p.allowDCD) && !p.useAccelerator && !p.evaluateConvergence &&
                                p.iterations > 0;
-        if ((p.sweepMode == "scenes" || p.sweepMode == "cluster") && !scenes_ok)
+        if ((p.sweepMode == "scenes" || p.sweepMode == "cluster" || p.sweepMode == "grid") && !scenes_ok)
             throw std::runtime_error("sweepMode \"" + p.sweepMode + "\" is not supported with contact detection, "
                                      "the accelerator or evaluateConvergence");
         if (p.sweepMode == "merged" || !scenes_ok || (p.sweepMode == "auto" && !p.autotune)) {
@@ -107,6 +108,8 @@ int gaia_vbd_initialize(gaia_vbd* h) {
             h->eng.reset(make(gaia::kSweepScenes));
         } else if (p.sweepMode == "cluster") {
             h->eng.reset(make(gaia::kSweepCluster));
+        } else if (p.sweepMode == "grid") {
+            h->eng.reset(make(gaia::kSweepGrid));
         } else {
             // autotuned: every schedule the scene allows is built and its sweep graph timed;
             // the fastest is kept (the cluster sweep only where every scene fits on-chip)
@@ -123,8 +126,8 @@ int gaia_vbd_initialize(gaia_vbd* h) {
                 largest = std::max(largest, n);
             }
             constexpr int64_t kSceneMajorMaxVertices = 65536;
-            for (int mode : {gaia::kSweepScenes, gaia::kSweepCluster}) {
-                if (largest > kSceneMajorMaxVertices) break;
+            for (int mode : {gaia::kSweepGrid, gaia::kSweepScenes, gaia::kSweepCluster}) {
+                if (mode != gaia::kSweepGrid && largest > kSceneMajorMaxVertices) break;
                 std::unique_ptr<gaia::EngineBase> e;
                 if (mode == gaia::kSweepCluster) {
                     try {
@@ -132,6 +135,16 @@ int gaia_vbd_initialize(gaia_vbd* h) {
                     } catch (const std::runtime_error& ex) {
                         if (std::string(ex.what()).find("does not fit") == std::string::npos) throw;
                         continue;  // a scene too large for a cluster's shared memory
+                    }
+                } else if (mode == gaia::kSweepGrid) {
+                    // a device or driver without cooperative launches in captured graphs: the
+                    // schedule is left out (sweep_ms_grid = -1); an explicit "grid" reports it
+                    try {
+                        e.reset(make(mode));
+                    } catch (const std::runtime_error&) {
+                        (void)cudaGetLastError();
+                        h->sweep_ms[mode] = -1.0;
+                        continue;
                     }
                 } else {
                     e.reset(make(mode));
@@ -455,6 +468,7 @@ int gaia_vbd_get_stats(gaia_vbd* h, gaia_vbd_stats* out) {
         out->sweep_ms_merged = h->sweep_ms[0];
         out->sweep_ms_scenes = h->sweep_ms[1];
         out->sweep_ms_cluster = h->sweep_ms[2];
+        out->sweep_ms_grid = h->sweep_ms[3];
     });
 }
 

@@ -28,6 +28,7 @@
 #include "tet_cd.hpp"
 #include "vbd_cluster.cuh"
 #include "vbd_convergence.cuh"
+#include "vbd_grid.cuh"
 #include "vbd_kernels.cuh"
 
 namespace gaia {
@@ -102,8 +103,9 @@ inline void make_record<double>(int4& n, dev::R4<double>& a, dev::R4<double>& b,
     *c = mv[2][2];
 }
 
-enum { kSweepMerged = 0, kSweepScenes = 1, kSweepCluster = 2 };
+enum { kSweepMerged = 0, kSweepScenes = 1, kSweepCluster = 2, kSweepGrid = 3 };
 constexpr int kVariantDeep = 4;  // solve variant: k_solve_deep
+constexpr int kVariantGrid = 5;  // solve variant: k_sweep_grid
 
 class EngineBase {
 public:
@@ -153,8 +155,10 @@ public:
     };
 
     // mode: kSweepMerged (one launch per merged color and iteration), kSweepScenes (one
-    // persistent launch per substep running every scene's iterations, scene-major slots) or
-    // kSweepCluster (the same on thread-block clusters with the scene in shared memory)
+    // persistent launch per substep running every scene's iterations, scene-major slots),
+    // kSweepCluster (the same on thread-block clusters with the scene in shared memory) or
+    // kSweepGrid (one cooperative launch per substep over the merged colors, a bounded grid
+    // barrier between colors)
     Engine(const Scene& s, int mode) : sc_(s), mode_(mode) {
         GAIA_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         GAIA_CUDA(cudaEventCreate(&ev_a_));
@@ -187,6 +191,10 @@ public:
             setup_cluster();
             if ((lanes_ == 0 || block_ == 0 || sc_.p.clusterSize == 0) && sc_.p.autotune) autotune_cluster();
             finalize_cluster();
+        } else if (mode_ == kSweepGrid) {
+            setup_grid();
+            if ((lanes_ == 0 || block_ == 0) && sc_.p.autotune) autotune_grid();
+            finalize_grid();
         } else {
             if ((lanes_ == 0 || block_ == 0 || variant_fixed_ < 0) && sc_.p.autotune) autotune_impl();
             finalize_cfg();
@@ -227,7 +235,7 @@ public:
         group_end_.clear();
         scene_colors_.clear();
         scene_ofs_.assign(1, 0);
-        if (mode_ != kSweepMerged) {
+        if (mode_ == kSweepScenes || mode_ == kSweepCluster) {
             // scene-major: mesh by mesh, within a mesh its vertices of merged color 0, 1, ...
             std::vector<std::vector<std::vector<int32_t>>> per(size_t(nmesh_),
                                                                std::vector<std::vector<int32_t>>(sc_.groups.size()));
@@ -817,6 +825,10 @@ public:
                     enqueue_cluster_sweep(scene_C_, scene_L_, scene_B_);
                     return;
                 }
+                if (mode_ == kSweepGrid) {
+                    enqueue_grid_sweep(scene_L_, scene_B_);
+                    return;
+                }
                 // evaluateConvergence at iteration -1, on the initial guess (VBDPhysics.cpp:866-870)
                 if (sc_.p.evaluateConvergence) enqueue_conv(true);
                 double omega = 1.0;
@@ -1194,6 +1206,114 @@ public:
         ccfg_.assign(sc_.groups.size(), ColorCfg{scene_L_, scene_B_, 3, float(tuned_ms_)});
     }
 
+    // ---- grid sweep (vbd_grid.cuh) -----------------------------------------------------
+    void setup_grid() {
+        std::vector<int2> colors;
+        for (size_t g = 0; g < group_beg_.size(); ++g)
+            if (group_end_[g] > group_beg_[g]) colors.push_back(make_int2(group_beg_[g], group_end_[g]));
+        grid_ncolors_ = int32_t(colors.size());
+        grid_max_color_ = 0;
+        for (const int2& c : colors) grid_max_color_ = std::max(grid_max_color_, c.y - c.x);
+        d_grid_colors_.upload(colors, &bytes_, st_);
+        d_grid_bar_.alloc(2, &bytes_);
+        int dev = 0, coop = 0;
+        GAIA_CUDA(cudaGetDevice(&dev));
+        GAIA_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, dev));
+        GAIA_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        if (!coop) throw std::runtime_error("sweepMode \"grid\" is not supported: no cooperative launch on this device");
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    // Blocks of the grid sweep: enough for the largest color at one vertex per group, at most
+    // as many as are resident at once (the cooperative launch requires it).
+    template <int L>
+    int grid_blocks(int B) const {
+        int per_sm = 0;
+        GAIA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::k_sweep_grid<L, ST, R>, B, 0));
+        if (per_sm < 1) throw std::runtime_error("grid sweep: no block of this size fits on an SM");
+        const int need = std::max(1, int(div_up(int64_t(grid_max_color_) * L, B)));
+        return std::min(need, per_sm * num_sms_);
+    }
+
+    template <int L>
+    void launch_grid_l(int B) {
+        dev::GridSweep G;
+        G.colors = d_grid_colors_.p;
+        G.ncolors = grid_ncolors_;
+        G.iterations = sc_.p.iterations;
+        G.friction_start = sc_.p.frictionStartIter;
+        G.bar = d_grid_bar_.p;
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cfg.gridDim = dim3(unsigned(grid_blocks<L>(B)));
+        cfg.blockDim = dim3(unsigned(B));
+        cfg.stream = st_;
+        GAIA_CUDA(cudaLaunchKernelEx(&cfg, dev::k_sweep_grid<L, ST, R>, ptrs(), c_, G));
+    }
+
+    // One substep's iterations: the barrier's counter and flag zeroed, one cooperative launch.
+    void enqueue_grid_sweep(int L, int B) {
+        if (grid_ncolors_ == 0 || sc_.p.iterations == 0) return;
+        GAIA_CUDA(cudaMemsetAsync(d_grid_bar_.p, 0, 2 * sizeof(uint32_t), st_));
+        switch (L) {
+            case 2: launch_grid_l<2>(B); break;
+            case 4: launch_grid_l<4>(B); break;
+            case 8: launch_grid_l<8>(B); break;
+            case 16: launch_grid_l<16>(B); break;
+            default: launch_grid_l<32>(B); break;
+        }
+    }
+
+    // Lanes per vertex and block size of the grid sweep, each pair timed on a full sweep of
+    // the current state (restored afterwards).
+    void autotune_grid() {
+        if (nactive_ == 0 || grid_ncolors_ == 0 || sc_.p.iterations == 0) return;
+        DevBuf<S4> save;
+        save.alloc(nslots_, nullptr);
+        GAIA_CUDA(cudaMemcpyAsync(save.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+        float best = 1e30f;
+        for (int L : {4, 8, 16, 32}) {
+            if (lanes_ && L != lanes_) continue;
+            for (int B : {128, 256}) {
+                if (block_ && B != block_) continue;
+                enqueue_grid_sweep(L, B);  // warm-up
+                GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+                GAIA_CUDA(cudaEventRecord(ev_a_, st_));
+                enqueue_grid_sweep(L, B);
+                GAIA_CUDA(cudaEventRecord(ev_b_, st_));
+                GAIA_CUDA(cudaEventSynchronize(ev_b_));
+                float ms = 0.f;
+                GAIA_CUDA(cudaEventElapsedTime(&ms, ev_a_, ev_b_));
+                GAIA_CUDA(cudaMemcpyAsync(d_pos_.p, save.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
+                if (ms < best) {
+                    best = ms;
+                    scene_L_ = L;
+                    scene_B_ = B;
+                }
+            }
+        }
+        GAIA_CUDA(cudaMemsetAsync(d_counters_.p, 0, dev::CNT_N * sizeof(unsigned long long), st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+        if (!(best < 1e30f)) throw std::runtime_error("grid sweep: no configuration was timed");
+        tuned_ms_ = double(best) / sc_.p.iterations;
+        tuned_ = true;
+    }
+
+    void finalize_grid() {
+        if (!tuned_) {
+            scene_L_ = lanes_ ? lanes_ : 16;
+            scene_B_ = block_ ? block_ : 256;
+        }
+        lanes_ = scene_L_;
+        block_ = scene_B_;
+        variant_ = kVariantGrid;
+        ccfg_.assign(sc_.groups.size(), ColorCfg{scene_L_, scene_B_, kVariantGrid, float(tuned_ms_)});
+    }
+
     void finalize_scenes() {
         if (!tuned_) {
             scene_L_ = lanes_ ? lanes_ : 8;
@@ -1238,6 +1358,9 @@ public:
         } else if (mode_ == kSweepCluster) {
             autotune_cluster();
             finalize_cluster();
+        } else if (mode_ == kSweepGrid) {
+            autotune_grid();
+            finalize_grid();
         } else {
             autotune_impl();
             finalize_cfg();
@@ -1618,8 +1741,8 @@ private:
     bool use_pdl_ = true;
     int small_color_ = 16384;
     int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma, 2 = k_sweep_scenes,
-                               // 3 = k_sweep_cluster, 4 = k_solve_deep
-    int mode_ = 0;             // kSweepMerged or kSweepScenes
+                               // 3 = k_sweep_cluster, 4 = k_solve_deep, 5 = k_sweep_grid
+    int mode_ = 0;             // kSweepMerged, kSweepScenes, kSweepCluster or kSweepGrid
     // scene-major mode: per mesh its color slot ranges, in sweep order
     std::vector<int2> scene_colors_;
     std::vector<int32_t> scene_ofs_;
@@ -1629,6 +1752,10 @@ private:
     DevBuf<int32_t> d_scene_ofs_, d_scene_order_, d_scene_work_;
     std::vector<ClusterFit> cluster_fits_;
     DevBuf<int4> d_scene_slots_;
+    // grid mode: the merged colors' slot ranges, the barrier's counter and abort flag
+    DevBuf<int2> d_grid_colors_;
+    DevBuf<uint32_t> d_grid_bar_;
+    int32_t grid_ncolors_ = 0, grid_max_color_ = 0;
     int variant_fixed_ = -1;   // from PhysicsParams solveVariant (-1 = autotune)
     std::map<std::pair<int, int>, int> maxrec_cache_;
     static constexpr size_t kTmaSmemMax = 200 * 1024;

@@ -493,12 +493,19 @@ __device__ __forceinline__ void prefetch_tail(const Ptrs<ST, R>& P, int v) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(P.rest + v));
 }
 
+// How the incidence loop reads neighbour states and records:
+//  kStateStream  states through the read-only cache (written by earlier launches only),
+//                records streamed (read once per launch);
+//  kStateBlock   states with plain loads (written earlier in the same kernel by the same
+//                block, ordered by a block barrier), records kept in the caches (read
+//                every iteration by the persistent sweeps);
+//  kStateGrid    states through L2 only (written earlier in the same kernel by other
+//                blocks, ordered by a grid barrier), records kept.
+enum StateRead { kStateStream = 0, kStateBlock = 1, kStateGrid = 2 };
+
 // The incidence loop of one lane: records r, r + L, ... below e, the first (`cur`) already
 // loaded; two-stage pipeline (the next record is in flight during this incidence).
-// COHERENT: neighbour states with plain loads, for a kernel that itself wrote them
-// earlier (the persistent sweep), and records kept in the caches (that kernel reads them
-// every iteration); otherwise states through the read-only cache and records streamed.
-template <int L, typename ST, typename R, bool COHERENT>
+template <int L, typename ST, typename R, int COHERENT>
 __device__ __forceinline__ void accumulate_records(const Ptrs<ST, R>& P, int r, int e, RecRaw<R> cur,
                                                    const typename ST::U& uo_full, R mu, R lmbd, Acc<R>& acc) {
     using U = typename ST::U;
@@ -507,11 +514,15 @@ __device__ __forceinline__ void accumulate_records(const Ptrs<ST, R>& P, int r, 
         const int rn = r + L;
         RecRaw<R> nxt;
         if (rn < e) {
-            if constexpr (COHERENT) nxt.load_kept(P.rec_n, P.rec_a, P.rec_b, P.rec_c, rn);
+            if constexpr (COHERENT != kStateStream) nxt.load_kept(P.rec_n, P.rec_a, P.rec_b, P.rec_c, rn);
             else nxt.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, rn);
         }
         U q0, q1, q2;
-        if constexpr (COHERENT) {
+        if constexpr (COHERENT == kStateGrid) {
+            q0 = ST::ldcg(P.u, cur.n.x);
+            q1 = ST::ldcg(P.u, cur.n.y);
+            q2 = ST::ldcg(P.u, cur.n.z);
+        } else if constexpr (COHERENT == kStateBlock) {
             q0 = ST::ld(P.u, cur.n.x);
             q1 = ST::ld(P.u, cur.n.y);
             q2 = ST::ld(P.u, cur.n.z);
@@ -566,7 +577,7 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
     pdl_wait();
     if (valid) {
         uo = P.u[v];
-        accumulate_records<L, ST, R, false>(P, r, e, cur, uo, mat.mu, mat.lmbd, acc);
+        accumulate_records<L, ST, R, kStateStream>(P, r, e, cur, uo, mat.mu, mat.lmbd, acc);
     }
     reduce_group<L, R>(acc);
     if (!valid || lane != 0) return;
@@ -920,8 +931,8 @@ __global__ void __launch_bounds__(MAXB) k_sweep_scenes(Ptrs<ST, R> P, Consts<R> 
                         RecRaw<R> cur;
                         if (r < e) cur.load_kept(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r);
                         if (lane == 0) prefetch_tail(P, v);
-                        uo = ST::ld(P.u, v);
-                        accumulate_records<L, ST, R, true>(P, r, e, cur, uo, mat.mu, mat.lmbd, acc);
+                        uo = ST::ld_own(P.u, v);
+                        accumulate_records<L, ST, R, kStateBlock>(P, r, e, cur, uo, mat.mu, mat.lmbd, acc);
                     }
                     reduce_group<L, R>(acc);
                     if (valid && lane == 0) vertex_tail<ST, R, false>(P, c, v, uo, mat, acc, friction, nullptr, rg.x, rg.y);

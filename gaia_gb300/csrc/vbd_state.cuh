@@ -58,11 +58,21 @@ struct StF32 {
         float4 v = __ldg(reinterpret_cast<const float4*>(p) + i);
         return U{v.x, v.y, v.z, v.w};
     }
-    // coherent load: for state written earlier in the same kernel (ordered by a barrier)
+    // coherent load: for state written earlier in the same kernel by the same block
+    // (ordered by a block barrier)
     __device__ static U ld(const U* p, int i) {
         float4 v = reinterpret_cast<const float4*>(p)[i];
         return U{v.x, v.y, v.z, v.w};
     }
+    // load through L2 only: for state written earlier in the same kernel by other blocks
+    // (ordered by a grid barrier; the reading SM's L1 may hold an older copy of the line)
+    __device__ static U ldcg(const U* p, int i) {
+        float4 v = __ldcg(reinterpret_cast<const float4*>(p) + i);
+        return U{v.x, v.y, v.z, v.w};
+    }
+    // the vertex's own state in full (ld / ldcg return what the incidence loop reads)
+    __device__ static U ld_own(const U* p, int i) { return ld(p, i); }
+    __device__ static U ldcg_own(const U* p, int i) { return ldcg(p, i); }
     // the state as the incidence loop uses it (the vertex's own, like its neighbours')
     __device__ static U nb(const U& u) { return u; }
     template <typename R>
@@ -98,6 +108,13 @@ struct StF64 {
         double2 a = q[0], b = q[1];
         return U{a.x, a.y, b.x, b.y};
     }
+    __device__ static U ldcg(const U* p, int i) {
+        const double2* q = reinterpret_cast<const double2*>(p + i);
+        double2 a = __ldcg(q), b = __ldcg(q + 1);
+        return U{a.x, a.y, b.x, b.y};
+    }
+    __device__ static U ld_own(const U* p, int i) { return ld(p, i); }
+    __device__ static U ldcg_own(const U* p, int i) { return ldcg(p, i); }
     __device__ static U nb(const U& u) { return u; }
     template <typename R>
     __device__ static void diff(const U& a, const U& b, R* o) {
@@ -144,6 +161,13 @@ struct StDF {
         float4 a = q[0], b = q[1];
         return U{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     }
+    __device__ static U ldcg(const U* p, int i) {
+        const float4* q = reinterpret_cast<const float4*>(p + i);
+        float4 a = __ldcg(q), b = __ldcg(q + 1);
+        return U{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    }
+    __device__ static U ld_own(const U* p, int i) { return ld(p, i); }
+    __device__ static U ldcg_own(const U* p, int i) { return ldcg(p, i); }
     __device__ static U nb(const U& u) { return u; }
     // (a.hi - b.hi) + (a.lo - b.lo): relative error ~2^-23 of the result
     template <typename R>
@@ -184,6 +208,13 @@ struct StDFH : StDF {
         const float4 a = reinterpret_cast<const float4*>(p + i)[0];
         return U{a.x, a.y, a.z, a.w, 0.f, 0.f, 0.f, 0.f};
     }
+    __device__ static U ldcg(const U* p, int i) {
+        const float4 a = __ldcg(reinterpret_cast<const float4*>(p + i));
+        return U{a.x, a.y, a.z, a.w, 0.f, 0.f, 0.f, 0.f};
+    }
+    // the own state keeps its low half (the update accumulates into both)
+    __device__ static U ld_own(const U* p, int i) { return StDF::ld(p, i); }
+    __device__ static U ldcg_own(const U* p, int i) { return StDF::ldcg(p, i); }
     __device__ static U nb(const U& u) { return U{u.hx, u.hy, u.hz, u.w, 0.f, 0.f, 0.f, 0.f}; }
 };
 

@@ -62,7 +62,7 @@ typedef struct {
     double autotune_ms_per_iteration; /* best measured sweep time per iteration (0 if not tuned) */
     int32_t solve_variant;        /* 0 = register-pipelined solve kernel, 1 = TMA-staged records,
                                      2 = scene-major persistent sweep, 3 = cluster sweep, 4 = register
-                                     pipeline two records deep (of the largest color) */
+                                     pipeline two records deep (of the largest color), 5 = grid sweep */
     int32_t reserved;
     /* tet-mesh contact detection (cumulative; 0 when contact is off) */
     int64_t contact_detections;       /* detection passes run */
@@ -74,11 +74,14 @@ typedef struct {
     int32_t sweep_mode;               /* color scheduling: 0 = merged colors (a launch per merged color
                                          and iteration), 1 = scene-major persistent sweep, one block per
                                          scene (solve_variant 2), 2 = scene-major sweep on thread-block
-                                         clusters with the scene in shared memory (solve_variant 3) */
+                                         clusters with the scene in shared memory (solve_variant 3),
+                                         3 = one cooperative launch per substep over the merged colors
+                                         with a bounded grid barrier between colors (solve_variant 5) */
     int32_t cluster_size;             /* blocks per cluster of the cluster sweep (0 otherwise) */
     double sweep_ms_merged;           /* sweep time per iteration the autotuner measured for each */
     double sweep_ms_scenes;           /* schedule (0 where it did not time it) */
     double sweep_ms_cluster;
+    double sweep_ms_grid;             /* (-1: the grid sweep could not be built here) */
 } gaia_vbd_stats;
 
 /* ---- life cycle ------------------------------------------------------------
@@ -92,10 +95,12 @@ typedef struct {
  * parallel groups and uploads everything. repo_root may be NULL.
  * Extra PhysicsParams keys: "gpuPrecision" ("fp32" | "mixed" | "dfhi" | "fp64"),
  * "lanesPerVertex", "blockSize" (0 = autotune), "autotune" (bool), "sweepMode"
- * ("auto" | "merged" | "scenes" | "cluster": color scheduling, see gaia_vbd_stats.sweep_mode;
- * auto times every schedule the scene allows and keeps the fastest; the scene-major sweeps
- * need contact detection, the accelerator and evaluateConvergence off, and the cluster sweep
- * scenes that fit in the shared memory of a cluster), "clusterSize" (0 = autotune, 2-16).
+ * ("auto" | "merged" | "scenes" | "cluster" | "grid": color scheduling, see
+ * gaia_vbd_stats.sweep_mode; auto times every schedule the scene allows and keeps the fastest;
+ * the persistent sweeps need contact detection, the accelerator and evaluateConvergence off,
+ * and the cluster sweep scenes that fit in the shared memory of a cluster), "clusterSize"
+ * (0 = autotune, 2-16), "waitPollLimit" (polls of a bounded device wait before it gives up:
+ * the staged records' wait and the grid barrier; default 2^20).
  */
 int gaia_vbd_create(const char* models_json, const char* params_json, const char* repo_root, gaia_vbd** out);
 /* The two halves of gaia_vbd_create. gaia_vbd_load is host-only (no GPU needed):

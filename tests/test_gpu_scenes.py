@@ -1,5 +1,6 @@
-"""The scene-major persistent sweeps (sweepMode "scenes", k_sweep_scenes; sweepMode
-"cluster", k_sweep_cluster) and the autotuned choice of color scheduling.
+"""The persistent sweeps (sweepMode "scenes", k_sweep_scenes; sweepMode "cluster",
+k_sweep_cluster; sweepMode "grid", k_sweep_grid) and the autotuned choice of color
+scheduling.
 
 In this mode one launch per substep runs every scene's iterations: each block takes whole
 meshes, their colors in the merged groups' order, a block barrier between colors. Meshes
@@ -9,6 +10,9 @@ do not interact there, so per mesh the update sequence equals the merged sweep's
 - bit-identical to the merged sweep when both use the same lanes per vertex;
 - the autotuner times both schedules and keeps the faster (stats report both times);
 - the mode is refused where it cannot hold: contact detection on.
+The grid sweep runs the merged colors in one cooperative launch per substep with a bounded
+grid barrier between colors: against the oracle, bit-identical to the per-color launches,
+and its barrier made to run out (a poll limit of zero) returns a status.
 """
 import numpy as np
 import pytest
@@ -115,9 +119,9 @@ def test_scenes_mode_equals_merged(batch, lanes):
 def test_autotuner_picks_schedule(plain_drop, batch):
     for mp, pp, _ in (plain_drop, batch):
         _, _, st = _run(mp, pp, "mixed", 1)
-        times = [st["sweep_ms_merged"], st["sweep_ms_scenes"], st["sweep_ms_cluster"]]
-        print(f"ms/iteration: merged {times[0]:.4f}, scenes {times[1]:.4f}, cluster {times[2]:.4f}: "
-              f"mode {st['sweep_mode']}")
+        times = [st["sweep_ms_merged"], st["sweep_ms_scenes"], st["sweep_ms_cluster"], st["sweep_ms_grid"]]
+        print(f"ms/iteration: merged {times[0]:.4f}, scenes {times[1]:.4f}, cluster {times[2]:.4f}, "
+              f"grid {times[3]:.4f}: mode {st['sweep_mode']}")
         assert all(t > 0 for t in times)
         assert st["sweep_mode"] == int(np.argmin(times))
 
@@ -215,5 +219,77 @@ def test_cluster_mode_refused_when_too_large(tmp_path, gaia_lib):
     phys2.loadRunningparameters(mp, scenes.set_precision(pp, "mixed", out_path=pp + ".auto.json"))
     phys2.initialize()
     st = phys2.stats()
-    assert st["sweep_mode"] in (0, 1) and st["sweep_ms_cluster"] == 0
+    assert st["sweep_mode"] in (0, 1, 3) and st["sweep_ms_cluster"] == 0
     phys2.close()
+
+
+# ---------------------------------------------------------------- the grid sweep
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "dfhi", "fp32"])
+def test_plain_drop_grid_mode(plain_drop, precision):
+    """The plain-drop configuration in one cooperative launch per substep (merged colors, a
+    grid barrier between colors), against the FP64 oracle."""
+    from tests.test_gpu_parity import FP32_DROP_BOUND
+
+    mp, pp, ref = plain_drop
+    x0, x, st = _run(mp, pp, precision, 100, sweepMode="grid")
+    assert st["sweep_mode"] == 3 and st["solve_variant"] == 5 and st["device_timeouts"] == 0
+    rel = _rel(x, ref, x0)
+    print(f"plain drop, grid mode, {precision}: rel {rel:.3e}, lanes {st['lanes_per_vertex']} block "
+          f"{st['block_size']}, {st['kernel_launches_per_step']} launches per step")
+    assert rel <= (FP32_DROP_BOUND if precision == "fp32" else TOL[precision])
+    assert st["kernel_launches_per_step"] <= 4
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_and_twist_grid_mode(batch, precision, tmp_path, oracle_lib):
+    mp, pp, ref = batch
+    x0, x, st = _run(mp, pp, precision, 30, sweepMode="grid")
+    assert st["sweep_mode"] == 3
+    assert _rel(x, ref, x0) <= TOL[precision]
+    from gaia_gb300 import scenes
+
+    mp, pp = scenes.twist_cube(str(tmp_path), n=10, iterations=20)
+    ref = _oracle(mp, pp, 20, oracle_lib)
+    x0, x, st = _run(mp, pp, precision, 20, sweepMode="grid")
+    assert _rel(x, ref, x0) <= TOL[precision]
+
+
+@pytest.mark.parametrize("lanes,block", [(4, 128), (16, 256)])
+def test_grid_mode_equals_merged(batch, lanes, block):
+    """Same lanes per vertex: the grid sweep and the per-color launches give bit-identical
+    positions (dfhi: own and neighbour states read through L2)."""
+    mp, pp, _ = batch
+    for precision in ("mixed", "dfhi"):
+        common = dict(lanesPerVertex=lanes, blockSize=block, autotune=False, smallColorVertices=0, solveVariant=0)
+        _, xa, sa = _run(mp, pp, precision, 10, sweepMode="merged", **common)
+        _, xg, sg = _run(mp, pp, precision, 10, sweepMode="grid", **common)
+        assert sa["sweep_mode"] == 0 and sg["sweep_mode"] == 3
+        np.testing.assert_array_equal(xa, xg)
+
+
+def test_grid_barrier_timeout_is_reported(plain_drop):
+    """waitPollLimit 0: a block that is not the last to arrive at a grid barrier gives up at
+    once, raises the abort flag, and every other block gives up at its next barrier; the
+    kernel ends, the next synchronizing call returns GAIA_VBD_E_DEVICE_TIMEOUT once, and the
+    state stays finite and readable."""
+    from gaia_gb300 import VBDPhysics, scenes
+    from gaia_gb300._lib import E_DEVICE_TIMEOUT
+
+    mp, pp, _ = plain_drop
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, scenes.set_precision(pp, "mixed", out_path=pp + ".gridto.json", sweepMode="grid",
+                                                        lanesPerVertex=16, blockSize=128, autotune=False,
+                                                        waitPollLimit=0))
+    phys.initialize()
+    phys.runStep(1)
+    with pytest.raises(GaiaError) as ei:
+        phys.synchronize()
+    assert ei.value.code == E_DEVICE_TIMEOUT, str(ei.value)
+    st = phys.stats()
+    assert st["device_timeouts"] > 0 and st["sweep_mode"] == 3
+    phys.synchronize()  # reported once
+    assert np.isfinite(phys.positions(0)).all()
+    phys.close()
+    # the built-in limit: no timeout
+    x0, x, st = _run(mp, pp, "mixed", 2, sweepMode="grid", lanesPerVertex=16, blockSize=128, autotune=False)
+    assert st["device_timeouts"] == 0 and np.isfinite(x).all()
