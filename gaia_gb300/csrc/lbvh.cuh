@@ -165,32 +165,45 @@ __global__ void k_karras(const unsigned long long* keys, int n, int2* child, int
     if (i == 0) parent[0] = -1;
 }
 
+// Arrival at an internal node of the refit: acquire-release at device scope, so the box
+// this thread wrote before is visible to the thread that arrives second, and that thread
+// sees the first one's box (no separate fences on the path up).
+__device__ __forceinline__ int refit_arrive(int* flag) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(flag) : "memory");
+    return old;
+}
+
 // Leaf boxes from the current positions, then bottom-up unions: the second thread to
-// reach an internal node computes its box (the first returns) and resets its flag.
+// reach an internal node computes its box (the first returns) and resets its flag. The
+// thread carries the box of the child it comes from in registers and loads only the
+// sibling's; the length of the walk (the hierarchy's depth, a few tens of levels) is the
+// kernel's critical path, one atomic and one box load per level.
 __global__ void k_refit(Prims t, const float4* xf, int n, const unsigned long long* keys, const int2* child,
                         const int* parent, float4* bmin, float4* bmax, int* flags, const int* req) {
     if (req && *req == 0) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const int node = (n - 1) + i;
+    int node = (n - 1) + i;
     float3 lo, hi;
     prim_box(t, xf, int(keys[i] & 0xffffffffull), lo, hi);
     bmin[node] = make_float4(lo.x, lo.y, lo.z, 0.f);
     bmax[node] = make_float4(hi.x, hi.y, hi.z, 0.f);
     if (n == 1) return;
-    __threadfence();
-    int p = parent[node];
+    int p = __ldg(&parent[node]);
     while (p >= 0) {
-        if (atomicAdd(&flags[p], 1) == 0) return;
+        const int2 c = __ldg(&child[p]);
+        const int pp = __ldg(&parent[p]);
+        if (refit_arrive(&flags[p]) == 0) return;
         flags[p] = 0;
-        __threadfence();
-        const int2 c = child[p];
-        const float4 l0 = __ldcg(&bmin[c.x]), l1 = __ldcg(&bmax[c.x]);
-        const float4 r0 = __ldcg(&bmin[c.y]), r1 = __ldcg(&bmax[c.y]);
-        bmin[p] = make_float4(fminf(l0.x, r0.x), fminf(l0.y, r0.y), fminf(l0.z, r0.z), 0.f);
-        bmax[p] = make_float4(fmaxf(l1.x, r1.x), fmaxf(l1.y, r1.y), fmaxf(l1.z, r1.z), 0.f);
-        __threadfence();
-        p = parent[p];
+        const int sib = c.x == node ? c.y : c.x;
+        const float4 s0 = __ldcg(&bmin[sib]), s1 = __ldcg(&bmax[sib]);
+        lo = make_float3(fminf(lo.x, s0.x), fminf(lo.y, s0.y), fminf(lo.z, s0.z));
+        hi = make_float3(fmaxf(hi.x, s1.x), fmaxf(hi.y, s1.y), fmaxf(hi.z, s1.z));
+        bmin[p] = make_float4(lo.x, lo.y, lo.z, 0.f);
+        bmax[p] = make_float4(hi.x, hi.y, hi.z, 0.f);
+        node = p;
+        p = pp;
     }
 }
 
