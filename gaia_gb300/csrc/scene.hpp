@@ -74,7 +74,8 @@ struct PhysicsParams {
     bool autotune = true;
     bool usePDL = true;                  // programmatic dependent launch between color kernels
     int smallColorVertices = 16384;      // colors up to this size use one warp per vertex
-    int solveVariant = -1;               // -1 autotune, 0 register-pipelined, 1 TMA-staged records
+    int solveVariant = -1;               // -1 autotune, 0 register-pipelined, 1 TMA-staged records, 4 deeper
+                                         // register pipeline, 6 next wave's records prefetched into L2
     std::string sweepMode = "auto";      // color scheduling: "auto", "merged", "scenes", "cluster", "grid"
     int clusterSize = 0;                 // blocks per cluster of the cluster sweep (0 = autotune; 2, 4, 8, 16)
     int waitPollLimit = -1;              // polls of a bounded device wait (-1: the built-in limit); tests

@@ -106,6 +106,7 @@ inline void make_record<double>(int4& n, dev::R4<double>& a, dev::R4<double>& b,
 enum { kSweepMerged = 0, kSweepScenes = 1, kSweepCluster = 2, kSweepGrid = 3 };
 constexpr int kVariantDeep = 4;  // solve variant: k_solve_deep
 constexpr int kVariantGrid = 5;  // solve variant: k_sweep_grid
+constexpr int kVariantPrefetch = 6;  // solve variant: k_solve with the next wave's records prefetched into L2
 
 class EngineBase {
 public:
@@ -177,10 +178,12 @@ public:
         small_color_ = sc_.p.smallColorVertices;
         set_tma_smem_limits();
         variant_fixed_ = sc_.p.solveVariant;
-        if (variant_fixed_ != -1 && variant_fixed_ != 0 && variant_fixed_ != 1 && variant_fixed_ != kVariantDeep)
-            throw std::runtime_error("solveVariant must be -1 (autotune), 0 (registers), 1 (TMA-staged) or 4 (registers, "
-                                     "deeper record pipeline)");
-        if (variant_fixed_ == 1 && sizeof(R) != 4) variant_fixed_ = 0;  // the FP64 engine has no TMA variant
+        if (variant_fixed_ != -1 && variant_fixed_ != 0 && variant_fixed_ != 1 && variant_fixed_ != kVariantDeep &&
+            variant_fixed_ != kVariantPrefetch)
+            throw std::runtime_error("solveVariant must be -1 (autotune), 0 (registers), 1 (TMA-staged), 4 (registers, "
+                                     "deeper record pipeline) or 6 (registers, next wave's records prefetched into L2)");
+        // the FP64 engine has neither the TMA variant nor the record prefetch
+        if ((variant_fixed_ == 1 || variant_fixed_ == kVariantPrefetch) && sizeof(R) != 4) variant_fixed_ = 0;
         if (variant_fixed_ >= 0) variant_ = variant_fixed_;
         if (mode_ == kSweepScenes) {
             setup_scenes();
@@ -574,7 +577,7 @@ public:
     // the previous kernel in the stream (its static-data prologue overlaps that
     // kernel's tail; k_solve waits on griddepcontrol before reading positions).
     template <bool PROBE, int L>
-    void launch_solve_l(int grid, int B, int beg, int end, int friction, double* probe, bool pdl) {
+    void launch_solve_l(int grid, int B, int beg, int end, int friction, double* probe, bool pdl, int pf = 0) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(grid);
         cfg.blockDim = dim3(B);
@@ -585,7 +588,7 @@ public:
         attr[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = pdl ? attr : nullptr;
         cfg.numAttrs = pdl ? 1 : 0;
-        GAIA_CUDA(cudaLaunchKernelEx(&cfg, dev::k_solve<L, ST, R, PROBE>, ptrs(), c_, beg, end, friction, probe));
+        GAIA_CUDA(cudaLaunchKernelEx(&cfg, dev::k_solve<L, ST, R, PROBE>, ptrs(), c_, beg, end, friction, probe, pf));
     }
 
     // Largest record count of any block of vpb consecutive vertices in [beg, end).
@@ -675,13 +678,34 @@ public:
             return;
         }
         int grid = div_up(int64_t(end - beg) * L, B);
+        const bool pf = !PROBE && variant == kVariantPrefetch;
         switch (L) {
-            case 2: launch_solve_l<PROBE, 2>(grid, B, beg, end, friction, probe, pdl); break;
-            case 4: launch_solve_l<PROBE, 4>(grid, B, beg, end, friction, probe, pdl); break;
-            case 8: launch_solve_l<PROBE, 8>(grid, B, beg, end, friction, probe, pdl); break;
-            case 16: launch_solve_l<PROBE, 16>(grid, B, beg, end, friction, probe, pdl); break;
-            default: launch_solve_l<PROBE, 32>(grid, B, beg, end, friction, probe, pdl); break;
+            case 2: launch_solve_l<PROBE, 2>(grid, B, beg, end, friction, probe, pdl, pf ? wave_blocks<2>(B) : 0); break;
+            case 4: launch_solve_l<PROBE, 4>(grid, B, beg, end, friction, probe, pdl, pf ? wave_blocks<4>(B) : 0); break;
+            case 8: launch_solve_l<PROBE, 8>(grid, B, beg, end, friction, probe, pdl, pf ? wave_blocks<8>(B) : 0); break;
+            case 16:
+                launch_solve_l<PROBE, 16>(grid, B, beg, end, friction, probe, pdl, pf ? wave_blocks<16>(B) : 0);
+                break;
+            default:
+                launch_solve_l<PROBE, 32>(grid, B, beg, end, friction, probe, pdl, pf ? wave_blocks<32>(B) : 0);
+                break;
         }
+    }
+
+    // Blocks of k_solve<L> resident on the whole device at once (one wave): the distance at
+    // which the prefetching variant fetches records ahead.
+    template <int L>
+    int wave_blocks(int B) {
+        const auto key = std::make_pair(L, B);
+        auto it = wave_cache_.find(key);
+        if (it != wave_cache_.end()) return it->second;
+        int per_sm = 0, dev = 0, sms = 0;
+        GAIA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::k_solve<L, ST, R, false>, B, 0));
+        GAIA_CUDA(cudaGetDevice(&dev));
+        GAIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const int w = std::max(1, per_sm * sms);
+        wave_cache_[key] = w;
+        return w;
     }
 
     // Launch configuration of every merged color. Colors differ in size and in
@@ -903,9 +927,13 @@ public:
         const int Ls[] = {2, 4, 8, 16, 32};
         const int Bs[] = {128, 256};
         // kernel variants: 0 register-pipelined, 1 TMA-staged (FP32 compute only), 4 deeper
-        // register pipeline
+        // register pipeline, 6 register-pipelined with the records of the block one resident
+        // wave ahead bulk-prefetched into L2 (FP32 compute only)
         std::vector<int> variants = {0, kVariantDeep};
-        if (sizeof(R) == 4) variants.push_back(1);
+        if (sizeof(R) == 4) {
+            variants.push_back(1);
+            variants.push_back(kVariantPrefetch);
+        }
         const int reps = 4;
         ccfg_.assign(group_beg_.size(), ColorCfg{});
         double total = 0.0;
@@ -1741,7 +1769,8 @@ private:
     bool use_pdl_ = true;
     int small_color_ = 16384;
     int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma, 2 = k_sweep_scenes,
-                               // 3 = k_sweep_cluster, 4 = k_solve_deep, 5 = k_sweep_grid
+                               // 3 = k_sweep_cluster, 4 = k_solve_deep, 5 = k_sweep_grid, 6 = k_solve with L2
+                               // prefetch of the next wave's records
     int mode_ = 0;             // kSweepMerged, kSweepScenes, kSweepCluster or kSweepGrid
     // scene-major mode: per mesh its color slot ranges, in sweep order
     std::vector<int2> scene_colors_;
@@ -1758,6 +1787,7 @@ private:
     int32_t grid_ncolors_ = 0, grid_max_color_ = 0;
     int variant_fixed_ = -1;   // from PhysicsParams solveVariant (-1 = autotune)
     std::map<std::pair<int, int>, int> maxrec_cache_;
+    std::map<std::pair<int, int>, int> wave_cache_;  // (lanes, block) -> resident blocks of k_solve
     static constexpr size_t kTmaSmemMax = 200 * 1024;
     static constexpr int kContactBlocks = 64;
     double tuned_ms_ = 0.0;

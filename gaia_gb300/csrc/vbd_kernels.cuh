@@ -543,6 +543,30 @@ __device__ __forceinline__ void accumulate_records(const Ptrs<ST, R>& P, int r, 
     }
 }
 
+// Bulk prefetch into L2 (no shared memory, no completion to wait for): addr and bytes
+// 16-byte aligned.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* addr, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(addr), "r"(bytes) : "memory");
+}
+
+// The FP32 records (three 16-byte arrays) of block b of a color launch with blockDim / L
+// vertices per block, prefetched into L2: the block that runs one resident wave later then
+// finds its record stream in L2, and the DRAM reads run ahead of the warps that consume
+// them (a latency-bound sweep keeps more bytes in flight than its warps' registers hold).
+template <int L, typename ST, typename R>
+__device__ __forceinline__ void prefetch_block_records(const Ptrs<ST, R>& P, int beg, int end, int b) {
+    const int vpb = int(blockDim.x) / L;
+    const long long v0l = (long long)beg + (long long)b * vpb;
+    if (v0l >= end) return;
+    const int v0 = int(v0l), v1 = min(end, v0 + vpb);
+    const int r0 = P.inc_ofs[v0], r1 = P.inc_ofs[v1];
+    if (r1 <= r0) return;
+    const uint32_t bytes = uint32_t(r1 - r0) * 16u;
+    bulk_prefetch_l2(P.rec_n + r0, bytes);
+    bulk_prefetch_l2(P.rec_a + r0, bytes);
+    bulk_prefetch_l2(P.rec_b + r0, bytes);
+}
+
 // Minimum resident blocks of 256 threads: caps FP32-compute kernels at 64
 // registers (32 warps per SM, no spills); the FP64 kernel keeps its registers.
 template <typename R>
@@ -552,7 +576,7 @@ struct SolveOcc {
 
 template <int L, typename ST, typename R, bool PROBE>
 __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
-    k_solve(Ptrs<ST, R> P, Consts<R> c, int beg, int end, int friction, double* probe_out) {
+    k_solve(Ptrs<ST, R> P, Consts<R> c, int beg, int end, int friction, double* probe_out, int pf) {
     using U = typename ST::U;
     using Sc = typename ST::Sc;
     pdl_launch_dependents();
@@ -565,6 +589,9 @@ __global__ void __launch_bounds__(256, SolveOcc<R>::kMinBlocks)
     MeshMat<R> mat;
     int r = 0, e = 0;
     RecRaw<R> cur;
+    // the records of the block pf blocks ahead (one resident wave later) into L2
+    if constexpr (sizeof(R) == 4 && !PROBE)
+        if (pf > 0 && threadIdx.x == 0) prefetch_block_records<L>(P, beg, end, int(blockIdx.x) + pf);
     // prologue on static data (records, CSR offsets, materials): overlaps the
     // previous color's tail when launched as a programmatic dependent
     if (valid) {

@@ -62,7 +62,9 @@ typedef struct {
     double autotune_ms_per_iteration; /* best measured sweep time per iteration (0 if not tuned) */
     int32_t solve_variant;        /* 0 = register-pipelined solve kernel, 1 = TMA-staged records,
                                      2 = scene-major persistent sweep, 3 = cluster sweep, 4 = register
-                                     pipeline two records deep (of the largest color), 5 = grid sweep */
+                                     pipeline two records deep, 6 = register pipeline with the records
+                                     of the next resident wave prefetched into L2 (of the largest
+                                     color), 5 = grid sweep */
     int32_t reserved;
     /* tet-mesh contact detection (cumulative; 0 when contact is off) */
     int64_t contact_detections;       /* detection passes run */

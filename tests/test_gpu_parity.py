@@ -88,18 +88,30 @@ def test_lanes_per_vertex_agree(drop_scene, drop_ref, lanes):
     assert _rel(xs[0], drop_ref[0], x0[0]) <= TOL["fp64"]
 
 
-@pytest.mark.parametrize("variant", [0, 1, 4])
+@pytest.mark.parametrize("variant", [0, 1, 4, 6])
 @pytest.mark.parametrize("lanes", [4, 32])
 @pytest.mark.parametrize("precision", ["mixed", "dfhi", "fp32"])
 def test_solve_variants_agree(drop_scene, drop_ref, variant, lanes, precision):
-    """Register-pipelined (0), TMA-staged (1) and two-deep register-pipelined (4) solve
-    kernels, with and without programmatic dependent launch, give the oracle's result."""
+    """Register-pipelined (0), TMA-staged (1), two-deep register-pipelined (4) and
+    register-pipelined with the next wave's records prefetched into L2 (6) solve kernels,
+    with and without programmatic dependent launch, give the oracle's result."""
     mp, pp = drop_scene
     for pdl in (True, False):
         x0, xs, st = _run_gpu(mp, pp, precision, 40, lanesPerVertex=lanes, blockSize=128, autotune=False,
                               solveVariant=variant, usePDL=pdl, smallColorVertices=0, sweepMode="merged")
         assert st["solve_variant"] == variant
         assert _rel(xs[0], drop_ref[0], x0[0]) <= TOL[precision], (variant, lanes, precision, pdl)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_prefetch_variant_is_bit_identical(drop_scene, precision):
+    """The L2 prefetch moves no result: variant 6 equals variant 0 bit for bit."""
+    mp, pp = drop_scene
+    common = dict(lanesPerVertex=4, blockSize=128, autotune=False, smallColorVertices=0, sweepMode="merged")
+    _, xa, sa = _run_gpu(mp, pp, precision, 20, solveVariant=0, **common)
+    _, xb, sb = _run_gpu(mp, pp, precision, 20, solveVariant=6, **common)
+    assert sa["solve_variant"] == 0 and sb["solve_variant"] == 6
+    np.testing.assert_array_equal(xa[0], xb[0])
 
 
 def test_twist(tmp_path, gaia_lib, oracle_lib):
