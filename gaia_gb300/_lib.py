@@ -36,7 +36,7 @@ class Stats(C.Structure):
         ("num_groups", C.c_int32), ("num_vertices", C.c_int64), ("num_active_vertices", C.c_int64),
         ("num_incidences", C.c_int64), ("kernel_launches_per_step", C.c_int64),
         ("fp64_fallback_solves", C.c_int64), ("failed_solves", C.c_int64), ("device_bytes", C.c_int64),
-        ("autotune_ms_per_iteration", C.c_double), ("solve_variant", C.c_int32), ("reserved", C.c_int32),
+        ("autotune_ms_per_iteration", C.c_double), ("solve_variant", C.c_int32), ("mesh_frames", C.c_int32),
         ("contact_detections", C.c_int64), ("contact_stack_overflow", C.c_int64),
         ("contact_traverse_bounds", C.c_int64), ("device_timeouts", C.c_int64), ("nonfinite_solves", C.c_int64),
         ("sweep_mode", C.c_int32), ("cluster_size", C.c_int32), ("sweep_ms_merged", C.c_double),

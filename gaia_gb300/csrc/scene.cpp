@@ -560,6 +560,7 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
         get(*pp, "waitPollLimit", p.waitPollLimit);
         get(*pp, "sweepMode", p.sweepMode);
         get(*pp, "clusterSize", p.clusterSize);
+        get(*pp, "meshFrames", p.meshFrames);
     }
     if (const json::Value* cp = params.find("CollisionParams")) {
         get(*cp, "allowCCD", p.allowCCD);

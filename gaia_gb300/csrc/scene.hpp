@@ -78,6 +78,8 @@ struct PhysicsParams {
                                          // register pipeline, 6 next wave's records prefetched into L2
     std::string sweepMode = "auto";      // color scheduling: "auto", "merged", "scenes", "cluster", "grid"
     int clusterSize = 0;                 // blocks per cluster of the cluster sweep (0 = autotune; 2, 4, 8, 16)
+    bool meshFrames = true;              // FP32-compute states relative to a per-mesh frame that follows
+                                         // the mesh (no contact detection, no deformers)
     int waitPollLimit = -1;              // polls of a bounded device wait (-1: the built-in limit); tests
                                          // lower it to make the wait run out
 };

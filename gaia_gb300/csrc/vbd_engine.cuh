@@ -168,6 +168,7 @@ public:
         build_layout();
         upload();
         setup_contact();
+        setup_frames();
         lanes_ = sc_.p.lanesPerVertex;
         block_ = sc_.p.blockSize;
         if (lanes_ != 0 && lanes_ != 2 && lanes_ != 4 && lanes_ != 8 && lanes_ != 16 && lanes_ != 32)
@@ -475,8 +476,51 @@ public:
         P.col_rel = rc.rel;
         P.mesh_fric = d_mesh_fric_.p;
         P.col_scratch = d_col_scratch_.p;
+        P.frame_shift = frames_ ? d_frame_shift_.p : nullptr;
+        P.frame_plane = frames_ ? d_frame_plane_.p : nullptr;
         return P;
     }
+
+    // ---- mesh frames --------------------------------------------------------------------
+    // FP32-compute engines keep each mesh's states relative to a frame offset F that follows
+    // the mesh (k_frame_update, once per substep). Off with contact detection (contacts
+    // couple meshes, whose frames differ) and with deformers (they set absolute positions).
+    void setup_frames() {
+        frames_ = sizeof(R) == 4 && sc_.p.meshFrames && !cd_.enabled() && h_def_slot_.empty() && nmesh_ > 0;
+        if (!frames_) return;
+        std::vector<int32_t> ref(size_t(nmesh_), -1);
+        for (int m = 0; m < nmesh_; ++m)
+            for (int v = 0; v < sc_.meshes[m].nv; ++v)
+                if (!sc_.meshes[m].fixed[v]) {
+                    ref[size_t(m)] = slot_of_[mesh_off_[m] + v];
+                    break;
+                }
+        d_frame_ref_.upload(ref, &bytes_, st_);
+        d_frame_F_.alloc(nmesh_, &bytes_);
+        d_frame_shift_.alloc(nmesh_, &bytes_);
+        d_frame_plane_.alloc(nmesh_, &bytes_);
+        reset_frames();
+    }
+
+    // F = 0, no shift, the planes as given
+    void reset_frames() {
+        if (!frames_) return;
+        GAIA_CUDA(cudaMemsetAsync(d_frame_F_.p, 0, nmesh_ * sizeof(double4), st_));
+        GAIA_CUDA(cudaMemsetAsync(d_frame_shift_.p, 0, nmesh_ * sizeof(float4), st_));
+        dev::FramePlane p;
+        for (int d = 0; d < 3; ++d) {
+            p.lo_h[d] = float(c_.lo[d]);
+            p.lo_l[d] = float(c_.lo[d] - double(p.lo_h[d]));
+            p.hi_h[d] = float(c_.hi[d]);
+            p.hi_l[d] = float(c_.hi[d] - double(p.hi_h[d]));
+        }
+        std::vector<dev::FramePlane> planes(size_t(nmesh_), p);
+        GAIA_CUDA(cudaMemcpyAsync(d_frame_plane_.p, planes.data(), planes.size() * sizeof(dev::FramePlane),
+                                  cudaMemcpyHostToDevice, st_));
+        GAIA_CUDA(cudaStreamSynchronize(st_));
+    }
+
+    const double4* frame_ptr() const { return frames_ ? d_frame_F_.p : nullptr; }
 
     // ---- tet-mesh contact -----------------------------------------------------------
     // Surface faces / vertices, surface rings and tets of all meshes in slot terms for
@@ -729,6 +773,11 @@ public:
 
     void enqueue_init(bool rebuild) {
         auto P = ptrs();
+        if (frames_) {
+            dev::k_frame_update<ST, R><<<div_up(nmesh_, 128), 128, 0, st_>>>(
+                d_pos_.p, d_frame_ref_.p, d_frame_F_.p, d_frame_shift_.p, d_frame_plane_.p, nmesh_, c_);
+            GAIA_CUDA(cudaGetLastError());
+        }
         dev::k_initial_step<ST, R><<<div_up(nslots_, 256), 256, 0, st_>>>(P, c_);
         GAIA_CUDA(cudaGetLastError());
         // contacts: DCD on the start-of-substep positions, CCD on the trajectories to the
@@ -1374,6 +1423,7 @@ public:
         GAIA_CUDA(cudaMemsetAsync(d_counters_.p + dev::CNT_NONFINITE, 0, 3 * sizeof(unsigned long long), st_));
         cd_.reset(st_);
         GAIA_CUDA(cudaStreamSynchronize(st_));
+        reset_frames();
     }
 
     void autotune() override {
@@ -1464,7 +1514,8 @@ public:
         mesh_range(mesh, off, n);
         if (n == 0) return;
         dev::k_gather_positions<ST><<<div_up(n, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, nullptr, d_stage_f64_.p,
-                                                                     d_slot_of_.p + off, int32_t(n));
+                                                                     d_slot_of_.p + off, int32_t(n), frame_ptr(),
+                                                                     d_slot_mesh_.p);
         GAIA_CUDA(cudaGetLastError());
         GAIA_CUDA(cudaMemcpyAsync(out, d_stage_f64_.p, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, st_));
         GAIA_CUDA(cudaStreamSynchronize(st_));
@@ -1485,7 +1536,8 @@ public:
         if (n == 0) return;
         GAIA_CUDA(cudaMemcpyAsync(d_stage_f64_.p, in, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st_));
         dev::k_scatter_positions_f64<ST><<<div_up(n, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, d_stage_f64_.p,
-                                                                          d_slot_of_.p + off, int32_t(n));
+                                                                          d_slot_of_.p + off, int32_t(n), frame_ptr(),
+                                                                          d_slot_mesh_.p);
         GAIA_CUDA(cudaGetLastError());
         GAIA_CUDA(cudaStreamSynchronize(st_));
     }
@@ -1495,7 +1547,8 @@ public:
         if (n == 0) return;
         GAIA_CUDA(cudaMemcpyAsync(d_stage_f64_.p, in, 3 * n * sizeof(double), cudaMemcpyHostToDevice, st_));
         dev::k_scatter_positions_f64<ST><<<div_up(n, 256), 256, 0, st_>>>(d_xprev_.p, d_rest_.p, d_stage_f64_.p,
-                                                                          d_slot_of_.p + off, int32_t(n));
+                                                                          d_slot_of_.p + off, int32_t(n), frame_ptr(),
+                                                                          d_slot_mesh_.p);
         GAIA_CUDA(cudaGetLastError());
         GAIA_CUDA(cudaStreamSynchronize(st_));
     }
@@ -1549,13 +1602,14 @@ public:
         if (v) GAIA_CUDA(cudaMemcpyAsync(dv, v, 3 * nslots_ * sizeof(float), cudaMemcpyHostToDevice, st_));
         dev::k_scatter_state<ST><<<div_up(nslots_, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, d_vel_.p, x ? dx : nullptr,
                                                                        v ? dv : nullptr, d_slot_of_.p,
-                                                                       int32_t(nslots_));
+                                                                       int32_t(nslots_), frame_ptr(), d_slot_mesh_.p);
         GAIA_CUDA(cudaGetLastError());
     }
 
     void get_positions_f32(float* x) override {
         dev::k_gather_positions<ST><<<div_up(nslots_, 256), 256, 0, st_>>>(d_pos_.p, d_rest_.p, d_stage_f32_.p,
-                                                                          nullptr, d_slot_of_.p, int32_t(nslots_));
+                                                                          nullptr, d_slot_of_.p, int32_t(nslots_),
+                                                                          frame_ptr(), d_slot_mesh_.p);
         GAIA_CUDA(cudaGetLastError());
         GAIA_CUDA(cudaMemcpyAsync(x, d_stage_f32_.p, 3 * nslots_ * sizeof(float), cudaMemcpyDeviceToHost, st_));
         GAIA_CUDA(cudaStreamSynchronize(st_));
@@ -1742,6 +1796,7 @@ public:
         s->device_bytes = int64_t(bytes_);
         s->autotune_ms_per_iteration = tuned_ms_;
         s->solve_variant = variant_;
+        s->mesh_frames = frames_ ? 1 : 0;
         unsigned long long cc[cloth::CC_N];
         cd_.counters(cc, st_);
         s->contact_detections = int64_t(cc[cloth::CC_DETECTIONS]);
@@ -1783,6 +1838,12 @@ private:
     DevBuf<int4> d_scene_slots_;
     // grid mode: the merged colors' slot ranges, the barrier's counter and abort flag
     DevBuf<int2> d_grid_colors_;
+    // mesh frames: per mesh the reference slot, the FP64 offset, this substep's shift, the planes
+    bool frames_ = false;
+    DevBuf<int32_t> d_frame_ref_;
+    DevBuf<double4> d_frame_F_;
+    DevBuf<float4> d_frame_shift_;
+    DevBuf<dev::FramePlane> d_frame_plane_;
     DevBuf<uint32_t> d_grid_bar_;
     int32_t grid_ncolors_ = 0, grid_max_color_ = 0;
     int variant_fixed_ = -1;   // from PhysicsParams solveVariant (-1 = autotune)

@@ -92,6 +92,12 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 // those, blocks whose final drain wait ran out too.
 enum { CNT_FP64_SOLVES = 0, CNT_FAILED_SOLVES = 1, CNT_NONFINITE = 2, CNT_TIMEOUT = 3, CNT_DRAIN = 4, CNT_N = 8 };
 
+// World-box planes of one mesh relative to its frame offset F (lo - F, hi - F per axis),
+// each split into a rounded float and the float of its remainder.
+struct FramePlane {
+    float lo_h[3], lo_l[3], hi_h[3], hi_l[3];
+};
+
 template <typename ST, typename R>
 struct Ptrs {
     typename ST::U* u;
@@ -115,7 +121,12 @@ struct Ptrs {
     const int32_t* col_rel;
     const double2* mesh_fric;      // per mesh: frictionDynamic, frictionEpsV
     R* col_scratch;                // 9 per slot: contact force (3) and Hessian (6) of the solve
+    // mesh frames (null when off): per mesh the shift that the substep's initial step takes
+    // out of every state of the mesh, and the world-box planes relative to the mesh's frame
+    const float4* frame_shift;
+    const FramePlane* frame_plane;
 };
+
 
 struct DeformerDev {
     int32_t type;              // 0 rotator, 1 translator
@@ -722,16 +733,19 @@ __device__ __forceinline__ bool vertex_tail(const Ptrs<ST, R>& P, const Consts<R
     if (c.plane) {
         const float4 X = P.rest[v];
         const float Xc[3] = {X.x, X.y, X.z};
+        const FramePlane* fp = P.frame_plane ? P.frame_plane + P.slot_mesh[v] : nullptr;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            // below = lo - x, above = x - hi (x = X + u)
-            R below = ST::template sub_from<R>(pick<Sc>(c.lo[d], c.lo_f[d]), Xc[d], uo, d);
+            // below = lo - x, above = x - hi (x = X + u, or X + F + u in a mesh frame F)
+            R below = fp ? ST::template sub_plane<R>(fp->lo_h[d], fp->lo_l[d], Xc[d], uo, d)
+                         : ST::template sub_from<R>(pick<Sc>(c.lo[d], c.lo_f[d]), Xc[d], uo, d);
             R depth;
             if (below > R(0)) {
                 depth = below;
                 f[d] += depth * c.kb;
             } else {
-                R above = -ST::template sub_from<R>(pick<Sc>(c.hi[d], c.hi_f[d]), Xc[d], uo, d);
+                R above = fp ? -ST::template sub_plane<R>(fp->hi_h[d], fp->hi_l[d], Xc[d], uo, d)
+                             : -ST::template sub_from<R>(pick<Sc>(c.hi[d], c.hi_f[d]), Xc[d], uo, d);
                 if (!(above > R(0))) continue;
                 depth = above;
                 f[d] -= depth * c.kb;
@@ -970,6 +984,40 @@ __global__ void __launch_bounds__(MAXB) k_sweep_scenes(Ptrs<ST, R> P, Consts<R> 
     }
 }
 
+// Mesh frames, at the start of every substep: per mesh, the FP32 head of its reference
+// vertex's state becomes the shift that k_initial_step takes out of every state of the mesh
+// (exactly in the double-float modes; the FP32 mode rounds u - s, which is small where the
+// mesh moves as a whole), the frame offset F accumulates it in FP64, and the world-box
+// planes are re-expressed relative to F. A mesh that falls or slides as a body then keeps
+// states of the size of its deformation and of one substep's motion, and every FP32
+// difference and update of the solve rounds at that scale instead of at the scale of the
+// distance travelled.
+template <typename ST, typename R>
+__global__ void k_frame_update(const typename ST::U* u, const int32_t* ref, double4* F, float4* shift,
+                               FramePlane* plane, int32_t nmesh, Consts<R> c) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmesh) return;
+    const int r = ref[m];
+    const float4 sh = r >= 0 ? ST::head(u[r]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    double4 f = F[m];
+    f.x += double(sh.x);
+    f.y += double(sh.y);
+    f.z += double(sh.z);
+    F[m] = f;
+    shift[m] = sh;
+    const double fc[3] = {f.x, f.y, f.z};
+    FramePlane p;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double lo = c.lo[d] - fc[d], hi = c.hi[d] - fc[d];
+        p.lo_h[d] = float(lo);
+        p.lo_l[d] = float(lo - double(p.lo_h[d]));
+        p.hi_h[d] = float(hi);
+        p.hi_l[d] = float(hi - double(p.hi_h[d]));
+    }
+    plane[m] = p;
+}
+
 // Initial step of a substep over all slots: VBD_BaseMaterial.h:201-259 and
 // VBD_BaseMaterial.cpp:7-31 (initialization types 0..4). Displacements: every
 // update is linear in x, so it reads as in positions.
@@ -981,11 +1029,18 @@ __global__ void k_initial_step(Ptrs<ST, R> P, Consts<R> c) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= P.nslots) return;
     const Sc dt = pick<Sc>(c.dt_d, c.dt_f);
-    const U x = P.u[s];
+    const int mesh = P.slot_mesh[s];
+    U x = P.u[s];
+    // mesh frames: the substep starts in the frame moved by this substep's shift (x, and the
+    // start-of-substep state, inertia target and initial guess derived from it)
+    if (P.frame_shift) {
+        const float4 sh = P.frame_shift[mesh];
+        x = ST::shift(x, sh.x, sh.y, sh.z);
+    }
     V v = P.vel[s];
     P.xprev[s] = x;
     const bool fixed = s >= P.nactive;
-    const int init_type = P.mats[P.slot_mesh[s]].init_type;
+    const int init_type = P.mats[mesh].init_type;
     if (init_type == 2 || init_type == 4) P.vprev[s] = v;
     const V vp = v;
     if (c.assoc_grav) {
@@ -1118,17 +1173,25 @@ __global__ void k_gather_xf(const typename ST::U* u, const typename ST::U* xprev
 // ---------------------------------------------------------------------------
 // Host-order state <-> slots (positions = X + u).
 // ---------------------------------------------------------------------------
+// Mesh frames (frame non-null): positions = X + F[mesh] + u, F per mesh in FP64.
+__device__ __forceinline__ double4 frame_of(const double4* frame, const int32_t* slot_mesh, int s) {
+    return frame ? frame[slot_mesh[s]] : make_double4(0.0, 0.0, 0.0, 0.0);
+}
+
 template <typename ST>
 __global__ void k_scatter_state(typename ST::U* u, const float4* rest, typename ST::V* vel, const float* x,
-                                const float* v, const int32_t* slot_of, int32_t n) {
+                                const float* v, const int32_t* slot_of, int32_t n, const double4* frame,
+                                const int32_t* slot_mesh) {
     using Sc = typename ST::Sc;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int s = slot_of[i];
     if (x) {
         const float4 X = rest[s];
-        double du[3] = {double(x[3 * size_t(i)]) - double(X.x), double(x[3 * size_t(i) + 1]) - double(X.y),
-                        double(x[3 * size_t(i) + 2]) - double(X.z)};
+        const double4 F = frame_of(frame, slot_mesh, s);
+        double du[3] = {double(x[3 * size_t(i)]) - double(X.x) - F.x,
+                        double(x[3 * size_t(i) + 1]) - double(X.y) - F.y,
+                        double(x[3 * size_t(i) + 2]) - double(X.z) - F.z};
         u[s] = ST::from_d(du, ST::mass(u[s]));
     }
     if (v) {
@@ -1139,16 +1202,18 @@ __global__ void k_scatter_state(typename ST::U* u, const float4* rest, typename 
 
 template <typename ST>
 __global__ void k_gather_positions(const typename ST::U* u, const float4* rest, float* out32, double* out64,
-                                   const int32_t* slot_of, int32_t n) {
+                                   const int32_t* slot_of, int32_t n, const double4* frame,
+                                   const int32_t* slot_mesh) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int s = slot_of[i];
     double p[3];
     ST::to_d(u[s], p);
     const float4 X = rest[s];
-    p[0] += double(X.x);
-    p[1] += double(X.y);
-    p[2] += double(X.z);
+    const double4 F = frame_of(frame, slot_mesh, s);
+    p[0] += double(X.x) + F.x;
+    p[1] += double(X.y) + F.y;
+    p[2] += double(X.z) + F.z;
     if (out32) {
         out32[3 * size_t(i)] = float(p[0]);
         out32[3 * size_t(i) + 1] = float(p[1]);
@@ -1178,13 +1243,15 @@ __global__ void k_gather_velocities(const V* vel, float* out32, double* out64, c
 
 template <typename ST>
 __global__ void k_scatter_positions_f64(typename ST::U* u, const float4* rest, const double* in,
-                                        const int32_t* slot_of, int32_t n) {
+                                        const int32_t* slot_of, int32_t n, const double4* frame,
+                                        const int32_t* slot_mesh) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int s = slot_of[i];
     const float4 X = rest[s];
-    double du[3] = {in[3 * size_t(i)] - double(X.x), in[3 * size_t(i) + 1] - double(X.y),
-                    in[3 * size_t(i) + 2] - double(X.z)};
+    const double4 F = frame_of(frame, slot_mesh, s);
+    double du[3] = {in[3 * size_t(i)] - double(X.x) - F.x, in[3 * size_t(i) + 1] - double(X.y) - F.y,
+                    in[3 * size_t(i) + 2] - double(X.z) - F.z};
     u[s] = ST::from_d(du, ST::mass(u[s]));
 }
 

@@ -84,6 +84,20 @@ struct StF32 {
         return a;
     }
     __device__ static float comp(const U& u, int d) { return d == 0 ? u.x : (d == 1 ? u.y : u.z); }
+    // the state moved into a frame shifted by (sx, sy, sz): u - s
+    __device__ static U shift(U u, float sx, float sy, float sz) {
+        u.x = __fsub_rn(u.x, sx);
+        u.y = __fsub_rn(u.y, sy);
+        u.z = __fsub_rn(u.z, sz);
+        return u;
+    }
+    // the FP32 part that a frame shift takes out (the state itself)
+    __device__ static float4 head(const U& u) { return make_float4(u.x, u.y, u.z, 0.f); }
+    // (ch + cl) - X - u for a plane constant split in two floats (frame-relative planes)
+    template <typename R>
+    __device__ static R sub_plane(float ch, float cl, float X, const U& u, int d) {
+        return R(__fadd_rn(__fsub_rn(__fsub_rn(ch, X), comp(u, d)), cl));
+    }
     template <typename R>
     __device__ static R sub_from(Sc c, float X, const U& u, int d) {
         return R((c - X) - comp(u, d));
@@ -125,6 +139,17 @@ struct StF64 {
         return a;
     }
     __device__ static double comp(const U& u, int d) { return d == 0 ? u.x : (d == 1 ? u.y : u.z); }
+    __device__ static U shift(U u, float sx, float sy, float sz) {
+        u.x -= double(sx);
+        u.y -= double(sy);
+        u.z -= double(sz);
+        return u;
+    }
+    __device__ static float4 head(const U& u) { return make_float4(float(u.x), float(u.y), float(u.z), 0.f); }
+    template <typename R>
+    __device__ static R sub_plane(float ch, float cl, float X, const U& u, int d) {
+        return R(((double(ch) + double(cl)) - double(X)) - comp(u, d));
+    }
     template <typename R>
     __device__ static R sub_from(Sc c, float X, const U& u, int d) {
         return R((c - double(X)) - comp(u, d));
@@ -187,6 +212,20 @@ struct StDF {
         float h = d == 0 ? u.hx : (d == 1 ? u.hy : u.hz);
         float l = d == 0 ? u.lx : (d == 1 ? u.ly : u.lz);
         return R(__fsub_rn(__fsub_rn(__fsub_rn(c, X), h), l));
+    }
+    // exact (double-float) u - s
+    __device__ static U shift(U u, float sx, float sy, float sz) {
+        df_add(u.hx, u.lx, -sx);
+        df_add(u.hy, u.ly, -sy);
+        df_add(u.hz, u.lz, -sz);
+        return u;
+    }
+    __device__ static float4 head(const U& u) { return make_float4(u.hx, u.hy, u.hz, 0.f); }
+    template <typename R>
+    __device__ static R sub_plane(float ch, float cl, float X, const U& u, int d) {
+        float h = d == 0 ? u.hx : (d == 1 ? u.hy : u.hz);
+        float l = d == 0 ? u.lx : (d == 1 ? u.ly : u.lz);
+        return R(__fadd_rn(__fsub_rn(__fsub_rn(ch, X), h), __fsub_rn(cl, l)));
     }
 };
 

@@ -65,7 +65,9 @@ typedef struct {
                                      pipeline two records deep, 6 = register pipeline with the records
                                      of the next resident wave prefetched into L2 (of the largest
                                      color), 5 = grid sweep */
-    int32_t reserved;
+    int32_t mesh_frames;          /* 1: states are kept relative to a per-mesh frame offset that
+                                     follows each mesh (PhysicsParams meshFrames; FP32-compute
+                                     precisions without contact detection or deformers) */
     /* tet-mesh contact detection (cumulative; 0 when contact is off) */
     int64_t contact_detections;       /* detection passes run */
     int64_t contact_stack_overflow;   /* hierarchy traversals that dropped a node (stack full) */
