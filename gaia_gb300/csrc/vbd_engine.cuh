@@ -507,7 +507,7 @@ public:
         if (!frames_) return;
         GAIA_CUDA(cudaMemsetAsync(d_frame_F_.p, 0, nmesh_ * sizeof(double4), st_));
         GAIA_CUDA(cudaMemsetAsync(d_frame_shift_.p, 0, nmesh_ * sizeof(float4), st_));
-        dev::FramePlane p;
+        dev::FramePlane p = {};
         for (int d = 0; d < 3; ++d) {
             p.lo_h[d] = float(c_.lo[d]);
             p.lo_l[d] = float(c_.lo[d] - double(p.lo_h[d]));

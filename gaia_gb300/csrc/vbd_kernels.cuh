@@ -93,9 +93,10 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 enum { CNT_FP64_SOLVES = 0, CNT_FAILED_SOLVES = 1, CNT_NONFINITE = 2, CNT_TIMEOUT = 3, CNT_DRAIN = 4, CNT_N = 8 };
 
 // World-box planes of one mesh relative to its frame offset F (lo - F, hi - F per axis),
-// each split into a rounded float and the float of its remainder.
-struct FramePlane {
+// each split into a rounded float and the float of its remainder; 64 B, so one cache line.
+struct alignas(64) FramePlane {
     float lo_h[3], lo_l[3], hi_h[3], hi_l[3];
+    float pad[4];
 };
 
 template <typename ST, typename R>
@@ -502,6 +503,7 @@ __device__ __forceinline__ void prefetch_tail(const Ptrs<ST, R>& P, int v) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(P.y + v));
     asm volatile("prefetch.global.L1 [%0];" ::"l"(P.xprev + v));
     asm volatile("prefetch.global.L1 [%0];" ::"l"(P.rest + v));
+    if (P.frame_plane) asm volatile("prefetch.global.L1 [%0];" ::"l"(P.frame_plane + P.slot_mesh[v]));
 }
 
 // How the incidence loop reads neighbour states and records:
@@ -888,6 +890,7 @@ __global__ void __launch_bounds__(256, 4)
         mat = P.mats[P.slot_mesh[v]];
         rb = P.inc_ofs[v] - r0 + lane;
         re = min(P.inc_ofs[v + 1] - r0, nrec);
+        if (lane == 0) prefetch_tail(P, v);
     }
     pdl_wait();
     U uo{};
@@ -1006,7 +1009,7 @@ __global__ void k_frame_update(const typename ST::U* u, const int32_t* ref, doub
     F[m] = f;
     shift[m] = sh;
     const double fc[3] = {f.x, f.y, f.z};
-    FramePlane p;
+    FramePlane p = {};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double lo = c.lo[d] - fc[d], hi = c.hi[d] - fc[d];
