@@ -104,7 +104,9 @@ typedef struct {
  * the persistent sweeps need contact detection, the accelerator and evaluateConvergence off,
  * and the cluster sweep scenes that fit in the shared memory of a cluster), "clusterSize"
  * (0 = autotune, 2-16), "waitPollLimit" (polls of a bounded device wait before it gives up:
- * the staged records' wait and the grid barrier; default 2^20).
+ * the staged records' wait and the grid barrier; default 2^20), "meshFrames" (default true:
+ * FP32-compute states relative to a per-mesh offset that follows the mesh, see
+ * gaia_vbd_stats.mesh_frames; positions in and out of the API are absolute either way).
  */
 int gaia_vbd_create(const char* models_json, const char* params_json, const char* repo_root, gaia_vbd** out);
 /* The two halves of gaia_vbd_create. gaia_vbd_load is host-only (no GPU needed):
