@@ -477,7 +477,9 @@ public:
         P.mesh_fric = d_mesh_fric_.p;
         P.col_scratch = d_col_scratch_.p;
         P.frame_shift = frames_ ? d_frame_shift_.p : nullptr;
-        P.frame_plane = frames_ ? d_frame_plane_.p : nullptr;
+        P.frame_F = frames_ ? d_frame_F_.p : nullptr;
+        P.rest_fh = frames_ ? d_rest_fh_.p : nullptr;
+        P.rest_fl = frames_ ? d_rest_fl_.p : nullptr;
         return P;
     }
 
@@ -498,25 +500,18 @@ public:
         d_frame_ref_.upload(ref, &bytes_, st_);
         d_frame_F_.alloc(nmesh_, &bytes_);
         d_frame_shift_.alloc(nmesh_, &bytes_);
-        d_frame_plane_.alloc(nmesh_, &bytes_);
+        d_rest_fh_.alloc(nslots_, &bytes_);
+        d_rest_fl_.alloc(nslots_, &bytes_);
         reset_frames();
     }
 
-    // F = 0, no shift, the planes as given
+    // F = 0, no shift, X + F = X
     void reset_frames() {
         if (!frames_) return;
         GAIA_CUDA(cudaMemsetAsync(d_frame_F_.p, 0, nmesh_ * sizeof(double4), st_));
         GAIA_CUDA(cudaMemsetAsync(d_frame_shift_.p, 0, nmesh_ * sizeof(float4), st_));
-        dev::FramePlane p = {};
-        for (int d = 0; d < 3; ++d) {
-            p.lo_h[d] = float(c_.lo[d]);
-            p.lo_l[d] = float(c_.lo[d] - double(p.lo_h[d]));
-            p.hi_h[d] = float(c_.hi[d]);
-            p.hi_l[d] = float(c_.hi[d] - double(p.hi_h[d]));
-        }
-        std::vector<dev::FramePlane> planes(size_t(nmesh_), p);
-        GAIA_CUDA(cudaMemcpyAsync(d_frame_plane_.p, planes.data(), planes.size() * sizeof(dev::FramePlane),
-                                  cudaMemcpyHostToDevice, st_));
+        GAIA_CUDA(cudaMemcpyAsync(d_rest_fh_.p, d_rest_.p, nslots_ * sizeof(float4), cudaMemcpyDeviceToDevice, st_));
+        GAIA_CUDA(cudaMemsetAsync(d_rest_fl_.p, 0, nslots_ * sizeof(float4), st_));
         GAIA_CUDA(cudaStreamSynchronize(st_));
     }
 
@@ -774,8 +769,8 @@ public:
     void enqueue_init(bool rebuild) {
         auto P = ptrs();
         if (frames_) {
-            dev::k_frame_update<ST, R><<<div_up(nmesh_, 128), 128, 0, st_>>>(
-                d_pos_.p, d_frame_ref_.p, d_frame_F_.p, d_frame_shift_.p, d_frame_plane_.p, nmesh_, c_);
+            dev::k_frame_update<ST><<<div_up(nmesh_, 128), 128, 0, st_>>>(d_pos_.p, d_frame_ref_.p, d_frame_F_.p,
+                                                                         d_frame_shift_.p, nmesh_);
             GAIA_CUDA(cudaGetLastError());
         }
         dev::k_initial_step<ST, R><<<div_up(nslots_, 256), 256, 0, st_>>>(P, c_);
@@ -1843,7 +1838,7 @@ private:
     DevBuf<int32_t> d_frame_ref_;
     DevBuf<double4> d_frame_F_;
     DevBuf<float4> d_frame_shift_;
-    DevBuf<dev::FramePlane> d_frame_plane_;
+    DevBuf<float4> d_rest_fh_, d_rest_fl_;
     DevBuf<uint32_t> d_grid_bar_;
     int32_t grid_ncolors_ = 0, grid_max_color_ = 0;
     int variant_fixed_ = -1;   // from PhysicsParams solveVariant (-1 = autotune)

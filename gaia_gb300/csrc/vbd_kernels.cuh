@@ -92,13 +92,6 @@ __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;"
 // those, blocks whose final drain wait ran out too.
 enum { CNT_FP64_SOLVES = 0, CNT_FAILED_SOLVES = 1, CNT_NONFINITE = 2, CNT_TIMEOUT = 3, CNT_DRAIN = 4, CNT_N = 8 };
 
-// World-box planes of one mesh relative to its frame offset F (lo - F, hi - F per axis),
-// each split into a rounded float and the float of its remainder; 64 B, so one cache line.
-struct alignas(64) FramePlane {
-    float lo_h[3], lo_l[3], hi_h[3], hi_l[3];
-    float pad[4];
-};
-
 template <typename ST, typename R>
 struct Ptrs {
     typename ST::U* u;
@@ -123,9 +116,12 @@ struct Ptrs {
     const double2* mesh_fric;      // per mesh: frictionDynamic, frictionEpsV
     R* col_scratch;                // 9 per slot: contact force (3) and Hessian (6) of the solve
     // mesh frames (null when off): per mesh the shift that the substep's initial step takes
-    // out of every state of the mesh, and the world-box planes relative to the mesh's frame
+    // out of every state of the mesh and the frame offset F (FP64); per slot the reference
+    // position X + F as a float pair, which the world-box test uses in place of X
     const float4* frame_shift;
-    const FramePlane* frame_plane;
+    const double4* frame_F;
+    float4* rest_fh;
+    float4* rest_fl;
 };
 
 
@@ -503,7 +499,10 @@ __device__ __forceinline__ void prefetch_tail(const Ptrs<ST, R>& P, int v) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(P.y + v));
     asm volatile("prefetch.global.L1 [%0];" ::"l"(P.xprev + v));
     asm volatile("prefetch.global.L1 [%0];" ::"l"(P.rest + v));
-    if (P.frame_plane) asm volatile("prefetch.global.L1 [%0];" ::"l"(P.frame_plane + P.slot_mesh[v]));
+    if (P.rest_fh) {
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(P.rest_fh + v));
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(P.rest_fl + v));
+    }
 }
 
 // How the incidence loop reads neighbour states and records:
@@ -733,21 +732,23 @@ __device__ __forceinline__ bool vertex_tail(const Ptrs<ST, R>& P, const Consts<R
     }
     // plane ground / world box with friction on each violated axis (VBDPhysics.cpp:2858-2953)
     if (c.plane) {
-        const float4 X = P.rest[v];
-        const float Xc[3] = {X.x, X.y, X.z};
-        const FramePlane* fp = P.frame_plane ? P.frame_plane + P.slot_mesh[v] : nullptr;
+        // x = X + u, or (X + F) + u in a mesh frame F, X + F held as a float pair per slot
+        const bool framed = P.rest_fh != nullptr;
+        const float4 X = framed ? P.rest_fh[v] : P.rest[v];
+        const float4 Xl = framed ? P.rest_fl[v] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float Xc[3] = {X.x, X.y, X.z}, Xlc[3] = {Xl.x, Xl.y, Xl.z};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            // below = lo - x, above = x - hi (x = X + u, or X + F + u in a mesh frame F)
-            R below = fp ? ST::template sub_plane<R>(fp->lo_h[d], fp->lo_l[d], Xc[d], uo, d)
-                         : ST::template sub_from<R>(pick<Sc>(c.lo[d], c.lo_f[d]), Xc[d], uo, d);
+            // below = lo - x, above = x - hi
+            R below = framed ? ST::template sub_plane<R>(pick<Sc>(c.lo[d], c.lo_f[d]), Xc[d], Xlc[d], uo, d)
+                             : ST::template sub_from<R>(pick<Sc>(c.lo[d], c.lo_f[d]), Xc[d], uo, d);
             R depth;
             if (below > R(0)) {
                 depth = below;
                 f[d] += depth * c.kb;
             } else {
-                R above = fp ? -ST::template sub_plane<R>(fp->hi_h[d], fp->hi_l[d], Xc[d], uo, d)
-                             : -ST::template sub_from<R>(pick<Sc>(c.hi[d], c.hi_f[d]), Xc[d], uo, d);
+                R above = framed ? -ST::template sub_plane<R>(pick<Sc>(c.hi[d], c.hi_f[d]), Xc[d], Xlc[d], uo, d)
+                                 : -ST::template sub_from<R>(pick<Sc>(c.hi[d], c.hi_f[d]), Xc[d], uo, d);
                 if (!(above > R(0))) continue;
                 depth = above;
                 f[d] -= depth * c.kb;
@@ -990,14 +991,13 @@ __global__ void __launch_bounds__(MAXB) k_sweep_scenes(Ptrs<ST, R> P, Consts<R> 
 // Mesh frames, at the start of every substep: per mesh, the FP32 head of its reference
 // vertex's state becomes the shift that k_initial_step takes out of every state of the mesh
 // (exactly in the double-float modes; the FP32 mode rounds u - s, which is small where the
-// mesh moves as a whole), the frame offset F accumulates it in FP64, and the world-box
-// planes are re-expressed relative to F. A mesh that falls or slides as a body then keeps
-// states of the size of its deformation and of one substep's motion, and every FP32
-// difference and update of the solve rounds at that scale instead of at the scale of the
-// distance travelled.
-template <typename ST, typename R>
+// mesh moves as a whole), and the frame offset F accumulates it in FP64. A mesh that falls
+// or slides as a body then keeps states of the size of its deformation and of one substep's
+// motion, and every FP32 difference and update of the solve rounds at that scale instead of
+// at the scale of the distance travelled.
+template <typename ST>
 __global__ void k_frame_update(const typename ST::U* u, const int32_t* ref, double4* F, float4* shift,
-                               FramePlane* plane, int32_t nmesh, Consts<R> c) {
+                               int32_t nmesh) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nmesh) return;
     const int r = ref[m];
@@ -1008,17 +1008,6 @@ __global__ void k_frame_update(const typename ST::U* u, const int32_t* ref, doub
     f.z += double(sh.z);
     F[m] = f;
     shift[m] = sh;
-    const double fc[3] = {f.x, f.y, f.z};
-    FramePlane p = {};
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const double lo = c.lo[d] - fc[d], hi = c.hi[d] - fc[d];
-        p.lo_h[d] = float(lo);
-        p.lo_l[d] = float(lo - double(p.lo_h[d]));
-        p.hi_h[d] = float(hi);
-        p.hi_l[d] = float(hi - double(p.hi_h[d]));
-    }
-    plane[m] = p;
 }
 
 // Initial step of a substep over all slots: VBD_BaseMaterial.h:201-259 and
@@ -1039,6 +1028,17 @@ __global__ void k_initial_step(Ptrs<ST, R> P, Consts<R> c) {
     if (P.frame_shift) {
         const float4 sh = P.frame_shift[mesh];
         x = ST::shift(x, sh.x, sh.y, sh.z);
+        // X + F of this slot for the world-box test, as a float pair
+        const float4 X = P.rest[s];
+        const double4 F = P.frame_F[mesh];
+        const double xf[3] = {double(X.x) + F.x, double(X.y) + F.y, double(X.z) + F.z};
+        float4 h, l;
+        h.x = float(xf[0]); l.x = float(xf[0] - double(h.x));
+        h.y = float(xf[1]); l.y = float(xf[1] - double(h.y));
+        h.z = float(xf[2]); l.z = float(xf[2] - double(h.z));
+        h.w = 0.f; l.w = 0.f;
+        P.rest_fh[s] = h;
+        P.rest_fl[s] = l;
     }
     V v = P.vel[s];
     P.xprev[s] = x;

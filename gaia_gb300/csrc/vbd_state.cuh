@@ -93,10 +93,10 @@ struct StF32 {
     }
     // the FP32 part that a frame shift takes out (the state itself)
     __device__ static float4 head(const U& u) { return make_float4(u.x, u.y, u.z, 0.f); }
-    // (ch + cl) - X - u for a plane constant split in two floats (frame-relative planes)
+    // c - (Xh + Xl) - u for a reference position split in two floats (X + F in a mesh frame)
     template <typename R>
-    __device__ static R sub_plane(float ch, float cl, float X, const U& u, int d) {
-        return R(__fadd_rn(__fsub_rn(__fsub_rn(ch, X), comp(u, d)), cl));
+    __device__ static R sub_plane(Sc c, float Xh, float Xl, const U& u, int d) {
+        return R(__fsub_rn(__fsub_rn(__fsub_rn(c, Xh), comp(u, d)), Xl));
     }
     template <typename R>
     __device__ static R sub_from(Sc c, float X, const U& u, int d) {
@@ -147,8 +147,8 @@ struct StF64 {
     }
     __device__ static float4 head(const U& u) { return make_float4(float(u.x), float(u.y), float(u.z), 0.f); }
     template <typename R>
-    __device__ static R sub_plane(float ch, float cl, float X, const U& u, int d) {
-        return R(((double(ch) + double(cl)) - double(X)) - comp(u, d));
+    __device__ static R sub_plane(Sc c, float Xh, float Xl, const U& u, int d) {
+        return R(((c - double(Xh)) - double(Xl)) - comp(u, d));
     }
     template <typename R>
     __device__ static R sub_from(Sc c, float X, const U& u, int d) {
@@ -222,10 +222,10 @@ struct StDF {
     }
     __device__ static float4 head(const U& u) { return make_float4(u.hx, u.hy, u.hz, 0.f); }
     template <typename R>
-    __device__ static R sub_plane(float ch, float cl, float X, const U& u, int d) {
+    __device__ static R sub_plane(Sc c, float Xh, float Xl, const U& u, int d) {
         float h = d == 0 ? u.hx : (d == 1 ? u.hy : u.hz);
         float l = d == 0 ? u.lx : (d == 1 ? u.ly : u.lz);
-        return R(__fadd_rn(__fsub_rn(__fsub_rn(ch, X), h), __fsub_rn(cl, l)));
+        return R(__fsub_rn(__fsub_rn(__fsub_rn(c, Xh), h), __fadd_rn(Xl, l)));
     }
 };
 
