@@ -544,7 +544,7 @@ def run_cloth(args, world, rank, local):
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": st["kernel_launches_per_step"] * args.steps,
         "fp64_fallback_solves": st["fp64_fallback_solves"], "failed_solves": st["failed_solves"],
         "overflow": {k: st[k] for k in ("vf_overflow", "ee_overflow", "fv_overflow", "candidate_overflow",
-                                        "stack_overflow", "ee_warp_fallbacks")},
+                                        "stack_overflow")},
     }
     if fp64:
         fp64["speedup_over_fp64"] = line["value"] / fp64["value"]

@@ -199,15 +199,67 @@ __global__ void k_fv_sort(CDTopo t, CDOut o, const int* req) {
     }
 }
 
-constexpr int EE_WARPS = 2;    // warps per block of the edge-edge query
-constexpr int EE_LEAVES = 96;  // hierarchy leaves per query kept for the warp's narrow phase
-constexpr int EE_INLINE = CAND_CAP - EE_LEAVES;  // accepted leaves a lane keeps beyond those
+// Edge-edge query of one simulated edge: triMeshEdgeContactQueryFunc
+// (ClothContactDetector.cpp:731-813) with the query sphere of contactQueryEE
+// (:1106-1135): centre at the edge midpoint, radius maxQueryDis + half the edge length.
+// The whole query in one thread: the warp kernel's path for warps whose queries reach more
+// leaves than its shared lists hold.
+__device__ void ee_query_one(const CDTopo& t, const bvh::LbvhDev& eb, const float4* xf, float r, const CDOut& o,
+                             int e) {
+    const int4 E = t.edges[e];
+    const int m1 = t.edgeInfo[e].z;
+    const float3 p1 = ld3(xf, E.x), p2 = ld3(xf, E.y);
+    const float3 dd = sub(p1, p2);
+    const float eLen = sqrtf(dot(dd, dd));
+    const float3 c = mul(0.5f, add(p1, p2));
+    const float rq = (r + eLen * 0.5f) * 1.0001f;
+    float minDis = r;
+    int cand[CAND_CAP];
+    int nc = 0;
+    bvh::traverse(eb, c, rq * rq, o.counters, [&](int e2) {
+        const int4 F = t.edges[e2];
+        const int m2 = t.edgeInfo[e2].z;
+        if (m1 == m2) {
+            if (e2 == e) return;
+            if (E.x == F.x || E.x == F.y || E.y == F.x || E.y == F.y) return;
+        }
+        const float3 q1 = ld3(xf, F.x), q2 = ld3(xf, F.y);
+        float3 c1, c2;
+        float s, tt;
+        closest_points_segments(p1, p2, q1, q2, c1, c2, s, tt);
+        const float3 df = sub(c1, c2);
+        const float d = sqrtf(dot(df, df));
+        minDis = fminf(minDis, d);
+        if (!(d < r)) return;
+        const float3 ev1 = sub(p2, p1), ev2 = sub(q2, q1);
+        const bool ok = (dot(sub(c2, p1), ev1) >= 0.f && dot(sub(p2, c2), ev1) >= 0.f) ||
+                        (dot(sub(c1, q1), ev2) >= 0.f && dot(sub(q2, c1), ev2) >= 0.f);
+        if (!ok) return;
+        if (nc < CAND_CAP) cand[nc++] = e2;
+        else atomicAdd(&o.counters[CC_CAND_OVERFLOW], 1ull);
+    });
+    for (int a = 1; a < nc; ++a) {
+        const int k = cand[a];
+        int b = a - 1;
+        while (b >= 0 && cand[b] > k) {
+            cand[b + 1] = cand[b];
+            --b;
+        }
+        cand[b + 1] = k;
+    }
+    if (nc > EE_CAP) {
+        atomicAdd(&o.counters[CC_EE_OVERFLOW], 1ull);
+        nc = EE_CAP;
+    }
+    for (int a = 0; a < nc; ++a) o.eeOther[size_t(e) * EE_CAP + a] = cand[a];
+    o.eeCount[e] = nc;
+    o.eeMinDis[e] = minDis;
+}
 
-// Edge-edge queries: triMeshEdgeContactQueryFunc (ClothContactDetector.cpp:731-813) with the
-// query sphere of contactQueryEE (:1106-1135): centre at the edge midpoint, radius
-// maxQueryDis + half the edge length.
-//
-// The queries of a warp, the narrow phase shared by the warp's lanes. Lane i takes
+constexpr int EE_WARPS = 2;    // warps per block of the edge-edge query
+constexpr int EE_LEAVES = 64;  // hierarchy leaves per query kept for the warp's narrow phase
+
+// The edge-edge queries of a warp, the narrow phase shared by the warp's lanes. Lane i takes
 // the edge of leaf i of the edge hierarchy (Morton order of the last build: the queries of
 // a warp are neighbours in space). Each lane walks the hierarchy for its own query and
 // only lists the leaves in reach (shared memory); the warp then runs the narrow phase of all
@@ -215,10 +267,8 @@ constexpr int EE_INLINE = CAND_CAP - EE_LEAVES;  // accepted leaves a lane keeps
 // are (one query per lane left most lanes idle in the narrow phase: 10 of 32 active). The
 // predicates are the per-thread query's, in the same order per pair; the minimum distance is
 // a minimum over the same values, and the accepted leaves are sorted by id as there, so the
-// results are identical. Leaves beyond the first EE_LEAVES of a query get their narrow phase
-// from the lane itself during its walk (such queries are counted in CC_EE_WARP_FALLBACK),
-// up to EE_INLINE accepted ones (more are counted in CC_CAND_OVERFLOW); they join the
-// shared list's accepted leaves before the sort.
+// results are identical. A warp with a query that reaches more than EE_LEAVES leaves runs
+// its queries one per lane instead (ee_query_one) and counts it in CC_EE_WARP_FALLBACK.
 __global__ void __launch_bounds__(32 * EE_WARPS) k_ee_query(CDTopo t, bvh::LbvhDev eb, const float4* xf, float r,
                                                              CDOut o, const int* req) {
     if (*req == 0) return;
@@ -233,10 +283,8 @@ __global__ void __launch_bounds__(32 * EE_WARPS) k_ee_query(CDTopo t, bvh::LbvhD
         if (e < 0 || e >= t.nSimE) e = -1;  // leaves of collider edges have no query
     }
     int4 E = make_int4(0, 0, 0, 0);
-    int m1 = -1, n = 0, nov = 0;
+    int m1 = -1, n = 0;
     float3 p1 = v3(0.f, 0.f, 0.f), p2 = p1;
-    float minOwn = r;       // minimum distance of the leaves this lane narrows itself
-    int ov[EE_INLINE];      // accepted leaves beyond the shared list
     int* L = s_leaf[w][lane];
     if (e >= 0) {
         E = t.edges[e];
@@ -247,39 +295,17 @@ __global__ void __launch_bounds__(32 * EE_WARPS) k_ee_query(CDTopo t, bvh::LbvhD
         const float eLen = sqrtf(dot(dd, dd));
         const float3 c = mul(0.5f, add(p1, p2));
         const float rq = (r + eLen * 0.5f) * 1.0001f;
-        bool counted = false;
         bvh::traverse(eb, c, rq * rq, o.counters, [&](int e2) {
-            if (n < EE_LEAVES) {
-                L[n++] = e2;
-                return;
-            }
-            if (!counted) {
-                atomicAdd(&o.counters[CC_EE_WARP_FALLBACK], 1ull);
-                counted = true;
-            }
-            const int4 F = t.edges[e2];
-            const int m2 = t.edgeInfo[e2].z;
-            if (m1 == m2) {
-                if (e2 == e) return;
-                if (E.x == F.x || E.x == F.y || E.y == F.x || E.y == F.y) return;
-            }
-            const float3 q1 = ld3(xf, F.x), q2 = ld3(xf, F.y);
-            float3 c1, c2;
-            float s, tt;
-            closest_points_segments(p1, p2, q1, q2, c1, c2, s, tt);
-            const float3 df = sub(c1, c2);
-            const float d = sqrtf(dot(df, df));
-            minOwn = fminf(minOwn, d);
-            if (!(d < r)) return;
-            const float3 ev1 = sub(p2, p1), ev2 = sub(q2, q1);
-            const bool ok = (dot(sub(c2, p1), ev1) >= 0.f && dot(sub(p2, c2), ev1) >= 0.f) ||
-                            (dot(sub(c1, q1), ev2) >= 0.f && dot(sub(q2, c1), ev2) >= 0.f);
-            if (!ok) return;
-            if (nov < EE_INLINE) ov[nov++] = e2;
-            else atomicAdd(&o.counters[CC_CAND_OVERFLOW], 1ull);
+            if (n < EE_LEAVES) L[n] = e2;
+            ++n;
         });
     }
     s_min[w][lane] = __float_as_int(r);
+    if (__ballot_sync(full, n > EE_LEAVES)) {
+        if (e >= 0) ee_query_one(t, eb, xf, r, o, e);
+        if (lane == 0) atomicAdd(&o.counters[CC_EE_WARP_FALLBACK], 1ull);
+        return;
+    }
     __syncwarp();
     // (query, leaf) pairs of the warp: exclusive prefix of the list lengths
     int incl = n;
@@ -327,17 +353,11 @@ __global__ void __launch_bounds__(32 * EE_WARPS) k_ee_query(CDTopo t, bvh::LbvhD
     }
     __syncwarp();
     if (e < 0) return;
-    // the accepted leaves of this lane's query (the shared list's, then its own), ascending;
-    // the list entries are compacted in place and the lane's own appended while there is room
+    // the accepted leaves of this lane's query, in traversal order, then ascending
     int na = 0;
     for (int a = 0; a < n; ++a) {
         const int x = L[a];
         if (x < 0) L[na++] = ~x;
-    }
-    int extra = 0;
-    for (int a = 0; a < nov; ++a) {
-        if (na < EE_LEAVES + 1) L[na++] = ov[a];
-        else ov[extra++] = ov[a];  // kept aside when the list is full
     }
     for (int a = 1; a < na; ++a) {
         const int kk = L[a];
@@ -348,31 +368,13 @@ __global__ void __launch_bounds__(32 * EE_WARPS) k_ee_query(CDTopo t, bvh::LbvhD
         }
         L[b + 1] = kk;
     }
-    // merge the (rare) leaves kept aside: ascending insertion into the output only
-    int out = 0;
-    const int total_acc = na + extra;
-    if (total_acc > EE_CAP) atomicAdd(&o.counters[CC_EE_OVERFLOW], 1ull);
-    if (extra == 0) {
-        out = min(na, EE_CAP);
-        for (int a = 0; a < out; ++a) o.eeOther[size_t(e) * EE_CAP + a] = L[a];
-    } else {
-        for (int a = 1; a < extra; ++a) {
-            const int kk = ov[a];
-            int b = a - 1;
-            while (b >= 0 && ov[b] > kk) {
-                ov[b + 1] = ov[b];
-                --b;
-            }
-            ov[b + 1] = kk;
-        }
-        int ia = 0, ib = 0;
-        while (out < EE_CAP && (ia < na || ib < extra)) {
-            const bool takeA = ib >= extra || (ia < na && L[ia] < ov[ib]);
-            o.eeOther[size_t(e) * EE_CAP + out++] = takeA ? L[ia++] : ov[ib++];
-        }
+    if (na > EE_CAP) {
+        atomicAdd(&o.counters[CC_EE_OVERFLOW], 1ull);
+        na = EE_CAP;
     }
-    o.eeCount[e] = out;
-    o.eeMinDis[e] = fminf(__int_as_float(s_min[w][lane]), minOwn);
+    for (int a = 0; a < na; ++a) o.eeOther[size_t(e) * EE_CAP + a] = L[a];
+    o.eeCount[e] = na;
+    o.eeMinDis[e] = __int_as_float(s_min[w][lane]);
 }
 
 inline int blocks(int n, int b) { return (n + b - 1) / b; }
