@@ -68,7 +68,7 @@ class ClothStats(C.Structure):
         ("kernel_launches_per_step", C.c_int64), ("detections", C.c_int64), ("truncations", C.c_int64),
         ("vf_overflow", C.c_int64), ("ee_overflow", C.c_int64), ("fv_overflow", C.c_int64),
         ("candidate_overflow", C.c_int64), ("stack_overflow", C.c_int64), ("fp64_fallback_solves", C.c_int64),
-        ("failed_solves", C.c_int64), ("device_bytes", C.c_int64), ("ee_warp_fallbacks", C.c_int64),
+        ("failed_solves", C.c_int64), ("device_bytes", C.c_int64),
     ]
 
     def as_dict(self) -> dict:

@@ -202,10 +202,16 @@ __global__ void k_fv_sort(CDTopo t, CDOut o, const int* req) {
 // Edge-edge query of one simulated edge: triMeshEdgeContactQueryFunc
 // (ClothContactDetector.cpp:731-813) with the query sphere of contactQueryEE
 // (:1106-1135): centre at the edge midpoint, radius maxQueryDis + half the edge length.
-// The whole query in one thread: the warp kernel's path for warps whose queries reach more
-// leaves than its shared lists hold.
-__device__ void ee_query_one(const CDTopo& t, const bvh::LbvhDev& eb, const float4* xf, float r, const CDOut& o,
-                             int e) {
+// Thread i takes the edge of leaf i of the edge hierarchy (Morton order of the last build),
+// so the queries of a warp are neighbours in space and walk much the same nodes; leaves of
+// collider edges have no query.
+__global__ void __launch_bounds__(128) k_ee_query(CDTopo t, bvh::LbvhDev eb, const float4* xf, float r, CDOut o,
+                                                  const int* req) {
+    if (*req == 0) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= eb.n) return;
+    const int e = int(eb.keys[i] & 0xffffffffull);
+    if (e < 0 || e >= t.nSimE) return;
     const int4 E = t.edges[e];
     const int m1 = t.edgeInfo[e].z;
     const float3 p1 = ld3(xf, E.x), p2 = ld3(xf, E.y);
@@ -254,127 +260,6 @@ __device__ void ee_query_one(const CDTopo& t, const bvh::LbvhDev& eb, const floa
     for (int a = 0; a < nc; ++a) o.eeOther[size_t(e) * EE_CAP + a] = cand[a];
     o.eeCount[e] = nc;
     o.eeMinDis[e] = minDis;
-}
-
-constexpr int EE_WARPS = 2;    // warps per block of the edge-edge query
-constexpr int EE_LEAVES = 64;  // hierarchy leaves per query kept for the warp's narrow phase
-
-// The edge-edge queries of a warp, the narrow phase shared by the warp's lanes. Lane i takes
-// the edge of leaf i of the edge hierarchy (Morton order of the last build: the queries of
-// a warp are neighbours in space). Each lane walks the hierarchy for its own query and
-// only lists the leaves in reach (shared memory); the warp then runs the narrow phase of all
-// its (query, leaf) pairs, 32 at a time, so the lanes stay busy however uneven the lists
-// are (one query per lane left most lanes idle in the narrow phase: 10 of 32 active). The
-// predicates are the per-thread query's, in the same order per pair; the minimum distance is
-// a minimum over the same values, and the accepted leaves are sorted by id as there, so the
-// results are identical. A warp with a query that reaches more than EE_LEAVES leaves runs
-// its queries one per lane instead (ee_query_one) and counts it in CC_EE_WARP_FALLBACK.
-__global__ void __launch_bounds__(32 * EE_WARPS) k_ee_query(CDTopo t, bvh::LbvhDev eb, const float4* xf, float r,
-                                                             CDOut o, const int* req) {
-    if (*req == 0) return;
-    __shared__ int s_leaf[EE_WARPS][32][EE_LEAVES + 1];  // +1: lanes' lists in different banks
-    __shared__ int s_min[EE_WARPS][32];
-    const unsigned full = 0xffffffffu;
-    const int w = int(threadIdx.x) >> 5, lane = int(threadIdx.x) & 31;
-    const int i = int(blockIdx.x * blockDim.x + threadIdx.x);
-    int e = -1;
-    if (i < eb.n) {
-        e = int(eb.keys[i] & 0xffffffffull);
-        if (e < 0 || e >= t.nSimE) e = -1;  // leaves of collider edges have no query
-    }
-    int4 E = make_int4(0, 0, 0, 0);
-    int m1 = -1, n = 0;
-    float3 p1 = v3(0.f, 0.f, 0.f), p2 = p1;
-    int* L = s_leaf[w][lane];
-    if (e >= 0) {
-        E = t.edges[e];
-        m1 = t.edgeInfo[e].z;
-        p1 = ld3(xf, E.x);
-        p2 = ld3(xf, E.y);
-        const float3 dd = sub(p1, p2);
-        const float eLen = sqrtf(dot(dd, dd));
-        const float3 c = mul(0.5f, add(p1, p2));
-        const float rq = (r + eLen * 0.5f) * 1.0001f;
-        bvh::traverse(eb, c, rq * rq, o.counters, [&](int e2) {
-            if (n < EE_LEAVES) L[n] = e2;
-            ++n;
-        });
-    }
-    s_min[w][lane] = __float_as_int(r);
-    if (__ballot_sync(full, n > EE_LEAVES)) {
-        if (e >= 0) ee_query_one(t, eb, xf, r, o, e);
-        if (lane == 0) atomicAdd(&o.counters[CC_EE_WARP_FALLBACK], 1ull);
-        return;
-    }
-    __syncwarp();
-    // (query, leaf) pairs of the warp: exclusive prefix of the list lengths
-    int incl = n;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const int y = __shfl_up_sync(full, incl, off);
-        if (lane >= off) incl += y;
-    }
-    const int excl = incl - n;
-    const int total = __shfl_sync(full, incl, 31);
-    for (int base = 0; base < total; base += 32) {
-        const int pr = base + lane;
-        // owner: the last lane whose list starts at or before pair pr
-        int q = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-            const int ex = __shfl_sync(full, excl, q + step);
-            if (ex <= pr) q += step;
-        }
-        const int k = pr - __shfl_sync(full, excl, q);
-        const int qe = __shfl_sync(full, e, q), qm = __shfl_sync(full, m1, q);
-        const int qE0 = __shfl_sync(full, E.x, q), qE1 = __shfl_sync(full, E.y, q);
-        const float3 a1 = v3(__shfl_sync(full, p1.x, q), __shfl_sync(full, p1.y, q), __shfl_sync(full, p1.z, q));
-        const float3 a2 = v3(__shfl_sync(full, p2.x, q), __shfl_sync(full, p2.y, q), __shfl_sync(full, p2.z, q));
-        if (pr >= total) continue;
-        const int e2 = s_leaf[w][q][k];
-        const int4 F = t.edges[e2];
-        const int m2 = t.edgeInfo[e2].z;
-        if (qm == m2) {
-            if (e2 == qe) continue;
-            if (qE0 == F.x || qE0 == F.y || qE1 == F.x || qE1 == F.y) continue;
-        }
-        const float3 q1 = ld3(xf, F.x), q2 = ld3(xf, F.y);
-        float3 c1, c2;
-        float s, tt;
-        closest_points_segments(a1, a2, q1, q2, c1, c2, s, tt);
-        const float3 df = sub(c1, c2);
-        const float d = sqrtf(dot(df, df));
-        if (d == d) atomicMin(&s_min[w][q], __float_as_int(d));  // d >= 0: int order = float order
-        if (!(d < r)) continue;
-        const float3 ev1 = sub(a2, a1), ev2 = sub(q2, q1);
-        const bool ok = (dot(sub(c2, a1), ev1) >= 0.f && dot(sub(a2, c2), ev1) >= 0.f) ||
-                        (dot(sub(c1, q1), ev2) >= 0.f && dot(sub(q2, c1), ev2) >= 0.f);
-        if (ok) s_leaf[w][q][k] = ~e2;  // accepted
-    }
-    __syncwarp();
-    if (e < 0) return;
-    // the accepted leaves of this lane's query, in traversal order, then ascending
-    int na = 0;
-    for (int a = 0; a < n; ++a) {
-        const int x = L[a];
-        if (x < 0) L[na++] = ~x;
-    }
-    for (int a = 1; a < na; ++a) {
-        const int kk = L[a];
-        int b = a - 1;
-        while (b >= 0 && L[b] > kk) {
-            L[b + 1] = L[b];
-            --b;
-        }
-        L[b + 1] = kk;
-    }
-    if (na > EE_CAP) {
-        atomicAdd(&o.counters[CC_EE_OVERFLOW], 1ull);
-        na = EE_CAP;
-    }
-    for (int a = 0; a < na; ++a) o.eeOther[size_t(e) * EE_CAP + a] = L[a];
-    o.eeCount[e] = na;
-    o.eeMinDis[e] = __int_as_float(s_min[w][lane]);
 }
 
 inline int blocks(int n, int b) { return (n + b - 1) / b; }
@@ -433,9 +318,7 @@ void ContactDetector::enqueue_detect(const float4* xf, float maxQueryDis, const 
     k_cd_reset<<<blocks(nr, 256), 256, 0, st>>>(t_, out_, maxQueryDis, d_req);
     if (t_.nV > 0) k_vf_query<<<blocks(t_.nV, 128), 128, 0, st>>>(t_, faceBvh_->dev(), xf, maxQueryDis, out_, d_req);
     if (t_.nSimF > 0) k_fv_sort<<<blocks(t_.nSimF, 128), 128, 0, st>>>(t_, out_, d_req);
-    if (t_.nSimE > 0)
-        k_ee_query<<<blocks(t_.nE, 32 * EE_WARPS), 32 * EE_WARPS, 0, st>>>(t_, edgeBvh_->dev(), xf, maxQueryDis, out_,
-                                                                          d_req);
+    if (t_.nSimE > 0) k_ee_query<<<blocks(t_.nE, 128), 128, 0, st>>>(t_, edgeBvh_->dev(), xf, maxQueryDis, out_, d_req);
     CD_CUDA(cudaGetLastError());
 }
 

@@ -28,7 +28,7 @@ enum PrimType : int { PrimVertex = 0, PrimEdge = 1, PrimFace = 2, PrimNone = 4 }
 
 // overflow / event counters
 enum { CC_VF_OVERFLOW = 0, CC_EE_OVERFLOW, CC_FV_OVERFLOW, CC_CAND_OVERFLOW, CC_STACK_OVERFLOW, CC_TRUNCATIONS,
-       CC_DETECTIONS, CC_FP64_SOLVES, CC_FAILED, CC_NONFINITE, CC_EE_WARP_FALLBACK, CC_N };
+       CC_DETECTIONS, CC_FP64_SOLVES, CC_FAILED, CC_NONFINITE, CC_N };
 
 // ---- vector helpers (float3 / double3, fixed operation order) --------------------
 __host__ __device__ __forceinline__ float3 v3(float x, float y, float z) { return make_float3(x, y, z); }

@@ -917,7 +917,6 @@ public:
         s->fp64_fallback_solves = int64_t(h[CC_FP64_SOLVES]);
         s->failed_solves = int64_t(h[CC_FAILED]);
         s->device_bytes = int64_t(bytes_ + cd_.device_bytes());
-        s->ee_warp_fallbacks = int64_t(h[CC_EE_WARP_FALLBACK]);
     }
 
 private:

@@ -41,9 +41,6 @@ typedef struct gaia_cloth_stats {
     int64_t vf_overflow, ee_overflow, fv_overflow, candidate_overflow, stack_overflow;
     int64_t fp64_fallback_solves, failed_solves;
     int64_t device_bytes;
-    int64_t ee_warp_fallbacks;      /* warps of the edge-edge query whose queries reached more
-                                       hierarchy leaves than the shared narrow phase holds (they ran
-                                       one query per lane; same results) */
 } gaia_cloth_stats;
 
 /* VBDClothSimulationFramework::loadRunningparameters: parse the inputs and build
