@@ -107,6 +107,7 @@ enum { kSweepMerged = 0, kSweepScenes = 1, kSweepCluster = 2, kSweepGrid = 3 };
 constexpr int kVariantDeep = 4;  // solve variant: k_solve_deep
 constexpr int kVariantGrid = 5;  // solve variant: k_sweep_grid
 constexpr int kVariantPrefetch = 6;  // solve variant: k_solve with the next wave's records prefetched into L2
+constexpr int kVariantPipe = 7;      // solve variant: k_solve_pipe, double-buffered TMA tiles on a persistent grid
 
 class EngineBase {
 public:
@@ -180,11 +181,14 @@ public:
         set_tma_smem_limits();
         variant_fixed_ = sc_.p.solveVariant;
         if (variant_fixed_ != -1 && variant_fixed_ != 0 && variant_fixed_ != 1 && variant_fixed_ != kVariantDeep &&
-            variant_fixed_ != kVariantPrefetch)
+            variant_fixed_ != kVariantPrefetch && variant_fixed_ != kVariantPipe)
             throw std::runtime_error("solveVariant must be -1 (autotune), 0 (registers), 1 (TMA-staged), 4 (registers, "
-                                     "deeper record pipeline) or 6 (registers, next wave's records prefetched into L2)");
-        // the FP64 engine has neither the TMA variant nor the record prefetch
-        if ((variant_fixed_ == 1 || variant_fixed_ == kVariantPrefetch) && sizeof(R) != 4) variant_fixed_ = 0;
+                                     "deeper record pipeline), 6 (registers, next wave's records prefetched into L2) or "
+                                     "7 (double-buffered TMA tiles on a persistent grid)");
+        // the FP64 engine has neither the TMA variants nor the record prefetch
+        if ((variant_fixed_ == 1 || variant_fixed_ == kVariantPrefetch || variant_fixed_ == kVariantPipe) &&
+            sizeof(R) != 4)
+            variant_fixed_ = 0;
         if (variant_fixed_ >= 0) variant_ = variant_fixed_;
         if (mode_ == kSweepScenes) {
             setup_scenes();
@@ -665,6 +669,56 @@ public:
         }
     }
 
+    // Double-buffered TMA pipeline on a persistent grid (FP32 compute, both tile buffers fit).
+    template <int L>
+    bool launch_solve_pipe_l(int B, int beg, int end, int friction, bool pdl) {
+        if constexpr (sizeof(R) != 4) {
+            return false;
+        } else {
+            const int vpt = B / L;
+            const int mr = max_records(beg, end, vpt);
+            const size_t smem = 16 + 2 * 48 * size_t(mr);
+            if (smem > kTmaSmemMax) return false;
+            auto kern = dev::k_solve_pipe<L, ST>;
+            const auto key = std::make_pair(L * 100000 + B, int(smem));
+            int per_sm = 0;
+            auto it = pipe_occ_.find(key);
+            if (it != pipe_occ_.end()) {
+                per_sm = it->second;
+            } else {
+                GAIA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, B, smem));
+                pipe_occ_[key] = per_sm;
+            }
+            if (per_sm < 1) return false;
+            int dev = 0, sms = 0;
+            GAIA_CUDA(cudaGetDevice(&dev));
+            GAIA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            const int ntiles = div_up(end - beg, vpt);
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(unsigned(std::min(ntiles, per_sm * sms)));
+            cfg.blockDim = dim3(B);
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = st_;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            attr[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = pdl ? attr : nullptr;
+            cfg.numAttrs = pdl ? 1 : 0;
+            GAIA_CUDA(cudaLaunchKernelEx(&cfg, kern, ptrs(), c_, beg, end, friction, mr));
+            return true;
+        }
+    }
+
+    bool launch_solve_pipe(int L, int B, int beg, int end, int friction, bool pdl) {
+        switch (L) {
+            case 2: return launch_solve_pipe_l<2>(B, beg, end, friction, pdl);
+            case 4: return launch_solve_pipe_l<4>(B, beg, end, friction, pdl);
+            case 8: return launch_solve_pipe_l<8>(B, beg, end, friction, pdl);
+            case 16: return launch_solve_pipe_l<16>(B, beg, end, friction, pdl);
+            default: return launch_solve_pipe_l<32>(B, beg, end, friction, pdl);
+        }
+    }
+
     // TMA-staged launch if this engine computes in FP32 and the block's records fit.
     bool launch_solve_tma(int L, int B, int beg, int end, int friction, bool pdl) {
         switch (L) {
@@ -683,6 +737,11 @@ public:
             GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_tma<8, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
             GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_tma<16, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
             GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_tma<32, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
+            GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_pipe<2, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
+            GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_pipe<4, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
+            GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_pipe<8, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
+            GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_pipe<16, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
+            GAIA_CUDA(cudaFuncSetAttribute(dev::k_solve_pipe<32, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kTmaSmemMax)));
         }
     }
 
@@ -705,6 +764,7 @@ public:
                       int variant = 0) {
         if (end <= beg) return;
         if (!PROBE && variant == 1 && launch_solve_tma(L, B, beg, end, friction, pdl)) return;
+        if (!PROBE && variant == kVariantPipe && launch_solve_pipe(L, B, beg, end, friction, pdl)) return;
         if (!PROBE && variant == kVariantDeep) {
             const int grid = div_up(int64_t(end - beg) * L, B);
             switch (L) {
@@ -969,14 +1029,17 @@ public:
         save.alloc(nslots_, nullptr);
         GAIA_CUDA(cudaMemcpyAsync(save.p, d_pos_.p, nslots_ * sizeof(S4), cudaMemcpyDeviceToDevice, st_));
         const int Ls[] = {2, 4, 8, 16, 32};
-        const int Bs[] = {128, 256};
+        // blocks of 64 too for the tile pipeline, whose two tile buffers bound the blocks per SM
+        const std::vector<int> Bs = {128, 256}, Bs_pipe = {64, 128, 256};
         // kernel variants: 0 register-pipelined, 1 TMA-staged (FP32 compute only), 4 deeper
         // register pipeline, 6 register-pipelined with the records of the block one resident
-        // wave ahead bulk-prefetched into L2 (FP32 compute only)
+        // wave ahead bulk-prefetched into L2 (FP32 compute only), 7 double-buffered TMA tiles
+        // on a persistent grid (FP32 compute only)
         std::vector<int> variants = {0, kVariantDeep};
         if (sizeof(R) == 4) {
             variants.push_back(1);
             variants.push_back(kVariantPrefetch);
+            variants.push_back(kVariantPipe);
         }
         const int reps = 4;
         ccfg_.assign(group_beg_.size(), ColorCfg{});
@@ -990,7 +1053,7 @@ public:
                 if (variant_fixed_ >= 0 && var != variant_fixed_) continue;
                 for (int L : Ls) {
                     if (lanes_ && L != lanes_) continue;
-                    for (int B : Bs) {
+                    for (int B : var == kVariantPipe ? Bs_pipe : Bs) {
                         if (block_ && B != block_) continue;
                         launch_solve<false>(L, B, beg, end, 1, nullptr, false, var);  // warm-up
                         GAIA_CUDA(cudaEventRecord(ev_a_, st_));
@@ -1820,7 +1883,7 @@ private:
     int small_color_ = 16384;
     int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma, 2 = k_sweep_scenes,
                                // 3 = k_sweep_cluster, 4 = k_solve_deep, 5 = k_sweep_grid, 6 = k_solve with L2
-                               // prefetch of the next wave's records
+                               // prefetch of the next wave's records, 7 = k_solve_pipe
     int mode_ = 0;             // kSweepMerged, kSweepScenes, kSweepCluster or kSweepGrid
     // scene-major mode: per mesh its color slot ranges, in sweep order
     std::vector<int2> scene_colors_;
@@ -1844,6 +1907,7 @@ private:
     int variant_fixed_ = -1;   // from PhysicsParams solveVariant (-1 = autotune)
     std::map<std::pair<int, int>, int> maxrec_cache_;
     std::map<std::pair<int, int>, int> wave_cache_;  // (lanes, block) -> resident blocks of k_solve
+    std::map<std::pair<int, int>, int> pipe_occ_;    // (lanes and block, shared bytes) -> k_solve_pipe blocks per SM
     static constexpr size_t kTmaSmemMax = 200 * 1024;
     static constexpr int kContactBlocks = 64;
     double tuned_ms_ = 0.0;

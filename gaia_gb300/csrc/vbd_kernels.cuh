@@ -942,6 +942,133 @@ __global__ void __launch_bounds__(256, 4)
 // are mesh m's color slot ranges in sweep order. MAXB bounds the block size (and so the
 // registers a thread may use: 256 leaves the compiler all it needs, 1024 caps it at 64).
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// Double-buffered TMA pipeline (FP32 compute). A persistent grid walks the color's tiles
+// of vpt = blockDim / L consecutive vertices (tile t of block b: t = b, b + grid, ...). The
+// records of a tile are one contiguous range; thread 0 stages the next tile's range into
+// the other shared-memory buffer (three cp.async.bulk copies on that buffer's mbarrier)
+// while the block computes the current one, so the record stream of the whole color is in
+// flight ahead of the warps without occupying their registers. Each lane then prefetches
+// the neighbour states of its next incidence (ids from shared memory) before evaluating the
+// current one: two incidences' gathers in flight per lane. Bounded waits as in k_solve_tma:
+// a block whose wait runs out counts a timeout, drains every copy it issued and returns.
+// max_rec bounds the records of any tile (the host sizes the buffers from it).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+template <int L, typename ST>
+__global__ void __launch_bounds__(256)
+    k_solve_pipe(Ptrs<ST, float> P, Consts<float> c, int beg, int end, int friction, int max_rec) {
+    using U = typename ST::U;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t bar0 = smem_u32(smem);
+    const size_t buf_bytes = 48 * size_t(max_rec);
+    auto s_n = [&](int b) { return reinterpret_cast<int4*>(smem + 16 + size_t(b) * buf_bytes); };
+    auto s_a = [&](int b) { return reinterpret_cast<float4*>(smem + 16 + size_t(b) * buf_bytes + 16 * size_t(max_rec)); };
+    auto s_b = [&](int b) { return reinterpret_cast<float4*>(smem + 16 + size_t(b) * buf_bytes + 32 * size_t(max_rec)); };
+    const int vpt = int(blockDim.x) / L;
+    const int ntiles = (end - beg + vpt - 1) / vpt;
+    pdl_launch_dependents();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // thread 0: the records of tile t into buffer b (records are static: no ordering with
+    // the previous color needed)
+    auto issue = [&](int t, int b) {
+        const int v0 = beg + t * vpt, v1 = min(end, v0 + vpt);
+        const int r0 = P.inc_ofs[v0];
+        const uint32_t bytes = uint32_t(min(P.inc_ofs[v1] - r0, max_rec)) * 16u;
+        const uint32_t bar = bar0 + 8u * uint32_t(b);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(3u * bytes) : "memory");
+        if (bytes) {
+            bulk_g2s(s_n(b), P.rec_n + r0, bytes, bar);
+            bulk_g2s(s_a(b), P.rec_a + r0, bytes, bar);
+            bulk_g2s(s_b(b), P.rec_b + r0, bytes, bar);
+        }
+    };
+    if (threadIdx.x == 0 && int(blockIdx.x) < ntiles) issue(int(blockIdx.x), 0);
+    pdl_wait();
+    const int lane = int(threadIdx.x) & (L - 1);
+    int k = 0;
+    for (int t = int(blockIdx.x); t < ntiles; t += int(gridDim.x), ++k) {
+        const int b = k & 1;
+        const uint32_t parity = uint32_t(k >> 1) & 1u;
+        const int tn = t + int(gridDim.x);
+        // the next tile into the other buffer (released by the barrier that ended the last tile)
+        if (threadIdx.x == 0 && tn < ntiles) issue(tn, b ^ 1);
+        const int v0 = beg + t * vpt, v1 = min(end, v0 + vpt);
+        const int r0 = P.inc_ofs[v0];
+        const int nrec = min(P.inc_ofs[v1] - r0, max_rec);
+        const int v = v0 + int(threadIdx.x) / L;
+        const bool valid = v < v1;
+        MeshMat<float> mat;
+        int rb = 0, re = 0;
+        U uo{};
+        if (valid) {
+            mat = P.mats[P.slot_mesh[v]];
+            rb = P.inc_ofs[v] - r0 + lane;
+            re = min(P.inc_ofs[v + 1] - r0, nrec);
+            if (lane == 0) prefetch_tail(P, v);
+            uo = P.u[v];
+        }
+        const bool ok = __syncthreads_and(mbar_wait(bar0 + 8u * uint32_t(b), parity, c.spin_limit)) != 0;
+        if (!ok) {
+            // this tile's records did not land within the limit: skip the block's remaining
+            // tiles (their vertices do not move), count it, and drain every copy issued (this
+            // tile's and, if issued, the next one's) before the block exits
+            if (threadIdx.x == 0) {
+                atomicAdd(&P.counters[CNT_TIMEOUT], 1ull);
+                bool drained = mbar_drain(bar0 + 8u * uint32_t(b), parity);
+                if (tn < ntiles) drained = mbar_drain(bar0 + 8u * uint32_t(b ^ 1), uint32_t((k + 1) >> 1) & 1u) && drained;
+                if (!drained) atomicAdd(&P.counters[CNT_DRAIN], 1ull);
+            }
+            return;
+        }
+        Acc<float> acc = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (valid && rb < re) {
+            const int4* sn = s_n(b);
+            const float4* sa = s_a(b);
+            const float4* sb = s_b(b);
+            const U uon = ST::nb(uo);
+            int4 n = sn[rb];
+            U q0 = ST::ldg(P.u, n.x), q1 = ST::ldg(P.u, n.y), q2 = ST::ldg(P.u, n.z);
+            for (int r = rb; r < re; r += L) {
+                const int rn = r + L;
+                int4 nn = n;
+                U p0 = q0, p1 = q1, p2 = q2;
+                if (rn < re) {  // the next incidence's gathers in flight during this one
+                    nn = sn[rn];
+                    p0 = ST::ldg(P.u, nn.x);
+                    p1 = ST::ldg(P.u, nn.y);
+                    p2 = ST::ldg(P.u, nn.z);
+                }
+                const float4 a = sa[r], bb = sb[r];
+                const float m0[3] = {a.x, a.y, a.z}, m1[3] = {a.w, bb.x, bb.y}, m2[3] = {bb.z, bb.w, f_bits(n.w)};
+                float e0[3], e1[3], e2[3];
+                ST::diff(q0, uon, e0);
+                ST::diff(q1, uon, e1);
+                ST::diff(q2, uon, e2);
+                incidence<float>(e0, e1, e2, m0, m1, m2, mat.mu, mat.lmbd, acc);
+                n = nn;
+                q0 = p0;
+                q1 = p1;
+                q2 = p2;
+            }
+        }
+        reduce_group<L, float>(acc);
+        if (valid && lane == 0) vertex_tail<ST, float, false>(P, c, v, uo, mat, acc, friction, nullptr, beg, end);
+        __syncthreads();  // every read of buffer b done before the next iteration refills it
+    }
+}
+
 template <int L, typename ST, typename R, int MAXB>
 __global__ void __launch_bounds__(MAXB) k_sweep_scenes(Ptrs<ST, R> P, Consts<R> c, const int2* colors,
                                                        const int32_t* scene_ofs, const int32_t* scene_order,

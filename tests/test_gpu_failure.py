@@ -1,8 +1,9 @@
 """Failure detection and the solve's fallback paths on the GPU, in safe forms only.
 
 - a bounded device wait that runs out: the TMA-staged solve's wait on its staged records
-  is given a limit of zero polls (the test-only PhysicsParams key waitPollLimit), so every
-  block gives up after its copies were issued; each block drains its copies before it
+  (and the tile pipeline's, whose blocks have two tiles' copies in flight) is given a limit
+  of zero polls (the test-only PhysicsParams key waitPollLimit), so every block gives up
+  after its copies were issued; each block drains its copies before it
   exits, skips its vertices, and the next synchronizing call returns
   GAIA_VBD_E_DEVICE_TIMEOUT (once). No vertex was moved by the solve: the positions equal
   those of a run with no iterations at all. Nothing hangs or faults: the drain completes
@@ -49,11 +50,13 @@ def drop6(tmp_path_factory, gaia_lib):
 
 
 @pytest.mark.parametrize("precision", ["fp32", "mixed"])
-def test_staged_wait_timeout_is_reported(drop6, precision):
+@pytest.mark.parametrize("variant", [1, 7])
+def test_staged_wait_timeout_is_reported(drop6, precision, variant):
     from gaia_gb300 import scenes
 
     mp, pp = drop6
-    common = dict(lanesPerVertex=4, blockSize=128, autotune=False, smallColorVertices=0, solveVariant=1)
+    common = dict(lanesPerVertex=4, blockSize=128, autotune=False, smallColorVertices=0, solveVariant=variant,
+                  sweepMode="merged")
     phys = _handle(mp, scenes.set_precision(pp, precision, waitPollLimit=0, **common))
     ref = _handle(mp, scenes.set_precision(pp, precision, out_path=pp + ".noiter.json", iterations=0, **common))
     ok = _handle(mp, scenes.set_precision(pp, precision, out_path=pp + ".ok.json", **common))
@@ -68,7 +71,7 @@ def test_staged_wait_timeout_is_reported(drop6, precision):
         phys.synchronize()
     assert ei.value.code == E_DEVICE_TIMEOUT, str(ei.value)
     st = phys.stats()
-    assert st["device_timeouts"] > 0 and st["solve_variant"] == 1
+    assert st["device_timeouts"] > 0 and st["solve_variant"] == variant
     # reported once: the state is readable afterwards, and no vertex was moved by a solve
     phys.synchronize()
     ref.runStep(1)
