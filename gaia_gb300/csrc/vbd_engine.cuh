@@ -898,7 +898,7 @@ public:
 
     // ---- graphs -----------------------------------------------------------------
     void destroy_graphs() {
-        for (auto* g : {&g_init_, &g_init_rb_, &g_sweep_, &g_vel_})
+        for (auto* g : {&g_init_, &g_init_rb_, &g_sweep_, &g_vel_, &g_step_, &g_step_rb_})
             if (*g) {
                 cudaGraphExecDestroy(*g);
                 *g = nullptr;
@@ -943,35 +943,50 @@ public:
         int64_t k_init = 0, k_init_rb = 0, k_sweep = 0, k_vel = 0;
         g_init_ = capture_one([&] { enqueue_init(false); }, &k_init);
         g_init_rb_ = cd_.enabled() ? capture_one([&] { enqueue_init(true); }, &k_init_rb) : nullptr;
-        g_sweep_ = capture_one(
-            [&] {
-                if (mode_ == kSweepScenes) {
-                    enqueue_scenes_sweep(scene_L_, scene_B_);
-                    return;
-                }
-                if (mode_ == kSweepCluster) {
-                    enqueue_cluster_sweep(scene_C_, scene_L_, scene_B_);
-                    return;
-                }
-                if (mode_ == kSweepGrid) {
-                    enqueue_grid_sweep(scene_L_, scene_B_);
-                    return;
-                }
-                // evaluateConvergence at iteration -1, on the initial guess (VBDPhysics.cpp:866-870)
-                if (sc_.p.evaluateConvergence) enqueue_conv(true);
-                double omega = 1.0;
-                for (int it = 0; it < sc_.p.iterations; ++it) enqueue_iteration(it, &omega, sc_.p.useAccelerator);
-            },
-            &k_sweep);
+        g_sweep_ = capture_one([&] { enqueue_sweep(); }, &k_sweep);
         g_vel_ = capture_one([&] { enqueue_velocity(); }, &k_vel);
+        // the whole substep as one graph (no gaps between the three): for untimed steps and
+        // for timed steps whose sweep time is measured apart
+        g_step_ = capture_one([&] {
+            enqueue_init(false);
+            enqueue_sweep();
+            enqueue_velocity();
+        });
+        g_step_rb_ = cd_.enabled() ? capture_one([&] {
+            enqueue_init(true);
+            enqueue_sweep();
+            enqueue_velocity();
+        })
+                                   : nullptr;
         const int64_t nsub = sc_.p.numSubsteps;
         launches_per_step_ = nsub * (k_init + k_sweep + k_vel) + (g_init_rb_ ? k_init_rb - k_init : 0);
         launches_per_substep_ = (launches_per_step_ + nsub - 1) / nsub;
     }
 
+    // One substep's iterations (the sweep graph's content).
+    void enqueue_sweep() {
+        if (mode_ == kSweepScenes) {
+            enqueue_scenes_sweep(scene_L_, scene_B_);
+            return;
+        }
+        if (mode_ == kSweepCluster) {
+            enqueue_cluster_sweep(scene_C_, scene_L_, scene_B_);
+            return;
+        }
+        if (mode_ == kSweepGrid) {
+            enqueue_grid_sweep(scene_L_, scene_B_);
+            return;
+        }
+        // evaluateConvergence at iteration -1, on the initial guess (VBDPhysics.cpp:866-870)
+        if (sc_.p.evaluateConvergence) enqueue_conv(true);
+        double omega = 1.0;
+        for (int it = 0; it < sc_.p.iterations; ++it) enqueue_iteration(it, &omega, sc_.p.useAccelerator);
+    }
+
     // The face hierarchy of the contact detector is rebuilt at the first substep of a
     // step and refitted in the others.
     cudaGraphExec_t init_graph(int sub) const { return sub == 0 && g_init_rb_ ? g_init_rb_ : g_init_; }
+    cudaGraphExec_t step_graph(int sub) const { return sub == 0 && g_step_rb_ ? g_step_rb_ : g_step_; }
 
     // The convergence log holds the records of the last step.
     void start_step_log() {
@@ -982,9 +997,7 @@ public:
         for (int k = 0; k < n; ++k)
             for (int sub = 0; sub < sc_.p.numSubsteps; ++sub) {
                 if (sub == 0) start_step_log();
-                GAIA_CUDA(cudaGraphLaunch(init_graph(sub), st_));
-                GAIA_CUDA(cudaGraphLaunch(g_sweep_, st_));
-                GAIA_CUDA(cudaGraphLaunch(g_vel_, st_));
+                GAIA_CUDA(cudaGraphLaunch(step_graph(sub), st_));
             }
     }
 
@@ -1869,6 +1882,7 @@ private:
     cudaStream_t st_ = nullptr;
     cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr, ev_c_ = nullptr;
     cudaGraphExec_t g_init_ = nullptr, g_init_rb_ = nullptr, g_sweep_ = nullptr, g_vel_ = nullptr;
+    cudaGraphExec_t g_step_ = nullptr, g_step_rb_ = nullptr;  // init + sweep + velocity of one substep
     tetcd::Detector cd_;
     DevBuf<float4> d_xf_;
     DevBuf<double2> d_mesh_fric_;
