@@ -12,7 +12,10 @@ One JSON line on rank 0 with:
   fp64    = the plain FP64 engine on the same workload (same kernels in FP64);
   error   = relative position error of the mixed engine vs the FP64 engine
             after --error-steps steps from the same initial state;
-  roofline, cpu_baseline, clocks, gpu_launches.
+  roofline, cpu_baseline, clocks, gpu_launches;
+  other_workloads = (twist on one GPU, unless --no-extra) the other configurations'
+            default runs (drop, batch, collide, cloth), each in a child process,
+            summarised: value, step time, precision, error and speed-up vs FP64.
 
 ``--impl reference`` times the CPU restatement of the reference's VBD path (the
 oracle, all host threads) on bounded samples of the same workload.
@@ -239,6 +242,46 @@ def l2_bytes(local: int) -> int:
         return int(torch.cuda.get_device_properties(local).L2_cache_size) or 129 << 20
     except Exception:
         return 129 << 20
+
+
+def other_workloads(timeout_s: float = 900.0) -> dict:
+    """The other configurations, each its own default bench run in a child process (so this
+    line carries their numbers too): value, step time, precision, error vs the FP64 engine,
+    speed-up over it, end-to-end rate, roofline fraction, and per workload its own figure
+    (the batch's scene-steps/s and its speed-up over a per-scene loop, the cloth's floors)."""
+    import subprocess
+    import sys
+
+    out = {}
+    for w in ("drop", "batch", "collide", "cloth"):
+        try:
+            r = subprocess.run([sys.executable, os.path.abspath(__file__), "--workload", w, "--no-extra"],
+                               capture_output=True, text=True, timeout=timeout_s)
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[w] = {"error": f"exit {r.returncode}: {r.stderr.strip().splitlines()[-1:] or ''}"}
+                continue
+            d = json.loads(lines[-1])
+        except Exception as ex:  # a failed child leaves the headline intact
+            out[w] = {"error": str(ex)}
+            continue
+        e = d.get("error_vs_fp64") or {}
+        summary = {"workload": d["config"].get("workload"), "value": d["value"], "unit": d["unit"],
+                   "ms_per_step": d["ms_per_step"], "precision": d["config"].get("precision", "fp32"),
+                   "error_vs_fp64": e.get("rel"),
+                   "speedup_over_fp64": (d.get("fp64") or {}).get("speedup_over_fp64"),
+                   "e2e": (d.get("e2e") or {}).get("value"), "roofline_frac": (d.get("roofline") or {}).get("frac"),
+                   "cpu_baseline": (d.get("cpu_baseline") or {}).get("value"),
+                   "schedule": (d["config"].get("schedule") or {}).get("sweep_mode"),
+                   "clocks": d.get("clocks")}
+        if d.get("batching"):
+            summary["scenes_steps_per_s"] = d["batching"]["scenes_steps_per_s"]
+            summary["speedup_over_per_scene_loop"] = d["batching"]["speedup_over_loop"]
+        if "fp64_vs_fp64_summation_order" in e:
+            summary["fp64_vs_fp64_summation_order"] = e["fp64_vs_fp64_summation_order"]
+            summary["without_friction"] = e.get("without_friction")
+        out[w] = summary
+    return out
 
 
 def timed_steps(phys, steps: int, local: int) -> tuple[float, float, str]:
@@ -612,6 +655,9 @@ def main():
     ap.add_argument("--block", type=int, default=0, help="solve block size (0 = autotune)")
     ap.add_argument("--param", action="append", default=[],
                     help="PhysicsParams override key=json_value (e.g. usePDL=false)")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="twist on 1 GPU: do not also run the other workloads (drop, batch, collide, cloth) "
+                         "and summarise them in the line's other_workloads")
     args = ap.parse_args()
     if args.iterations <= 0:
         args.iterations = {"twist": 50, "collide": 30}.get(args.workload, 20)
@@ -728,6 +774,9 @@ def main():
                     "avg_launch_us": 1e3 * head["sweep_ms"] / launches_solve}
         if fp64:
             fp64["speedup_over_fp64"] = head["value"] / fp64["value"]
+        extra = None
+        if args.workload == "twist" and world == 1 and not args.no_extra:
+            extra = other_workloads()
         line = {
             "metric": METRIC, "value": head["value"], "unit": "vertex-solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"],
@@ -759,6 +808,8 @@ def main():
             # tet-mesh contact detection of the timed engine (cumulative over its life)
             line["contact"] = {k: st[k] for k in ("contact_detections", "contact_stack_overflow",
                                                    "contact_traverse_bounds")}
+        if extra is not None:
+            line["other_workloads"] = extra
         print(json.dumps(line), flush=True)
 
 
