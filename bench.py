@@ -42,6 +42,9 @@ METRIC = "VBD vertex-solves/s & steps/s, FP32-mixed vs plain FP64 at <=1e-5 rel 
 # ncu: FP32 on 8 color launches of the 100^3 twist (4.8 M incidences each), double-float on
 # colors 0-2 of the 60^3 twist (3 x ~1.01 M incidences); see profiles/
 TRAFFIC_BYTES_PER_INCIDENCE = {"fp32": 54.4, "mixed": 59.9}
+# DRAM bytes (read + write) of one k_sweep_scenes launch per solved incidence and iteration:
+# 44.65 GB over 20 iterations of the 512-cube batch's 38.95 M incidences (FP32, mesh frames)
+SCENES_TRAFFIC_BYTES_PER_INCIDENCE_ITERATION = 57.3
 
 
 def load_peaks() -> tuple[float, str]:
@@ -764,11 +767,17 @@ def main():
         # DRAM bytes per solved incidence (records + per-vertex data) from the ncu captures
         # (TRAFFIC_BYTES_PER_INCIDENCE), scaled to one average launch here
         per_inc = TRAFFIC_BYTES_PER_INCIDENCE.get(head["precision"])
-        traffic = per_inc * ninc / st["num_groups"] if per_inc and sweep_mode == 0 else None
+        traffic, source = None, None
+        if per_inc and sweep_mode == 0:
+            traffic = per_inc * ninc / st["num_groups"]
+            source = ("ncu DRAM bytes per incidence (FP32: 100^3 twist launches; double-float: 60^3 twist), times "
+                      "this launch's incidences")
+        elif sweep_mode == 1 and head["precision"] == "fp32":
+            traffic = SCENES_TRAFFIC_BYTES_PER_INCIDENCE_ITERATION * ninc * args.iterations
+            source = ("ncu DRAM bytes of the scene-major sweep per incidence and iteration (512-cube batch, FP32), "
+                      "times this launch's incidences and iterations")
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                    "traffic": traffic,
-                    "traffic_source": "ncu DRAM bytes per incidence (FP32: 100^3 twist launches; double-float: 60^3 "
-                                      "twist), times this launch's incidences",
+                    "traffic": traffic, "traffic_source": source,
                     "peak_kind": peak_kind, "kernel": kernel,
                     "algorithmic_bytes_per_launch": per_launch,
                     "avg_launch_us": 1e3 * head["sweep_ms"] / launches_solve}
