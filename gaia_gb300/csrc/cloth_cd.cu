@@ -93,21 +93,22 @@ __global__ void k_cd_reset(CDTopo t, CDOut o, float maxQueryDis, const int* req)
 // update the vertex's and the face's minimum distance; they are then taken in ascending
 // face order, de-duplicated on (closest-point primitive type, mesh-local primitive id),
 // checked for the feasible region and recorded; contacts on simulated faces are linked
-// back to the face.
+// back to the face. Thread v takes vertex v (grid order: a warp's vertices are neighbours in
+// space), and the warp walks the face hierarchy once for all of them (traverse_warp).
 __global__ void __launch_bounds__(128) k_vf_query(CDTopo t, bvh::LbvhDev fb, const float4* xf, float r, CDOut o,
                                                   const int* req) {
     if (*req == 0) return;
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= t.nV) return;
-    const float3 p = ld3(xf, v);
-    const int2 vi = t.vInfo[v];
+    const bool valid = v < t.nV;  // every lane walks with the warp; lanes past the end without a query
+    const float3 p = valid ? ld3(xf, v) : v3(0.f, 0.f, 0.f);
+    const int2 vi = valid ? t.vInfo[v] : make_int2(0, 0);
     const bool vSim = vi.x < t.numSimMeshes;
     float minDis = r;
     int cf[CAND_CAP];
     unsigned char ct[CAND_CAP];
     int nc = 0;
     const float rq = r * 1.0001f;
-    bvh::traverse(fb, p, rq * rq, o.counters, [&](int f) {
+    bvh::traverse_warp(fb, p, rq * rq, valid, o.counters, [&](int f) {
         const int4 fv = t.faces[f];
         const bool fSim = fv.w < t.numSimMeshes;
         if (!fSim && !vSim) return;
@@ -127,6 +128,7 @@ __global__ void __launch_bounds__(128) k_vf_query(CDTopo t, bvh::LbvhDev fb, con
             atomicAdd(&o.counters[CC_CAND_OVERFLOW], 1ull);
         }
     });
+    if (!valid) return;
     // ascending face order
     for (int a = 1; a < nc; ++a) {
         const int kf = cf[a];
@@ -203,18 +205,18 @@ __global__ void k_fv_sort(CDTopo t, CDOut o, const int* req) {
 // (ClothContactDetector.cpp:731-813) with the query sphere of contactQueryEE
 // (:1106-1135): centre at the edge midpoint, radius maxQueryDis + half the edge length.
 // Thread i takes the edge of leaf i of the edge hierarchy (Morton order of the last build),
-// so the queries of a warp are neighbours in space and walk much the same nodes; leaves of
-// collider edges have no query.
+// so the queries of a warp are neighbours in space, and the warp walks the hierarchy once
+// for all of them (traverse_warp); leaves of collider edges have no query.
 __global__ void __launch_bounds__(128) k_ee_query(CDTopo t, bvh::LbvhDev eb, const float4* xf, float r, CDOut o,
                                                   const int* req) {
     if (*req == 0) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= eb.n) return;
-    const int e = int(eb.keys[i] & 0xffffffffull);
-    if (e < 0 || e >= t.nSimE) return;
-    const int4 E = t.edges[e];
-    const int m1 = t.edgeInfo[e].z;
-    const float3 p1 = ld3(xf, E.x), p2 = ld3(xf, E.y);
+    int e = i < eb.n ? int(eb.keys[i] & 0xffffffffull) : -1;
+    const bool valid = e >= 0 && e < t.nSimE;  // lanes past the end or on collider edges walk without a query
+    if (!valid) e = 0;
+    const int4 E = valid ? t.edges[e] : make_int4(0, 0, 0, 0);
+    const int m1 = valid ? t.edgeInfo[e].z : -1;
+    const float3 p1 = valid ? ld3(xf, E.x) : v3(0.f, 0.f, 0.f), p2 = valid ? ld3(xf, E.y) : p1;
     const float3 dd = sub(p1, p2);
     const float eLen = sqrtf(dot(dd, dd));
     const float3 c = mul(0.5f, add(p1, p2));
@@ -222,7 +224,7 @@ __global__ void __launch_bounds__(128) k_ee_query(CDTopo t, bvh::LbvhDev eb, con
     float minDis = r;
     int cand[CAND_CAP];
     int nc = 0;
-    bvh::traverse(eb, c, rq * rq, o.counters, [&](int e2) {
+    bvh::traverse_warp(eb, c, rq * rq, valid, o.counters, [&](int e2) {
         const int4 F = t.edges[e2];
         const int m2 = t.edgeInfo[e2].z;
         if (m1 == m2) {
@@ -244,6 +246,7 @@ __global__ void __launch_bounds__(128) k_ee_query(CDTopo t, bvh::LbvhDev eb, con
         if (nc < CAND_CAP) cand[nc++] = e2;
         else atomicAdd(&o.counters[CC_CAND_OVERFLOW], 1ull);
     });
+    if (!valid) return;
     for (int a = 1; a < nc; ++a) {
         const int k = cand[a];
         int b = a - 1;

@@ -259,6 +259,51 @@ __device__ __forceinline__ void traverse(const LbvhDev& b, float3 p, float r2, u
     }
 }
 
+// Packet traversal: the warp walks the hierarchy once for all its lanes' queries (lane i its
+// own sphere p, r2; lanes without a query take part with active = false). A node is
+// descended when its box passes the test of any lane; a leaf is visited by exactly the
+// lanes whose own test its box passes — the leaves traverse() visits for that lane, since a
+// node's box contains its children's — and the visiting lanes take the same primitive at
+// the same time. For queries that are neighbours in space (a warp of consecutive grid
+// vertices, or of consecutive leaves in Morton order) the warp's walk is little longer than
+// one lane's, and the node loads and tests are shared instead of diverging. Every lane of
+// the warp calls it.
+template <typename F>
+__device__ __forceinline__ void traverse_warp(const LbvhDev& b, float3 p, float r2, bool active,
+                                              unsigned long long* counters, F&& leaf) {
+    const unsigned full = 0xffffffffu;
+    if (b.n <= 0) return;
+    const bool hr = active && sphere_box(p, r2, b.bmin[0], b.bmax[0]);
+    if (!__any_sync(full, hr)) return;
+    if (b.n == 1) {
+        if (hr) leaf(int(b.keys[0] & 0xffffffffull));
+        return;
+    }
+    int stack[64];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const int node = stack[--sp];
+        const int2 c = b.child[node];
+        const float4 lo0 = b.bmin[c.x], hi0 = b.bmax[c.x], lo1 = b.bmin[c.y], hi1 = b.bmax[c.y];
+        const bool h0 = active && sphere_box(p, r2, lo0, hi0), h1 = active && sphere_box(p, r2, lo1, hi1);
+        const bool a0 = __any_sync(full, h0), a1 = __any_sync(full, h1);
+        const int ch[2] = {c.x, c.y};
+        const bool hit[2] = {h0, h1}, any[2] = {a0, a1};
+#pragma unroll
+        for (int k = 1; k >= 0; --k) {
+            if (!any[k]) continue;
+            if (ch[k] >= b.n - 1) {
+                if (hit[k]) leaf(int(b.keys[ch[k] - (b.n - 1)] & 0xffffffffull));
+            } else if (sp + 1 > 64) {
+                if ((threadIdx.x & 31) == 0) atomicAdd(&counters[CC_STACK_OVERFLOW], 1ull);
+            } else {
+                stack[sp++] = ch[k];
+            }
+        }
+    }
+}
+
 class Lbvh {
 public:
     int n = 0;
