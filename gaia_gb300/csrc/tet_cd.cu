@@ -542,36 +542,29 @@ __global__ void k_clear_hits(Dev D) {
     if (i < D.nsv) D.hit[i] = -1;
 }
 
-// DCD of one surface vertex per thread. The warp walks each hierarchy once for its lanes'
-// queries (surface vertices in mesh order: neighbours in space): a node is taken when any
-// lane's own test passes and each lane acts only where its own test passes, so every lane
-// evaluates the leaves, in the order, of a walk of its own (a leaf's box lies inside its
-// ancestors', and the closest-face bound only shrinks) and the results are those of one walk
-// per lane.
+// DCD of one surface vertex per thread.
 template <bool INTERMEDIATE>
 __global__ void k_dcd(Dev D, bvh::LbvhDev tb, bvh::LbvhDev fb, const float4* xf, const int* vol_flag, int ccd_on,
                       int handle_self, int check_feasible, float eps, float off, TraverseCfg tc) {
-    const unsigned full = 0xffffffffu;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = i < D.nsv;
-    const int2 q = in ? D.sv[i] : make_int2(0, 0);
+    if (i >= D.nsv) return;
+    const int2 q = D.sv[i];
     const int slot = q.x, m = q.y;
     const float4* P = INTERMEDIATE ? xf : xf + D.nslots;
-    bool query = false;
-    if (in) {
-        if (INTERMEDIATE) {
-            query = D.pen[i] || !ccd_on;
-        } else {
-            query = xf[D.nslots + slot].y < off;
-            D.pen[i] = 0;
-        }
-        if (query) D.hit[i] = -1;
+    bool query;
+    if (INTERMEDIATE) {
+        query = D.pen[i] || !ccd_on;
+    } else {
+        query = xf[D.nslots + slot].y < off;
+        D.pen[i] = 0;
     }
-    if (!*vol_flag) return;  // the same for every thread
-    const float3 p = query ? ld3(P, slot) : v3(0.f, 0.f, 0.f);
+    if (!query) return;
+    D.hit[i] = -1;
+    if (!*vol_flag) return;
+    const float3 p = ld3(P, slot);
     // vertexCollisionDetection: the lowest (mesh, tet) that strictly contains p
     int32_t best_t = 0x7fffffff;
-    bvh::traverse_warp(tb, p, 0.f, query, D.counters, [&](int t) {
+    bvh::traverse(tb, p, 0.f, D.counters, [&](int t) {
         if (t >= best_t) return;
         const int tm = D.tet_mesh[t];
         if (!handle_self && tm == m) return;
@@ -579,13 +572,12 @@ __global__ void k_dcd(Dev D, bvh::LbvhDev tb, bvh::LbvhDev fb, const float4* xf,
         if (tm == m && (tv.x == slot || tv.y == slot || tv.z == slot || tv.w == slot)) return;
         if (point_in_tet(p, ld3(P, tv.x), ld3(P, tv.y), ld3(P, tv.z), ld3(P, tv.w))) best_t = t;
     });
-    const bool found = query && best_t != 0x7fffffff;
-    if (!__any_sync(full, found)) return;
-    if (found && !INTERMEDIATE) D.pen[i] = 1;
-    const int im = found ? D.tet_mesh[best_t] : -1;
+    if (best_t == 0x7fffffff) return;
+    if (!INTERMEDIATE) D.pen[i] = 1;
+    const int im = D.tet_mesh[best_t];
     // closestPointQuery: nearest feasible surface face of mesh im from which the
     // tetrahedral traversal reaches best_t, ties to the lower face
-    const bool traverse = found && tc.check && (im == m || tc.non_self);
+    const bool traverse = tc.check && (im == m || tc.non_self);
     float3 target = p;
     if (traverse && tc.shift_center) {
         const int4 tv = D.tets[best_t];
@@ -599,10 +591,8 @@ __global__ void k_dcd(Dev D, bvh::LbvhDev tb, bvh::LbvhDev fb, const float4* xf,
     if (fb.n > 0) stack[sp++] = 0;
     while (sp > 0) {
         const int node = stack[--sp];
-        const bool need = found && box_dist2(p, fb.bmin[node], fb.bmax[node]) <= best * best * 1.0001f;
-        if (!__any_sync(full, need)) continue;
+        if (box_dist2(p, fb.bmin[node], fb.bmax[node]) > best * best * 1.0001f) continue;
         if (node >= fb.n - 1) {
-            if (!need) continue;
             const int g = int(fb.keys[node - (fb.n - 1)] & 0xffffffffull);
             const int4 fv = D.faces[g];
             if (fv.w != im) continue;
@@ -618,7 +608,7 @@ __global__ void k_dcd(Dev D, bvh::LbvhDev tb, bvh::LbvhDev fb, const float4* xf,
             bestg = g;
         } else {
             if (sp + 2 > kStack) {
-                if ((threadIdx.x & 31) == 0) atomicAdd(&D.counters[cloth::CC_STACK_OVERFLOW], 1ull);
+                atomicAdd(&D.counters[cloth::CC_STACK_OVERFLOW], 1ull);
                 continue;
             }
             const int2 c = fb.child[node];
@@ -626,22 +616,18 @@ __global__ void k_dcd(Dev D, bvh::LbvhDev tb, bvh::LbvhDev fb, const float4* xf,
             stack[sp++] = c.x;
         }
     }
-    if (!found) return;
     D.hit[i] = bestg;
     D.hit_tt[i] = -1.f;
 }
 
-// CCD of one surface vertex per thread: the first face its trajectory crosses. The warp walks
-// the face hierarchy once for its lanes' trajectory boxes (as in k_dcd).
+// CCD of one surface vertex per thread: the first face its trajectory crosses.
 __global__ void k_ccd(Dev D, bvh::LbvhDev fb, const float4* xf, float off) {
-    const unsigned full = 0xffffffffu;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = i < D.nsv;
-    const int slot = in ? D.sv[i].x : 0;
-    const float3 p1 = in ? ld3(xf, slot) : v3(0.f, 0.f, 0.f);
-    const bool active = in && p1.y < off && !D.pen[i];
-    if (!__any_sync(full, active)) return;
-    const float3 p0 = active ? ld3(xf, D.nslots + slot) : p1;
+    if (i >= D.nsv) return;
+    const int slot = D.sv[i].x;
+    const float3 p1 = ld3(xf, slot);
+    if (!(p1.y < off) || D.pen[i]) return;
+    const float3 p0 = ld3(xf, D.nslots + slot);
     const float dx = p1.x - p0.x, dy = p1.y - p0.y, dz = p1.z - p0.z;
     const float len = sqrtf(dx * dx + dy * dy + dz * dz);
     const float3 lo = v3(fminf(p0.x, p1.x), fminf(p0.y, p1.y), fminf(p0.z, p1.z));
@@ -653,10 +639,8 @@ __global__ void k_ccd(Dev D, bvh::LbvhDev fb, const float4* xf, float off) {
     if (fb.n > 0) stack[sp++] = 0;
     while (sp > 0) {
         const int node = stack[--sp];
-        const bool need = active && box_overlap(lo, hi, fb.bmin[node], fb.bmax[node]);
-        if (!__any_sync(full, need)) continue;
+        if (!box_overlap(lo, hi, fb.bmin[node], fb.bmax[node])) continue;
         if (node >= fb.n - 1) {
-            if (!need) continue;
             const int g = int(fb.keys[node - (fb.n - 1)] & 0xffffffffull);
             const int4 fv = D.faces[g];
             if (fv.x == slot || fv.y == slot || fv.z == slot) continue;
@@ -672,7 +656,7 @@ __global__ void k_ccd(Dev D, bvh::LbvhDev fb, const float4* xf, float off) {
             }
         } else {
             if (sp + 2 > kStack) {
-                if ((threadIdx.x & 31) == 0) atomicAdd(&D.counters[cloth::CC_STACK_OVERFLOW], 1ull);
+                atomicAdd(&D.counters[cloth::CC_STACK_OVERFLOW], 1ull);
                 continue;
             }
             const int2 c = fb.child[node];
@@ -680,11 +664,11 @@ __global__ void k_ccd(Dev D, bvh::LbvhDev fb, const float4* xf, float off) {
             stack[sp++] = c.x;
         }
     }
-    if (!active) return;
     D.hit[i] = bestg;
     D.hit_tt[i] = besttt;
 }
 
+// Own contacts and relation keys (face vertex slot, surface vertex, order).
 __global__ void k_own(Dev D, uint8_t* info, int4* own, unsigned long long* keys) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) atomicAdd(&D.counters[cloth::CC_DETECTIONS], 1ull);  // one per detection pass
