@@ -183,11 +183,20 @@ def test_error_codes(tmp_path, gaia_lib):
     mp5, pp5 = scenes._write_json(str(tmp_path / "deg"), [scenes.model_entry(tp, cp)], scenes.physics_params(0.01, 2))
     _expect_error(mp5, pp5, _lib.E_MESH)
     # bad parameter values
-    P = json.load(open(pp))
-    P["PhysicsParams"]["gpuPrecision"] = "fp16"
     pbad = tmp_path / "pbad.json"
-    json.dump(P, open(pbad, "w"))
-    _expect_error(mp, str(pbad), _lib.E_INPUT)
+    for key, value in (("gpuPrecision", "fp16"), ("sweepMode", "tiles"), ("clusterSize", 3),
+                       ("evaluationSteps", 0)):
+        P = json.load(open(pp))
+        P["PhysicsParams"][key] = value
+        json.dump(P, open(pbad, "w"))
+        _expect_error(mp, str(pbad), _lib.E_INPUT)
+    # the engine keys beyond the reference's load on a host without a GPU
+    for key, value in (("sweepMode", "grid"), ("sweepMode", "cluster"), ("meshFrames", False),
+                       ("gpuPrecision", "dfhi"), ("solveVariant", 7), ("waitPollLimit", 0)):
+        P = json.load(open(pp))
+        P["PhysicsParams"][key] = value
+        json.dump(P, open(pbad, "w"))
+        _load(mp, str(pbad)).close()
 
 
 def test_initialize_without_gpu_reports_no_device(tmp_path, gaia_lib):
