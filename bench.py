@@ -487,10 +487,13 @@ def run_cloth(args, world, rank, local):
                 "unit": "vertex-solves/s", "ms_per_step": t64 / args.fp64_steps}
     err = None
     if xref is not None:
-        ce = cloth_engine(mp, pp, "fp32")
-        ce.runStep(args.error_steps)
-        x = ce.positions(0)
-        ce.close()
+        xm = {}
+        for prec in ("fp32", "mixed"):
+            ce = cloth_engine(mp, pp, prec)
+            ce.runStep(args.error_steps)
+            xm[prec] = ce.positions(0)
+            ce.close()
+        x = xm["fp32"]
         # the divergence floor of the drape: two FP64 runs that differ only in summation order
         # (one and two lanes per vertex, all else equal); a precision mode cannot get closer
         # to an FP64 run than two FP64 runs get to each other
@@ -502,6 +505,7 @@ def run_cloth(args, world, rank, local):
             cf.close()
         err = {"steps": args.error_steps, "rel": float(np.linalg.norm(x - xref) / np.linalg.norm(xref - x0)),
                "max_abs_m": float(np.abs(x - xref).max()), "reference": "fp64 engine, same kernels",
+               "mixed_rel": float(np.linalg.norm(xm["mixed"] - xref) / np.linalg.norm(xref - x0)),
                "fp64_vs_fp64_summation_order": float(np.linalg.norm(floor[0] - floor[1]) /
                                                      np.linalg.norm(xref - x0))}
         # the same drape without friction: the friction Hessian's jump at zero tangential
@@ -513,19 +517,24 @@ def run_cloth(args, world, rank, local):
         extra = {"lanesPerVertex": args.lanes} if args.lanes else {}
         mpf, ppf = _sc.cloth_on_sphere(dnf, n=args.size, iterations=args.iterations, precision="fp32", friction=0.0,
                                        **extra)
-        xs = {}
+        xs, x1 = {}, {}
         for key, prec, over in (("fp64", "fp64", {"lanesPerVertex": 1}), ("fp64_l2", "fp64", {"lanesPerVertex": 2}),
-                                ("fp32", "fp32", {})):
+                                ("fp32", "fp32", {}), ("mixed", "mixed", {})):
             cf = cloth_engine(mpf, ppf, prec, **over)
             if key == "fp64":
                 xf0 = cf.positions(0)
-            cf.runStep(args.error_steps)
+            cf.runStep(1)
+            x1[key] = cf.positions(0)  # after one step: before the first truncation flip
+            cf.runStep(args.error_steps - 1)
             xs[key] = cf.positions(0)
             cf.close()
         den = np.linalg.norm(xs["fp64"] - xf0)
-        err["without_friction"] = {"steps": args.error_steps,
-                                   "rel": float(np.linalg.norm(xs["fp32"] - xs["fp64"]) / den),
-                                   "fp64_vs_fp64_summation_order": float(np.linalg.norm(xs["fp64_l2"] - xs["fp64"]) / den)}
+        den1 = np.linalg.norm(x1["fp64"] - xf0)
+        err["without_friction"] = {
+            "steps": args.error_steps, "rel": float(np.linalg.norm(xs["fp32"] - xs["fp64"]) / den),
+            "mixed_rel": float(np.linalg.norm(xs["mixed"] - xs["fp64"]) / den),
+            "fp64_vs_fp64_summation_order": float(np.linalg.norm(xs["fp64_l2"] - xs["fp64"]) / den),
+            "after_1_step": {k: float(np.linalg.norm(x1[k] - x1["fp64"]) / den1) for k in ("fp32", "mixed", "fp64_l2")}}
     c = cloth_engine(mp, pp, "fp32")
     nv = c.numVertices(0)
     for _ in range(args.warmup):
@@ -557,6 +566,16 @@ def run_cloth(args, world, rank, local):
         vh = c.velocities(0)
     e2e_s = allmax(world, time.perf_counter() - t0)
     c.close()
+    # the double-float mode's rate on the same drape
+    cmx = cloth_engine(mp, pp, "mixed")
+    for _ in range(args.warmup):
+        cmx.runStep(1)
+    if not args.lanes:
+        cmx.autotune()
+    cmx.runStep(1)
+    cmx.synchronize()
+    mixed_ms = allmax(world, cmx.run_steps_timed(args.steps))
+    cmx.close()
     cpu = None
     if rank == 0 and not args.no_cpu:
         s = cloth_cpu_sample(mp, pp, args.cpu_iters, args.cpu_reps)
@@ -583,6 +602,10 @@ def run_cloth(args, world, rank, local):
         "e2e": {"value": solves * e2e_steps / e2e_s, "unit": "vertex-solves/s", "h2d_bytes_per_step": 48 * nv,
                 "d2h_bytes_per_step": 48 * nv, "steps": e2e_steps},
         "error_vs_fp64": err, "fp64": fp64,
+        "modes": {"fp32": {"value": solves * args.steps / (total_ms / 1e3), "ms_per_step": total_ms / args.steps,
+                           "error_vs_fp64": err["rel"] if err else None},
+                  "mixed": {"value": solves * args.steps / (mixed_ms / 1e3), "ms_per_step": mixed_ms / args.steps,
+                            "error_vs_fp64": err["mixed_rel"] if err else None}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_kind": peak_kind, "kernel": "cloth k_solve + k_commit (all colors)",
                      "algorithmic_bytes_per_launch": alg / max(ngroups, 1),

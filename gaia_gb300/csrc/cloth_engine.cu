@@ -116,6 +116,12 @@ struct Args {
     P4<R>* xprev;
     P4<R>* y;
     P4<R>* xnext;
+    // low halves of the double-float state (position = x + xlo, ...): null unless the
+    // FP32 engine keeps double-float positions
+    P4<float>* xlo;
+    P4<float>* xprevlo;
+    P4<float>* ylo;
+    P4<float>* xnextlo;
     P4<R>* xcd;
     P4<R>* v;
     P4<R>* vprev;
@@ -157,6 +163,48 @@ template <typename R>
 __device__ __forceinline__ void st(P4<R>* p, int i, typename Vec<R>::T v) {
     p[i] = P4<R>{v.x, v.y, v.z, R(0)};
 }
+
+// A solving vertex's frame: every position enters its terms relative to the vertex's own
+// position, so the FP32 differences carry the digits of the distances between nearby
+// vertices rather than of the coordinates (all terms are translation invariant; the world
+// box takes the absolute position from the origin). With the double-float state the low
+// halves join the differences: (hi_i - hi_o) + (lo_i - lo_o).
+template <typename R>
+struct Org {
+    typename Vec<R>::T h;
+    float lx, ly, lz;  // the low half of the vertex's position (0 without the double-float state)
+};
+template <typename R>
+__device__ __forceinline__ Org<R> origin(const Args<R>& a, int v) {
+    Org<R> o;
+    o.h = ld(a.x, v);
+    o.lx = o.ly = o.lz = 0.f;
+    if (a.xlo) {
+        const P4<float> q = a.xlo[v];
+        o.lx = q.x;
+        o.ly = q.y;
+        o.lz = q.z;
+    }
+    return o;
+}
+// position i of the array (hi, lo) relative to the origin; arrays without a low half are
+// taken as exact in their high half
+template <typename R>
+__device__ __forceinline__ typename Vec<R>::T rel(const P4<R>* hi, const P4<float>* lo, int i, const Org<R>& o) {
+    const P4<R> p = hi[i];
+    typename Vec<R>::T d{p.x - o.h.x, p.y - o.h.y, p.z - o.h.z};
+    if (lo) {
+        const P4<float> q = lo[i];
+        d.x += R(q.x - o.lx);
+        d.y += R(q.y - o.ly);
+        d.z += R(q.z - o.lz);
+    } else if (o.lx != 0.f || o.ly != 0.f || o.lz != 0.f) {
+        d.x -= R(o.lx);
+        d.y -= R(o.ly);
+        d.z -= R(o.lz);
+    }
+    return d;
+}
 template <typename V, typename R>
 __device__ __forceinline__ V normalized(V a) {
     const R nn = dot(a, a);
@@ -178,10 +226,10 @@ __device__ __forceinline__ void add_outer(R* H, R s, R nx, R ny, R nz) {
 // The face's vertex ids and positions come in already loaded (the face-side loop loads them
 // once per face).
 template <typename R>
-__device__ void vf_term_at(const Args<R>& a, const Consts<R>& c, int u, int4 fv, typename Vec<R>::T A,
-                           typename Vec<R>::T B, typename Vec<R>::T C, int order, R* f, R* H) {
+__device__ void vf_term_at(const Args<R>& a, const Consts<R>& c, const Org<R>& o, int u, int4 fv,
+                           typename Vec<R>::T A, typename Vec<R>::T B, typename Vec<R>::T C, int order, R* f, R* H) {
     using V = typename Vec<R>::T;
-    const V xu = ld(a.x, u);
+    const V xu = rel(a.x, a.xlo, u, o);
     V bary, cp;
     closest_point_triangle<V, R>(xu, A, B, C, bary, cp);
     const V diff = sub(xu, cp);
@@ -196,8 +244,9 @@ __device__ void vf_term_at(const Args<R>& a, const Consts<R>& c, int u, int4 fv,
     f[1] += b * lambda * n.y;
     f[2] += b * lambda * n.z;
     add_outer(H, d2E * b * b, n.x, n.y, n.z);
-    const V dx3 = sub(xu, ld(a.xprev, u));
-    const V cprev = add(add(mul(bary.x, ld(a.xprev, fv.x)), mul(bary.y, ld(a.xprev, fv.y))), mul(bary.z, ld(a.xprev, fv.z)));
+    const V dx3 = sub(xu, rel(a.xprev, a.xprevlo, u, o));
+    const V cprev = add(add(mul(bary.x, rel(a.xprev, a.xprevlo, fv.x, o)), mul(bary.y, rel(a.xprev, a.xprevlo, fv.y, o))),
+                        mul(bary.z, rel(a.xprev, a.xprevlo, fv.z, o)));
     const V dx = sub(dx3, sub(cp, cprev));
     const V e0 = normalized<V, R>(sub(B, A));
     const V e1 = normalized<V, R>(cross(e0, n));
@@ -210,20 +259,22 @@ __device__ void vf_term_at(const Args<R>& a, const Consts<R>& c, int u, int4 fv,
 }
 
 template <typename R>
-__device__ __forceinline__ void vf_term(const Args<R>& a, const Consts<R>& c, int u, int face, int order, R* f, R* H) {
+__device__ __forceinline__ void vf_term(const Args<R>& a, const Consts<R>& c, const Org<R>& o, int u, int face, int order,
+                                        R* f, R* H) {
     const int4 fv = a.faces[face];
-    vf_term_at(a, c, u, fv, ld(a.x, fv.x), ld(a.x, fv.y), ld(a.x, fv.z), order, f, H);
+    vf_term_at(a, c, o, u, fv, rel(a.x, a.xlo, fv.x, o), rel(a.x, a.xlo, fv.y, o), rel(a.x, a.xlo, fv.z, o), order, f,
+               H);
 }
 
 // One edge-edge contact of edge e (this vertex has order 0/1 on it) with edge e2:
 // accumulateEEContactForceAndHessian (VBDClothPhysics.cpp:1323-1399). Edge e's vertex ids
 // and positions come in already loaded (the edge loop loads them once per edge).
 template <typename R>
-__device__ void ee_term_at(const Args<R>& a, const Consts<R>& c, int4 E, typename Vec<R>::T p1,
+__device__ void ee_term_at(const Args<R>& a, const Consts<R>& c, const Org<R>& o, int4 E, typename Vec<R>::T p1,
                            typename Vec<R>::T p2, int e2, int order, R* f, R* H) {
     using V = typename Vec<R>::T;
     const int4 F = a.edges[e2];
-    const V q1 = ld(a.x, F.x), q2 = ld(a.x, F.y);
+    const V q1 = rel(a.x, a.xlo, F.x, o), q2 = rel(a.x, a.xlo, F.y, o);
     V c1, c2;
     R s, t;
     closest_points_segments(p1, p2, q1, q2, c1, c2, s, t);
@@ -242,8 +293,8 @@ __device__ void ee_term_at(const Args<R>& a, const Consts<R>& c, int4 E, typenam
     f[1] += b * lambda * n.y;
     f[2] += b * lambda * n.z;
     add_outer(H, d2E * b * b, n.x, n.y, n.z);
-    const V c1p = add(mul(R(1) - s, ld(a.xprev, E.x)), mul(s, ld(a.xprev, E.y)));
-    const V c2p = add(mul(R(1) - t, ld(a.xprev, F.x)), mul(t, ld(a.xprev, F.y)));
+    const V c1p = add(mul(R(1) - s, rel(a.xprev, a.xprevlo, E.x, o)), mul(s, rel(a.xprev, a.xprevlo, E.y, o)));
+    const V c2p = add(mul(R(1) - t, rel(a.xprev, a.xprevlo, F.x, o)), mul(t, rel(a.xprev, a.xprevlo, F.y, o)));
     const V dx = sub(sub(c1, c1p), sub(c2, c2p));
     const V e0 = normalized<V, R>(v1);
     const V e1 = normalized<V, R>(cross(e0, n));
@@ -284,14 +335,14 @@ __device__ __forceinline__ bool solve_block<double>(const double* H, const doubl
 // Dr^T Dr = Dm^T Dm), G = DmInv^T (Dr^T dU + dU^T Dr + dU^T dU) DmInv / 2, so FP32 keeps
 // the strain's own digits instead of those of F^T F - I.
 template <typename R>
-__device__ __forceinline__ void membrane(const Args<R>& a, const ClothMat<R>& mat, int2 fo, R* f, R* Hm) {
+__device__ __forceinline__ void membrane(const Args<R>& a, const Org<R>& o, const ClothMat<R>& mat, int2 fo, R* f,
+                                         R* Hm) {
     using V = typename Vec<R>::T;
     const int4 fv = a.faces[fo.x];
-    const V x0 = ld(a.x, fv.x), x1 = ld(a.x, fv.y), x2 = ld(a.x, fv.z);
+    const V x0 = rel(a.x, a.xlo, fv.x, o), x1 = rel(a.x, a.xlo, fv.y, o), x2 = rel(a.x, a.xlo, fv.z, o);
     const V X0 = ld(a.xrest, fv.x), X1 = ld(a.xrest, fv.y), X2 = ld(a.xrest, fv.z);
-    const V u0 = sub(x0, X0);
-    const V e1 = sub(X1, X0), e2 = sub(X2, X0);                 // rest edges
-    const V w1 = sub(sub(x1, X1), u0), w2 = sub(sub(x2, X2), u0);  // edge displacements
+    const V e1 = sub(X1, X0), e2 = sub(X2, X0);                      // rest edges
+    const V w1 = sub(sub(x1, x0), e1), w2 = sub(sub(x2, x0), e2);    // edge displacements
     const P4<R> D = a.faceDmInv[fo.x];  // m00 m10 m01 m11
     const V d1 = add(e1, w1), d2 = add(e2, w2);
     const V f0 = add(mul(D.x, d1), mul(D.y, d2));
@@ -340,11 +391,12 @@ __device__ __forceinline__ void membrane(const Args<R>& a, const ClothMat<R>& ma
 // Quadratic bending of one stencil (accumlateBendingForceAndHessian,
 // VBDTriMeshStVK.cpp:913-982): E = k/2 X^T Q X over its 4 vertices, Rayleigh damping.
 template <typename R>
-__device__ __forceinline__ void bending(const Args<R>& a, const Consts<R>& c, const ClothMat<R>& mat,
+__device__ __forceinline__ void bending(const Args<R>& a, const Consts<R>& c, const Org<R>& o, const ClothMat<R>& mat,
                                         typename Vec<R>::T x, typename Vec<R>::T xp, int2 eo, R* f, R* H) {
     using V = typename Vec<R>::T;
     const int4 E = a.edges[eo.x];
-    const V X0 = ld(a.x, E.x), X1 = ld(a.x, E.y), X2 = ld(a.x, E.z), X3 = ld(a.x, E.w);
+    const V X0 = rel(a.x, a.xlo, E.x, o), X1 = rel(a.x, a.xlo, E.y, o), X2 = rel(a.x, a.xlo, E.z, o),
+            X3 = rel(a.x, a.xlo, E.w, o);
     const V n1 = cross(sub(X1, X0), sub(X2, X0));
     const V n2 = cross(sub(X2, X3), sub(X1, X3));
     if (dot(n1, n1) < c.degThr2 || dot(n2, n2) < c.degThr2) return;
@@ -365,8 +417,8 @@ __device__ __forceinline__ void bending(const Args<R>& a, const Consts<R>& c, co
 // (faces = 0: items of the incident edges' EE contacts) contact terms of one lane: items
 // lane, lane + L, ... of the concatenation, in order.
 template <int L, typename R, int CAP>
-__device__ __forceinline__ void flat_items(const Args<R>& a, const Consts<R>& c, int lane, const int2* list, int n,
-                                           const int* counts, int faces, R* f, R* H) {
+__device__ __forceinline__ void flat_items(const Args<R>& a, const Consts<R>& c, const Org<R>& org, int lane,
+                                           const int2* list, int n, const int* counts, int faces, R* f, R* H) {
     using V = typename Vec<R>::T;
     int i = -1, first = 0, cnt = 0;  // current primitive, its first flattened item, its item count
     int4 ids = make_int4(0, 0, 0, 0);
@@ -381,19 +433,19 @@ __device__ __forceinline__ void flat_items(const Args<R>& a, const Consts<R>& c,
             if (k < first + cnt) {
                 if (faces) {
                     ids = a.faces[o.x];
-                    A = ld(a.x, ids.x);
-                    B = ld(a.x, ids.y);
-                    C = ld(a.x, ids.z);
+                    A = rel(a.x, a.xlo, ids.x, org);
+                    B = rel(a.x, a.xlo, ids.y, org);
+                    C = rel(a.x, a.xlo, ids.z, org);
                 } else {
                     ids = a.edges[o.x];
-                    A = ld(a.x, ids.x);
-                    B = ld(a.x, ids.y);
+                    A = rel(a.x, a.xlo, ids.x, org);
+                    B = rel(a.x, a.xlo, ids.y, org);
                 }
             }
         }
         const int j = k - first;
-        if (faces) vf_term_at(a, c, a.cd.fvVert[size_t(o.x) * CAP + j], ids, A, B, C, o.y, f, H);
-        else ee_term_at(a, c, ids, A, B, a.cd.eeOther[size_t(o.x) * CAP + j], o.y, f, H);
+        if (faces) vf_term_at(a, c, org, a.cd.fvVert[size_t(o.x) * CAP + j], ids, A, B, C, o.y, f, H);
+        else ee_term_at(a, c, org, ids, A, B, a.cd.eeOther[size_t(o.x) * CAP + j], o.y, f, H);
     }
 }
 
@@ -402,15 +454,16 @@ __device__ __forceinline__ void flat_items(const Args<R>& a, const Consts<R>& c,
 // vertices linked to each incident face, flattened over faces) and EE contacts (flattened
 // over the incident edges). Within each kind, lane k takes items k, k + L, ...
 template <int L, typename R>
-__device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, const ClothMat<R>& mat, int v, int lane,
-                                        typename Vec<R>::T x, typename Vec<R>::T xp, R* f, R* H, R* Hm) {
+__device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, const Org<R>& o, const ClothMat<R>& mat,
+                                        int v, int lane, typename Vec<R>::T x, typename Vec<R>::T xp, R* f, R* H,
+                                        R* Hm) {
     const int fa = a.vfOfs[v], nF = a.vfOfs[v + 1] - fa;
     const int ba = a.vbOfs[v], nB = mat.kBend != R(0) ? a.vbOfs[v + 1] - ba : 0;
     const int nVF = min(a.cd.vfCount[v], VF_CAP);
     // one loop per kind of item, so that the lanes of a warp run the same code together
-    for (int k = lane; k < nF; k += L) membrane(a, mat, a.vfList[fa + k], f, Hm);
-    for (int k = lane; k < nB; k += L) bending(a, c, mat, x, xp, a.vbList[ba + k], f, H);
-    for (int k = lane; k < nVF; k += L) vf_term(a, c, v, a.cd.vfFace[size_t(v) * VF_CAP + k], 3, f, H);
+    for (int k = lane; k < nF; k += L) membrane(a, o, mat, a.vfList[fa + k], f, Hm);
+    for (int k = lane; k < nB; k += L) bending(a, c, o, mat, x, xp, a.vbList[ba + k], f, H);
+    for (int k = lane; k < nVF; k += L) vf_term(a, c, o, v, a.cd.vfFace[size_t(v) * VF_CAP + k], 3, f, H);
     // Face side: items (incident face i, link j) in face order; edges: items (incident edge
     // i, contact j) in edge order. Lane `lane` takes the items whose flattened index is
     // lane, lane + L, ..., so every lane of the group has work until the last L items
@@ -418,8 +471,8 @@ __device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, co
     // faces would leave the other lanes idle). The face (edge) of each item follows from the
     // prefix of the item counts, which a lane walks forward as its index grows; the face's
     // (edge's) ids and positions are loaded again only when the lane's face (edge) changes.
-    flat_items<L, R, FV_CAP>(a, c, lane, a.vfList + fa, nF, a.cd.fvCount, 1, f, H);
-    flat_items<L, R, EE_CAP>(a, c, lane, a.veList + a.veOfs[v], a.veOfs[v + 1] - a.veOfs[v], a.cd.eeCount, 0, f,
+    flat_items<L, R, FV_CAP>(a, c, o, lane, a.vfList + fa, nF, a.cd.fvCount, 1, f, H);
+    flat_items<L, R, EE_CAP>(a, c, o, lane, a.veList + a.veOfs[v], a.veOfs[v + 1] - a.veOfs[v], a.cd.eeCount, 0, f,
                              H);
 }
 
@@ -427,8 +480,9 @@ __device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, co
 // (VBDBaseTriMesh.cpp:316-323) and the world box (accumlateBoundaryForceAndHessian,
 // VBDClothPhysics.cpp:1401-1463).
 template <typename R>
-__device__ __forceinline__ void vertex_terms(const Args<R>& a, const Consts<R>& c, const ClothMat<R>& mat, int v,
-                                             typename Vec<R>::T x, typename Vec<R>::T xp, R* f, R* H, const R* Hm) {
+__device__ __forceinline__ void vertex_terms(const Args<R>& a, const Consts<R>& c, const Org<R>& o,
+                                             const ClothMat<R>& mat, int v, typename Vec<R>::T x, typename Vec<R>::T xp,
+                                             R* f, R* H, const R* Hm) {
     using V = typename Vec<R>::T;
     const R dmp = mat.dampStVK / c.dt;
     const V du = sub(x, xp);
@@ -437,22 +491,25 @@ __device__ __forceinline__ void vertex_terms(const Args<R>& a, const Consts<R>& 
     f[2] -= dmp * (Hm[2] * du.x + Hm[4] * du.y + Hm[5] * du.z);
     for (int k = 0; k < 6; ++k) H[k] += Hm[k] * (R(1) + dmp);
     const R mh = a.mass[v] * c.dtSqrRecip;
-    const V yv = ld(a.y, v);
+    const V yv = rel(a.y, a.ylo, v, o);
     f[0] += mh * (yv.x - x.x);
     f[1] += mh * (yv.y - x.y);
     f[2] += mh * (yv.z - x.z);
     H[0] += mh;
     H[3] += mh;
     H[5] += mh;
-    const R xs[3] = {x.x, x.y, x.z}, dxs[3] = {x.x - xp.x, x.y - xp.y, x.z - xp.z};
+    // the world box on the absolute position: the origin (high and low half) plus x
+    const R xs[3] = {o.h.x + x.x, o.h.y + x.y, o.h.z + x.z}, xl[3] = {R(o.lx), R(o.ly), R(o.lz)};
+    const R dxs[3] = {x.x - xp.x, x.y - xp.y, x.z - xp.z};
     const int diag[3] = {0, 3, 5};
     for (int d = 0; d < 3; ++d) {
         R pen;
-        if (xs[d] < c.lo[d]) {
-            pen = c.lo[d] - xs[d];
+        const R below = (c.lo[d] - xs[d]) - xl[d], above = (xs[d] - c.hi[d]) + xl[d];
+        if (below > R(0)) {
+            pen = below;
             f[d] += pen * c.kb;
-        } else if (xs[d] > c.hi[d]) {
-            pen = xs[d] - c.hi[d];
+        } else if (above > R(0)) {
+            pen = above;
             f[d] -= pen * c.kb;
         } else {
             continue;
@@ -479,11 +536,12 @@ __device__ __forceinline__ void group_sum(R* v, int n, unsigned mask) {
 template <typename R>
 __device__ void accumulate(const Args<R>& a, const Consts<R>& c, int v, R* f, R* H) {
     using V = typename Vec<R>::T;
-    const V x = ld(a.x, v), xp = ld(a.xprev, v);
+    const Org<R> o = origin(a, v);
+    const V x = rel(a.x, a.xlo, v, o), xp = rel(a.xprev, a.xprevlo, v, o);
     const ClothMat<R> mat = a.mats[a.vInfo[v].x];
     R Hm[6] = {0, 0, 0, 0, 0, 0};
-    partial<1, R>(a, c, mat, v, 0, x, xp, f, H, Hm);
-    vertex_terms(a, c, mat, v, x, xp, f, H, Hm);
+    partial<1, R>(a, c, o, mat, v, 0, x, xp, f, H, Hm);
+    vertex_terms(a, c, o, mat, v, x, xp, f, H, Hm);
 }
 
 // The block solve of the vertices of one color, L lanes per vertex:
@@ -498,22 +556,23 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 1) k_solve(Args<R> a
     const int v = verts[i];
     if (a.fixed[v]) return;
     const unsigned mask = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1)));
-    const V x = ld(a.x, v), xp = ld(a.xprev, v);
+    const Org<R> o = origin(a, v);
+    const V x = rel(a.x, a.xlo, v, o), xp = rel(a.xprev, a.xprevlo, v, o);  // x is the origin: zero
     const ClothMat<R> mat = a.mats[a.vInfo[v].x];
     R acc[15];  // f[3], H[6], Hm[6]
 #pragma unroll
     for (int k = 0; k < 15; ++k) acc[k] = R(0);
-    partial<L, R>(a, c, mat, v, lane, x, xp, acc, acc + 3, acc + 9);
+    partial<L, R>(a, c, o, mat, v, lane, x, xp, acc, acc + 3, acc + 9);
     if (L > 1) group_sum<L, R>(acc, 15, mask);
     if (lane != 0) return;
     R* f = acc;
     R* H = acc + 3;
-    vertex_terms(a, c, mat, v, x, xp, f, H, acc + 9);
+    vertex_terms(a, c, o, mat, v, x, xp, f, H, acc + 9);
     R dx[3];
-    V xn = x;
+    V xn = x;  // relative to the origin
     if (solve_block<R>(H, f, dx, a.counters)) {
         xn = V{x.x + c.stepSize * dx[0], x.y + c.stepSize * dx[1], x.z + c.stepSize * dx[2]};
-        const V xc = ld(a.xcd, v);
+        const V xc = rel(a.xcd, static_cast<const P4<float>*>(nullptr), v, o);
         const V disp = sub(xn, xc);
         const R s = sqrt(dot(disp, disp));
         const R bnd = a.bound[v];
@@ -529,7 +588,17 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 1) k_solve(Args<R> a
     } else {
         atomicAdd(&a.counters[CC_FAILED], 1ull);
     }
-    st(a.xnext, v, xn);
+    // back to absolute: the origin plus the step (double-float add with the low halves)
+    if (a.xnextlo) {
+        float hx = float(o.h.x), hy = float(o.h.y), hz = float(o.h.z), lx = o.lx, ly = o.ly, lz = o.lz;
+        gaia::dev::df_add(hx, lx, float(xn.x));
+        gaia::dev::df_add(hy, ly, float(xn.y));
+        gaia::dev::df_add(hz, lz, float(xn.z));
+        a.xnext[v] = P4<R>{R(hx), R(hy), R(hz), R(0)};
+        a.xnextlo[v] = P4<float>{lx, ly, lz, 0.f};
+    } else {
+        st(a.xnext, v, add(o.h, xn));
+    }
 }
 
 // One vertex's force and Hessian, for parity tests of the accumulation.
@@ -547,7 +616,28 @@ __global__ void k_commit(Args<R> a, const int* verts, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int v = verts[i];
-    if (!a.fixed[v]) a.x[v] = a.xnext[v];
+    if (!a.fixed[v]) {
+        a.x[v] = a.xnext[v];
+        if (a.xlo) a.xlo[v] = a.xnextlo[v];
+    }
+}
+
+// (hi, lo) + d per component, d an increment in the working precision (the double-float
+// state's update; without low halves a plain add)
+template <typename R>
+__device__ __forceinline__ void add_state(P4<R>* hi, P4<float>* lo, int v, typename Vec<R>::T base,
+                                          const P4<float>& base_lo, typename Vec<R>::T d) {
+    if (lo) {
+        float hx = float(base.x), hy = float(base.y), hz = float(base.z);
+        float lx = base_lo.x, ly = base_lo.y, lz = base_lo.z;
+        gaia::dev::df_add(hx, lx, float(d.x));
+        gaia::dev::df_add(hy, ly, float(d.y));
+        gaia::dev::df_add(hz, lz, float(d.z));
+        hi[v] = P4<R>{R(hx), R(hy), R(hz), R(0)};
+        lo[v] = P4<float>{lx, ly, lz, 0.f};
+    } else {
+        st(hi, v, add(base, d));
+    }
 }
 
 // applyInitialStep + forwardStep_intertia (VBDCloth/VBDBaseTriMesh.cpp:55-178, 180-196).
@@ -558,7 +648,9 @@ __global__ void k_init_step(Args<R> a, Consts<R> c) {
     if (v >= c.nSimV) return;
     const bool hasPrev = a.state[0] > 0;
     const V x = ld(a.x, v);
+    const P4<float> xl = a.xlo ? a.xlo[v] : P4<float>{0.f, 0.f, 0.f, 0.f};
     st(a.xprev, v, x);
+    if (a.xprevlo) a.xprevlo[v] = xl;
     V vel = ld(a.v, v);
     if (hasPrev) st(a.accel, v, mul(R(1) / c.dt, sub(vel, ld(a.vprev, v))));
     const V vp = vel;
@@ -566,12 +658,14 @@ __global__ void k_init_step(Args<R> a, Consts<R> c) {
     if (c.assocGrav) vel = V{vel.x + c.dt * c.g[0], vel.y + c.dt * c.g[1], vel.z + c.dt * c.g[2]};
     if (a.fixed[v]) vel = V{0, 0, 0};
     st(a.v, v, vel);
-    const V y = add(x, mul(c.dt, vel));
-    st(a.y, v, y);
+    // the inertia target and the initial guess as increments of x (added to the double-float
+    // state exactly where there is one)
+    const V dy = mul(c.dt, vel);
+    add_state(a.y, a.ylo, v, x, xl, dy);
     const int type = a.mats[a.vInfo[v].x].initType;
-    V xn = x;
+    V inc{R(0), R(0), R(0)};
     if (type == 0) {
-        xn = y;
+        inc = dy;
     } else if (type == 1) {
         if (hasPrev) {
             const R gn = sqrt(c.g[0] * c.g[0] + c.g[1] * c.g[1] + c.g[2] * c.g[2]);
@@ -579,18 +673,18 @@ __global__ void k_init_step(Args<R> a, Consts<R> c) {
             R ac = dot(ld(a.accel, v), gd);
             ac = ac < gn ? ac : gn;
             ac = ac > R(1e-5) ? ac : R(0);
-            xn = add(add(x, mul(c.dt, vp)), mul(c.dt * c.dt * ac, gd));
+            inc = add(mul(c.dt, vp), mul(c.dt * c.dt * ac, gd));
         } else {
-            xn = y;
+            inc = dy;
         }
     } else if (type == 3) {
-        V step = sub(y, x);
+        V step = dy;
         const R s = sqrt(dot(step, step));
         const R bnd = a.bound[v];
         if (c.handleCollision && s > bnd && s != R(0)) step = mul(bnd / s, step);
-        xn = add(x, step);
+        inc = step;
     }
-    st(a.x, v, xn);
+    add_state(a.x, a.xlo, v, x, xl, inc);
 }
 
 // updateVelocity (VBDClothPhysics.cpp:2318-2360).
@@ -600,7 +694,12 @@ __global__ void k_velocity(Args<R> a, Consts<R> c) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v == 0) a.state[0] += 1;
     if (v >= c.nSimV) return;
-    V vel = mul(R(1) / c.dt, sub(ld(a.x, v), ld(a.xprev, v)));
+    V dxv = sub(ld(a.x, v), ld(a.xprev, v));
+    if (a.xlo) {  // the low halves' difference
+        const P4<float> l = a.xlo[v], lp = a.xprevlo[v];
+        dxv = V{dxv.x + R(l.x - lp.x), dxv.y + R(l.y - lp.y), dxv.z + R(l.z - lp.z)};
+    }
+    V vel = mul(R(1) / c.dt, dxv);
     const ClothMat<R> m = a.mats[a.vInfo[v].x];
     const R vm = sqrt(dot(vel, vel));
     if (m.hasNoGrav && m.maxVel > R(0) && vel.y > m.noGravThr) {
@@ -717,7 +816,10 @@ public:
 template <typename R>
 class ClothEngine : public ClothEngineBase {
 public:
-    explicit ClothEngine(const Scene& s) : sc_(s) {
+    // df: FP32 arithmetic on double-float positions (x, xprev, y, xnext as high + low halves)
+    explicit ClothEngine(const Scene& s, bool df = false) : sc_(s), df_(df && sizeof(R) == 4) {
+        if (df_ && sc_.p.applyAcceleration)
+            throw std::runtime_error("gpuPrecision \"mixed\" is not supported with applyAcceleration");
         CL_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
         CL_CUDA(cudaEventCreate(&ev0_));
         CL_CUDA(cudaEventCreate(&ev1_));
@@ -757,7 +859,10 @@ public:
         check_nonfinite();
     }
 
-    void get_positions(int mesh, double* out) override { copy_out(x_.p, mesh, out); }
+    void get_positions(int mesh, double* out) override {
+        copy_out(x_.p, mesh, out);
+        if (df_) add_lo(xlo_.p, mesh, out);
+    }
     void get_velocities(int mesh, double* out) override {
         if (mesh >= sc_.numSim) {
             std::fill(out, out + 3 * size_t(sc_.meshes[mesh].nv), 0.0);
@@ -767,8 +872,10 @@ public:
     }
     void set_positions(int mesh, const double* in) override {
         copy_in(x_.p, mesh, in);
+        if (df_) copy_in_lo(xlo_.p, mesh, in);
         if (mesh >= sc_.numSim) {  // colliders: their previous positions and the detector copy too
             copy_in(xprev_.p, mesh, in);
+            if (df_) copy_in_lo(xprevlo_.p, mesh, in);
             std::vector<float4> h(sc_.meshes[mesh].nv);
             for (size_t i = 0; i < h.size(); ++i)
                 h[i] = make_float4(float(in[3 * i]), float(in[3 * i + 1]), float(in[3 * i + 2]), 0.f);
@@ -858,6 +965,11 @@ public:
         Buf<int> rsave;
         rsave.alloc(1, nullptr);
         CL_CUDA(cudaMemcpyAsync(save.p, x_.p, x_.n * sizeof(P4<R>), cudaMemcpyDeviceToDevice, st_));
+        Buf<P4<float>> save_lo;
+        if (df_) {
+            save_lo.alloc(xlo_.n, nullptr);
+            CL_CUDA(cudaMemcpyAsync(save_lo.p, xlo_.p, xlo_.n * sizeof(P4<float>), cudaMemcpyDeviceToDevice, st_));
+        }
         CL_CUDA(cudaMemcpyAsync(csave.p, counters_.p, CC_N * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st_));
         CL_CUDA(cudaMemcpyAsync(rsave.p, req_.p, sizeof(int), cudaMemcpyDeviceToDevice, st_));
         auto sweep = [&] {
@@ -876,6 +988,8 @@ public:
         float ms = 0.f;
         CL_CUDA(cudaEventElapsedTime(&ms, ev0_, ev1_));
         CL_CUDA(cudaMemcpyAsync(x_.p, save.p, x_.n * sizeof(P4<R>), cudaMemcpyDeviceToDevice, st_));
+        if (df_)
+            CL_CUDA(cudaMemcpyAsync(xlo_.p, save_lo.p, xlo_.n * sizeof(P4<float>), cudaMemcpyDeviceToDevice, st_));
         CL_CUDA(cudaMemcpyAsync(counters_.p, csave.p, CC_N * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st_));
         CL_CUDA(cudaMemcpyAsync(req_.p, rsave.p, sizeof(int), cudaMemcpyDeviceToDevice, st_));
         CL_CUDA(cudaStreamSynchronize(st_));
@@ -900,7 +1014,7 @@ public:
         CL_CUDA(cudaMemcpyAsync(h, counters_.p, sizeof(h), cudaMemcpyDeviceToHost, st_));
         CL_CUDA(cudaStreamSynchronize(st_));
         std::memset(s, 0, sizeof(*s));
-        s->precision = sizeof(R) == 4 ? 32 : 64;
+        s->precision = sizeof(R) == 4 ? (df_ ? 48 : 32) : 64;
         s->num_groups = int32_t(groups_.size());
         s->num_vertices = cdt_.nV;
         s->num_sim_vertices = cdt_.nSimV;
@@ -943,6 +1057,29 @@ private:
         for (int i = 0; i < nv; ++i) h[i] = P4<R>{R(in[3 * i]), R(in[3 * i + 1]), R(in[3 * i + 2]), R(0)};
         CL_CUDA(cudaMemcpyAsync(dst + vbase_[mesh], h.data(), nv * sizeof(P4<R>), cudaMemcpyHostToDevice, st_));
         CL_CUDA(cudaStreamSynchronize(st_));
+    }
+    // the low halves of the double-float positions: in - float(in), and their sum back
+    void copy_in_lo(P4<float>* dst, int mesh, const double* in) {
+        const int nv = sc_.meshes.at(mesh).nv;
+        std::vector<P4<float>> h(nv);
+        for (int i = 0; i < nv; ++i) {
+            float l[3];
+            for (int k = 0; k < 3; ++k) l[k] = float(in[3 * i + k] - double(float(in[3 * i + k])));
+            h[i] = P4<float>{l[0], l[1], l[2], 0.f};
+        }
+        CL_CUDA(cudaMemcpyAsync(dst + vbase_[mesh], h.data(), nv * sizeof(P4<float>), cudaMemcpyHostToDevice, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+    }
+    void add_lo(const P4<float>* src, int mesh, double* out) {
+        const int nv = sc_.meshes.at(mesh).nv;
+        std::vector<P4<float>> h(nv);
+        CL_CUDA(cudaMemcpyAsync(h.data(), src + vbase_[mesh], nv * sizeof(P4<float>), cudaMemcpyDeviceToHost, st_));
+        CL_CUDA(cudaStreamSynchronize(st_));
+        for (int i = 0; i < nv; ++i) {
+            out[3 * i] += double(h[i].x);
+            out[3 * i + 1] += double(h[i].y);
+            out[3 * i + 2] += double(h[i].z);
+        }
     }
 
     void build() {
@@ -1074,6 +1211,22 @@ private:
         xprev_.upload(hx, tb, st_);
         y_.upload(hx, tb, st_);
         xnext_.upload(hx, tb, st_);
+        if (df_) {
+            // low halves: the remainder of each FP64 input position after its FP32 rounding
+            std::vector<P4<float>> hl(nV, P4<float>{0.f, 0.f, 0.f, 0.f});
+            for (int m = 0; m < nm; ++m) {
+                const TriMesh& M = sc_.meshes[m];
+                for (int i = 0; i < M.nv; ++i) {
+                    float l[3];
+                    for (int k = 0; k < 3; ++k) l[k] = float(M.X[3 * i + k] - double(float(M.X[3 * i + k])));
+                    hl[vbase_[m] + i] = P4<float>{l[0], l[1], l[2], 0.f};
+                }
+            }
+            xlo_.upload(hl, tb, st_);
+            xprevlo_.upload(hl, tb, st_);
+            ylo_.upload(hl, tb, st_);
+            xnextlo_.upload(hl, tb, st_);
+        }
         xcd_.upload(hx, tb, st_);
         xPrevIter_.upload(hx, tb, st_);
         xrest_.upload(hx, tb, st_);
@@ -1139,6 +1292,10 @@ private:
         a.xprev = xprev_.p;
         a.y = y_.p;
         a.xnext = xnext_.p;
+        a.xlo = df_ ? xlo_.p : nullptr;
+        a.xprevlo = df_ ? xprevlo_.p : nullptr;
+        a.ylo = df_ ? ylo_.p : nullptr;
+        a.xnextlo = df_ ? xnextlo_.p : nullptr;
         a.xcd = xcd_.p;
         a.v = v_.p;
         a.vprev = vprev_.p;
@@ -1194,6 +1351,11 @@ private:
         Buf<unsigned long long> csave;
         csave.alloc(CC_N, nullptr);
         CL_CUDA(cudaMemcpyAsync(save.p, x_.p, x_.n * sizeof(P4<R>), cudaMemcpyDeviceToDevice, st_));
+        Buf<P4<float>> save_lo;
+        if (df_) {
+            save_lo.alloc(xlo_.n, nullptr);
+            CL_CUDA(cudaMemcpyAsync(save_lo.p, xlo_.p, xlo_.n * sizeof(P4<float>), cudaMemcpyDeviceToDevice, st_));
+        }
         CL_CUDA(cudaMemcpyAsync(csave.p, counters_.p, CC_N * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st_));
         if (sc_.p.handleCollision) {
             rebuild_bvh();
@@ -1223,6 +1385,8 @@ private:
         // back to the state before tuning (positions, counters, the detection flag); the
         // contact sets and bounds are recomputed by the detection that opens the next step
         CL_CUDA(cudaMemcpyAsync(x_.p, save.p, x_.n * sizeof(P4<R>), cudaMemcpyDeviceToDevice, st_));
+        if (df_)
+            CL_CUDA(cudaMemcpyAsync(xlo_.p, save_lo.p, xlo_.n * sizeof(P4<float>), cudaMemcpyDeviceToDevice, st_));
         CL_CUDA(cudaMemcpyAsync(counters_.p, csave.p, CC_N * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st_));
         CL_CUDA(cudaMemsetAsync(req_.p, 0, sizeof(int), st_));
         CL_CUDA(cudaStreamSynchronize(st_));
@@ -1316,6 +1480,8 @@ private:
     size_t bytes_ = 0;
     std::vector<int> vbase_, fbase_, ebase_, vmesh_, vlocal_, fmesh_, emesh_;
     Buf<P4<R>> x_, xprev_, y_, xnext_, xcd_, xPrevIter_, xrest_, v_, vprev_, accel_;
+    bool df_ = false;                                    // double-float positions (FP32 engine)
+    Buf<P4<float>> xlo_, xprevlo_, ylo_, xnextlo_;       // their low halves
     Buf<R> bound_, mass_, area_, bendQ_;
     Buf<uint8_t> fixed_, active_;
     Buf<int2> vInfo_, vfList_, veList_, vbList_;
@@ -1413,7 +1579,7 @@ int gaia_cloth_initialize(gaia_cloth* h) {
     }
     return cguard(h, [&] {
         if (h->scene.p.gpuPrecision == "fp64") h->eng.reset(new gaia::cloth::ClothEngine<double>(h->scene));
-        else h->eng.reset(new gaia::cloth::ClothEngine<float>(h->scene));
+        else h->eng.reset(new gaia::cloth::ClothEngine<float>(h->scene, h->scene.p.gpuPrecision == "mixed"));
     });
 }
 

@@ -382,8 +382,8 @@ void load_scene(const std::string& models_json, const std::string& params_json, 
     if (p.numSubsteps <= 0 || p.timeStep <= 0) throw std::runtime_error("timeStep and numSubsteps must be positive");
     if (p.iterations < 0) throw std::runtime_error("iterations must be >= 0");
     if (p.useNewton) throw std::runtime_error("useNewton = true (Newton solver) is not part of the VBD cloth step");
-    if (p.gpuPrecision != "fp32" && p.gpuPrecision != "fp64")
-        throw std::runtime_error("cloth gpuPrecision must be \"fp32\" or \"fp64\"");
+    if (p.gpuPrecision != "fp32" && p.gpuPrecision != "fp64" && p.gpuPrecision != "mixed")
+        throw std::runtime_error("cloth gpuPrecision must be \"fp32\", \"mixed\" or \"fp64\"");
     if (p.blockSize < 32 || p.blockSize > 128 || p.blockSize % 32)
         throw std::runtime_error("blockSize must be 32, 64, 96 or 128");
     if (p.lanesPerVertex != 0 && p.lanesPerVertex != 1 && p.lanesPerVertex != 2 && p.lanesPerVertex != 4 &&

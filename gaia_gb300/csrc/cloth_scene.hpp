@@ -45,7 +45,8 @@ struct PhysicsParams {
     // derived (BasePhysicsFramework.cpp:245-249)
     double dt = -1.0, dtSqrReciprocal = -1.0;
     // GB300 engine keys (extensions; absent in reference files -> defaults)
-    std::string gpuPrecision = "fp32";     // "fp32" or "fp64" (the FP64 engine is the error reference)
+    std::string gpuPrecision = "fp32";     // "fp32", "mixed" (FP32 arithmetic, double-float positions) or
+                                           // "fp64" (the FP64 engine is the error reference)
     bool contactDetectionEveryIteration = false;  // also run detection when no vertex was truncated
     int blockSize = 128;
     int lanesPerVertex = 0;                // lanes per vertex of the solve; 0 = autotune per color

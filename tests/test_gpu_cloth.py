@@ -28,7 +28,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-8, "fp32": 1e-4}
+TOL = {"fp64": 1e-8, "fp32": 1e-4, "mixed": 1e-4}
 
 
 def _scene(tmp_path, precision="fp32", **kw):
@@ -105,7 +105,7 @@ def test_contact_pairs_bit_exact(tmp_path, gaia_lib, oracle_lib):
     c.close()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "mixed"])
 def test_vertex_force_hessian(precision, tmp_path, gaia_lib, oracle_lib):
     """Per-vertex force and Hessian (contacts, inertia, membrane, bending) in a state draped
     on the collider and in a folded, jittered state full of vertex-face and edge-edge
@@ -120,7 +120,8 @@ def test_vertex_force_hessian(precision, tmp_path, gaia_lib, oracle_lib):
     draped = walk.positions(0)
     rng = np.random.Generator(np.random.PCG64(5))
     folded = _folded(x0, 0.004) + rng.uniform(-2e-3, 2e-3, size=x0.shape)
-    tol = 1e-9 if precision == "fp64" else 5e-3
+    # mixed: FP32 arithmetic on positions taken relative to the vertex in double-float
+    tol = {"fp64": 1e-9, "fp32": 5e-3, "mixed": 5e-4}[precision]
     for name, x in (("draped", draped), ("folded", folded)):
         o = oc.ClothOracle(sc, nthreads=4)
         c = _engine(mp, pp)
@@ -146,7 +147,7 @@ def test_vertex_force_hessian(precision, tmp_path, gaia_lib, oracle_lib):
         c.close()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "mixed"])
 def test_drape_trajectory(precision, tmp_path, gaia_lib, oracle_lib):
     from oracle import cloth as oc
 
@@ -212,3 +213,26 @@ def test_cloth_features_fp64(variant, tmp_path, gaia_lib, oracle_lib):
     if variant == "fixed":
         assert np.array_equal(x[[0, 11]], x0[[0, 11]])
     c.close()
+
+
+def test_mixed_state_round_trip_and_refusals(tmp_path, gaia_lib):
+    """The double-float positions: what is written is read back to FP64 rounding (the FP32
+    engine keeps ~7 digits), and the mode is refused with the accelerator."""
+    import json
+
+    from gaia_gb300 import GaiaError
+
+    mp, pp = _scene(tmp_path, precision="mixed", density=20.0)
+    c = _engine(mp, pp)
+    assert c.stats()["precision"] == 48
+    x = c.positions(0) + 1.234567890123e-7
+    c.setPositions(0, x)
+    assert np.abs(c.positions(0) - x).max() <= 1e-14
+    c.runStep(2)
+    assert np.isfinite(c.positions(0)).all()
+    c.close()
+    P = json.load(open(pp))
+    P["PhysicsParams"]["applyAcceleration"] = True
+    json.dump(P, open(pp, "w"))
+    with pytest.raises(GaiaError):
+        _engine(mp, pp)
