@@ -164,22 +164,27 @@ __device__ __forceinline__ void st(P4<R>* p, int i, typename Vec<R>::T v) {
     p[i] = P4<R>{v.x, v.y, v.z, R(0)};
 }
 
-// A solving vertex's frame: every position enters its terms relative to the vertex's own
-// position, so the FP32 differences carry the digits of the distances between nearby
-// vertices rather than of the coordinates (all terms are translation invariant; the world
-// box takes the absolute position from the origin). With the double-float state the low
-// halves join the differences: (hi_i - hi_o) + (lo_i - lo_o).
+// Where a solving vertex's terms take positions from. OrgAbs: the stored coordinates as they
+// are (the FP32 and FP64 engines). OrgRel (the double-float state): every position relative
+// to the vertex's own, (hi_i - hi_o) + (lo_i - lo_o), so the FP32 arithmetic works on the
+// distances between nearby vertices with the digits of the double-float positions (all
+// terms are translation invariant; the world box takes the absolute position from the
+// origin).
 template <typename R>
-struct Org {
-    typename Vec<R>::T h;
-    float lx, ly, lz;  // the low half of the vertex's position (0 without the double-float state)
+struct OrgAbs {
+    static constexpr bool kRel = false;
 };
 template <typename R>
-__device__ __forceinline__ Org<R> origin(const Args<R>& a, int v) {
-    Org<R> o;
-    o.h = ld(a.x, v);
-    o.lx = o.ly = o.lz = 0.f;
-    if (a.xlo) {
+struct OrgRel {
+    static constexpr bool kRel = true;
+    typename Vec<R>::T h;  // the vertex's position: high half
+    float lx, ly, lz;      // and low half
+};
+template <typename O, typename R>
+__device__ __forceinline__ O origin(const Args<R>& a, int v) {
+    O o{};
+    if constexpr (O::kRel) {
+        o.h = ld(a.x, v);
         const P4<float> q = a.xlo[v];
         o.lx = q.x;
         o.ly = q.y;
@@ -187,22 +192,20 @@ __device__ __forceinline__ Org<R> origin(const Args<R>& a, int v) {
     }
     return o;
 }
-// position i of the array (hi, lo) relative to the origin; arrays without a low half are
-// taken as exact in their high half
+// position i of the array (hi, lo) as the terms take it; an array without a low half (the
+// detection snapshot) is taken as exact in its high half
 template <typename R>
-__device__ __forceinline__ typename Vec<R>::T rel(const P4<R>* hi, const P4<float>* lo, int i, const Org<R>& o) {
+__device__ __forceinline__ typename Vec<R>::T rel(const P4<R>* hi, const P4<float>*, int i, const OrgAbs<R>&) {
+    return ld(hi, i);
+}
+template <typename R>
+__device__ __forceinline__ typename Vec<R>::T rel(const P4<R>* hi, const P4<float>* lo, int i, const OrgRel<R>& o) {
     const P4<R> p = hi[i];
     typename Vec<R>::T d{p.x - o.h.x, p.y - o.h.y, p.z - o.h.z};
-    if (lo) {
-        const P4<float> q = lo[i];
-        d.x += R(q.x - o.lx);
-        d.y += R(q.y - o.ly);
-        d.z += R(q.z - o.lz);
-    } else if (o.lx != 0.f || o.ly != 0.f || o.lz != 0.f) {
-        d.x -= R(o.lx);
-        d.y -= R(o.ly);
-        d.z -= R(o.lz);
-    }
+    const float qx = lo ? lo[i].x : 0.f, qy = lo ? lo[i].y : 0.f, qz = lo ? lo[i].z : 0.f;
+    d.x += R(qx - o.lx);
+    d.y += R(qy - o.ly);
+    d.z += R(qz - o.lz);
     return d;
 }
 template <typename V, typename R>
@@ -225,8 +228,8 @@ __device__ __forceinline__ void add_outer(R* H, R s, R nx, R ny, R nz) {
 // the closest point recomputed from the current positions (updateVFContactPointInfo).
 // The face's vertex ids and positions come in already loaded (the face-side loop loads them
 // once per face).
-template <typename R>
-__device__ void vf_term_at(const Args<R>& a, const Consts<R>& c, const Org<R>& o, int u, int4 fv,
+template <typename R, typename O>
+__device__ void vf_term_at(const Args<R>& a, const Consts<R>& c, const O& o, int u, int4 fv,
                            typename Vec<R>::T A, typename Vec<R>::T B, typename Vec<R>::T C, int order, R* f, R* H) {
     using V = typename Vec<R>::T;
     const V xu = rel(a.x, a.xlo, u, o);
@@ -258,8 +261,8 @@ __device__ void vf_term_at(const Args<R>& a, const Consts<R>& c, const Org<R>& o
     friction<R>(mu, lambda, t0, t1, dot(e0, dx), dot(e1, dx), epsU, b, f, H);
 }
 
-template <typename R>
-__device__ __forceinline__ void vf_term(const Args<R>& a, const Consts<R>& c, const Org<R>& o, int u, int face, int order,
+template <typename R, typename O>
+__device__ __forceinline__ void vf_term(const Args<R>& a, const Consts<R>& c, const O& o, int u, int face, int order,
                                         R* f, R* H) {
     const int4 fv = a.faces[face];
     vf_term_at(a, c, o, u, fv, rel(a.x, a.xlo, fv.x, o), rel(a.x, a.xlo, fv.y, o), rel(a.x, a.xlo, fv.z, o), order, f,
@@ -269,8 +272,8 @@ __device__ __forceinline__ void vf_term(const Args<R>& a, const Consts<R>& c, co
 // One edge-edge contact of edge e (this vertex has order 0/1 on it) with edge e2:
 // accumulateEEContactForceAndHessian (VBDClothPhysics.cpp:1323-1399). Edge e's vertex ids
 // and positions come in already loaded (the edge loop loads them once per edge).
-template <typename R>
-__device__ void ee_term_at(const Args<R>& a, const Consts<R>& c, const Org<R>& o, int4 E, typename Vec<R>::T p1,
+template <typename R, typename O>
+__device__ void ee_term_at(const Args<R>& a, const Consts<R>& c, const O& o, int4 E, typename Vec<R>::T p1,
                            typename Vec<R>::T p2, int e2, int order, R* f, R* H) {
     using V = typename Vec<R>::T;
     const int4 F = a.edges[e2];
@@ -334,15 +337,23 @@ __device__ __forceinline__ bool solve_block<double>(const double* H, const doubl
 // The strain is formed from displacements u = x - X: with Ds = Dr + dU (Dr the rest edges,
 // Dr^T Dr = Dm^T Dm), G = DmInv^T (Dr^T dU + dU^T Dr + dU^T dU) DmInv / 2, so FP32 keeps
 // the strain's own digits instead of those of F^T F - I.
-template <typename R>
-__device__ __forceinline__ void membrane(const Args<R>& a, const Org<R>& o, const ClothMat<R>& mat, int2 fo, R* f,
+template <typename R, typename O>
+__device__ __forceinline__ void membrane(const Args<R>& a, const O& o, const ClothMat<R>& mat, int2 fo, R* f,
                                          R* Hm) {
     using V = typename Vec<R>::T;
     const int4 fv = a.faces[fo.x];
     const V x0 = rel(a.x, a.xlo, fv.x, o), x1 = rel(a.x, a.xlo, fv.y, o), x2 = rel(a.x, a.xlo, fv.z, o);
     const V X0 = ld(a.xrest, fv.x), X1 = ld(a.xrest, fv.y), X2 = ld(a.xrest, fv.z);
-    const V e1 = sub(X1, X0), e2 = sub(X2, X0);                      // rest edges
-    const V w1 = sub(sub(x1, x0), e1), w2 = sub(sub(x2, x0), e2);    // edge displacements
+    const V e1 = sub(X1, X0), e2 = sub(X2, X0);  // rest edges
+    V w1, w2;                                      // edge displacements
+    if constexpr (O::kRel) {  // positions relative to the solving vertex: edge vectors minus rest edges
+        w1 = sub(sub(x1, x0), e1);
+        w2 = sub(sub(x2, x0), e2);
+    } else {  // coordinates: displacements from the rest positions
+        const V u0 = sub(x0, X0);
+        w1 = sub(sub(x1, X1), u0);
+        w2 = sub(sub(x2, X2), u0);
+    }
     const P4<R> D = a.faceDmInv[fo.x];  // m00 m10 m01 m11
     const V d1 = add(e1, w1), d2 = add(e2, w2);
     const V f0 = add(mul(D.x, d1), mul(D.y, d2));
@@ -390,8 +401,8 @@ __device__ __forceinline__ void membrane(const Args<R>& a, const Org<R>& o, cons
 
 // Quadratic bending of one stencil (accumlateBendingForceAndHessian,
 // VBDTriMeshStVK.cpp:913-982): E = k/2 X^T Q X over its 4 vertices, Rayleigh damping.
-template <typename R>
-__device__ __forceinline__ void bending(const Args<R>& a, const Consts<R>& c, const Org<R>& o, const ClothMat<R>& mat,
+template <typename R, typename O>
+__device__ __forceinline__ void bending(const Args<R>& a, const Consts<R>& c, const O& o, const ClothMat<R>& mat,
                                         typename Vec<R>::T x, typename Vec<R>::T xp, int2 eo, R* f, R* H) {
     using V = typename Vec<R>::T;
     const int4 E = a.edges[eo.x];
@@ -416,8 +427,8 @@ __device__ __forceinline__ void bending(const Args<R>& a, const Consts<R>& c, co
 // The flattened face-side (faces = 1: items of the incident faces' FV links) or edge
 // (faces = 0: items of the incident edges' EE contacts) contact terms of one lane: items
 // lane, lane + L, ... of the concatenation, in order.
-template <int L, typename R, int CAP>
-__device__ __forceinline__ void flat_items(const Args<R>& a, const Consts<R>& c, const Org<R>& org, int lane,
+template <int L, typename R, int CAP, typename O>
+__device__ __forceinline__ void flat_items(const Args<R>& a, const Consts<R>& c, const O& org, int lane,
                                            const int2* list, int n, const int* counts, int faces, R* f, R* H) {
     using V = typename Vec<R>::T;
     int i = -1, first = 0, cnt = 0;  // current primitive, its first flattened item, its item count
@@ -453,8 +464,8 @@ __device__ __forceinline__ void flat_items(const Args<R>& a, const Consts<R>& c,
 // for the Rayleigh term), bending, vertex-side VF contacts, face-side VF contacts (the
 // vertices linked to each incident face, flattened over faces) and EE contacts (flattened
 // over the incident edges). Within each kind, lane k takes items k, k + L, ...
-template <int L, typename R>
-__device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, const Org<R>& o, const ClothMat<R>& mat,
+template <int L, typename R, typename O>
+__device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, const O& o, const ClothMat<R>& mat,
                                         int v, int lane, typename Vec<R>::T x, typename Vec<R>::T xp, R* f, R* H,
                                         R* Hm) {
     const int fa = a.vfOfs[v], nF = a.vfOfs[v + 1] - fa;
@@ -479,8 +490,8 @@ __device__ __forceinline__ void partial(const Args<R>& a, const Consts<R>& c, co
 // Per-vertex terms: the membrane's Rayleigh damping on its own Hessian, inertia
 // (VBDBaseTriMesh.cpp:316-323) and the world box (accumlateBoundaryForceAndHessian,
 // VBDClothPhysics.cpp:1401-1463).
-template <typename R>
-__device__ __forceinline__ void vertex_terms(const Args<R>& a, const Consts<R>& c, const Org<R>& o,
+template <typename R, typename O>
+__device__ __forceinline__ void vertex_terms(const Args<R>& a, const Consts<R>& c, const O& o,
                                              const ClothMat<R>& mat, int v, typename Vec<R>::T x, typename Vec<R>::T xp,
                                              R* f, R* H, const R* Hm) {
     using V = typename Vec<R>::T;
@@ -498,8 +509,17 @@ __device__ __forceinline__ void vertex_terms(const Args<R>& a, const Consts<R>& 
     H[0] += mh;
     H[3] += mh;
     H[5] += mh;
-    // the world box on the absolute position: the origin (high and low half) plus x
-    const R xs[3] = {o.h.x + x.x, o.h.y + x.y, o.h.z + x.z}, xl[3] = {R(o.lx), R(o.ly), R(o.lz)};
+    // the world box on the absolute position (relative terms: the origin, high and low half,
+    // plus x)
+    R xs[3] = {x.x, x.y, x.z}, xl[3] = {R(0), R(0), R(0)};
+    if constexpr (O::kRel) {
+        xs[0] = o.h.x + x.x;
+        xs[1] = o.h.y + x.y;
+        xs[2] = o.h.z + x.z;
+        xl[0] = R(o.lx);
+        xl[1] = R(o.ly);
+        xl[2] = R(o.lz);
+    }
     const R dxs[3] = {x.x - xp.x, x.y - xp.y, x.z - xp.z};
     const int diag[3] = {0, 3, 5};
     for (int d = 0; d < 3; ++d) {
@@ -533,21 +553,21 @@ __device__ __forceinline__ void group_sum(R* v, int n, unsigned mask) {
 
 // Force and Hessian (sym 00 01 02 11 12 22) of vertex v at the current positions
 // (one thread): VBDStepWithExistingCollisions up to its solve.
-template <typename R>
+template <typename R, typename O>
 __device__ void accumulate(const Args<R>& a, const Consts<R>& c, int v, R* f, R* H) {
     using V = typename Vec<R>::T;
-    const Org<R> o = origin(a, v);
+    const O o = origin<O>(a, v);
     const V x = rel(a.x, a.xlo, v, o), xp = rel(a.xprev, a.xprevlo, v, o);
     const ClothMat<R> mat = a.mats[a.vInfo[v].x];
     R Hm[6] = {0, 0, 0, 0, 0, 0};
-    partial<1, R>(a, c, o, mat, v, 0, x, xp, f, H, Hm);
+    partial<1, R, O>(a, c, o, mat, v, 0, x, xp, f, H, Hm);
     vertex_terms(a, c, o, mat, v, x, xp, f, H, Hm);
 }
 
 // The block solve of the vertices of one color, L lanes per vertex:
 // VBDStepWithExistingCollisions (VBDClothPhysics.cpp:1026-1154) with the conservative
 // bound truncation (applyConservativeBoundTruncation, :1223-1246). Writes x_next.
-template <int L, typename R>
+template <int L, typename R, typename O>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 1) k_solve(Args<R> a, Consts<R> c, const int* verts, int n) {
     using V = typename Vec<R>::T;
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -556,13 +576,13 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 1) k_solve(Args<R> a
     const int v = verts[i];
     if (a.fixed[v]) return;
     const unsigned mask = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << ((threadIdx.x & 31) & ~(L - 1)));
-    const Org<R> o = origin(a, v);
-    const V x = rel(a.x, a.xlo, v, o), xp = rel(a.xprev, a.xprevlo, v, o);  // x is the origin: zero
+    const O o = origin<O>(a, v);
+    const V x = rel(a.x, a.xlo, v, o), xp = rel(a.xprev, a.xprevlo, v, o);  // relative terms: x is zero
     const ClothMat<R> mat = a.mats[a.vInfo[v].x];
     R acc[15];  // f[3], H[6], Hm[6]
 #pragma unroll
     for (int k = 0; k < 15; ++k) acc[k] = R(0);
-    partial<L, R>(a, c, o, mat, v, lane, x, xp, acc, acc + 3, acc + 9);
+    partial<L, R, O>(a, c, o, mat, v, lane, x, xp, acc, acc + 3, acc + 9);
     if (L > 1) group_sum<L, R>(acc, 15, mask);
     if (lane != 0) return;
     R* f = acc;
@@ -588,8 +608,8 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 1) k_solve(Args<R> a
     } else {
         atomicAdd(&a.counters[CC_FAILED], 1ull);
     }
-    // back to absolute: the origin plus the step (double-float add with the low halves)
-    if (a.xnextlo) {
+    if constexpr (O::kRel) {
+        // back to absolute: the origin plus the step (double-float add with the low halves)
         float hx = float(o.h.x), hy = float(o.h.y), hz = float(o.h.z), lx = o.lx, ly = o.ly, lz = o.lz;
         gaia::dev::df_add(hx, lx, float(xn.x));
         gaia::dev::df_add(hy, ly, float(xn.y));
@@ -597,16 +617,16 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? 6 : 1) k_solve(Args<R> a
         a.xnext[v] = P4<R>{R(hx), R(hy), R(hz), R(0)};
         a.xnextlo[v] = P4<float>{lx, ly, lz, 0.f};
     } else {
-        st(a.xnext, v, add(o.h, xn));
+        st(a.xnext, v, xn);
     }
 }
 
 // One vertex's force and Hessian, for parity tests of the accumulation.
-template <typename R>
+template <typename R, typename O>
 __global__ void k_probe(Args<R> a, Consts<R> c, int v, double* out) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     R f[3] = {0, 0, 0}, H[6] = {0, 0, 0, 0, 0, 0};
-    accumulate(a, c, v, f, H);
+    accumulate<R, O>(a, c, v, f, H);
     for (int k = 0; k < 3; ++k) out[k] = double(f[k]);
     for (int k = 0; k < 6; ++k) out[3 + k] = double(H[k]);
 }
@@ -1001,7 +1021,8 @@ public:
             throw std::invalid_argument("vertex out of range");
         Buf<double> out;
         out.alloc(9, nullptr);
-        kern::k_probe<R><<<1, 32, 0, st_>>>(a_, c_, vbase_[mesh] + v, out.p);
+        if (df_) kern::k_probe<R, kern::OrgRel<R>><<<1, 32, 0, st_>>>(a_, c_, vbase_[mesh] + v, out.p);
+        else kern::k_probe<R, kern::OrgAbs<R>><<<1, 32, 0, st_>>>(a_, c_, vbase_[mesh] + v, out.p);
         double h[9];
         CL_CUDA(cudaMemcpyAsync(h, out.p, sizeof(h), cudaMemcpyDeviceToHost, st_));
         CL_CUDA(cudaStreamSynchronize(st_));
@@ -1326,18 +1347,29 @@ private:
         a.counters = counters_.p;
     }
 
-    void launch_solve(int L, const int* verts, int n) {
+    template <typename O>
+    void launch_solve_o(int L, const int* verts, int n) {
         const int B = sc_.p.blockSize;
         const int64_t threads = int64_t(n) * L;
         switch (L) {
-            case 1: kern::k_solve<1, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
-            case 2: kern::k_solve<2, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
-            case 4: kern::k_solve<4, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
-            case 8: kern::k_solve<8, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
-            case 16: kern::k_solve<16, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
-            case 32: kern::k_solve<32, R><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 1: kern::k_solve<1, R, O><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 2: kern::k_solve<2, R, O><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 4: kern::k_solve<4, R, O><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 8: kern::k_solve<8, R, O><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 16: kern::k_solve<16, R, O><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
+            case 32: kern::k_solve<32, R, O><<<nblk(threads, B), B, 0, st_>>>(a_, c_, verts, n); break;
             default: throw std::invalid_argument("lanesPerVertex must be 1, 2, 4, 8, 16 or 32");
         }
+    }
+    // the double-float state's terms relative to each vertex; the others on the coordinates
+    void launch_solve(int L, const int* verts, int n) {
+        if constexpr (sizeof(R) == 4) {
+            if (df_) {
+                launch_solve_o<kern::OrgRel<R>>(L, verts, n);
+                return;
+            }
+        }
+        launch_solve_o<kern::OrgAbs<R>>(L, verts, n);
     }
 
     // Lanes per vertex of each color's solve: fixed by lanesPerVertex, or the fastest of
