@@ -29,7 +29,8 @@ extern "C" {
 typedef struct gaia_cloth gaia_cloth;
 
 typedef struct gaia_cloth_stats {
-    int32_t precision;              /* 32 or 64 */
+    int32_t precision;              /* 32, 48 (FP32 arithmetic on double-float positions:
+                                       gpuPrecision "mixed") or 64 */
     int32_t num_groups;             /* merged colors */
     int64_t num_vertices;           /* all meshes, colliders included */
     int64_t num_sim_vertices;
