@@ -63,15 +63,13 @@ def plain_drop(tmp_path_factory, gaia_lib, oracle_lib):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed", "fp32"])
 def test_plain_drop_scenes_mode(plain_drop, precision):
-    from tests.test_gpu_parity import FP32_DROP_BOUND
-
     mp, pp, ref = plain_drop
     x0, x, st = _run(mp, pp, precision, 100, sweepMode="scenes")
     assert st["sweep_mode"] == 1 and st["solve_variant"] == 2
     rel = _rel(x, ref, x0)
     print(f"plain drop, scenes mode, {precision}: rel {rel:.3e}, lanes {st['lanes_per_vertex']} block "
           f"{st['block_size']}, {st['kernel_launches_per_step']} launches per step")
-    assert rel <= (FP32_DROP_BOUND if precision == "fp32" else TOL[precision])
+    assert rel <= TOL[precision]
     assert st["kernel_launches_per_step"] <= 4
 
 
@@ -149,15 +147,13 @@ def test_plain_drop_cluster_mode(plain_drop, precision):
     """The plain-drop configuration on a thread-block cluster with the scene in distributed
     shared memory (every copy of the states updated through DSMEM, a cluster barrier per
     color), against the FP64 oracle."""
-    from tests.test_gpu_parity import FP32_DROP_BOUND
-
     mp, pp, ref = plain_drop
     x0, x, st = _run(mp, pp, precision, 100, sweepMode="cluster")
     assert st["sweep_mode"] == 2 and st["solve_variant"] == 3 and st["cluster_size"] in (2, 4, 8, 16)
     rel = _rel(x, ref, x0)
     print(f"plain drop, cluster mode, {precision}: rel {rel:.3e}, cluster {st['cluster_size']} lanes "
           f"{st['lanes_per_vertex']} block {st['block_size']}")
-    assert rel <= (FP32_DROP_BOUND if precision == "fp32" else TOL[precision])
+    assert rel <= TOL[precision]
 
 
 @pytest.mark.parametrize("precision,cluster", [("fp64", 8), ("fp64", 16), ("mixed", 4), ("mixed", 16)])
@@ -228,15 +224,13 @@ def test_cluster_mode_refused_when_too_large(tmp_path, gaia_lib):
 def test_plain_drop_grid_mode(plain_drop, precision):
     """The plain-drop configuration in one cooperative launch per substep (merged colors, a
     grid barrier between colors), against the FP64 oracle."""
-    from tests.test_gpu_parity import FP32_DROP_BOUND
-
     mp, pp, ref = plain_drop
     x0, x, st = _run(mp, pp, precision, 100, sweepMode="grid")
     assert st["sweep_mode"] == 3 and st["solve_variant"] == 5 and st["device_timeouts"] == 0
     rel = _rel(x, ref, x0)
     print(f"plain drop, grid mode, {precision}: rel {rel:.3e}, lanes {st['lanes_per_vertex']} block "
           f"{st['block_size']}, {st['kernel_launches_per_step']} launches per step")
-    assert rel <= (FP32_DROP_BOUND if precision == "fp32" else TOL[precision])
+    assert rel <= TOL[precision]
     assert st["kernel_launches_per_step"] <= 4
 
 
