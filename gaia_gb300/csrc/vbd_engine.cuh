@@ -108,7 +108,6 @@ constexpr int kVariantDeep = 4;  // solve variant: k_solve_deep
 constexpr int kVariantGrid = 5;  // solve variant: k_sweep_grid
 constexpr int kVariantPrefetch = 6;  // solve variant: k_solve with the next wave's records prefetched into L2
 constexpr int kVariantPipe = 7;      // solve variant: k_solve_pipe, double-buffered TMA tiles on a persistent grid
-constexpr int kVariantAhead = 8;     // solve variant: k_solve_ahead, neighbour gathers one incidence ahead
 
 class EngineBase {
 public:
@@ -182,14 +181,12 @@ public:
         set_tma_smem_limits();
         variant_fixed_ = sc_.p.solveVariant;
         if (variant_fixed_ != -1 && variant_fixed_ != 0 && variant_fixed_ != 1 && variant_fixed_ != kVariantDeep &&
-            variant_fixed_ != kVariantPrefetch && variant_fixed_ != kVariantPipe && variant_fixed_ != kVariantAhead)
+            variant_fixed_ != kVariantPrefetch && variant_fixed_ != kVariantPipe)
             throw std::runtime_error("solveVariant must be -1 (autotune), 0 (registers), 1 (TMA-staged), 4 (registers, "
-                                     "deeper record pipeline), 6 (registers, next wave's records prefetched into L2), "
-                                     "7 (double-buffered TMA tiles on a persistent grid) or 8 (registers, neighbour "
-                                     "gathers one incidence ahead)");
-        // the FP64 engine has neither the TMA variants, the record prefetch nor the gathers ahead
-        if ((variant_fixed_ == 1 || variant_fixed_ == kVariantPrefetch || variant_fixed_ == kVariantPipe ||
-             variant_fixed_ == kVariantAhead) &&
+                                     "deeper record pipeline), 6 (registers, next wave's records prefetched into L2) or "
+                                     "7 (double-buffered TMA tiles on a persistent grid)");
+        // the FP64 engine has neither the TMA variants nor the record prefetch
+        if ((variant_fixed_ == 1 || variant_fixed_ == kVariantPrefetch || variant_fixed_ == kVariantPipe) &&
             sizeof(R) != 4)
             variant_fixed_ = 0;
         if (variant_fixed_ >= 0) variant_ = variant_fixed_;
@@ -762,22 +759,6 @@ public:
         GAIA_CUDA(cudaLaunchKernelEx(&cfg, dev::k_solve_deep<L, ST, R>, ptrs(), c_, beg, end, friction));
     }
 
-    template <int L>
-    void launch_solve_ahead_l(int grid, int B, int beg, int end, int friction, bool pdl) {
-        if constexpr (sizeof(R) == 4) {
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(grid);
-            cfg.blockDim = dim3(B);
-            cfg.stream = st_;
-            cudaLaunchAttribute attr[1];
-            attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-            attr[0].val.programmaticStreamSerializationAllowed = 1;
-            cfg.attrs = pdl ? attr : nullptr;
-            cfg.numAttrs = pdl ? 1 : 0;
-            GAIA_CUDA(cudaLaunchKernelEx(&cfg, dev::k_solve_ahead<L, ST, R>, ptrs(), c_, beg, end, friction));
-        }
-    }
-
     template <bool PROBE>
     void launch_solve(int L, int B, int beg, int end, int friction, double* probe, bool pdl = false,
                       int variant = 0) {
@@ -792,17 +773,6 @@ public:
                 case 8: launch_solve_deep_l<8>(grid, B, beg, end, friction, pdl); break;
                 case 16: launch_solve_deep_l<16>(grid, B, beg, end, friction, pdl); break;
                 default: launch_solve_deep_l<32>(grid, B, beg, end, friction, pdl); break;
-            }
-            return;
-        }
-        if (!PROBE && variant == kVariantAhead && sizeof(R) == 4) {
-            const int grid = div_up(int64_t(end - beg) * L, B);
-            switch (L) {
-                case 2: launch_solve_ahead_l<2>(grid, B, beg, end, friction, pdl); break;
-                case 4: launch_solve_ahead_l<4>(grid, B, beg, end, friction, pdl); break;
-                case 8: launch_solve_ahead_l<8>(grid, B, beg, end, friction, pdl); break;
-                case 16: launch_solve_ahead_l<16>(grid, B, beg, end, friction, pdl); break;
-                default: launch_solve_ahead_l<32>(grid, B, beg, end, friction, pdl); break;
             }
             return;
         }
@@ -1077,14 +1047,12 @@ public:
         // kernel variants: 0 register-pipelined, 1 TMA-staged (FP32 compute only), 4 deeper
         // register pipeline, 6 register-pipelined with the records of the block one resident
         // wave ahead bulk-prefetched into L2 (FP32 compute only), 7 double-buffered TMA tiles
-        // on a persistent grid (FP32 compute only), 8 register-pipelined with the neighbour
-        // gathers one incidence ahead (FP32 compute only)
+        // on a persistent grid (FP32 compute only)
         std::vector<int> variants = {0, kVariantDeep};
         if (sizeof(R) == 4) {
             variants.push_back(1);
             variants.push_back(kVariantPrefetch);
             variants.push_back(kVariantPipe);
-            variants.push_back(kVariantAhead);
         }
         const int reps = 4;
         ccfg_.assign(group_beg_.size(), ColorCfg{});
@@ -1929,7 +1897,7 @@ private:
     int small_color_ = 16384;
     int variant_ = 0;          // 0 = register-pipelined k_solve, 1 = TMA-staged k_solve_tma, 2 = k_sweep_scenes,
                                // 3 = k_sweep_cluster, 4 = k_solve_deep, 5 = k_sweep_grid, 6 = k_solve with L2
-                               // prefetch of the next wave's records, 7 = k_solve_pipe, 8 = k_solve_ahead
+                               // prefetch of the next wave's records, 7 = k_solve_pipe
     int mode_ = 0;             // kSweepMerged, kSweepScenes, kSweepCluster or kSweepGrid
     // scene-major mode: per mesh its color slot ranges, in sweep order
     std::vector<int2> scene_colors_;

@@ -712,88 +712,6 @@ __global__ void __launch_bounds__(256, sizeof(R) == 8 ? 2 : 3)
     vertex_tail<ST, R, false>(P, c, v, uo, mat, acc, friction, nullptr, beg, end);
 }
 
-// The incidence loop with the neighbour gathers one incidence ahead as well: while
-// incidence r is evaluated, the three states of incidence r + L and the record of r + 2L
-// are loading (`cur` and `nx1` already loaded, the states of `cur` issued by the caller's
-// prologue). In the plain loop every record is followed by an L2 round trip for its three
-// states before the element can start; here that round trip overlaps the element of the
-// incidence before. Same records per lane in the same order: the plain loop's sums bit for
-// bit.
-template <int L, typename ST, typename R>
-__device__ __forceinline__ void accumulate_records_ahead(const Ptrs<ST, R>& P, int r, int e, RecRaw<R> cur,
-                                                         RecRaw<R> nx1, typename ST::U c0, typename ST::U c1,
-                                                         typename ST::U c2, const typename ST::U& uo_full, R mu,
-                                                         R lmbd, Acc<R>& acc) {
-    using U = typename ST::U;
-    const U uo = ST::nb(uo_full);
-    while (r < e) {
-        const int r1 = r + L, r2 = r + 2 * L;
-        RecRaw<R> nx2;
-        if (r2 < e) nx2.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r2);
-        U n0 = c0, n1 = c1, n2 = c2;
-        if (r1 < e) {
-            n0 = ST::ldg(P.u, nx1.n.x);
-            n1 = ST::ldg(P.u, nx1.n.y);
-            n2 = ST::ldg(P.u, nx1.n.z);
-        }
-        R m0[3], m1[3], m2[3];
-        cur.rows(m0, m1, m2);
-        R e0[3], e1[3], e2[3];
-        ST::diff(c0, uo, e0);
-        ST::diff(c1, uo, e1);
-        ST::diff(c2, uo, e2);
-        incidence<R>(e0, e1, e2, m0, m1, m2, mu, lmbd, acc);
-        cur = nx1;
-        nx1 = nx2;
-        c0 = n0;
-        c1 = n1;
-        c2 = n2;
-        r = r1;
-    }
-}
-
-// k_solve with the gathers one incidence ahead (variant 8, FP32 compute): the prologue
-// loads each lane's first two records before the programmatic-dependency wait and the
-// first incidence's states right after it. Three resident blocks of 256 threads leave it
-// the registers of the second record and the three states in flight.
-template <int L, typename ST, typename R>
-__global__ void __launch_bounds__(256, 3)
-    k_solve_ahead(Ptrs<ST, R> P, Consts<R> c, int beg, int end, int friction) {
-    using U = typename ST::U;
-    pdl_launch_dependents();
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = tid & (L - 1);
-    const int v = beg + tid / L;
-    const bool valid = v < end;
-    Acc<R> acc = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    U uo{};
-    MeshMat<R> mat;
-    int r = 0, e = 0;
-    RecRaw<R> cur, nx1;
-    if (valid) {
-        mat = P.mats[P.slot_mesh[v]];
-        r = P.inc_ofs[v] + lane;
-        e = P.inc_ofs[v + 1];
-        if (r < e) cur.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r);
-        if (r + L < e) nx1.load(P.rec_n, P.rec_a, P.rec_b, P.rec_c, r + L);
-        if (lane == 0) prefetch_tail(P, v);
-    }
-    pdl_wait();
-    if (valid) {
-        uo = P.u[v];
-        U c0{}, c1{}, c2{};
-        if (r < e) {
-            c0 = ST::ldg(P.u, cur.n.x);
-            c1 = ST::ldg(P.u, cur.n.y);
-            c2 = ST::ldg(P.u, cur.n.z);
-        }
-        accumulate_records_ahead<L, ST, R>(P, r, e, cur, nx1, c0, c1, c2, uo, mat.mu, mat.lmbd, acc);
-    }
-    reduce_group<L, R>(acc);
-    if (!valid || lane != 0) return;
-    vertex_tail<ST, R, false>(P, c, v, uo, mat, acc, friction, nullptr, beg, end);
-}
-
 // ---- per-vertex tail (lane 0 of a vertex group): damping, inertia, ground and
 // friction, 3x3 solve, update ------------------------------------------------------
 // The new state goes to P.u[v], or to *unew when given; returns whether the vertex moved.

@@ -84,15 +84,14 @@ def test_lanes_per_vertex_agree(drop_scene, drop_ref, lanes):
     assert _rel(xs[0], drop_ref[0], x0[0]) <= TOL["fp64"]
 
 
-@pytest.mark.parametrize("variant", [0, 1, 4, 6, 7, 8])
+@pytest.mark.parametrize("variant", [0, 1, 4, 6, 7])
 @pytest.mark.parametrize("lanes", [4, 32])
 @pytest.mark.parametrize("precision", ["mixed", "dfhi", "fp32"])
 def test_solve_variants_agree(drop_scene, drop_ref, variant, lanes, precision):
     """Register-pipelined (0), TMA-staged (1), two-deep register-pipelined (4),
-    register-pipelined with the next wave's records prefetched into L2 (6), double-buffered
-    TMA tiles on a persistent grid (7) and register-pipelined with the neighbour gathers one
-    incidence ahead (8) solve kernels, with and without programmatic dependent launch, give
-    the oracle's result."""
+    register-pipelined with the next wave's records prefetched into L2 (6) and double-buffered
+    TMA tiles on a persistent grid (7) solve kernels, with and without programmatic dependent
+    launch, give the oracle's result."""
     mp, pp = drop_scene
     for pdl in (True, False):
         x0, xs, st = _run_gpu(mp, pp, precision, 40, lanesPerVertex=lanes, blockSize=128, autotune=False,
@@ -102,11 +101,10 @@ def test_solve_variants_agree(drop_scene, drop_ref, variant, lanes, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp32", "mixed"])
-@pytest.mark.parametrize("variant,block", [(1, 128), (6, 128), (7, 64), (7, 256), (8, 128), (8, 256)])
+@pytest.mark.parametrize("variant,block", [(1, 128), (6, 128), (7, 64), (7, 256)])
 def test_variants_are_bit_identical(drop_scene, precision, variant, block):
-    """Staging records in shared memory (1, 7), prefetching them into L2 (6) or loading the
-    neighbour states one incidence ahead (8) moves no result: the same records per lane in
-    the same order, so variant 0 bit for bit."""
+    """Staging records in shared memory (1, 7) or prefetching them into L2 (6) moves no
+    result: the same records per lane in the same order, so variant 0 bit for bit."""
     mp, pp = drop_scene
     common = dict(lanesPerVertex=4, blockSize=block, autotune=False, smallColorVertices=0, sweepMode="merged")
     _, xa, sa = _run_gpu(mp, pp, precision, 20, solveVariant=0, **common)
