@@ -5,13 +5,14 @@ twist test (1.0 M vertices, 4.85 M tets, both x faces Dirichlet, one rotating at
 2 rad/s), dt = 1/300 s, 50 VBD iterations per step, synthetic seeded inputs.
 
 One JSON line on rank 0 with:
-  value   = vertex-solves/s of the FP32-mixed engine, inputs resident in HBM,
-            device-timed with CUDA events on the library's stream;
+  value   = vertex-solves/s of the fastest FP32-compute mode (fp32, dfhi, mixed) whose
+            error is within --tolerance (1e-5), inputs resident in HBM, device-timed with
+            CUDA events on the library's stream;
   e2e     = the same metric through the public C ABI with host buffers
             (per step: H2D of positions+velocities, the step, D2H of both);
   fp64    = the plain FP64 engine on the same workload (same kernels in FP64);
-  error   = relative position error of the mixed engine vs the FP64 engine
-            after --error-steps steps from the same initial state;
+  error   = relative position error of that mode vs the FP64 engine after
+            --error-steps steps from the same initial state;
   roofline, cpu_baseline, clocks, gpu_launches;
   other_workloads = (twist on one GPU, unless --no-extra) the other configurations'
             default runs (drop, batch, collide, cloth), each in a child process,
