@@ -289,30 +289,43 @@ def other_workloads(timeout_s: float = 900.0) -> dict:
 
 
 def timed_steps(phys, steps: int, local: int) -> tuple[float, float, str]:
-    """Device time of `steps` steps (total, solve sweeps) and how L2 was handled: scenes
-    whose device data is under 4x L2 run each timed step alone after writing a buffer of
-    2x L2 (L2 flushed between timed steps); larger scenes run the steps back to back."""
+    """Device time of `steps` steps, the time of the solve sweeps of `steps` more, and how L2
+    was handled. The steps are timed as runStep runs them (one graph per substep, timed as a
+    whole); the sweep time, for the roofline, comes from as many further steps run with the
+    substep's initial step, sweeps and velocity update as three graphs and CUDA events
+    around every sweep. Scenes whose device data is under 4x L2 run each timed step alone
+    after writing a buffer of 2x L2 (L2 flushed between timed steps); larger scenes run the
+    steps back to back."""
     import torch
 
     l2 = l2_bytes(local)
     data = phys.stats()["device_bytes"]
-    # an NVTX range around the timed steps, so that a profiler can select their launches
-    # (ncu --nvtx --nvtx-include "timed_steps/")
-    torch.cuda.nvtx.range_push("timed_steps")
-    if data >= 4 * l2:
-        tot, sw = phys.run_steps_timed(steps)
+    apart = data < 4 * l2
+    buf = torch.empty(2 * l2 // 4, dtype=torch.float32, device=f"cuda:{local}") if apart else None
+
+    def region(name: str, sweeps: bool) -> tuple[float, float | None]:
+        # an NVTX range around each timed region, so that a profiler can select its launches
+        # (ncu --nvtx --nvtx-include "timed_steps/")
+        torch.cuda.nvtx.range_push(name)
+        if not apart:
+            tot, sw = phys.run_steps_timed(steps, sweeps)
+        else:
+            tot, sw = 0.0, (0.0 if sweeps else None)
+            for _ in range(steps):
+                buf.fill_(1.0)
+                torch.cuda.synchronize()
+                t, s = phys.run_steps_timed(1, sweeps)
+                tot += t
+                if sweeps:
+                    sw += s
         torch.cuda.nvtx.range_pop()
-        return tot, sw, f"inputs larger than L2 ({data / 1e6:.0f} MB of device data, L2 {l2 / 1e6:.0f} MB)"
-    buf = torch.empty(2 * l2 // 4, dtype=torch.float32, device=f"cuda:{local}")
-    tot = sw = 0.0
-    for _ in range(steps):
-        buf.fill_(1.0)
-        torch.cuda.synchronize()
-        t, s = phys.run_steps_timed(1)
-        tot += t
-        sw += s
-    torch.cuda.nvtx.range_pop()
+        return tot, sw
+
+    tot, _ = region("timed_steps", False)
+    _, sw = region("timed_sweeps", True)
     del buf
+    if not apart:
+        return tot, sw, f"inputs larger than L2 ({data / 1e6:.0f} MB of device data, L2 {l2 / 1e6:.0f} MB)"
     return tot, sw, (f"L2 flushed before every timed step ({2 * l2 / 1e6:.0f} MB write; {data / 1e6:.0f} MB of "
                      f"device data), steps timed one at a time")
 

@@ -1001,7 +1001,21 @@ public:
             }
     }
 
+    // Device time of n steps. Without sweep_ms the steps run as run_steps runs them (one
+    // graph per substep) and are timed as a whole; with it the substep's initial step, sweep
+    // and velocity update run as three graphs with events around every sweep, so that the
+    // solve kernels are timed apart.
     void run_steps_timed(int n, float* total_ms, float* sweep_ms) override {
+        if (!sweep_ms) {
+            GAIA_CUDA(cudaEventRecord(ev_a_, st_));
+            run_steps(n);
+            GAIA_CUDA(cudaEventRecord(ev_b_, st_));
+            GAIA_CUDA(cudaEventSynchronize(ev_b_));
+            float tot = 0.f;
+            GAIA_CUDA(cudaEventElapsedTime(&tot, ev_a_, ev_b_));
+            if (total_ms) *total_ms = tot;
+            return;
+        }
         // per-substep sweep events: [start, end] pairs recorded around the sweep graph
         int nsub = n * sc_.p.numSubsteps;
         std::vector<cudaEvent_t> ev(2 * size_t(nsub));

@@ -131,10 +131,13 @@ class VBDPhysics:
     def synchronize(self) -> None:
         _check(lib().gaia_vbd_synchronize(self.handle), self.handle)
 
-    def run_steps_timed(self, n: int) -> tuple[float, float]:
+    def run_steps_timed(self, n: int, sweeps: bool = True) -> tuple[float, float | None]:
+        """Device time (ms) of n steps and of their color sweeps. sweeps=False: the steps run
+        as runStep runs them (one graph per substep) and only the total is timed."""
         tot, sw = C.c_float(), C.c_float()
-        _check(lib().gaia_vbd_run_step_timed(self.handle, n, C.byref(tot), C.byref(sw)), self.handle)
-        return tot.value, sw.value
+        _check(lib().gaia_vbd_run_step_timed(self.handle, n, C.byref(tot), C.byref(sw) if sweeps else None),
+               self.handle)
+        return tot.value, (sw.value if sweeps else None)
 
     def reset(self) -> None:
         """Back to the initial state (rest positions, initial velocities, t = 0)."""

@@ -166,8 +166,11 @@ int gaia_vbd_set_prev_positions(gaia_vbd* h, int32_t mesh, const double* xyz);
 int gaia_vbd_collide(gaia_vbd* h, int32_t* n_contacts);
 int gaia_vbd_get_contacts(gaia_vbd* h, int32_t* rows, int32_t cap, int32_t* n_rows);
 
-/* Runs n_steps and times them with CUDA events on the handle's stream:
- * total_ms = all device work, sweep_ms = the color sweeps (solve kernels) only. */
+/* Runs n_steps and times them with CUDA events on the handle's stream: total_ms = all
+ * device work. With sweep_ms NULL the steps run as gaia_vbd_run_step runs them (one CUDA
+ * graph per substep); otherwise each substep's initial step, color sweeps and velocity
+ * update run as three graphs with events around the sweeps, and sweep_ms = the color
+ * sweeps (solve kernels) only. */
 int gaia_vbd_run_step_timed(gaia_vbd* h, int32_t n_steps, float* total_ms, float* sweep_ms);
 /* Restore the state gaia_vbd_initialize produced: rest positions, initial velocities,
  * substep clock at 0 (counters are kept). The reference recovers a saved state with

@@ -62,6 +62,28 @@ def drop_ref(drop_scene, oracle_lib):
     return _run_oracle(mp, pp, 40, oracle_lib)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_timed_steps_advance_like_run_step(drop_scene, precision):
+    """Both forms of the timed steps (the one graph per substep that runStep launches, timed
+    as a whole; the substep's three graphs with the sweeps timed apart) advance the state
+    exactly as runStep does."""
+    from gaia_gb300 import VBDPhysics, scenes
+
+    mp, pp = drop_scene
+    fixed = dict(lanesPerVertex=8, blockSize=128, autotune=False, solveVariant=0, sweepMode="merged")
+    _, xs, _ = _run_gpu(mp, pp, precision, 6, **fixed)
+    phys = VBDPhysics()
+    phys.loadRunningparameters(mp, scenes.set_precision(pp, precision, **fixed))
+    phys.initialize()
+    tot, sw = phys.run_steps_timed(3, sweeps=False)
+    assert tot > 0 and sw is None
+    tot2, sw2 = phys.run_steps_timed(3)
+    assert 0 < sw2 <= tot2
+    x = phys.positions(0)
+    phys.close()
+    np.testing.assert_array_equal(x, xs[0])
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed", "dfhi", "fp32"])
 def test_drop_cube_trajectory(drop_scene, drop_ref, precision):
     """8^3 cube dropped 2 cm onto the ground, 40 steps x 10 iterations: lands, slides, settles."""
