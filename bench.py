@@ -288,14 +288,15 @@ def other_workloads(timeout_s: float = 900.0) -> dict:
     return out
 
 
-def timed_steps(phys, steps: int, local: int) -> tuple[float, float, str]:
-    """Device time of `steps` steps, the time of the solve sweeps of `steps` more, and how L2
-    was handled. The steps are timed as runStep runs them (one graph per substep, timed as a
-    whole); the sweep time, for the roofline, comes from as many further steps run with the
-    substep's initial step, sweeps and velocity update as three graphs and CUDA events
-    around every sweep. Scenes whose device data is under 4x L2 run each timed step alone
-    after writing a buffer of 2x L2 (L2 flushed between timed steps); larger scenes run the
-    steps back to back."""
+def timed_steps(phys, steps: int, local: int, rewind=None) -> tuple[float, float | None, str]:
+    """Device time of `steps` steps, the time of their solve sweeps, and how L2 was handled.
+    The steps are timed as runStep runs them (one graph per substep, timed as a whole); the
+    sweep time, for the roofline, comes from the same steps run again from the same state
+    (`rewind()` brings the handle back to it; no sweep time without it) with the substep's
+    initial step, sweeps and velocity update as three graphs and CUDA events around every
+    sweep. Scenes whose device data is under 4x L2 run each timed step alone after writing a
+    buffer of 2x L2 (L2 flushed between timed steps); larger scenes run the steps back to
+    back."""
     import torch
 
     l2 = l2_bytes(local)
@@ -322,7 +323,10 @@ def timed_steps(phys, steps: int, local: int) -> tuple[float, float, str]:
         return tot, sw
 
     tot, _ = region("timed_steps", False)
-    _, sw = region("timed_sweeps", True)
+    sw = None
+    if rewind is not None:
+        rewind()
+        _, sw = region("timed_sweeps", True)
     del buf
     if not apart:
         return tot, sw, f"inputs larger than L2 ({data / 1e6:.0f} MB of device data, L2 {l2 / 1e6:.0f} MB)"
@@ -353,19 +357,25 @@ def measure_mode(args, mp, pp, precision, overrides, world, local, xref=None):
         err = {"steps": args.error_steps, "rel": float(np.linalg.norm(x - xref) / np.linalg.norm(xref - x0)),
                "max_abs_m": float(np.abs(x - xref).max()), "reference": "fp64 engine, same kernels"}
         phys.reset()
-    for _ in range(args.warmup):
-        phys.runStep(1)
-    phys.synchronize()
+    def rewind():
+        # the state the timed steps start from: the initial state and the warm-up steps
+        phys.reset()
+        for _ in range(args.warmup):
+            phys.runStep(1)
+        phys.synchronize()
+
+    rewind()
     clk = ClockSampler(local)
     clk.start()
     barrier(world)
-    total_ms, sweep_ms, l2_how = timed_steps(phys, args.steps, local)
+    total_ms, sweep_ms, l2_how = timed_steps(phys, args.steps, local, rewind)
     clocks = clk.stop()
     total_ms = allmax(world, total_ms)
     sweep_ms = allmax(world, sweep_ms)
     st = phys.stats()
-    # e2e through the C ABI with page-locked host buffers: per step H2D of positions and
-    # velocities, the step, D2H of positions and velocities
+    # e2e through the C ABI with page-locked host buffers, from the state the timed steps
+    # started from: per step H2D of positions and velocities, the step, D2H of both
+    rewind()
     xh = torch.empty(3 * n, dtype=torch.float32, pin_memory=True)
     vh = torch.empty(3 * n, dtype=torch.float32, pin_memory=True)
     phys.get_positions_f32(xh.data_ptr())
@@ -750,8 +760,15 @@ def main():
             p64.runStep(args.error_steps)
             xref = np.concatenate([p64.positions(m) for m in range(p64.numMeshes())])
             p64.reset()
-        p64.runStep(2)
-        p64.synchronize()
+
+        def rewind64():
+            # the state the FP32-compute engines' timed steps start from too
+            p64.reset()
+            for _ in range(args.warmup):
+                p64.runStep(1)
+            p64.synchronize()
+
+        rewind64()
         t64, _, _ = timed_steps(p64, args.fp64_steps, local)
         nact64 = p64.stats()["num_active_vertices"]
         p64.close()
