@@ -356,7 +356,7 @@ def measure_mode(args, mp, pp, precision, overrides, world, local, xref=None):
         x = np.concatenate([phys.positions(m) for m in range(phys.numMeshes())])
         err = {"steps": args.error_steps, "rel": float(np.linalg.norm(x - xref) / np.linalg.norm(xref - x0)),
                "max_abs_m": float(np.abs(x - xref).max()), "reference": "fp64 engine, same kernels"}
-        phys.reset()
+
     def rewind():
         # the state the timed steps start from: the initial state and the warm-up steps
         phys.reset()
