@@ -71,3 +71,27 @@ def test_oracle_writer_equals_library_writer(tmp_path, gaia_lib, oracle_lib, kin
         np.testing.assert_array_equal(Xa, Xb)
         ca = m["verticesColoringCategoriesPath"]
         assert json.load(open(ca)) == json.load(open(ca.replace(da, db))), (kind, os.path.basename(ta))
+
+
+def test_stored_colorings_equal_the_library_tool(gaia_lib, oracle_lib):
+    """The stored colorings the reference arm reads for the two meshes too large for the
+    oracle's O(V^2) coloring tool (the 100^3 twist lattice, the 512 x 512 cloth) are the
+    library's tool colorings of those meshes, as the GPU arm's scene writer makes them."""
+    from gaia_gb300 import physics, scenes
+    from gaia_gb300.cloth import color_trimesh_tool
+    from oracle import scene_colorings
+
+    n = 100
+    half = 0.5 * 0.01 * (n - 1)
+    X, T = scenes.lattice_cube((n, n, n), 0.01, (0.0, -half, -half), jitter=1e-4, seed=1)
+    colors, order = physics.color_tool(len(X), T)
+    stored = scene_colorings.stored(len(X), T, "tet_tool")
+    assert stored is not None
+    np.testing.assert_array_equal(colors, stored[0])
+    np.testing.assert_array_equal(order, stored[1])
+    Xc, F = scenes.cloth_grid(512, 1.0, 0.3 + 0.01, 1e-3, 1)
+    colors, order = color_trimesh_tool(len(Xc), F)
+    stored = scene_colorings.stored(len(Xc), F, "tri_tool")
+    assert stored is not None
+    np.testing.assert_array_equal(colors, stored[0])
+    np.testing.assert_array_equal(order, stored[1])
