@@ -75,7 +75,8 @@ struct PhysicsParams {
     bool usePDL = true;                  // programmatic dependent launch between color kernels
     int smallColorVertices = 16384;      // colors up to this size use one warp per vertex
     int solveVariant = -1;               // -1 autotune, 0 register-pipelined, 1 TMA-staged records, 4 deeper
-                                         // register pipeline, 6 next wave's records prefetched into L2
+                                         // register pipeline, 6 next wave's records prefetched into L2,
+                                         // 7 double-buffered TMA tiles on a persistent grid
     std::string sweepMode = "auto";      // color scheduling: "auto", "merged", "scenes", "cluster", "grid"
     int clusterSize = 0;                 // blocks per cluster of the cluster sweep (0 = autotune; 2, 4, 8, 16)
     bool meshFrames = true;              // FP32-compute states relative to a per-mesh frame that follows

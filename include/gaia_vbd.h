@@ -62,9 +62,10 @@ typedef struct {
     double autotune_ms_per_iteration; /* best measured sweep time per iteration (0 if not tuned) */
     int32_t solve_variant;        /* 0 = register-pipelined solve kernel, 1 = TMA-staged records,
                                      2 = scene-major persistent sweep, 3 = cluster sweep, 4 = register
-                                     pipeline two records deep, 6 = register pipeline with the records
-                                     of the next resident wave prefetched into L2 (of the largest
-                                     color), 5 = grid sweep */
+                                     pipeline two records deep, 5 = grid sweep, 6 = register pipeline
+                                     with the records of the next resident wave prefetched into L2,
+                                     7 = double-buffered TMA tiles on a persistent grid (of the
+                                     largest color) */
     int32_t mesh_frames;          /* 1: states are kept relative to a per-mesh frame offset that
                                      follows each mesh (PhysicsParams meshFrames; FP32-compute
                                      precisions without contact detection or deformers) */
