@@ -856,7 +856,10 @@ def main():
                                     "cluster_size": st.get("cluster_size", 0),
                                     "autotuned_ms_per_iteration": {k: st.get(f"sweep_ms_{k}", 0.0) for k in
                                                                    ("merged", "scenes", "cluster", "grid")}},
-                       "l2": head["l2"]},
+                       "l2": head["l2"],
+                       "timing": ("value: the timed steps launched as runStep launches them (one CUDA graph per "
+                                  "substep), CUDA events around the steps; roofline: the same steps from the same "
+                                  "state with CUDA events around each substep's sweep graph")},
             "e2e": {"value": head["e2e_value"], "unit": "vertex-solves/s", "h2d_bytes_per_step": 24 * n,
                     "d2h_bytes_per_step": 24 * n, "steps": head["e2e_steps"]},
             "error_vs_fp64": head["error"], "fp64": fp64, "batching": batching,
